@@ -1,0 +1,867 @@
+// amg_host.cpp - AMG setup on the host: strength, C/F splitting, interpolation,
+// truncation, Galerkin product and the coarsest-level factorisation.
+//
+// Each function states the reference routine whose integer and floating-point
+// behaviour it reproduces.  Data structures are this library's own (CSR rows,
+// a binary heap with lazy deletion instead of a red-black tree); where the
+// reference's row-list type has visible side effects (the explicit (i, 0.0)
+// entry every new row starts with, the row reset when a last element is
+// removed) those effects are reproduced because they decide sparsity patterns.
+#include "amg_host.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <queue>
+
+namespace lina {
+namespace {
+
+// ------------------------------------------------------------------ rows
+struct Row {
+    std::vector<int> c;
+    std::vector<double> v;
+};
+
+// insert_sparse (linear_algebra.c:1124): accumulate into an existing column
+// or insert at the sorted position.
+inline void row_insert(Row& r, double a, int j) {
+    auto it = std::lower_bound(r.c.begin(), r.c.end(), j);
+    size_t pos = size_t(it - r.c.begin());
+    if (it != r.c.end() && *it == j) {
+        r.v[pos] += a;
+    } else {
+        r.c.insert(it, j);
+        r.v.insert(r.v.begin() + pos, a);
+    }
+}
+
+// remove_element (linear_algebra.c:1181)
+inline void row_remove(Row& r, int j) {
+    auto it = std::lower_bound(r.c.begin(), r.c.end(), j);
+    if (it != r.c.end() && *it == j) {
+        size_t pos = size_t(it - r.c.begin());
+        r.c.erase(it);
+        r.v.erase(r.v.begin() + pos);
+    }
+}
+
+// delete_zeros (linear_algebra.c:793) on one row whose index is i: rows of
+// length > 1 lose their zero entries; a row that would become empty is reset
+// to the single entry (i, 0.0) as remove_element_at does (:1161-1178).
+inline void row_delete_zeros(std::vector<int>& c, std::vector<double>& v, int i) {
+    if (c.size() <= 1) return;
+    size_t w = 0;
+    for (size_t k = 0; k < c.size(); k++)
+        if (v[k] != 0.0) {
+            c[w] = c[k];
+            v[w] = v[k];
+            w++;
+        }
+    if (w == 0) {
+        c.assign(1, i);
+        v.assign(1, 0.0);
+    } else {
+        c.resize(w);
+        v.resize(w);
+    }
+}
+
+inline double csr_diag(const Csr& A, int i) {  // get_diag (linear_algebra.c:3434)
+    auto b = A.col.begin() + A.ptr[i], e = A.col.begin() + A.ptr[i + 1];
+    auto it = std::lower_bound(b, e, i);
+    if (it != e && *it == i) return A.val[size_t(it - A.col.begin())];
+    return 0.0;
+}
+
+// ------------------------------------------------------------ lists (CSR of ints)
+struct Lists {
+    std::vector<int> ptr{0};
+    std::vector<int> idx;
+    int size(int i) const { return ptr[i + 1] - ptr[i]; }
+    const int* row(int i) const { return idx.data() + ptr[i]; }
+};
+
+// Transpose lists: T[k] lists j in increasing j for every k in S[j]
+// (get_strong_connection_sets, Multigrid.c:240-258).
+Lists transpose_lists(const Lists& S, int n) {
+    Lists T;
+    T.ptr.assign(n + 1, 0);
+    for (int k : S.idx) T.ptr[k + 1]++;
+    for (int i = 0; i < n; i++) T.ptr[i + 1] += T.ptr[i];
+    T.idx.resize(S.idx.size());
+    std::vector<int> fill(T.ptr.begin(), T.ptr.end() - 1);
+    int n_s = (int)S.ptr.size() - 1;
+    for (int j = 0; j < n_s; j++)
+        for (int p = S.ptr[j]; p < S.ptr[j + 1]; p++) T.idx[fill[S.idx[p]]++] = j;
+    return T;
+}
+
+// get_max_coupled + get_strong_connected (Multigrid.c:86-97, :156-184):
+// j is strong for i when (same unknown and) a_ij < -eps_minus|a_i,min| or
+// a_ij > eps_plus|a_i,min|, where a_i,min is the most negative off-diagonal.
+Lists strong_connections(const Csr& A, const std::vector<int>& lev, double em, double ep) {
+    Lists S;
+    S.ptr.resize(A.n + 1);
+    S.ptr[0] = 0;
+    S.idx.reserve(A.col.size());
+    for (int i = 0; i < A.n; i++) {
+        double mn = 0.0;
+        int mi = -1;
+        for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++)
+            if (A.col[p] != i && A.val[p] < mn) {
+                mn = A.val[p];
+                mi = p;
+            }
+        if (mi >= 0) {
+            double lo = -em * std::fabs(A.val[mi]);
+            double hi = ep * std::fabs(A.val[mi]);
+            for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
+                int J = A.col[p];
+                if (J == i) continue;
+                double a = (lev[i] == lev[J]) ? A.val[p] : 0.0;
+                if (a < lo || a > hi) S.idx.push_back(J);
+            }
+        }
+        S.ptr[i + 1] = (int)S.idx.size();
+    }
+    return S;
+}
+
+// Graph view for the coarsener: stored pattern plus "value != 0" flags.
+struct Graph {
+    int n = 0;
+    std::vector<int> ptr, col;
+    std::vector<char> nz;
+};
+
+Graph graph_of(const Csr& A) {
+    Graph g;
+    g.n = A.n;
+    g.ptr = A.ptr;
+    g.col = A.col;
+    g.nz.resize(A.val.size());
+    for (size_t k = 0; k < A.val.size(); k++) g.nz[k] = (A.val[k] != 0.0);
+    return g;
+}
+
+// Max-priority queue with the ordering of the reference's red-black tree
+// (red_black_tree.c:174-197, :513-523, :620-658): keys compare with '>';
+// a new node goes after every node whose key is <= its own, and the largest
+// is the rightmost node, so among equal keys the latest insertion wins.  A
+// binary heap on (key, insertion sequence) with lazy deletion yields the same
+// choice.
+class ImportanceQueue {
+   public:
+    explicit ImportanceQueue(int n) : live_(n, 0) {}
+    bool contains(int i) const { return live_[i] != 0; }
+    void insert(int i, double key) {
+        uint64_t s = ++seq_;
+        live_[i] = s;
+        heap_.push(Entry{key, s, i});
+    }
+    void remove(int i) { live_[i] = 0; }
+    int pop_largest() {
+        while (!heap_.empty()) {
+            Entry e = heap_.top();
+            if (live_[e.node] == e.seq) {
+                heap_.pop();
+                live_[e.node] = 0;
+                return e.node;
+            }
+            heap_.pop();
+        }
+        return -1;
+    }
+
+   private:
+    struct Entry {
+        double key;
+        uint64_t seq;
+        int node;
+        bool operator<(const Entry& o) const {
+            if (key > o.key) return false;
+            if (o.key > key) return true;
+            return seq < o.seq;
+        }
+    };
+    std::priority_queue<Entry> heap_;
+    std::vector<uint64_t> live_;
+    uint64_t seq_ = 0;
+};
+
+// AMG_get_lambda (Multigrid.c:364-375)
+inline double lambda_of(const std::vector<int>& label, const Lists& T, int i, int size) {
+    int undec = 0, fine = 0;
+    for (int p = T.ptr[i]; p < T.ptr[i + 1]; p++) {
+        int J = T.idx[p];
+        if (label[J] == kUndecided) undec++;
+        if (label[J] == kFine) fine++;
+    }
+    return (double)i / size + undec + 2 * fine;
+}
+
+// AMG_coarsener (Multigrid.c:377-473).  `lev` is indexed by the graph's own
+// node numbers, exactly as the reference indexes its Levels argument (which,
+// in the aggressive second pass, is the fine-level array; the reference's
+// behaviour in that case is reproduced, not corrected).
+void coarsener(const Graph& A, std::vector<int>& label, std::vector<double>& imp, const Lists& S, const Lists& T,
+               ImportanceQueue& q, const int* lev, int lev_size, int size, int seed, std::vector<int>& cursor) {
+    auto level_of = [&](int i) { return (i < lev_size) ? lev[i] : -1; };
+    int level = level_of(seed);
+    int next = seed;
+    do {
+        label[next] = kCoarse;
+        const int b = A.ptr[next], e = A.ptr[next + 1];
+        for (int p = b; p < e; p++) {
+            int I = A.col[p];
+            if (label[I] == kUndecided && A.nz[p] && !q.contains(I)) q.insert(I, imp[I]);
+        }
+        for (int p = T.ptr[next]; p < T.ptr[next + 1]; p++) {
+            int I = T.idx[p];
+            if (q.contains(I)) {
+                label[I] = kFine;
+                q.remove(I);
+            }
+        }
+        for (int p = b; p < e; p++) {
+            int I = A.col[p];
+            if (A.nz[p] && q.contains(I)) {
+                double lam = lambda_of(label, T, I, size);
+                if (lam != imp[I]) {
+                    q.remove(I);
+                    imp[I] = lam;
+                    q.insert(I, lam);
+                }
+            }
+        }
+        for (int p = b; p < e; p++) {
+            int I = A.col[p];
+            if (I == next) continue;
+            for (int r = A.ptr[I]; r < A.ptr[I + 1]; r++) {
+                int J = A.col[r];
+                if (label[J] == kUndecided && A.nz[r] && !q.contains(J)) q.insert(J, imp[J]);
+            }
+            for (int r = S.ptr[I]; r < S.ptr[I + 1]; r++) {
+                int J = S.idx[r];
+                if (label[J] == kUndecided) {
+                    double lam = lambda_of(label, T, J, size);
+                    if (lam != imp[J]) {
+                        q.remove(J);
+                        imp[J] = lam;
+                        q.insert(J, lam);
+                    }
+                }
+            }
+        }
+        next = q.pop_largest();
+        if (next < 0) {
+            // first undecided node of the seed's unknown; labels never return
+            // to undecided, so a per-level cursor finds the same node
+            int& c = cursor[level + 1];
+            while (c < size && !(label[c] == kUndecided && level_of(c) == level)) c++;
+            next = (c < size) ? c : -1;
+        }
+    } while (next >= 0);
+}
+
+// AMG_is_isolated (Multigrid.c:498-503)
+inline bool is_isolated(const Csr& A, int i) {
+    int n = 0;
+    for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++)
+        if (A.val[p] != 0.0) n++;
+    return n == 1;
+}
+
+// standard_coarsening (Multigrid.c:506-548)
+int standard_coarsening(const Csr& A, const std::vector<int>& lev, int dof, const Lists& S, const Lists& T,
+                        std::vector<int>& label, bool stand_alone) {
+    int n = A.n;
+    label.assign(n, kUndecided);
+    for (int i = 0; i < n; i++) {
+        if (S.size(i) == 0) label[i] = is_isolated(A, i) ? kIsolated : kCoarse;
+    }
+    std::vector<double> imp(n, 0.0);
+    ImportanceQueue q(n);
+    Graph g = graph_of(A);
+    std::vector<int> cursor(dof + 2, 0);
+    for (int d = 0; d < dof; d++) {
+        int seed = -1;
+        for (int j = 0; j < n; j++)
+            if (label[j] == kUndecided && lev[j] == d) {
+                seed = j;
+                break;
+            }
+        if (seed >= 0) coarsener(g, label, imp, S, T, q, lev.data(), n, n, seed, cursor);
+    }
+    int coarse = 0;
+    for (int i = 0; i < n; i++) {
+        if (label[i] == kUndecided) label[i] = kFine;
+        if (label[i] == kCoarse) coarse++;
+    }
+    if (stand_alone)
+        for (int i = 0; i < n; i++)
+            if (label[i] == kIsolated) coarse++;
+    return coarse;
+}
+
+// aggressive_coarsening (Multigrid.c:550-607) with Get_2nd_strong_connected
+// (:187-217), get_2nd_max_coupled (:99-119) and the distance-two pattern of
+// get_2nd_strong_connection_sets (:260-292).
+int aggressive_coarsening(const Csr& A, const std::vector<int>& lev, int dof, const Lists& S, const Lists& T,
+                          double em, double ep, std::vector<int>& label) {
+    int n = A.n;
+    std::vector<int> pre;
+    int pre_size = standard_coarsening(A, lev, dof, S, T, pre, false);
+    label = pre;
+    std::vector<int> map(n, -1), inv(pre_size);
+    {
+        int k = 0;
+        for (int i = 0; i < n; i++)
+            if (pre[i] == kCoarse) {
+                map[i] = k;
+                inv[k] = i;
+                k++;
+            }
+    }
+    std::vector<double> diag(n);
+    for (int i = 0; i < n; i++) diag[i] = csr_diag(A, i);
+    Lists M2;
+    M2.ptr.assign(pre_size + 1, 0);
+    Graph g2;
+    g2.n = pre_size;
+    g2.ptr.assign(pre_size + 1, 0);
+    std::vector<int> cand;
+    for (int I = 0; I < pre_size; I++) {
+        int i = inv[I];
+        double maxv = 0.0;
+        for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
+            int J = A.col[p];
+            double val = A.val[p];
+            if (J != i && val != 0.0) {
+                double d = diag[J];
+                for (int r = A.ptr[J]; r < A.ptr[J + 1]; r++) {
+                    int K = A.col[r];
+                    double val2 = A.val[r];
+                    double pv = std::fabs(val * val2 / d);
+                    if (K != J && K != i && val2 != 0.0 && pv > maxv) maxv = pv;
+                }
+            }
+        }
+        if (maxv > 0.0) {
+            double mn = -em * maxv, mx = ep * maxv;
+            for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
+                int J = A.col[p];
+                double a = A.val[p];
+                double d = diag[J];
+                if (J != i && a != 0.0 && lev[i] == lev[J]) {
+                    for (int r = A.ptr[J]; r < A.ptr[J + 1]; r++) {
+                        int K = A.col[r];
+                        double bb = A.val[r];
+                        if (pre[K] == kCoarse && K != J && K != i && a * bb / d > 0 && lev[K] == lev[i]) {
+                            if (-a * bb / d < mn || a * bb / d > mx) M2.idx.push_back(map[K]);
+                        }
+                    }
+                }
+            }
+        }
+        M2.ptr[I + 1] = (int)M2.idx.size();
+        // pattern row I: distinct Map[K] over distance-two coarse neighbours, plus (I, 0.0)
+        cand.clear();
+        cand.push_back(I);
+        for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
+            int J = A.col[p];
+            if (J != i && A.val[p] != 0.0)
+                for (int r = A.ptr[J]; r < A.ptr[J + 1]; r++) {
+                    int K = A.col[r];
+                    if (pre[K] == kCoarse && K != J && K != i && A.val[r] != 0.0) cand.push_back(map[K]);
+                }
+        }
+        std::sort(cand.begin(), cand.end());
+        cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+        for (int c : cand) {
+            g2.col.push_back(c);
+            g2.nz.push_back(c != I);
+        }
+        g2.ptr[I + 1] = (int)g2.col.size();
+    }
+    Lists T2 = transpose_lists(M2, pre_size);
+    std::vector<int> label2(pre_size, kUndecided);
+    std::vector<double> imp2(pre_size, 0.0);  // malloc'd without initialisation in the reference
+    ImportanceQueue q(pre_size);
+    std::vector<int> cursor(dof + 2, 0);
+    for (int d = 0; d < dof; d++) {
+        int seed = -1;
+        for (int I = 0; I < pre_size; I++)
+            if (lev[inv[I]] == d) {
+                seed = I;
+                break;
+            }
+        if (seed >= 0) coarsener(g2, label2, imp2, M2, T2, q, lev.data(), n, pre_size, seed, cursor);
+    }
+    int coarse = 0;
+    for (int i = 0; i < n; i++) {
+        if (label[i] == kCoarse) {
+            label[i] = label2[map[i]];
+            if (label[i] == kCoarse) coarse++;
+        } else if (label[i] == kIsolated) {
+            coarse++;
+        }
+    }
+    return coarse;
+}
+
+// get_AMG_index_map (Multigrid.c:323-338) with WITH_ISOLATED: every non-fine
+// node gets the next coarse index.
+int coarse_map(const std::vector<int>& label, std::vector<int>& map) {
+    int k = 0;
+    map.assign(label.size(), -1);
+    for (size_t i = 0; i < label.size(); i++)
+        if (label[i] != kFine) map[i] = k++;
+    return k;
+}
+
+// AMG_simple_standard_interpolation (Multigrid.c:989-1079) followed by
+// sparse_approximate (linear_algebra.c:1418-1442) and normalize_row_sum
+// (:455-464).  Returns false if a zero diagonal makes the reference abort.
+bool interpolation(const Csr& A, const std::vector<int>& label, const std::vector<int>& lev,
+                   const std::vector<int>& map, int iter, double tol, Csr& P, std::string& err, bool& broke) {
+    int n = A.n;
+    std::vector<double> D(n);
+    for (int i = 0; i < n; i++) {
+        D[i] = csr_diag(A, i);
+        if (D[i] == 0.0) {
+            char buf[128];
+            snprintf(buf, sizeof buf, "diagonal zero at index %d: standard interpolation not possible", i);
+            err = buf;
+            return false;
+        }
+    }
+    std::vector<Row> Prow(n);
+    for (int i = 0; i < n; i++) {  // sparse_zero: every row starts as (i, 0.0)
+        Prow[i].c.assign(1, i);
+        Prow[i].v.assign(1, 0.0);
+    }
+    broke = false;
+    Row q, snap;
+    for (int i = 0; i < n && !broke; i++) {
+        if (label[i] != kFine) {
+            row_insert(Prow[i], 1.0, map[i]);
+            continue;
+        }
+        q.c.assign(A.col.begin() + A.ptr[i], A.col.begin() + A.ptr[i + 1]);
+        q.v.resize(q.c.size());
+        for (int p = A.ptr[i], k = 0; p < A.ptr[i + 1]; p++, k++) q.v[k] = A.val[p] / D[i];
+        for (int pass = 0; pass < iter; pass++) {
+            snap = q;
+            for (size_t j = 0; j < snap.c.size(); j++) {
+                int J = snap.c[j];
+                double qv = snap.v[j];
+                if (J != i && label[J] == kFine && qv != 0.0) {
+                    row_remove(q, J);
+                    for (int r = A.ptr[J]; r < A.ptr[J + 1]; r++) {
+                        int L = A.col[r];
+                        double a = A.val[r] / D[J];
+                        if (L != J && a != 0.0) row_insert(q, -a * qv, L);
+                    }
+                }
+            }
+        }
+        // drop couplings to other unknowns (order preserving)
+        {
+            size_t w = 0;
+            for (size_t k = 0; k < q.c.size(); k++)
+                if (lev[q.c[k]] == lev[i]) {
+                    q.c[w] = q.c[k];
+                    q.v[w] = q.v[k];
+                    w++;
+                }
+            q.c.resize(w);
+            q.v.resize(w);
+        }
+        double s_p = 0, c_p = 0, s_m = 0, c_m = 0;
+        double Di = D[i];
+        for (size_t k = 0; k < q.c.size(); k++) {
+            int J = q.c[k];
+            double qv = q.v[k];
+            if (J != i) {
+                if (qv < 0) {
+                    s_m += qv;
+                    if (label[J] == kCoarse) c_m += qv;
+                } else {
+                    s_p += qv;
+                    if (label[J] == kCoarse) c_p += qv;
+                }
+            } else {
+                Di = qv;
+            }
+        }
+        double alpha = 0, beta = 0;
+        if (c_m != 0) alpha = -s_m / c_m; else Di += s_m;
+        if (c_p != 0) beta = -s_p / c_p; else Di += s_p;
+        if (alpha == 0 && beta == 0) {
+            // the reference prints and leaves the row loop here (Multigrid.c:1057-1059)
+            broke = true;
+            break;
+        }
+        alpha /= Di;
+        beta /= Di;
+        for (size_t k = 0; k < q.c.size(); k++) {
+            int J = q.c[k];
+            double qv = q.v[k];
+            if (J != i && label[J] == kCoarse) {
+                if (qv < 0 && alpha != 0) row_insert(Prow[i], alpha * qv, map[J]);
+                if (qv > 0 && beta != 0) row_insert(Prow[i], beta * qv, map[J]);
+            }
+        }
+    }
+    // delete_zeros, sparse_approximate, normalize_row_sum
+    P = Csr();
+    P.n = n;
+    P.ptr.assign(n + 1, 0);
+    for (int i = 0; i < n; i++) {
+        Row& r = Prow[i];
+        row_delete_zeros(r.c, r.v, i);
+        double mx = 0;
+        for (size_t k = 0; k < r.c.size(); k++) {
+            double a = std::fabs(r.v[k]);
+            if (r.c[k] != i && a > mx) mx = a;
+        }
+        size_t w = 0;
+        for (size_t k = 0; k < r.c.size(); k++) {
+            if (r.c[k] != i && std::fabs(r.v[k]) < mx * tol) continue;
+            r.c[w] = r.c[k];
+            r.v[w] = r.v[k];
+            w++;
+        }
+        r.c.resize(w);
+        r.v.resize(w);
+        double sum = 0;
+        for (double x : r.v) sum += x;
+        if (sum != 0)
+            for (double& x : r.v) x *= 1.0 / sum;
+        P.col.insert(P.col.end(), r.c.begin(), r.c.end());
+        P.val.insert(P.val.end(), r.v.begin(), r.v.end());
+        P.ptr[i + 1] = (int)P.col.size();
+    }
+    return true;
+}
+
+// get_AMG_transposed (Multigrid.c:308-321): nonzero entries of P transposed
+// into rows that start as (k, 0.0); no zero deletion afterwards.
+Csr amg_transpose(const Csr& P, int nc) {
+    Csr R;
+    R.n = nc;
+    R.ncols = P.n;
+    std::vector<int> cnt(nc + 1, 0);
+    for (int k = 0; k < nc; k++) cnt[k + 1] = 1;
+    for (int i = 0; i < P.n; i++)
+        for (int p = P.ptr[i]; p < P.ptr[i + 1]; p++)
+            if (P.val[p] != 0.0 && P.col[p] != i) cnt[P.col[p] + 1]++;
+    // (an entry whose fine row index equals its coarse column accumulates onto the (k, 0.0) entry)
+    R.ptr.assign(nc + 1, 0);
+    for (int k = 0; k < nc; k++) R.ptr[k + 1] = R.ptr[k] + cnt[k + 1];
+    R.col.assign(R.ptr[nc], 0);
+    R.val.assign(R.ptr[nc], 0.0);
+    std::vector<int> fill(nc, 0);
+    std::vector<char> diag_done(nc, 0);
+    // rows are produced in increasing fine index i; the (k, 0.0) entry sits at column k
+    for (int i = 0; i < P.n; i++) {
+        for (int p = P.ptr[i]; p < P.ptr[i + 1]; p++) {
+            double a = P.val[p];
+            int k = P.col[p];
+            if (a == 0.0) continue;
+            int base = R.ptr[k];
+            if (!diag_done[k] && k < i) {  // the initial (k, 0.0) precedes column i
+                R.col[base + fill[k]] = k;
+                R.val[base + fill[k]] = 0.0;
+                fill[k]++;
+                diag_done[k] = 1;
+            }
+            if (k == i) {
+                R.col[base + fill[k]] = k;
+                R.val[base + fill[k]] = 0.0 + a;
+                fill[k]++;
+                diag_done[k] = 1;
+            } else {
+                R.col[base + fill[k]] = i;
+                R.val[base + fill[k]] = a;
+                fill[k]++;
+            }
+        }
+    }
+    for (int k = 0; k < nc; k++)
+        if (!diag_done[k]) {  // (k, 0.0) is the last entry of row k
+            R.col[R.ptr[k] + fill[k]] = k;
+            R.val[R.ptr[k] + fill[k]] = 0.0;
+            fill[k]++;
+        }
+    return R;
+}
+
+// square_matrix_clean (linear_algebra.c:3100-3120)
+bool square_clean(Csr& A) {
+    int n = A.n;
+    Csr B;
+    B.n = n;
+    B.ncols = n;
+    B.ptr.assign(n + 1, 0);
+    B.col.reserve(A.col.size());
+    B.val.reserve(A.val.size());
+    for (int i = 0; i < n; i++) {
+        size_t start = B.col.size();
+        for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
+            int c = A.col[p];
+            double v = A.val[p];
+            if (c >= n) {
+                if (v != 0.0) return false;
+                continue;
+            }
+            if (v == 0.0 && c != i) continue;
+            B.col.push_back(c);
+            B.val.push_back(v);
+        }
+        if (B.col.size() == start) {
+            B.col.push_back(i);
+            B.val.push_back(0.0);
+        }
+        B.ptr[i + 1] = (int)B.col.size();
+    }
+    A = std::move(B);
+    return true;
+}
+
+// sparse_LU_factorization (linear_algebra.c:3040-3062): the rows holding more
+// than one nonzero form a dense block factorised without pivoting; the other
+// rows are solved by their diagonal.  The block is stored as its inverse so
+// that the GPU coarse solve is one dense matrix-vector product.
+bool coarse_factor(const Csr& A, CoarseSolver& cs, std::string& err) {
+    int n = A.n;
+    cs = CoarseSolver();
+    cs.n = n;
+    cs.in_block.assign(n, 0);
+    cs.diag_inv.assign(n, 0.0);
+    std::vector<int> map(n, -1);
+    for (int i = 0; i < n; i++) {
+        int cnt = 0;
+        for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++)
+            if (A.val[p] != 0.0) cnt++;
+        if (cnt > 1) {
+            map[i] = (int)cs.block_rows.size();
+            cs.block_rows.push_back(i);
+            cs.in_block[i] = 1;
+        } else {
+            double d = csr_diag(A, i);
+            cs.diag_inv[i] = 1.0 / d;
+        }
+    }
+    int m = (int)cs.block_rows.size();
+    std::vector<double> M((size_t)m * m, 0.0);
+    for (int I = 0; I < m; I++) {
+        int i = cs.block_rows[I];
+        for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
+            int J = map[A.col[p]];
+            if (J >= 0) M[(size_t)I * m + J] = A.val[p];
+        }
+    }
+    // in-place Gauss-Jordan inversion without pivoting (the reference's LU does not pivot)
+    std::vector<double>& X = M;
+    for (int k = 0; k < m; k++) {
+        double piv = X[(size_t)k * m + k];
+        if (piv == 0.0) {
+            char buf[128];
+            snprintf(buf, sizeof buf, "coarsest level: zero pivot at block row %d", k);
+            err = buf;
+            return false;
+        }
+        double ip = 1.0 / piv;
+        double* rk = &X[(size_t)k * m];
+        for (int j = 0; j < m; j++) rk[j] *= ip;
+        rk[k] = ip;
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < m; i++) {
+            if (i == k) continue;
+            double* ri = &X[(size_t)i * m];
+            double f = ri[k];
+            if (f == 0.0) continue;
+            ri[k] = 0.0;
+            for (int j = 0; j < m; j++) ri[j] -= f * rk[j];
+        }
+    }
+    cs.inv = std::move(X);
+    return true;
+}
+
+}  // namespace
+
+// sparse_product (linear_algebra.c:186-222): row i of the result starts as
+// (i, 0.0); a*b is accumulated per column in the order of A's row entries;
+// zero factors are skipped; delete_zeros runs at the end.
+Csr spgemm_ref(const Csr& A, const Csr& B) {
+    Csr C;
+    C.n = A.n;
+    C.ncols = B.ncols;
+    C.ptr.assign(A.n + 1, 0);
+    int width = std::max(B.ncols, A.n) + 1;
+    for (int c : B.col) width = std::max(width, c + 1);
+    std::vector<double> acc(width, 0.0);
+    std::vector<int> mark(width, -1);
+    std::vector<int> cols;
+    std::vector<double> vals;
+    C.col.reserve(A.col.size() * 2);
+    C.val.reserve(A.col.size() * 2);
+    for (int i = 0; i < A.n; i++) {
+        cols.clear();
+        mark[i] = i;
+        acc[i] = 0.0;
+        cols.push_back(i);
+        for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
+            double a = A.val[p];
+            if (a == 0.0) continue;
+            int k = A.col[p];
+            for (int r = B.ptr[k]; r < B.ptr[k + 1]; r++) {
+                double b = B.val[r];
+                if (b == 0.0) continue;
+                int j = B.col[r];
+                if (mark[j] != i) {
+                    mark[j] = i;
+                    acc[j] = a * b;
+                    cols.push_back(j);
+                } else {
+                    acc[j] += a * b;
+                }
+            }
+        }
+        std::sort(cols.begin(), cols.end());
+        vals.resize(cols.size());
+        for (size_t k = 0; k < cols.size(); k++) vals[k] = acc[cols[k]];
+        row_delete_zeros(cols, vals, i);
+        C.col.insert(C.col.end(), cols.begin(), cols.end());
+        C.val.insert(C.val.end(), vals.begin(), vals.end());
+        C.ptr[i + 1] = (int)C.col.size();
+    }
+    return C;
+}
+
+int greedy_colouring(const Csr& A, std::vector<int>& colour) {
+    int n = A.n;
+    std::vector<int> tptr(n + 1, 0);
+    for (int i = 0; i < n; i++)
+        for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
+            int j = A.col[p];
+            if (j != i && j < n && A.val[p] != 0.0) tptr[j + 1]++;
+        }
+    for (int i = 0; i < n; i++) tptr[i + 1] += tptr[i];
+    std::vector<int> tadj(tptr[n]);
+    std::vector<int> fill(tptr.begin(), tptr.end() - 1);
+    for (int i = 0; i < n; i++)
+        for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
+            int j = A.col[p];
+            if (j != i && j < n && A.val[p] != 0.0) tadj[fill[j]++] = i;
+        }
+    colour.assign(n, -1);
+    std::vector<int> mark(n + 2, -1);
+    int ncol = 0;
+    for (int i = 0; i < n; i++) {
+        for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
+            int j = A.col[p];
+            if (j != i && j < n && A.val[p] != 0.0 && colour[j] >= 0) mark[colour[j]] = i;
+        }
+        for (int p = tptr[i]; p < tptr[i + 1]; p++)
+            if (colour[tadj[p]] >= 0) mark[colour[tadj[p]]] = i;
+        int c = 0;
+        while (mark[c] == i) c++;
+        colour[i] = c;
+        ncol = std::max(ncol, c + 1);
+    }
+    return ncol;
+}
+
+bool amg_setup_host(const Csr& Ain, const AmgParams& p, HostHierarchy& h) {
+    h = HostHierarchy();
+    h.params = p;
+    const int depth = p.depth;
+    if (depth < 1 || Ain.n <= 0) {
+        h.error = "invalid depth or empty matrix";
+        return false;
+    }
+    h.lv.resize(depth);
+    // clone + make_positive_diag (linear_algebra.c:2612-2620)
+    HostLevel& fine = h.lv[depth - 1];
+    fine.A = Ain;
+    fine.A.ncols = Ain.n;
+    h.signs.assign(Ain.n, 1.0);
+    for (int i = 0; i < Ain.n; i++) {
+        if (csr_diag(fine.A, i) < 0) {
+            for (int q = fine.A.ptr[i]; q < fine.A.ptr[i + 1]; q++) fine.A.val[q] *= -1.0;
+            h.signs[i] = -1.0;
+        }
+    }
+    // AMG_init_finest_tupels (Multigrid.c:785-804): block unknown ordering
+    {
+        int n = Ain.n;
+        int mesh = n / p.dof;
+        fine.dof_level.assign(n, 0);
+        for (int k = 0; k < n; k++) fine.dof_level[k] = (mesh > 0) ? std::min(k / mesh, p.dof - 1) : 0;
+    }
+    for (int i = depth - 1; i > 0; i--) {
+        HostLevel& L = h.lv[i];
+        HostLevel& C = h.lv[i - 1];
+        const std::vector<int>& lev = L.dof_level;
+        Lists S = strong_connections(L.A, lev, p.eps_minus, p.eps_plus);
+        Lists T = transpose_lists(S, L.A.n);
+        bool aggressive = (p.coarsening == kAggressive && i == depth - 1);
+        if (aggressive)
+            L.coarse_size = aggressive_coarsening(L.A, lev, p.dof, S, T, p.eps_minus, p.eps_plus, L.labels);
+        else
+            L.coarse_size = standard_coarsening(L.A, lev, p.dof, S, T, L.labels, true);
+        std::vector<int> map;
+        int nc = coarse_map(L.labels, map);
+        if (nc != L.coarse_size) {
+            h.error = "coarse size disagrees with the number of non-fine labels";
+            return false;
+        }
+        C.dof_level.assign(nc, 0);
+        for (int k = 0; k < L.A.n; k++)
+            if (map[k] >= 0) C.dof_level[map[k]] = lev[k];
+        bool broke = false;
+        if (!interpolation(L.A, L.labels, lev, map, aggressive ? 2 : 1, p.matrix_tol, L.P, h.error, broke))
+            return false;
+        L.P.ncols = nc;
+        if (broke) fprintf(stderr, "LinA-GB300 warning: AMG level %d has a fine row without coarse interpolation\n", i);
+        L.R = amg_transpose(L.P, nc);
+        Csr AP = spgemm_ref(L.A, L.P);
+        AP.ncols = nc;
+        C.A = spgemm_ref(L.R, AP);
+        C.A.ncols = nc;
+        if (!square_clean(C.A)) {
+            h.error = "erroneous coarse matrix";
+            return false;
+        }
+    }
+    return coarse_factor(h.lv[0].A, h.coarse, h.error);
+}
+
+bool amg_recompute_host(HostHierarchy& h, const Csr& A) {
+    const int depth = h.params.depth;
+    if ((int)h.lv.size() != depth || A.n != h.lv[depth - 1].A.n) {
+        h.error = "matrix size does not match the hierarchy";
+        return false;
+    }
+    h.lv[depth - 1].A = A;
+    h.lv[depth - 1].A.ncols = A.n;
+    for (int i = depth - 1; i > 0; i--) {
+        HostLevel& L = h.lv[i];
+        Csr AP = spgemm_ref(L.A, L.P);
+        AP.ncols = L.coarse_size;
+        h.lv[i - 1].A = spgemm_ref(L.R, AP);
+        h.lv[i - 1].A.ncols = L.coarse_size;
+        if (!square_clean(h.lv[i - 1].A)) {
+            h.error = "erroneous coarse matrix";
+            return false;
+        }
+    }
+    return coarse_factor(h.lv[0].A, h.coarse, h.error);
+}
+
+}  // namespace lina

@@ -1,0 +1,81 @@
+// amg_host.h - host-side AMG hierarchy construction (setup phase) for the GB300 LinA library.
+//
+// The setup is a serial algorithm by definition in the reference (greedy C/F
+// splitting driven by a max-priority queue), so it runs on the host here and
+// produces CSR arrays that are uploaded once; the solve phase runs on the GPU.
+// Every step reproduces the reference's integer output (labels, sparsity
+// patterns) and its floating-point operation order, so that patterns and
+// values agree bit for bit with LinA/Multigrid.c.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace lina {
+
+// labels of LinA/Multigrid.h:23-27
+enum { kUndecided = 0, kCoarse = 1, kFine = 2, kIsolated = 3 };
+enum { kAggressive = 1, kStandard = 2 };
+
+struct Csr {
+    int n = 0;      // rows
+    int ncols = 0;  // columns (informational)
+    std::vector<int> ptr{0};
+    std::vector<int> col;
+    std::vector<double> val;
+    int64_t nnz() const { return (int64_t)col.size(); }
+};
+
+struct AmgParams {
+    int dof = 1;
+    int depth = 2;
+    int smoothing_iterations = 2;
+    int aggr_smoothing_iterations = 2;
+    int coarsening = kStandard;   // kAggressive: finest level coarsened aggressively
+    double eps_minus = 0.3;       // strength thresholds (Multigrid.c:35-36)
+    double eps_plus = 0.5;
+    double matrix_tol = 0.1;      // interpolation truncation (Multigrid.c:37)
+};
+
+struct HostLevel {
+    Csr A;                      // the level operator
+    std::vector<int> labels;    // C/F/ISOLATED labels (levels >= 1)
+    std::vector<int> dof_level; // which unknown (0..dof-1) each row belongs to
+    Csr P;                      // prolongation (n x coarse_size), levels >= 1
+    Csr R;                      // restriction (coarse_size x n), levels >= 1
+    int coarse_size = 0;
+};
+
+struct CoarseSolver {
+    int n = 0;                      // coarsest level size
+    std::vector<int> block_rows;    // rows with more than one nonzero (dense block)
+    std::vector<double> inv;        // dense inverse of the block, row-major, m x m
+    std::vector<double> diag_inv;   // 1/a_ii for rows outside the block (0 inside)
+    std::vector<int> in_block;      // 1 if row is part of the dense block
+};
+
+struct HostHierarchy {
+    AmgParams params;
+    std::vector<HostLevel> lv;      // lv[depth-1] is the finest level
+    std::vector<double> signs;      // make_positive_diag signs of the finest rows
+    CoarseSolver coarse;
+    std::string error;
+};
+
+// Build the full hierarchy (AMG_setup, LinA/Multigrid.c:1613-1754).  A is the
+// caller's matrix in CSR with sorted columns (explicit zeros allowed).
+// Returns false and sets h.error on a condition where the reference aborts.
+bool amg_setup_host(const Csr& A, const AmgParams& p, HostHierarchy& h);
+
+// Numeric re-setup with the P/R of an existing hierarchy
+// (AMG_recompute_coarse_matrices, LinA/Multigrid.c:1756-1780).
+bool amg_recompute_host(HostHierarchy& h, const Csr& A);
+
+// Reference-semantics SpGEMM (sparse_product, LinA/linear_algebra.c:186-222).
+Csr spgemm_ref(const Csr& A, const Csr& B);
+
+// Greedy first-fit colouring of the symmetric nonzero graph (smoother ordering).
+int greedy_colouring(const Csr& A, std::vector<int>& colour);
+
+}  // namespace lina

@@ -1,0 +1,1162 @@
+// gpu_amg.cu - sm_103a kernels and device-side driver of the AMG-preconditioned
+// Krylov solve (the solve phase of LinA's AMG_solve / pcg on one GB300).
+//
+// Layout in HBM, per level: CSR with int32 row pointers and column indices and
+// two value arrays (FP64 for the plain path, FP32 for the mixed-precision
+// preconditioner), the inverse diagonal in both precisions, the rows of each
+// colour class (multicolour SOR), and per-level work vectors.  The coarsest
+// level is a dense FP64 inverse of its non-isolated block (one GEMV per
+// V-cycle).  Every kernel is bandwidth-bound; the arithmetic is CUDA-core
+// FP64/FP32.  Reductions are single-pass: each block writes one partial and the
+// last block to finish (atomic ticket, no waiting) sums the partials in a fixed
+// order, so results are bitwise reproducible from run to run.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "amg_host.h"
+#include "lina_gpu.h"
+
+namespace {
+
+std::string g_err;
+
+void set_err(const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+}
+
+#define CK(call)                                                                   \
+    do {                                                                           \
+        cudaError_t e_ = (call);                                                   \
+        if (e_ != cudaSuccess) {                                                   \
+            set_err("%s failed: %s", #call, cudaGetErrorString(e_));               \
+            return LINA_GPU_ECUDA;                                                 \
+        }                                                                          \
+    } while (0)
+
+constexpr int kThreads = 256;
+constexpr int kMaxBlocks = 2048;      // partials per reduction value
+constexpr int kGridCap = 152 * 12;    // grid-stride cap: 152 SMs x 12 blocks of 256
+
+// ---------------------------------------------------------------- reductions
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sum v[0..NV) over the whole grid.  Each block stores a partial; the last
+// block (ticket) adds the partials in index order and calls fin(sum[]).
+template <int NV, typename Fin>
+__device__ void grid_reduce(double (&v)[NV], double* partials, unsigned* ticket, Fin fin) {
+    __shared__ double sm[NV][32];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+        double x = warp_sum(v[k]);
+        if (lane == 0) sm[k][wid] = x;
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            double x = (lane < nw) ? sm[k][lane] : 0.0;
+            x = warp_sum(x);
+            if (lane == 0) partials[k * kMaxBlocks + blockIdx.x] = x;
+        }
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        unsigned t = atomicAdd(ticket, 1u);
+        last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double tot[NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+        double x = 0.0;
+        for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) x += __ldcg(partials + k * kMaxBlocks + i);
+        x = warp_sum(x);
+        __syncthreads();
+        if (lane == 0) sm[k][wid] = x;
+        __syncthreads();
+        double y = (lane < nw) ? sm[k][lane] : 0.0;
+        tot[k] = warp_sum(y);
+    }
+    if (threadIdx.x == 0) {
+        fin(tot);
+        *ticket = 0u;
+    }
+}
+
+// Krylov scalars kept on the device so that no host round trip sits between kernels.
+struct KScalars {
+    double s, s_old, pq, t, rr, alpha, beta, r0, norm2, aux;
+    int iter;
+    int pad;
+};
+
+// ---------------------------------------------------------------- CSR kernels
+enum { M_SPMV = 0, M_RESID = 1, M_JACOBI = 2, M_SOR = 3, M_ADD = 4, M_DOT = 5 };
+
+// One group of S lanes per row; the warp walks rows in grid-stride steps.
+//  M_SPMV : y = A x
+//  M_RESID: y = b - A x
+//  M_JACOBI: y = x + w dinv (b - A x)              (y != x)
+//  M_SOR  : x = x + w dinv (b - A x) on rows[]      (in place, one colour)
+//  M_ADD  : y = z + A x                             (z may alias y)
+//  M_DOT  : y = A x, and sum_i x_i y_i -> sc->pq
+template <typename TV, typename TX, int S, int MODE>
+__global__ void __launch_bounds__(kThreads) csr_kernel(int nrows, const int* __restrict__ rows,
+                                                       const int* __restrict__ ptr, const int* __restrict__ col,
+                                                       const TV* __restrict__ val, const TX* x, TX* y,
+                                                       const TX* __restrict__ b, const TX* __restrict__ dinv, TX w,
+                                                       const TX* z, double* partials, unsigned* ticket,
+                                                       KScalars* sc) {
+    const int lane = threadIdx.x & 31;
+    const int sub = lane & (S - 1);
+    const int groups_per_warp = 32 / S;
+    const long warp_global = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long nwarps = ((long)gridDim.x * blockDim.x) >> 5;
+    double dot = 0.0;
+    for (long gb = warp_global * groups_per_warp; gb < nrows; gb += nwarps * groups_per_warp) {
+        const long g = gb + lane / S;
+        const bool valid = g < nrows;
+        int i = 0, s = 0, e = 0;
+        if (valid) {
+            i = rows ? rows[g] : (int)g;
+            s = ptr[i];
+            e = ptr[i + 1];
+        }
+        TX sum = TX(0);
+        for (int k = s + sub; k < e; k += S) sum += TX(val[k]) * x[col[k]];
+#pragma unroll
+        for (int o = S / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, S);
+        if (valid && sub == 0) {
+            if constexpr (MODE == M_SPMV) {
+                y[i] = sum;
+            } else if constexpr (MODE == M_RESID) {
+                y[i] = b[i] - sum;
+            } else if constexpr (MODE == M_JACOBI) {
+                y[i] = x[i] + w * dinv[i] * (b[i] - sum);
+            } else if constexpr (MODE == M_SOR) {
+                y[i] = x[i] + w * dinv[i] * (b[i] - sum);
+            } else if constexpr (MODE == M_ADD) {
+                y[i] = z[i] + sum;
+            } else if constexpr (MODE == M_DOT) {
+                y[i] = sum;
+                dot += double(x[i]) * double(sum);
+            }
+        }
+    }
+    if constexpr (MODE == M_DOT) {
+        double v[1] = {dot};
+        grid_reduce<1>(v, partials, ticket, [sc](double* t) { sc->pq = t[0]; });
+    }
+}
+
+// first pre-smoothing sweep from the zero guess: x = w dinv b (no SpMV); rows
+// solved exactly by the isolated-row fix keep b / a (AMG_fix_isolated,
+// LinA/Multigrid.c:1301-1319).  TB may be wider than TX (FP64 residual entering
+// the FP32 V-cycle); the converted right-hand side is stored in bout if given.
+template <typename TB, typename TX>
+__global__ void jacobi_first_kernel(int n, const TB* __restrict__ b, const double* __restrict__ sign,
+                                    const TX* __restrict__ dinv, const double* __restrict__ isoinv, TX w,
+                                    TX* __restrict__ x, TX* __restrict__ bout) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        double bd = double(b[i]);
+        if (sign) bd *= sign[i];
+        TX bi = TX(bd);
+        if (bout) bout[i] = bi;
+        if (isoinv && isoinv[i] != 0.0)
+            x[i] = TX(bd * isoinv[i]);
+        else
+            x[i] = w * dinv[i] * bi;
+    }
+}
+
+// x = isolated-row fix (zero elsewhere), optional conversion of b
+template <typename TB, typename TX>
+__global__ void init_x_kernel(int n, const TB* __restrict__ b, const double* __restrict__ sign,
+                              const double* __restrict__ isoinv, TX* __restrict__ x, TX* __restrict__ bout) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        double bd = double(b[i]);
+        if (sign) bd *= sign[i];
+        if (bout) bout[i] = TX(bd);
+        x[i] = (isoinv && isoinv[i] != 0.0) ? TX(bd * isoinv[i]) : TX(0);
+    }
+}
+
+// coarsest level: gather the block right-hand side, solve the single-nonzero rows
+template <typename TX>
+__global__ void coarse_gather_kernel(int n, const TX* __restrict__ b, const int* __restrict__ inblock,
+                                     const int* __restrict__ blockpos, const double* __restrict__ dginv,
+                                     double* __restrict__ bblk, TX* __restrict__ x) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (inblock[i])
+            bblk[blockpos[i]] = double(b[i]);
+        else
+            x[i] = TX(double(b[i]) * dginv[i]);
+    }
+}
+
+// dense FP64 GEMV with the block inverse: one warp per block row
+template <typename TX>
+__global__ void coarse_gemv_kernel(int m, const double* __restrict__ inv, const double* __restrict__ bblk,
+                                   const int* __restrict__ brows, TX* __restrict__ x) {
+    const int lane = threadIdx.x & 31;
+    for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < m;
+         r += ((long)gridDim.x * blockDim.x) >> 5) {
+        const double* row = inv + r * (long)m;
+        double s = 0.0;
+        for (int j = lane; j < m; j += 32) s += row[j] * bblk[j];
+        s = warp_sum(s);
+        if (lane == 0) x[brows[r]] = TX(s);
+    }
+}
+
+template <typename TA, typename TB>
+__global__ void convert_kernel(long n, const TA* __restrict__ a, TB* __restrict__ b) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) b[i] = TB(a[i]);
+}
+
+__global__ void scale_kernel(long n, double* __restrict__ v, const double* __restrict__ f, int invert) {
+    double s = invert ? 1.0 / (*f) : (*f);
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) v[i] *= s;
+}
+
+// ------------------------------------------------------------ Krylov kernels
+// s_old = s; s = r.z; t = z.q (flexible CG)
+template <typename TZ>
+__global__ void __launch_bounds__(kThreads) dot_rz_kernel(int n, const double* __restrict__ r,
+                                                          const TZ* __restrict__ z, const double* __restrict__ q,
+                                                          int flexible, double* partials, unsigned* ticket,
+                                                          KScalars* sc) {
+    double v[2] = {0.0, 0.0};
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        double zi = double(z[i]);
+        v[0] += r[i] * zi;
+        if (flexible) v[1] += zi * q[i];
+    }
+    grid_reduce<2>(v, partials, ticket, [sc](double* t) {
+        sc->s_old = sc->s;
+        sc->s = t[0];
+        sc->t = t[1];
+    });
+}
+
+// p = z + beta p;  beta = s/s_old (CG) or -alpha_prev t / s_old (flexible CG); p = z on the first step
+template <typename TZ>
+__global__ void update_p_kernel(int n, const TZ* __restrict__ z, double* __restrict__ p, int flexible,
+                                KScalars* sc) {
+    const bool first = (sc->iter == 0);
+    double beta = 0.0;
+    if (!first) beta = flexible ? (-sc->alpha * sc->t / sc->s_old) : (sc->s / sc->s_old);
+    if (blockIdx.x == 0 && threadIdx.x == 0) sc->beta = beta;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        p[i] = first ? double(z[i]) : double(z[i]) + beta * p[i];
+}
+
+// alpha = s / (p.q); x += alpha p; r -= alpha q; rr = r.r
+__global__ void __launch_bounds__(kThreads) update_xr_kernel(int n, double* __restrict__ x, double* __restrict__ r,
+                                                             const double* __restrict__ p,
+                                                             const double* __restrict__ q, double* partials,
+                                                             unsigned* ticket, KScalars* sc) {
+    const double alpha = sc->s / sc->pq;
+    double v[1] = {0.0};
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        x[i] += alpha * p[i];
+        double ri = r[i] - alpha * q[i];
+        r[i] = ri;
+        v[0] += ri * ri;
+    }
+    grid_reduce<1>(v, partials, ticket, [sc, alpha](double* t) {
+        sc->rr = t[0];
+        sc->alpha = alpha;
+        sc->iter += 1;
+    });
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) norm2_kernel(int n, const T* __restrict__ v, double* partials,
+                                                         unsigned* ticket, KScalars* sc) {
+    double a[1] = {0.0};
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        double x = double(v[i]);
+        a[0] += x * x;
+    }
+    grid_reduce<1>(a, partials, ticket, [sc](double* t) { sc->norm2 = t[0]; });
+}
+
+}  // namespace
+
+// ======================================================================= host
+namespace {
+
+struct DCsr {
+    int n = 0, ncols = 0;
+    long nnz = 0;
+    int* ptr = nullptr;
+    int* col = nullptr;
+    double* v64 = nullptr;
+    float* v32 = nullptr;
+    int lanes = 8;
+};
+
+struct DLevel {
+    int n = 0;
+    DCsr A, P, R;
+    double* dinv64 = nullptr;
+    float* dinv32 = nullptr;
+    int ncolours = 0;
+    std::vector<int> cptr;
+    int* crows = nullptr;
+    double *x64 = nullptr, *t64 = nullptr, *b64 = nullptr, *r64 = nullptr;
+    float *x32 = nullptr, *t32 = nullptr, *b32 = nullptr, *r32 = nullptr;
+};
+
+int lanes_for(long nnz, int n) {
+    double avg = n > 0 ? double(nnz) / n : 1.0;
+    if (avg <= 6.0) return 4;
+    if (avg <= 12.0) return 8;
+    if (avg <= 24.0) return 16;
+    return 32;
+}
+
+int grid_for(long items, int per_block) {
+    long g = (items + per_block - 1) / per_block;
+    if (g < 1) g = 1;
+    if (g > kGridCap) g = kGridCap;
+    return (int)g;
+}
+
+int grid_red(long items) {
+    long g = (items + kThreads - 1) / kThreads;
+    if (g < 1) g = 1;
+    if (g > kMaxBlocks) g = kMaxBlocks;
+    if (g > kGridCap) g = kGridCap;
+    return (int)g;
+}
+
+}  // namespace
+
+struct lina_gpu_amg {
+    lina::HostHierarchy host;
+    lina_gpu_amg_options opt{};
+    int depth = 0;
+    std::vector<DLevel> lv;
+    // coarsest dense block
+    int cm = 0;
+    int* c_brows = nullptr;
+    int* c_inblock = nullptr;
+    int* c_blockpos = nullptr;
+    double* c_inv = nullptr;
+    double* c_dginv = nullptr;
+    double* c_bblk = nullptr;
+    // finest-level extras
+    double* isoinv = nullptr;  // 1/a for isolated rows of the finest level, 0 elsewhere
+    double* signs = nullptr;   // only when make_positive_diag flipped a row
+    DCsr Aorig;                // unflipped finest matrix when signs exist (Krylov SpMV)
+    bool has_signs = false;
+    // Krylov work
+    double *kr = nullptr, *kz = nullptr, *kp = nullptr, *kq = nullptr, *kx = nullptr, *kb = nullptr,
+           *kt = nullptr;
+    float* kz32 = nullptr;
+    double* partials = nullptr;
+    unsigned* ticket = nullptr;
+    KScalars* sc = nullptr;
+    KScalars* sc_host = nullptr;
+    double* hscal = nullptr;  // device scalar for normalisation
+    cudaStream_t stream = nullptr;
+    long dev_bytes = 0;
+    std::vector<void*> allocations;
+    // smoother timing
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_pool;
+    int ev_used = 0;
+
+    ~lina_gpu_amg() {
+        for (void* p : allocations) cudaFree(p);
+        if (sc_host) cudaFreeHost(sc_host);
+        for (auto e : ev_pool) cudaEventDestroy(e);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    template <typename T>
+    int alloc(T** p, size_t count) {
+        if (count == 0) count = 1;
+        cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+        if (e != cudaSuccess) {
+            set_err("cudaMalloc(%zu bytes) failed: %s", count * sizeof(T), cudaGetErrorString(e));
+            *p = nullptr;
+            return LINA_GPU_ECUDA;
+        }
+        allocations.push_back((void*)*p);
+        dev_bytes += (long)(count * sizeof(T));
+        return 0;
+    }
+    template <typename T>
+    int upload(T** p, const T* src, size_t count) {
+        int rc = alloc(p, count);
+        if (rc) return rc;
+        if (count) CK(cudaMemcpyAsync(*p, src, count * sizeof(T), cudaMemcpyHostToDevice, stream));
+        return 0;
+    }
+    int upload_csr(DCsr& d, const lina::Csr& c) {
+        d.n = c.n;
+        d.ncols = c.ncols;
+        d.nnz = c.nnz();
+        d.lanes = lanes_for(d.nnz, d.n);
+        std::vector<float> v32(c.val.begin(), c.val.end());
+        int rc;
+        if ((rc = upload(&d.ptr, c.ptr.data(), c.ptr.size()))) return rc;
+        if ((rc = upload(&d.col, c.col.data(), c.col.size()))) return rc;
+        if ((rc = upload(&d.v64, c.val.data(), c.val.size()))) return rc;
+        if ((rc = upload(&d.v32, v32.data(), v32.size()))) return rc;
+        // the float copy must outlive the async copy
+        return cudaStreamSynchronize(stream) == cudaSuccess ? 0 : LINA_GPU_ECUDA;
+    }
+
+    // ------------------------------------------------------------ timing
+    void ev_record_pair_start(cudaEvent_t* a) {
+        if (ev_used + 2 > (int)ev_pool.size()) {
+            for (int k = 0; k < 64; k++) {
+                cudaEvent_t e;
+                cudaEventCreate(&e);
+                ev_pool.push_back(e);
+            }
+        }
+        *a = ev_pool[ev_used];
+        cudaEventRecord(*a, stream);
+        ev_used += 1;
+    }
+    void ev_record_pair_end() {
+        cudaEventRecord(ev_pool[ev_used], stream);
+        ev_used += 1;
+    }
+
+    // ------------------------------------------------------------ kernels
+    template <typename TV, typename TX, int MODE>
+    void launch_csr_t(const DCsr& m, const TV* val, int nrows, const int* rows, const TX* x, TX* y, const TX* b,
+                      const TX* dinv, TX w, const TX* z) {
+        const int S = m.lanes;
+        const int groups = kThreads / S;
+        int grid = (MODE == M_DOT) ? grid_red((long)nrows * S) : grid_for(nrows, groups);
+        if (MODE == M_DOT) grid = std::min(grid, kMaxBlocks);
+#define LINA_CSR_CASE(SS)                                                                                     \
+    case SS:                                                                                                  \
+        csr_kernel<TV, TX, SS, MODE><<<grid, kThreads, 0, stream>>>(nrows, rows, m.ptr, m.col, val, x, y, b, \
+                                                                    dinv, w, z, partials, ticket, sc);       \
+        break;
+        switch (S) {
+            LINA_CSR_CASE(4)
+            LINA_CSR_CASE(8)
+            LINA_CSR_CASE(16)
+            default:
+                LINA_CSR_CASE(32)
+        }
+#undef LINA_CSR_CASE
+    }
+
+    template <typename TX, int MODE>
+    void csr(const DCsr& m, int nrows, const int* rows, const TX* x, TX* y, const TX* b = nullptr,
+             const TX* dinv = nullptr, TX w = TX(0), const TX* z = nullptr) {
+        if constexpr (sizeof(TX) == 8)
+            launch_csr_t<double, TX, MODE>(m, m.v64, nrows, rows, x, y, b, dinv, w, z);
+        else
+            launch_csr_t<float, TX, MODE>(m, m.v32, nrows, rows, x, y, b, dinv, w, z);
+    }
+
+    // ------------------------------------------------------------ V-cycle
+    template <typename TX>
+    TX* lvx(DLevel& L, int which) {  // 0 x, 1 t, 2 b, 3 r
+        if constexpr (sizeof(TX) == 8) {
+            double* v[4] = {L.x64, L.t64, L.b64, L.r64};
+            return v[which];
+        } else {
+            float* v[4] = {L.x32, L.t32, L.b32, L.r32};
+            return v[which];
+        }
+    }
+    template <typename TX>
+    const TX* lvdinv(DLevel& L) {
+        if constexpr (sizeof(TX) == 8)
+            return L.dinv64;
+        else
+            return L.dinv32;
+    }
+
+    template <typename TX>
+    void coarse_solve(const TX* b, TX* x) {
+        const int n = lv[0].n;
+        coarse_gather_kernel<TX><<<grid_for(n, kThreads), kThreads, 0, stream>>>(n, b, c_inblock, c_blockpos,
+                                                                                 c_dginv, c_bblk, x);
+        if (cm > 0) coarse_gemv_kernel<TX><<<grid_for((long)cm * 32, kThreads), kThreads, 0, stream>>>(
+            cm, c_inv, c_bblk, c_brows, x);
+    }
+
+    // pre-smoothing from the zero guess (plus the isolated-row fix on the finest level)
+    template <typename TB, typename TX>
+    void presmooth(DLevel& L, int nu, const TB* bin, const double* sign, const double* iso, TX* b, TX* x,
+                   bool time_it) {
+        const TX w = TX(opt.omega);
+        const TX* dinv = lvdinv<TX>(L);
+        TX* t = lvx<TX>(L, 1);
+        TX* bout = ((const void*)bin == (const void*)b) ? nullptr : b;
+        if (opt.smoother == LINA_SMOOTHER_JACOBI && nu > 0) {
+            TX* cur = ((nu - 1) % 2 == 0) ? x : t;
+            jacobi_first_kernel<TB, TX><<<grid_for(L.n, kThreads), kThreads, 0, stream>>>(L.n, bin, sign, dinv,
+                                                                                           iso, w, cur, bout);
+            for (int k = 1; k < nu; k++) {
+                TX* nxt = (cur == x) ? t : x;
+                cudaEvent_t e0;
+                if (time_it) ev_record_pair_start(&e0);
+                csr<TX, M_JACOBI>(L.A, L.n, nullptr, cur, nxt, b, dinv, w);
+                if (time_it) ev_record_pair_end();
+                cur = nxt;
+            }
+        } else {
+            init_x_kernel<TB, TX><<<grid_for(L.n, kThreads), kThreads, 0, stream>>>(L.n, bin, sign, iso, x, bout);
+            for (int k = 0; k < nu; k++) sor_sweep(L, b, x, time_it);
+        }
+    }
+
+    template <typename TX>
+    void sor_sweep(DLevel& L, const TX* b, TX* x, bool time_it) {
+        const TX w = TX(opt.omega);
+        for (int c = 0; c < L.ncolours; c++) {
+            int cnt = L.cptr[c + 1] - L.cptr[c];
+            if (cnt == 0) continue;
+            cudaEvent_t e0;
+            if (time_it) ev_record_pair_start(&e0);
+            csr<TX, M_SOR>(L.A, cnt, L.crows + L.cptr[c], x, x, b, lvdinv<TX>(L), w);
+            if (time_it) ev_record_pair_end();
+        }
+    }
+
+    // post-smoothing after the coarse correction x += P e; result ends in x
+    template <typename TX>
+    void correct_and_postsmooth(int l, DLevel& L, int nu, const TX* b, TX* x, const TX* e, bool time_it) {
+        const TX w = TX(opt.omega);
+        const TX* dinv = lvdinv<TX>(L);
+        TX* t = lvx<TX>(L, 1);
+        if (opt.smoother == LINA_SMOOTHER_JACOBI) {
+            TX* cur = (nu % 2 == 0) ? x : t;
+            csr<TX, M_ADD>(L.P, L.n, nullptr, e, cur, nullptr, nullptr, TX(0), x);
+            for (int k = 0; k < nu; k++) {
+                TX* nxt = (cur == x) ? t : x;
+                cudaEvent_t e0;
+                if (time_it) ev_record_pair_start(&e0);
+                csr<TX, M_JACOBI>(L.A, L.n, nullptr, cur, nxt, b, dinv, w);
+                if (time_it) ev_record_pair_end();
+                cur = nxt;
+            }
+        } else {
+            csr<TX, M_ADD>(L.P, L.n, nullptr, e, x, nullptr, nullptr, TX(0), x);
+            for (int k = 0; k < nu; k++) sor_sweep(L, b, x, time_it);
+        }
+        (void)l;
+    }
+
+    template <typename TX>
+    void vcycle_level(int l, const TX* b, TX* x, bool time_it) {
+        if (l == 0) {
+            coarse_solve<TX>(b, x);
+            return;
+        }
+        DLevel& L = lv[l];
+        const int nu = (opt.coarsening == LINA_AGGRESSIVE && l == depth - 1) ? opt.aggr_smoothing_iterations
+                                                                             : opt.smoothing_iterations;
+        presmooth<TX, TX>(L, nu, b, nullptr, nullptr, const_cast<TX*>(b), x, false);
+        run_rest<TX>(l, L, nu, b, x, time_it);
+    }
+
+    template <typename TX>
+    void run_rest(int l, DLevel& L, int nu, const TX* b, TX* x, bool time_it) {
+        TX* r = lvx<TX>(L, 3);
+        DLevel& C = lv[l - 1];
+        TX* cb = lvx<TX>(C, 2);
+        TX* cx = lvx<TX>(C, 0);
+        csr<TX, M_RESID>(L.A, L.n, nullptr, x, r, b);
+        csr<TX, M_SPMV>(L.R, C.n, nullptr, r, cb);
+        vcycle_level<TX>(l - 1, cb, cx, false);
+        correct_and_postsmooth<TX>(l, L, nu, b, x, cx, time_it);
+    }
+
+    // z = M^-1 r on the finest level (r FP64 on the device); mixed precision
+    // leaves the result in kz32 (FP32), FP64 in z.
+    void precondition(const double* r, double* z, bool time_it) {
+        const int l = depth - 1;
+        DLevel& L = lv[l];
+        if (depth == 1) {
+            if (opt.precision == LINA_PREC_MIXED) {
+                convert_kernel<double, float><<<grid_for(L.n, kThreads), kThreads, 0, stream>>>(L.n, r, L.b32);
+                coarse_solve<float>(L.b32, kz32);
+            } else {
+                coarse_solve<double>(r, z);
+            }
+            return;
+        }
+        const int nu = (opt.coarsening == LINA_AGGRESSIVE) ? opt.aggr_smoothing_iterations : opt.smoothing_iterations;
+        const double* sign = has_signs ? signs : nullptr;
+        if (opt.precision == LINA_PREC_MIXED) {
+            presmooth<double, float>(L, nu, r, sign, isoinv, L.b32, kz32, time_it);
+            run_rest<float>(l, L, nu, L.b32, kz32, time_it);
+        } else {
+            double* b = const_cast<double*>(r);
+            if (has_signs) b = L.b64;
+            presmooth<double, double>(L, nu, r, sign, isoinv, b, z, time_it);
+            run_rest<double>(l, L, nu, b, z, time_it);
+        }
+    }
+
+    const DCsr& krylov_matrix() const { return has_signs ? Aorig : lv[depth - 1].A; }
+};
+
+namespace {
+
+int upload_hierarchy(lina_gpu_amg* h) {
+    lina::HostHierarchy& H = h->host;
+    const int depth = h->depth;
+    h->lv.assign(depth, DLevel());
+    int rc;
+    for (int l = 0; l < depth; l++) {
+        lina::HostLevel& hl = H.lv[l];
+        DLevel& L = h->lv[l];
+        L.n = hl.A.n;
+        if ((rc = h->upload_csr(L.A, hl.A))) return rc;
+        std::vector<double> dinv(L.n, 0.0);
+        for (int i = 0; i < L.n; i++) {
+            double d = 0.0;
+            for (int p = hl.A.ptr[i]; p < hl.A.ptr[i + 1]; p++)
+                if (hl.A.col[p] == i) d = hl.A.val[p];
+            bool skip = (l > 0 && !hl.labels.empty() && hl.labels[i] == lina::kUndecided);
+            dinv[i] = (skip || d == 0.0) ? 0.0 : 1.0 / d;
+        }
+        std::vector<float> dinv32(dinv.begin(), dinv.end());
+        if ((rc = h->upload(&L.dinv64, dinv.data(), dinv.size()))) return rc;
+        if ((rc = h->upload(&L.dinv32, dinv32.data(), dinv32.size()))) return rc;
+        if (l > 0) {
+            if ((rc = h->upload_csr(L.P, hl.P))) return rc;
+            if ((rc = h->upload_csr(L.R, hl.R))) return rc;
+            std::vector<int> colour;
+            L.ncolours = lina::greedy_colouring(hl.A, colour);
+            L.cptr.assign(L.ncolours + 1, 0);
+            for (int c : colour) L.cptr[c + 1]++;
+            for (int c = 0; c < L.ncolours; c++) L.cptr[c + 1] += L.cptr[c];
+            std::vector<int> rows(L.n);
+            std::vector<int> fill(L.cptr.begin(), L.cptr.end() - 1);
+            for (int i = 0; i < L.n; i++) rows[fill[colour[i]]++] = i;
+            if ((rc = h->upload(&L.crows, rows.data(), rows.size()))) return rc;
+            CK(cudaStreamSynchronize(h->stream));
+        }
+        // work vectors
+        if ((rc = h->alloc(&L.x64, L.n))) return rc;
+        if ((rc = h->alloc(&L.t64, L.n))) return rc;
+        if ((rc = h->alloc(&L.b64, L.n))) return rc;
+        if ((rc = h->alloc(&L.r64, L.n))) return rc;
+        if ((rc = h->alloc(&L.x32, L.n))) return rc;
+        if ((rc = h->alloc(&L.t32, L.n))) return rc;
+        if ((rc = h->alloc(&L.b32, L.n))) return rc;
+        if ((rc = h->alloc(&L.r32, L.n))) return rc;
+    }
+    // coarsest block
+    lina::CoarseSolver& cs = H.coarse;
+    h->cm = (int)cs.block_rows.size();
+    std::vector<int> blockpos(cs.n, 0);
+    for (int k = 0; k < h->cm; k++) blockpos[cs.block_rows[k]] = k;
+    if ((rc = h->upload(&h->c_brows, cs.block_rows.data(), cs.block_rows.size()))) return rc;
+    if ((rc = h->upload(&h->c_inblock, cs.in_block.data(), cs.in_block.size()))) return rc;
+    if ((rc = h->upload(&h->c_blockpos, blockpos.data(), blockpos.size()))) return rc;
+    if ((rc = h->upload(&h->c_inv, cs.inv.data(), cs.inv.size()))) return rc;
+    if ((rc = h->upload(&h->c_dginv, cs.diag_inv.data(), cs.diag_inv.size()))) return rc;
+    if ((rc = h->alloc(&h->c_bblk, std::max(h->cm, 1)))) return rc;
+    // finest extras
+    const int nf = H.lv[depth - 1].A.n;
+    {
+        std::vector<double> iso(nf, 0.0);
+        if (depth > 1) {
+            const lina::HostLevel& F = H.lv[depth - 1];
+            for (int i = 0; i < nf; i++)
+                if (F.labels[i] == lina::kIsolated)
+                    for (int p = F.A.ptr[i]; p < F.A.ptr[i + 1]; p++)
+                        if (F.A.val[p] != 0.0) {
+                            iso[i] = 1.0 / F.A.val[p];
+                            break;
+                        }
+        }
+        if ((rc = h->upload(&h->isoinv, iso.data(), iso.size()))) return rc;
+    }
+    h->has_signs = false;
+    for (double s : H.signs)
+        if (s < 0) h->has_signs = true;
+    if (h->has_signs) {
+        if ((rc = h->upload(&h->signs, H.signs.data(), H.signs.size()))) return rc;
+    }
+    if ((rc = h->alloc(&h->kr, nf))) return rc;
+    if ((rc = h->alloc(&h->kz, nf))) return rc;
+    if ((rc = h->alloc(&h->kp, nf))) return rc;
+    if ((rc = h->alloc(&h->kq, nf))) return rc;
+    if ((rc = h->alloc(&h->kx, nf))) return rc;
+    if ((rc = h->alloc(&h->kb, nf))) return rc;
+    if ((rc = h->alloc(&h->kt, nf))) return rc;
+    if ((rc = h->alloc(&h->kz32, nf))) return rc;
+    if ((rc = h->alloc(&h->partials, 2 * kMaxBlocks))) return rc;
+    if ((rc = h->alloc(&h->ticket, 4))) return rc;
+    if ((rc = h->alloc(&h->sc, 1))) return rc;
+    if ((rc = h->alloc(&h->hscal, 2))) return rc;
+    CK(cudaMemsetAsync(h->ticket, 0, 4 * sizeof(unsigned), h->stream));
+    CK(cudaMemsetAsync(h->sc, 0, sizeof(KScalars), h->stream));
+    if (!h->sc_host) CK(cudaMallocHost((void**)&h->sc_host, sizeof(KScalars)));
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
+lina::Csr csr_from(int n, const int* rowptr, const int* col, const double* val) {
+    lina::Csr A;
+    A.n = n;
+    A.ncols = n;
+    A.ptr.assign(rowptr, rowptr + n + 1);
+    long nnz = rowptr[n];
+    A.col.assign(col, col + nnz);
+    A.val.assign(val, val + nnz);
+    return A;
+}
+
+bool valid_csr(int n, const int* rowptr, const int* col) {
+    if (n <= 0 || !rowptr || !col || rowptr[0] != 0) return false;
+    for (int i = 0; i < n; i++) {
+        if (rowptr[i + 1] < rowptr[i]) return false;
+        for (int p = rowptr[i]; p < rowptr[i + 1]; p++) {
+            if (col[p] < 0 || col[p] >= n) return false;
+            if (p > rowptr[i] && col[p] <= col[p - 1]) return false;
+        }
+    }
+    return true;
+}
+
+// true residual b - A x (FP64), norm into sc->norm2; result left in kt
+int true_residual(lina_gpu_amg* h, const double* b, const double* x) {
+    const DCsr& A = h->krylov_matrix();
+    h->csr<double, M_RESID>(A, A.n, nullptr, x, h->kt, b);
+    norm2_kernel<double><<<grid_red(A.n), kThreads, 0, h->stream>>>(A.n, h->kt, h->partials, h->ticket, h->sc);
+    return 0;
+}
+
+int read_scalars(lina_gpu_amg* h) {
+    CK(cudaMemcpyAsync(h->sc_host, h->sc, sizeof(KScalars), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
+}  // namespace
+
+// =================================================================== C-ABI
+extern "C" {
+
+void lina_gpu_default_options(lina_gpu_amg_options* o) {
+    if (!o) return;
+    o->dof = 1;
+    o->depth = 2;
+    o->smoothing_iterations = 2;
+    o->aggr_smoothing_iterations = 2;
+    o->coarsening = LINA_STANDARD;
+    o->eps_minus = 0.3;
+    o->eps_plus = 0.5;
+    o->matrix_tol = 0.1;
+    o->smoother = LINA_SMOOTHER_JACOBI;
+    o->omega = 0.6;
+    o->precision = LINA_PREC_FP64;
+}
+
+const char* lina_gpu_last_error(void) { return g_err.c_str(); }
+
+int lina_gpu_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+    return n;
+}
+
+static int amg_create_impl(int n, const int* rowptr, const int* col, const double* val,
+                           const lina_gpu_amg_options* opt, lina_gpu_amg** out, bool host_only) {
+    if (!out || !opt || !val || !valid_csr(n, rowptr, col)) {
+        set_err("lina_gpu_amg_create: invalid CSR input or options");
+        return LINA_GPU_EINVAL;
+    }
+    if (opt->depth < 1 || opt->dof < 1 || opt->smoothing_iterations < 0 || opt->aggr_smoothing_iterations < 0 ||
+        (opt->smoother != LINA_SMOOTHER_JACOBI && opt->smoother != LINA_SMOOTHER_MC_SOR) ||
+        (opt->precision != LINA_PREC_FP64 && opt->precision != LINA_PREC_MIXED)) {
+        set_err("lina_gpu_amg_create: invalid options");
+        return LINA_GPU_EINVAL;
+    }
+    *out = nullptr;
+    lina_gpu_amg* h = new lina_gpu_amg();
+    h->opt = *opt;
+    h->depth = opt->depth;
+    lina::AmgParams p;
+    p.dof = opt->dof;
+    p.depth = opt->depth;
+    p.smoothing_iterations = opt->smoothing_iterations;
+    p.aggr_smoothing_iterations = opt->aggr_smoothing_iterations;
+    p.coarsening = opt->coarsening == LINA_AGGRESSIVE ? lina::kAggressive : lina::kStandard;
+    p.eps_minus = opt->eps_minus;
+    p.eps_plus = opt->eps_plus;
+    p.matrix_tol = opt->matrix_tol;
+    if (!lina::amg_setup_host(csr_from(n, rowptr, col, val), p, h->host)) {
+        set_err("AMG setup: %s", h->host.error.c_str());
+        delete h;
+        return LINA_GPU_ESETUP;
+    }
+    if (host_only) {
+        *out = h;
+        return 0;
+    }
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        set_err("cudaStreamCreate failed");
+        delete h;
+        return LINA_GPU_ECUDA;
+    }
+    int rc = upload_hierarchy(h);
+    if (rc) {
+        delete h;
+        return rc;
+    }
+    if (h->has_signs) {
+        rc = h->upload_csr(h->Aorig, csr_from(n, rowptr, col, val));
+        if (rc) {
+            delete h;
+            return rc;
+        }
+    }
+    *out = h;
+    return 0;
+}
+
+int lina_gpu_amg_create(int n, const int* rowptr, const int* col, const double* val,
+                        const lina_gpu_amg_options* opt, lina_gpu_amg** out) {
+    return amg_create_impl(n, rowptr, col, val, opt, out, false);
+}
+
+int lina_gpu_amg_create_host_only(int n, const int* rowptr, const int* col, const double* val,
+                                  const lina_gpu_amg_options* opt, lina_gpu_amg** out) {
+    return amg_create_impl(n, rowptr, col, val, opt, out, true);
+}
+
+int lina_gpu_amg_recompute(lina_gpu_amg* h, int n, const int* rowptr, const int* col, const double* val) {
+    if (!h || !valid_csr(n, rowptr, col) || !val) {
+        set_err("lina_gpu_amg_recompute: invalid input");
+        return LINA_GPU_EINVAL;
+    }
+    if (!lina::amg_recompute_host(h->host, csr_from(n, rowptr, col, val))) {
+        set_err("AMG recompute: %s", h->host.error.c_str());
+        return LINA_GPU_ESETUP;
+    }
+    // the reference keeps the setup's signs and does not flip the new matrix
+    bool had_signs = h->has_signs;
+    std::vector<double> keep_signs = h->host.signs;
+    for (void* p : h->allocations) cudaFree(p);
+    h->allocations.clear();
+    h->dev_bytes = 0;
+    h->Aorig = DCsr();
+    int rc = upload_hierarchy(h);
+    if (rc) return rc;
+    (void)had_signs;
+    (void)keep_signs;
+    if (h->has_signs) rc = h->upload_csr(h->Aorig, csr_from(n, rowptr, col, val));
+    return rc;
+}
+
+int lina_gpu_amg_destroy(lina_gpu_amg* h) {
+    delete h;
+    return 0;
+}
+
+int lina_gpu_amg_set_smoother(lina_gpu_amg* h, int smoother, double omega, int precision) {
+    if (!h || (smoother != LINA_SMOOTHER_JACOBI && smoother != LINA_SMOOTHER_MC_SOR) ||
+        (precision != LINA_PREC_FP64 && precision != LINA_PREC_MIXED)) {
+        set_err("lina_gpu_amg_set_smoother: invalid argument");
+        return LINA_GPU_EINVAL;
+    }
+    h->opt.smoother = smoother;
+    h->opt.omega = omega;
+    h->opt.precision = precision;
+    return 0;
+}
+
+int lina_gpu_vcycle(lina_gpu_amg* h, const double* r_dev, double* z_dev) {
+    if (!h || !r_dev || !z_dev) {
+        set_err("lina_gpu_vcycle: invalid argument");
+        return LINA_GPU_EINVAL;
+    }
+    const int n = h->lv[h->depth - 1].n;
+    h->precondition(r_dev, z_dev, false);
+    if (h->opt.precision == LINA_PREC_MIXED)
+        convert_kernel<float, double><<<grid_for(n, kThreads), kThreads, 0, h->stream>>>(n, h->kz32, z_dev);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
+int lina_gpu_spmv(lina_gpu_amg* h, int level, const double* x_dev, double* y_dev) {
+    if (!h || level < 0 || level >= h->depth || !x_dev || !y_dev) {
+        set_err("lina_gpu_spmv: invalid argument");
+        return LINA_GPU_EINVAL;
+    }
+    const DCsr& A = h->lv[level].A;
+    h->csr<double, M_SPMV>(A, A.n, nullptr, x_dev, y_dev);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
+int lina_gpu_pcg(lina_gpu_amg* h, const double* b_in, double* x_out, double tol, int max_iter, int stop_rule,
+                 int flags, lina_gpu_solve_info* info) {
+    if (!h || !b_in || !x_out || max_iter < 1 ||
+        (stop_rule != LINA_STOP_REFERENCE && stop_rule != LINA_STOP_RELATIVE)) {
+        set_err("lina_gpu_pcg: invalid argument");
+        return LINA_GPU_EINVAL;
+    }
+    lina_gpu_solve_info local{};
+    lina_gpu_solve_info* inf = info ? info : &local;
+    memset(inf, 0, sizeof *inf);
+    const int n = h->lv[h->depth - 1].n;
+    const bool dev = (flags & LINA_PCG_DEVICE_PTRS) != 0;
+    const bool mixed = (h->opt.precision == LINA_PREC_MIXED);
+    const int flexible = mixed ? 1 : 0;
+    const bool time_it = (flags & LINA_PCG_TIME_KERNELS) != 0;
+    h->ev_used = 0;
+    cudaStream_t st = h->stream;
+    double *b = h->kb, *x = h->kx, *r = h->kr, *z = h->kz, *p = h->kp, *q = h->kq;
+    // inputs
+    if (dev)
+        CK(cudaMemcpyAsync(b, b_in, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    else
+        CK(cudaMemcpyAsync(b, b_in, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (flags & LINA_PCG_USE_X0) {
+        CK(cudaMemcpyAsync(x, x_out, n * sizeof(double), dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                           st));
+    } else {
+        CK(cudaMemsetAsync(x, 0, n * sizeof(double), st));
+    }
+    CK(cudaMemsetAsync(h->sc, 0, sizeof(KScalars), st));
+    const int gv = grid_for(n, kThreads);
+    const int gr = grid_red(n);
+    // ||b||
+    norm2_kernel<double><<<gr, kThreads, 0, st>>>(n, b, h->partials, h->ticket, h->sc);
+    if (read_scalars(h)) return LINA_GPU_ECUDA;
+    double bnorm = std::sqrt(h->sc_host->norm2);
+    double hscale = 1.0;
+    if (flags & LINA_PCG_NORMALIZE) {
+        hscale = (bnorm == 0.0) ? 1.0 : bnorm;
+        double inv = 1.0 / hscale;
+        CK(cudaMemcpyAsync(h->hscal, &inv, sizeof(double), cudaMemcpyHostToDevice, st));
+        scale_kernel<<<gv, kThreads, 0, st>>>(n, b, h->hscal, 0);
+        scale_kernel<<<gv, kThreads, 0, st>>>(n, x, h->hscal, 0);
+        bnorm *= inv;
+    }
+    // r = b - A x
+    const DCsr& A = h->krylov_matrix();
+    h->csr<double, M_RESID>(A, n, nullptr, x, r, b);
+    // w = M^-1 r (kept as the first z)
+    auto zptr_norm = [&]() {
+        if (mixed)
+            norm2_kernel<float><<<gr, kThreads, 0, st>>>(n, h->kz32, h->partials, h->ticket, h->sc);
+        else
+            norm2_kernel<double><<<gr, kThreads, 0, st>>>(n, z, h->partials, h->ticket, h->sc);
+    };
+    double r0 = 0.0;
+    bool have_z = false;
+    if (stop_rule == LINA_STOP_REFERENCE) {
+        h->precondition(r, z, time_it);
+        zptr_norm();
+        CK(cudaGetLastError());
+        if (read_scalars(h)) return LINA_GPU_ECUDA;
+        r0 = std::sqrt(h->sc_host->norm2);
+        have_z = true;
+        if (r0 == 0.0) {
+            inf->iterations = 0;
+            goto finish;
+        }
+    } else {
+        r0 = bnorm;
+        if (r0 == 0.0) {
+            CK(cudaMemsetAsync(x, 0, n * sizeof(double), st));
+            inf->iterations = 0;
+            goto finish;
+        }
+    }
+    {
+        int it = 0;
+        int restarts = 0;
+        double rel = 0.0;
+        for (;;) {
+            if (!have_z) h->precondition(r, z, time_it);
+            have_z = false;
+            if (mixed)
+                dot_rz_kernel<float><<<gr, kThreads, 0, st>>>(n, r, h->kz32, q, flexible, h->partials, h->ticket,
+                                                               h->sc);
+            else
+                dot_rz_kernel<double><<<gr, kThreads, 0, st>>>(n, r, z, q, flexible, h->partials, h->ticket, h->sc);
+            if (mixed)
+                update_p_kernel<float><<<gv, kThreads, 0, st>>>(n, h->kz32, p, flexible, h->sc);
+            else
+                update_p_kernel<double><<<gv, kThreads, 0, st>>>(n, z, p, flexible, h->sc);
+            h->csr<double, M_DOT>(A, n, nullptr, p, q);
+            update_xr_kernel<<<gr, kThreads, 0, st>>>(n, x, r, p, q, h->partials, h->ticket, h->sc);
+            CK(cudaGetLastError());
+            if (read_scalars(h)) return LINA_GPU_ECUDA;
+            it++;
+            double rr = h->sc_host->rr;
+            rel = std::sqrt(rr) / r0;
+            if (!std::isfinite(rel)) {
+                inf->status = LINA_GPU_EBREAKDOWN;
+                break;
+            }
+            bool converged = rel <= tol;
+            if (converged && stop_rule == LINA_STOP_RELATIVE && restarts < 8) {
+                // confirm on the true residual; restart the recurrence from it if needed
+                true_residual(h, b, x);
+                if (read_scalars(h)) return LINA_GPU_ECUDA;
+                double trel = std::sqrt(h->sc_host->norm2) / r0;
+                if (trel > tol) {
+                    CK(cudaMemcpyAsync(r, h->kt, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+                    int zero = 0;
+                    CK(cudaMemcpyAsync(&h->sc->iter, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
+                    restarts++;
+                    converged = false;
+                }
+            }
+            if (converged || it >= max_iter) break;
+        }
+        inf->iterations = it;
+        inf->rel_residual = rel;
+        if (inf->status == 0 && rel > tol) inf->status = LINA_GPU_ENOCONV;
+    }
+finish:
+    if ((flags & LINA_PCG_FINAL_PRECON) && r0 != 0.0 && stop_rule == LINA_STOP_REFERENCE) {
+        h->precondition(r, z, false);
+        zptr_norm();
+        if (read_scalars(h)) return LINA_GPU_ECUDA;
+        inf->pcg_residuum = std::sqrt(h->sc_host->norm2) / r0;
+    }
+    true_residual(h, b, x);
+    if (read_scalars(h)) return LINA_GPU_ECUDA;
+    inf->true_rel_residual = (bnorm > 0) ? std::sqrt(h->sc_host->norm2) / bnorm : 0.0;
+    if (flags & LINA_PCG_NORMALIZE) {
+        CK(cudaMemcpyAsync(h->hscal, &hscale, sizeof(double), cudaMemcpyHostToDevice, st));
+        scale_kernel<<<gv, kThreads, 0, st>>>(n, x, h->hscal, 0);
+    }
+    if (dev)
+        CK(cudaMemcpyAsync(x_out, x, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    else
+        CK(cudaMemcpyAsync(x_out, x, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (time_it && h->ev_used >= 2) {
+        double tot = 0.0;
+        for (int k = 0; k + 1 < h->ev_used; k += 2) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, h->ev_pool[k], h->ev_pool[k + 1]);
+            tot += ms;
+        }
+        inf->smoother_ms = tot;
+        inf->smoother_launches = h->ev_used / 2;
+        const DLevel& L = h->lv[h->depth - 1];
+        double nnz = (double)L.A.nnz, nn = (double)L.n;
+        if (h->opt.smoother == LINA_SMOOTHER_JACOBI)
+            inf->smoother_bytes = mixed ? (8 * nnz + 4 * (nn + 1) + 16 * nn) : (12 * nnz + 4 * (nn + 1) + 32 * nn);
+        else  // one colour launch: average share of the sweep
+            inf->smoother_bytes =
+                (mixed ? (8 * nnz + 4 * (nn + 1) + 16 * nn) : (12 * nnz + 4 * (nn + 1) + 32 * nn)) / L.ncolours;
+    }
+    return inf->status;
+}
+
+int lina_gpu_amg_depth(const lina_gpu_amg* h) { return h ? h->depth : 0; }
+
+int lina_gpu_level_sizes(const lina_gpu_amg* h, int level, int* n, long* nnz_A, long* nnz_P, long* nnz_R,
+                         int* n_colours) {
+    if (!h || level < 0 || level >= h->depth) return LINA_GPU_EINVAL;
+    const lina::HostLevel& L = h->host.lv[level];
+    if (n) *n = L.A.n;
+    if (nnz_A) *nnz_A = (long)L.A.nnz();
+    if (nnz_P) *nnz_P = (long)L.P.nnz();
+    if (nnz_R) *nnz_R = (long)L.R.nnz();
+    if (n_colours) *n_colours = (level < (int)h->lv.size()) ? h->lv[level].ncolours : 0;
+    return 0;
+}
+
+int lina_gpu_level_export(const lina_gpu_amg* h, int level, int* labels, int* A_ptr, int* A_col, double* A_val,
+                          int* P_ptr, int* P_col, double* P_val, int* R_ptr, int* R_col, double* R_val) {
+    if (!h || level < 0 || level >= h->depth) return LINA_GPU_EINVAL;
+    const lina::HostLevel& L = h->host.lv[level];
+    auto cp = [](const lina::Csr& c, int* pp, int* cc, double* vv) {
+        if (pp) std::copy(c.ptr.begin(), c.ptr.end(), pp);
+        if (cc) std::copy(c.col.begin(), c.col.end(), cc);
+        if (vv) std::copy(c.val.begin(), c.val.end(), vv);
+    };
+    if (labels && !L.labels.empty()) std::copy(L.labels.begin(), L.labels.end(), labels);
+    cp(L.A, A_ptr, A_col, A_val);
+    if (level > 0) {
+        cp(L.P, P_ptr, P_col, P_val);
+        cp(L.R, R_ptr, R_col, R_val);
+    }
+    return 0;
+}
+
+int lina_gpu_level_colours(const lina_gpu_amg* h, int level, int* colour) {
+    if (!h || level < 0 || level >= h->depth || !colour) return LINA_GPU_EINVAL;
+    std::vector<int> c;
+    lina::greedy_colouring(h->host.lv[level].A, c);
+    std::copy(c.begin(), c.end(), colour);
+    return 0;
+}
+
+int lina_gpu_coarse_block_size(const lina_gpu_amg* h) { return h ? h->cm : 0; }
+
+long lina_gpu_amg_device_bytes(const lina_gpu_amg* h) { return h ? h->dev_bytes : 0; }
+
+void* lina_gpu_malloc(size_t bytes) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, bytes ? bytes : 1) != cudaSuccess) {
+        set_err("cudaMalloc(%zu) failed", bytes);
+        return nullptr;
+    }
+    return p;
+}
+
+int lina_gpu_free(void* p) {
+    CK(cudaFree(p));
+    return 0;
+}
+
+int lina_gpu_memcpy_h2d(void* dst, const void* src, size_t bytes) {
+    CK(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+    return 0;
+}
+
+int lina_gpu_memcpy_d2h(void* dst, const void* src, size_t bytes) {
+    CK(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+int lina_gpu_synchronize(void) {
+    CK(cudaDeviceSynchronize());
+    return 0;
+}
+
+}  // extern "C"

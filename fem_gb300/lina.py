@@ -1,0 +1,296 @@
+"""Python binding of the GB300 LinA library's C-ABI (include/lina_gpu.h).
+
+The product is the shared library ``fem_gb300/_build/libLinA_gb300.so``: host
+C/C++ plus sm_103a kernels.  This module is a thin ctypes layer over its
+exported ``lina_gpu_*`` functions for tests and benchmarks; it contains no
+numerical code and has no fallback: if the library is missing it raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libLinA_gb300.so")
+
+AGGRESSIVE, STANDARD = 1, 2
+SMOOTHER_JACOBI, SMOOTHER_MC_SOR = 0, 1
+PREC_FP64, PREC_MIXED = 0, 1
+STOP_REFERENCE, STOP_RELATIVE = 0, 1
+PCG_DEVICE_PTRS, PCG_USE_X0, PCG_FINAL_PRECON, PCG_TIME_KERNELS, PCG_NORMALIZE = 1, 2, 4, 8, 16
+UNDECIDED, COARSE, FINE, ISOLATED = 0, 1, 2, 3
+
+
+class AmgOptions(C.Structure):
+    _fields_ = [
+        ("dof", C.c_int),
+        ("depth", C.c_int),
+        ("smoothing_iterations", C.c_int),
+        ("aggr_smoothing_iterations", C.c_int),
+        ("coarsening", C.c_int),
+        ("eps_minus", C.c_double),
+        ("eps_plus", C.c_double),
+        ("matrix_tol", C.c_double),
+        ("smoother", C.c_int),
+        ("omega", C.c_double),
+        ("precision", C.c_int),
+    ]
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [
+        ("iterations", C.c_int),
+        ("status", C.c_int),
+        ("rel_residual", C.c_double),
+        ("true_rel_residual", C.c_double),
+        ("pcg_residuum", C.c_double),
+        ("smoother_ms", C.c_double),
+        ("smoother_launches", C.c_int),
+        ("smoother_bytes", C.c_double),
+    ]
+
+
+class LinaError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def lib():
+    """Load the product library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise LinaError(f"GB300 LinA library not built: {LIB_PATH} missing (run __graft_entry__.build())")
+    L = C.CDLL(LIB_PATH)
+    vp, ip, dp, lp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_long)
+    sig = {
+        "lina_gpu_default_options": (None, [C.POINTER(AmgOptions)]),
+        "lina_gpu_amg_create": (C.c_int, [C.c_int, ip, ip, dp, C.POINTER(AmgOptions), C.POINTER(vp)]),
+        "lina_gpu_amg_create_host_only": (C.c_int, [C.c_int, ip, ip, dp, C.POINTER(AmgOptions), C.POINTER(vp)]),
+        "lina_gpu_amg_recompute": (C.c_int, [vp, C.c_int, ip, ip, dp]),
+        "lina_gpu_amg_destroy": (C.c_int, [vp]),
+        "lina_gpu_amg_set_smoother": (C.c_int, [vp, C.c_int, C.c_double, C.c_int]),
+        "lina_gpu_pcg": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, C.POINTER(SolveInfo)]),
+        "lina_gpu_vcycle": (C.c_int, [vp, vp, vp]),
+        "lina_gpu_spmv": (C.c_int, [vp, C.c_int, vp, vp]),
+        "lina_gpu_amg_depth": (C.c_int, [vp]),
+        "lina_gpu_level_sizes": (C.c_int, [vp, C.c_int, ip, lp, lp, lp, ip]),
+        "lina_gpu_level_export": (C.c_int, [vp, C.c_int, ip, ip, ip, dp, ip, ip, dp, ip, ip, dp]),
+        "lina_gpu_level_colours": (C.c_int, [vp, C.c_int, ip]),
+        "lina_gpu_coarse_block_size": (C.c_int, [vp]),
+        "lina_gpu_amg_device_bytes": (C.c_long, [vp]),
+        "lina_gpu_malloc": (vp, [C.c_size_t]),
+        "lina_gpu_free": (C.c_int, [vp]),
+        "lina_gpu_memcpy_h2d": (C.c_int, [vp, vp, C.c_size_t]),
+        "lina_gpu_memcpy_d2h": (C.c_int, [vp, vp, C.c_size_t]),
+        "lina_gpu_synchronize": (C.c_int, []),
+        "lina_gpu_device_count": (C.c_int, []),
+        "lina_gpu_last_error": (C.c_char_p, []),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    return lib().lina_gpu_last_error().decode()
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise LinaError(f"{what} failed ({rc}): {last_error()}")
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def options(**kw) -> AmgOptions:
+    o = AmgOptions()
+    lib().lina_gpu_default_options(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+@dataclass
+class Level:
+    n: int
+    A: tuple
+    labels: np.ndarray | None
+    P: tuple | None
+    R: tuple | None
+    n_colours: int
+
+
+class DeviceArray:
+    """A device buffer owned through the library's allocator (FP64 or int32)."""
+
+    def __init__(self, n, dtype=np.float64):
+        self.n = int(n)
+        self.dtype = np.dtype(dtype)
+        self.nbytes = self.n * self.dtype.itemsize
+        self.ptr = lib().lina_gpu_malloc(max(self.nbytes, 1))
+        if not self.ptr:
+            raise LinaError(f"device allocation of {self.nbytes} bytes failed: {last_error()}")
+
+    @classmethod
+    def from_host(cls, a):
+        a = np.ascontiguousarray(a)
+        d = cls(a.size, a.dtype)
+        _check(lib().lina_gpu_memcpy_h2d(d.ptr, a.ctypes.data, d.nbytes), "h2d copy")
+        return d
+
+    def to_host(self):
+        out = np.empty(self.n, dtype=self.dtype)
+        _check(lib().lina_gpu_memcpy_d2h(out.ctypes.data, self.ptr, self.nbytes), "d2h copy")
+        return out
+
+    def free(self):
+        if self.ptr:
+            lib().lina_gpu_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class AMG:
+    """A hierarchy built by the library (AMG_setup) and held on the GPU."""
+
+    def __init__(self, n, indptr, indices, data, host_only=False, **opts):
+        self.n = int(n)
+        self._ip = np.ascontiguousarray(indptr, dtype=np.int32)
+        self._ix = np.ascontiguousarray(indices, dtype=np.int32)
+        self._dv = np.ascontiguousarray(data, dtype=np.float64)
+        self.opts = options(**opts)
+        h = C.c_void_p()
+        fn = lib().lina_gpu_amg_create_host_only if host_only else lib().lina_gpu_amg_create
+        _check(fn(self.n, _ip(self._ip), _ip(self._ix), _dp(self._dv), C.byref(self.opts), C.byref(h)), "AMG setup")
+        self.h = h
+        self.depth = lib().lina_gpu_amg_depth(self.h)
+
+    @classmethod
+    def from_system(cls, s, host_only=False, **opts):
+        opts.setdefault("dof", s.dof)
+        return cls(s.n, s.indptr, s.indices, s.data, host_only=host_only, **opts)
+
+    def level(self, lv) -> Level:
+        L = lib()
+        n, na, np_, nr, nc = C.c_int(), C.c_long(), C.c_long(), C.c_long(), C.c_int()
+        _check(L.lina_gpu_level_sizes(self.h, lv, C.byref(n), C.byref(na), C.byref(np_), C.byref(nr), C.byref(nc)),
+               "level sizes")
+        n = n.value
+        A = (np.zeros(n + 1, np.int32), np.zeros(max(na.value, 1), np.int32), np.zeros(max(na.value, 1)))
+        labels = np.zeros(n, np.int32)
+        if lv > 0:
+            P = (np.zeros(n + 1, np.int32), np.zeros(max(np_.value, 1), np.int32), np.zeros(max(np_.value, 1)))
+            nrr = P and None
+            # R has one row per coarse point
+            R = None
+        _Pp = _Pc = _Pv = _Rp = _Rc = _Rv = None
+        if lv > 0:
+            ncoarse = self.level_size(lv - 1)
+            R = (np.zeros(ncoarse + 1, np.int32), np.zeros(max(nr.value, 1), np.int32), np.zeros(max(nr.value, 1)))
+            _Pp, _Pc, _Pv = (_ip(P[0]), _ip(P[1]), _dp(P[2]))
+            _Rp, _Rc, _Rv = (_ip(R[0]), _ip(R[1]), _dp(R[2]))
+        _check(L.lina_gpu_level_export(self.h, lv, _ip(labels), _ip(A[0]), _ip(A[1]), _dp(A[2]),
+                                       _Pp, _Pc, _Pv, _Rp, _Rc, _Rv), "level export")
+        A = (A[0], A[1][:na.value], A[2][:na.value])
+        if lv == 0:
+            return Level(n, A, None, None, None, nc.value)
+        P = (P[0], P[1][:np_.value], P[2][:np_.value])
+        R = (R[0], R[1][:nr.value], R[2][:nr.value])
+        return Level(n, A, labels, P, R, nc.value)
+
+    def level_size(self, lv):
+        n = C.c_int()
+        _check(lib().lina_gpu_level_sizes(self.h, lv, C.byref(n), None, None, None, None), "level sizes")
+        return n.value
+
+    def sizes(self):
+        return [self.level_size(lv) for lv in range(self.depth)]
+
+    def colours(self, lv):
+        c = np.zeros(self.level_size(lv), np.int32)
+        _check(lib().lina_gpu_level_colours(self.h, lv, _ip(c)), "colours")
+        return c
+
+    def set_smoother(self, smoother, omega, precision):
+        _check(lib().lina_gpu_amg_set_smoother(self.h, smoother, omega, precision), "set smoother")
+
+    def recompute(self, indptr, indices, data):
+        ip_ = np.ascontiguousarray(indptr, dtype=np.int32)
+        ix_ = np.ascontiguousarray(indices, dtype=np.int32)
+        dv_ = np.ascontiguousarray(data, dtype=np.float64)
+        _check(lib().lina_gpu_amg_recompute(self.h, self.n, _ip(ip_), _ip(ix_), _dp(dv_)), "AMG recompute")
+
+    def pcg(self, b, x0=None, tol=1e-8, max_iter=1000, stop=STOP_RELATIVE, flags=0):
+        """Solve on host arrays (copies inside); returns (x, SolveInfo)."""
+        bb = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros(self.n) if x0 is None else np.array(x0, dtype=np.float64)
+        if x0 is not None:
+            flags |= PCG_USE_X0
+        info = SolveInfo()
+        rc = lib().lina_gpu_pcg(self.h, bb.ctypes.data, x.ctypes.data, tol, max_iter, stop, flags, C.byref(info))
+        if rc not in (0, -5):
+            raise LinaError(f"pcg failed ({rc}): {last_error()}")
+        return x, info
+
+    def pcg_device(self, b_dev: DeviceArray, x_dev: DeviceArray, tol=1e-8, max_iter=1000, stop=STOP_RELATIVE,
+                   flags=0):
+        info = SolveInfo()
+        rc = lib().lina_gpu_pcg(self.h, b_dev.ptr, x_dev.ptr, tol, max_iter, stop, flags | PCG_DEVICE_PTRS,
+                                C.byref(info))
+        if rc not in (0, -5):
+            raise LinaError(f"pcg failed ({rc}): {last_error()}")
+        return info
+
+    def vcycle(self, r):
+        rd = DeviceArray.from_host(np.asarray(r, dtype=np.float64))
+        zd = DeviceArray(self.n)
+        _check(lib().lina_gpu_vcycle(self.h, rd.ptr, zd.ptr), "vcycle")
+        return zd.to_host()
+
+    def spmv(self, x, level=None):
+        lv = self.depth - 1 if level is None else level
+        n = self.level_size(lv)
+        xd = DeviceArray.from_host(np.asarray(x, dtype=np.float64))
+        yd = DeviceArray(n)
+        _check(lib().lina_gpu_spmv(self.h, lv, xd.ptr, yd.ptr), "spmv")
+        return yd.to_host()
+
+    @property
+    def device_bytes(self):
+        return lib().lina_gpu_amg_device_bytes(self.h)
+
+    @property
+    def coarse_block(self):
+        return lib().lina_gpu_coarse_block_size(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().lina_gpu_amg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

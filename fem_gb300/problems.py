@@ -1,0 +1,232 @@
+"""Seeded synthetic linear systems for the LinA solve path.
+
+The reference assembles P1 (linear triangle) stiffness matrices in FEM2D
+(``FEM2D/FEM2D.c:2783-2888`` for the element integrals, ``:5949-5968`` for the
+row loop, ``insert_A_bbV_a`` at ``:4728`` for the scalar Laplacian) and feeds
+them to LinA as row-list ``sparse_matrix`` objects.  This module restates that
+element arithmetic on a structured grid so that the same CSR matrix and
+right-hand side can be handed to the GPU library, to the CPU oracle and to the
+reference itself.  It is harness code, not part of the solve path.
+
+Grid: ``m x m`` nodes on the unit square, node ``k = r*m + c`` at
+``(x, y) = (c*h, r*h)``, ``h = 1/(m-1)``.  Every cell is split along the
+diagonal from ``(r, c)`` to ``(r+1, c+1)`` into a lower triangle
+``[(r,c), (r,c+1), (r+1,c+1)]`` and an upper triangle
+``[(r,c), (r+1,c+1), (r+1,c)]``.  Each node therefore couples to 7 nodes
+(itself, the 4 axis neighbours and the two diagonal neighbours); the stored
+pattern keeps all 7 even where the coupling is an exact zero (the Laplacian's
+hypotenuse couplings), as the reference's assembly does.
+
+Dirichlet conditions are imposed by symmetric elimination: known values are
+lifted into the right-hand side, the constrained columns are removed from the
+free rows and each constrained row becomes an identity row.  This keeps the
+matrix symmetric so that CG applies (the reference's ``Set_dirichlet_BC`` in
+``Crack/crack.c:6445-6459`` resets rows only, which would make it
+nonsymmetric).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+# stencil slots sorted by column offset: SW, S, W, C, E, N, NE  as (dr, dc)
+_SLOTS = [(-1, -1), (-1, 0), (0, -1), (0, 0), (0, 1), (1, 0), (1, 1)]
+_SLOT_OF = {o: s for s, o in enumerate(_SLOTS)}
+# local (dr, dc) of the three vertices of the two triangles of a cell
+_TRI_LOWER = [(0, 0), (0, 1), (1, 1)]
+_TRI_UPPER = [(0, 0), (1, 1), (1, 0)]
+
+
+@dataclass
+class CSRSystem:
+    """A square CSR matrix with int32 indices and FP64 values plus a RHS."""
+
+    n: int
+    indptr: np.ndarray
+    indices: np.ndarray
+    data: np.ndarray
+    b: np.ndarray
+    dof: int = 1          # number of unknowns per node, block ordering [u0..., u1...]
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def nnz(self) -> int:
+        return int(self.indptr[-1])
+
+    def matvec(self, x: np.ndarray) -> np.ndarray:
+        """y = A x in FP64 (row-wise, columns in stored order)."""
+        prod = self.data * x[self.indices]
+        return np.add.reduceat(prod, self.indptr[:-1]) if self.nnz else np.zeros(self.n)
+
+
+def _tri_geometry(tri, h):
+    """b, c coefficient vectors and |area| of a triangle given local offsets."""
+    xs = np.array([dc * h for (dr, dc) in tri])
+    ys = np.array([dr * h for (dr, dc) in tri])
+    b = np.array([ys[1] - ys[2], ys[2] - ys[0], ys[0] - ys[1]])
+    c = np.array([xs[2] - xs[1], xs[0] - xs[2], xs[1] - xs[0]])
+    area2 = xs[0] * (ys[1] - ys[2]) + xs[1] * (ys[2] - ys[0]) + xs[2] * (ys[0] - ys[1])
+    return b, c, abs(area2) / 2.0
+
+
+def _laplace_element(tri, h):
+    """3x3 P1 stiffness  K_ab = (b_a b_b + c_a c_b) / (4|T|)."""
+    b, c, area = _tri_geometry(tri, h)
+    return (np.outer(b, b) + np.outer(c, c)) / (4.0 * area)
+
+
+def _elastic_element(tri, h, E, nu):
+    """6x6 plane-strain P1 stiffness, dofs ordered (ux0, uy0, ux1, uy1, ux2, uy2)."""
+    b, c, area = _tri_geometry(tri, h)
+    B = np.zeros((3, 6))
+    B[0, 0::2] = b
+    B[1, 1::2] = c
+    B[2, 0::2] = c
+    B[2, 1::2] = b
+    B /= 2.0 * area
+    f = E / ((1.0 + nu) * (1.0 - 2.0 * nu))
+    D = f * np.array([[1.0 - nu, nu, 0.0], [nu, 1.0 - nu, 0.0], [0.0, 0.0, (1.0 - 2.0 * nu) / 2.0]])
+    return area * (B.T @ D @ B)
+
+
+def _assemble(m, dof, elem_mats, cell_factor):
+    """Stencil-slot assembly. Returns vals[dof, m*m, dof*7] (zeros where absent) and a mask."""
+    nn = m * m
+    nc = m - 1
+    vals = np.zeros((dof, nn, dof * 7))
+    rr, cc = np.meshgrid(np.arange(nc), np.arange(nc), indexing="ij")
+    rr = rr.ravel()
+    cc = cc.ravel()
+    for t, (tri, ke) in enumerate(elem_mats):
+        g = cell_factor[t] if cell_factor is not None else None
+        for a, (ar, ac) in enumerate(tri):
+            node_a = (rr + ar) * m + (cc + ac)
+            for bb, (br, bc) in enumerate(tri):
+                slot = _SLOT_OF[(br - ar, bc - ac)]
+                for p in range(dof):
+                    for q in range(dof):
+                        k = ke[a * dof + p, bb * dof + q]
+                        contrib = k if g is None else g * k
+                        vals[p, node_a, q * 7 + slot] += contrib
+    # valid slots: neighbour inside the grid
+    r = np.arange(nn) // m
+    c = np.arange(nn) % m
+    valid = np.zeros((nn, 7), dtype=bool)
+    for s, (dr, dc) in enumerate(_SLOTS):
+        valid[:, s] = (r + dr >= 0) & (r + dr < m) & (c + dc >= 0) & (c + dc < m)
+    return vals, valid
+
+
+def _to_csr(m, dof, vals, valid, fixed, fixed_val):
+    """Eliminate fixed dofs symmetrically and compress to CSR (columns sorted)."""
+    nn = m * m
+    n = dof * nn
+    offs = np.array([dr * m + dc for (dr, dc) in _SLOTS], dtype=np.int64)
+    node = np.arange(nn, dtype=np.int64)
+    cols = np.empty((dof, nn, dof * 7), dtype=np.int64)
+    mask = np.empty((dof, nn, dof * 7), dtype=bool)
+    for p in range(dof):
+        for q in range(dof):
+            cols[p, :, q * 7:(q + 1) * 7] = q * nn + node[:, None] + offs[None, :]
+            mask[p, :, q * 7:(q + 1) * 7] = valid
+    cols = cols.reshape(n, dof * 7)
+    vals = vals.reshape(n, dof * 7)
+    mask = mask.reshape(n, dof * 7)
+    safe_cols = np.where(mask, cols, 0)
+    # lift known values: b = -A u_D on free rows
+    u_d = np.zeros(n)
+    u_d[fixed] = fixed_val
+    b = -np.sum(np.where(mask, vals * u_d[safe_cols], 0.0), axis=1)
+    is_fixed = np.zeros(n, dtype=bool)
+    is_fixed[fixed] = True
+    keep = mask & ~is_fixed[safe_cols]
+    keep[is_fixed, :] = False
+    rows_fixed = np.nonzero(is_fixed)[0]
+    # identity rows for the constrained dofs: keep only the diagonal slot
+    diag_slot = (np.arange(n) // nn) * 7 + 3
+    keep[rows_fixed, diag_slot[rows_fixed]] = True
+    vals = vals.copy()
+    vals[rows_fixed, diag_slot[rows_fixed]] = 1.0
+    b[rows_fixed] = u_d[rows_fixed]
+    counts = keep.sum(axis=1)
+    indptr = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(counts, out=indptr[1:])
+    indices = cols[keep].astype(np.int32)
+    data = vals[keep].astype(np.float64)
+    return indptr.astype(np.int32), indices, data, b
+
+
+def poisson_p1(m: int, seed: int = 0) -> CSRSystem:
+    """Scalar P1 Laplacian on an m x m grid, homogeneous Dirichlet on all edges.
+
+    RHS i.i.d. uniform in [-1, 1] from ``numpy.random.default_rng(seed)``,
+    zero on the boundary rows.
+    """
+    h = 1.0 / (m - 1)
+    elems = [(_TRI_LOWER, _laplace_element(_TRI_LOWER, h)), (_TRI_UPPER, _laplace_element(_TRI_UPPER, h))]
+    vals, valid = _assemble(m, 1, elems, None)
+    r = np.arange(m * m) // m
+    c = np.arange(m * m) % m
+    bnd = np.nonzero((r == 0) | (r == m - 1) | (c == 0) | (c == m - 1))[0]
+    indptr, indices, data, _ = _to_csr(m, 1, vals, valid, bnd, 0.0)
+    rng = np.random.default_rng(seed)
+    b = rng.uniform(-1.0, 1.0, m * m)
+    b[bnd] = 0.0
+    return CSRSystem(m * m, indptr, indices, data, b, dof=1,
+                     meta={"kind": "poisson_p1", "m": m, "seed": seed, "n_boundary": len(bnd)})
+
+
+def notch_damage(m: int, ell: float | None = None) -> np.ndarray:
+    """Per-element damage d = exp(-dist/ell) to the notch (0,0.5)-(0.5,0.5).
+
+    Returned as [2, (m-1)^2] (lower, upper triangle of each cell) evaluated at
+    the triangle centroids; ``ell`` defaults to 2h.
+    """
+    h = 1.0 / (m - 1)
+    if ell is None:
+        ell = 2.0 * h
+    nc = m - 1
+    rr, cc = np.meshgrid(np.arange(nc), np.arange(nc), indexing="ij")
+    out = []
+    for tri in (_TRI_LOWER, _TRI_UPPER):
+        cx = (cc.ravel() + np.mean([dc for (dr, dc) in tri])) * h
+        cy = (rr.ravel() + np.mean([dr for (dr, dc) in tri])) * h
+        dx = np.where(cx > 0.5, cx - 0.5, 0.0)
+        dist = np.sqrt(dx * dx + (cy - 0.5) ** 2)
+        out.append(np.exp(-dist / ell))
+    return np.stack(out)
+
+
+def elasticity_p1(m: int, E: float = 210.0, nu: float = 0.3, degraded: bool = True,
+                  top_uy: float = 1e-3, residual_stiffness: float = 1e-6,
+                  young: np.ndarray | None = None) -> CSRSystem:
+    """Plane-strain P1 elasticity, block dof ordering [u_x(all nodes), u_y(all nodes)].
+
+    Stiffness of each element scaled by ``(1-d)^2 + residual_stiffness`` with
+    ``d`` the notch damage field (``degraded=True``), or by ``young/E`` when a
+    per-element Young's modulus array ``young[2, (m-1)^2]`` is given.  Bottom
+    edge clamped (u_x = u_y = 0); top edge u_y = ``top_uy`` with u_x free.
+    """
+    h = 1.0 / (m - 1)
+    elems = [(_TRI_LOWER, _elastic_element(_TRI_LOWER, h, E, nu)),
+             (_TRI_UPPER, _elastic_element(_TRI_UPPER, h, E, nu))]
+    if young is not None:
+        factor = np.asarray(young, dtype=np.float64) / E
+    elif degraded:
+        d = notch_damage(m)
+        factor = (1.0 - d) ** 2 + residual_stiffness
+    else:
+        factor = None
+    vals, valid = _assemble(m, 2, elems, factor)
+    nn = m * m
+    r = np.arange(nn) // m
+    bottom = np.nonzero(r == 0)[0]
+    top = np.nonzero(r == m - 1)[0]
+    fixed = np.concatenate([bottom, nn + bottom, nn + top])
+    fixed_val = np.concatenate([np.zeros(2 * len(bottom)), np.full(len(top), top_uy)])
+    order = np.argsort(fixed)
+    indptr, indices, data, b = _to_csr(m, 2, vals, valid, fixed[order], fixed_val[order])
+    return CSRSystem(2 * nn, indptr, indices, data, b, dof=2,
+                     meta={"kind": "elasticity_p1", "m": m, "E": E, "nu": nu,
+                           "degraded": degraded, "top_uy": top_uy, "n_fixed": len(fixed)})

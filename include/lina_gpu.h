@@ -1,0 +1,130 @@
+/*
+ * lina_gpu.h - the thin C-ABI between LinA host code and the GB300 (sm_103a)
+ * kernels of the sparse solve path.
+ *
+ * Plain pointers and sizes only.  Matrices are CSR with int32 row pointers
+ * and column indices (columns sorted within a row, explicit zeros allowed) and
+ * FP64 values, which is the reference's row-list sparse_matrix
+ * (LinA/linear_algebra.h:29-34) laid out contiguously.  One process, one GPU,
+ * one host thread: like the reference (whose solver state lives in
+ * file-static globals), the library is not thread-safe.
+ *
+ * Return codes: 0 on success, a negative LINA_GPU_E* code on failure; the
+ * text of the last failure is available from lina_gpu_last_error().
+ */
+#ifndef LINA_GPU_H
+#define LINA_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LINA_GPU_OK 0
+#define LINA_GPU_EINVAL -1      /* invalid argument                            */
+#define LINA_GPU_ECUDA -2       /* CUDA runtime error (allocation, launch)     */
+#define LINA_GPU_ESETUP -3      /* AMG setup hit a condition the reference aborts on */
+#define LINA_GPU_EBREAKDOWN -4  /* Krylov breakdown (zero or NaN inner product) */
+#define LINA_GPU_ENOCONV -5     /* iteration limit reached before the tolerance */
+
+/* coarsening strategies, values of LinA/Multigrid.h:29-31 */
+#define LINA_AGGRESSIVE 1
+#define LINA_STANDARD 2
+
+/* smoothers of the GPU V-cycle */
+#define LINA_SMOOTHER_JACOBI 0   /* damped Jacobi, x += w D^-1 (b - A x)                 */
+#define LINA_SMOOTHER_MC_SOR 1   /* SOR over a greedy multicolouring, colours in order    */
+
+/* precision of the preconditioner */
+#define LINA_PREC_FP64 0         /* everything FP64                                      */
+#define LINA_PREC_MIXED 1        /* FP32 V-cycle (values, vectors, accumulation), FP64 coarse solve,
+                                    FP64 flexible CG outside                              */
+
+/* stopping rules of lina_gpu_pcg */
+#define LINA_STOP_REFERENCE 0    /* ||r_k|| / ||M^-1 r_0|| <= tol, as pcg (LinA/PCGS.c:191-213) */
+#define LINA_STOP_RELATIVE 1     /* ||r_k|| / ||b|| <= tol, confirmed on the true residual b - A x */
+
+/* flags of lina_gpu_pcg */
+#define LINA_PCG_DEVICE_PTRS 1   /* b and x are device pointers (default: host pointers)  */
+#define LINA_PCG_USE_X0 2        /* start from the given x (default: x = 0)               */
+#define LINA_PCG_FINAL_PRECON 4  /* apply M^-1 once more after the loop for the reference's
+                                    pcg residuum (LinA/PCGS.c:217-218)                    */
+#define LINA_PCG_TIME_KERNELS 8  /* time the finest-level smoother launches with CUDA events */
+#define LINA_PCG_NORMALIZE 16    /* scale b and x by 1/||b|| during the solve, as pcg does */
+
+typedef struct lina_gpu_amg lina_gpu_amg;
+
+typedef struct lina_gpu_amg_options {
+    int dof;                       /* unknowns per node, block ordering [u0 ..., u1 ...]  */
+    int depth;                     /* number of levels                                    */
+    int smoothing_iterations;      /* sweeps per pre/post smoothing                       */
+    int aggr_smoothing_iterations; /* sweeps on the finest level when coarsening is aggressive */
+    int coarsening;                /* LINA_AGGRESSIVE or LINA_STANDARD                    */
+    double eps_minus, eps_plus;    /* strength thresholds (set_connection_thresholds)     */
+    double matrix_tol;             /* interpolation truncation (AMG_set_matrix_tolerance) */
+    int smoother;                  /* LINA_SMOOTHER_*                                     */
+    double omega;                  /* relaxation factor of the smoother                   */
+    int precision;                 /* LINA_PREC_*                                         */
+} lina_gpu_amg_options;
+
+typedef struct lina_gpu_solve_info {
+    int iterations;
+    int status;                    /* 0 or a negative LINA_GPU_E* code                    */
+    double rel_residual;           /* value tested by the stopping rule at exit           */
+    double true_rel_residual;      /* ||b - A x|| / ||b|| recomputed in FP64 at exit       */
+    double pcg_residuum;           /* ||M^-1 r|| / ||M^-1 r_0|| (LINA_PCG_FINAL_PRECON)    */
+    double smoother_ms;            /* total time of the timed smoother launches           */
+    int smoother_launches;         /* number of timed smoother launches                   */
+    double smoother_bytes;         /* algorithmic bytes of one timed launch               */
+} lina_gpu_solve_info;
+
+void lina_gpu_default_options(lina_gpu_amg_options* opt);
+
+/* AMG_setup (LinA/Multigrid.c:1613) on a CSR matrix: host setup, then upload of every level. */
+int lina_gpu_amg_create(int n, const int* rowptr, const int* col, const double* val,
+                        const lina_gpu_amg_options* opt, lina_gpu_amg** out);
+/* the same setup without touching the GPU (hierarchy inspection and tests on machines without one);
+   the handle supports only the inspection functions below and lina_gpu_amg_destroy */
+int lina_gpu_amg_create_host_only(int n, const int* rowptr, const int* col, const double* val,
+                                  const lina_gpu_amg_options* opt, lina_gpu_amg** out);
+/* AMG_recompute_coarse_matrices (LinA/Multigrid.c:1756): new fine matrix, same P and R. */
+int lina_gpu_amg_recompute(lina_gpu_amg* h, int n, const int* rowptr, const int* col, const double* val);
+int lina_gpu_amg_destroy(lina_gpu_amg* h);
+/* change smoother, relaxation or precision of an existing hierarchy */
+int lina_gpu_amg_set_smoother(lina_gpu_amg* h, int smoother, double omega, int precision);
+
+/* AMG-preconditioned CG on the hierarchy's finest matrix (pcg, LinA/PCGS.c:163). */
+int lina_gpu_pcg(lina_gpu_amg* h, const double* b, double* x, double tol, int max_iter,
+                 int stop_rule, int flags, lina_gpu_solve_info* info);
+/* one preconditioner application z = M^-1 r (device pointers), zero initial guess */
+int lina_gpu_vcycle(lina_gpu_amg* h, const double* r_dev, double* z_dev);
+/* y = A_level x on the device (level = depth-1 is the finest) */
+int lina_gpu_spmv(lina_gpu_amg* h, int level, const double* x_dev, double* y_dev);
+
+/* hierarchy inspection (host copies of what the GPU holds) */
+int lina_gpu_amg_depth(const lina_gpu_amg* h);
+int lina_gpu_level_sizes(const lina_gpu_amg* h, int level, int* n, long* nnz_A, long* nnz_P, long* nnz_R,
+                         int* n_colours);
+int lina_gpu_level_export(const lina_gpu_amg* h, int level, int* labels, int* A_ptr, int* A_col, double* A_val,
+                          int* P_ptr, int* P_col, double* P_val, int* R_ptr, int* R_col, double* R_val);
+int lina_gpu_level_colours(const lina_gpu_amg* h, int level, int* colour);
+int lina_gpu_coarse_block_size(const lina_gpu_amg* h);
+/* bytes held on the device by the hierarchy */
+long lina_gpu_amg_device_bytes(const lina_gpu_amg* h);
+
+/* device memory helpers so that callers need no CUDA runtime of their own */
+void* lina_gpu_malloc(size_t bytes);
+int lina_gpu_free(void* p);
+int lina_gpu_memcpy_h2d(void* dst, const void* src, size_t bytes);
+int lina_gpu_memcpy_d2h(void* dst, const void* src, size_t bytes);
+int lina_gpu_synchronize(void);
+int lina_gpu_device_count(void);
+
+const char* lina_gpu_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LINA_GPU_H */

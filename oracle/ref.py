@@ -1,0 +1,199 @@
+"""ctypes front end to oracle/_ref/libLinA_ref.so (the reference LinA built from its sources).
+
+Test infrastructure only: tests and the CPU-baseline leg of bench.py use this
+to obtain the reference's own answers.  The library exists only where the
+reference tree was available to build it (``make -C oracle ref``); callers
+check :func:`available` first.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_ref", "libLinA_ref.so")
+
+# labels of LinA/Multigrid.h:23-27
+UNDECIDED, COARSE, FINE, ISOLATED = 0, 1, 2, 3
+STANDARD, AGGRESSIVE = 2, 1
+SMOOTHER_REF_SOR, SMOOTHER_REF_JACOBI, SMOOTHER_DAMPED_JACOBI, SMOOTHER_MC_SOR = 0, 1, 2, 3
+
+_lib = None
+
+
+def available() -> bool:
+    if not os.path.exists(LIB_PATH):
+        return False
+    try:
+        lib()
+    except OSError:
+        return False
+    return True
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    L = C.CDLL(LIB_PATH)
+    vp, ip, dp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)
+    sig = {
+        "rs_silence": (None, [C.c_int]),
+        "rs_malloc_zero": (None, []),
+        "rs_from_csr": (vp, [C.c_int, ip, ip, dp]),
+        "rs_free": (None, [vp]),
+        "rs_size": (C.c_int, [vp]),
+        "rs_nnz": (C.c_long, [vp]),
+        "rs_to_csr": (None, [vp, ip, ip, dp]),
+        "rs_amg_setup": (vp, [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
+        "rs_amg_depth": (C.c_int, [vp]),
+        "rs_amg_fine_size": (C.c_int, [vp, C.c_int]),
+        "rs_amg_coarse_size": (C.c_int, [vp, C.c_int]),
+        "rs_amg_A": (vp, [vp, C.c_int]),
+        "rs_amg_P": (vp, [vp, C.c_int]),
+        "rs_amg_R": (vp, [vp, C.c_int]),
+        "rs_amg_L": (vp, [vp, C.c_int]),
+        "rs_amg_U": (vp, [vp, C.c_int]),
+        "rs_amg_signs": (vp, [vp]),
+        "rs_amg_labels": (ip, [vp, C.c_int]),
+        "rs_amg_free": (None, [vp]),
+        "rs_amg_recompute": (None, [vp, vp]),
+        "rs_greedy_colouring": (C.c_int, [vp, ip]),
+        "rs_forget_colouring": (None, []),
+        "rs_set_smoother": (None, [C.c_int, C.c_double]),
+        "rs_pcg_amg": (C.c_int, [vp, vp, dp, dp, C.c_double, C.c_int, dp]),
+        "rs_amg_solve": (C.c_int, [vp, dp, dp, C.c_double, C.c_int]),
+        "rs_vcycle_zero": (None, [vp, dp, dp]),
+        "rs_spmv": (None, [vp, dp, dp]),
+        "rs_product": (vp, [vp, vp]),
+        "rs_transpose": (vp, [vp, C.c_int]),
+        "rs_ilu": (C.c_int, [vp, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
+        "rs_ilu_apply": (None, [vp, vp, dp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    L.rs_malloc_zero()
+    _lib = L
+    return L
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class RefMatrix:
+    """Owning handle to a reference row-list sparse_matrix."""
+
+    def __init__(self, ptr, owned=True):
+        self.ptr = ptr
+        self.owned = owned
+
+    @classmethod
+    def from_csr(cls, n, indptr, indices, data):
+        ip_ = np.ascontiguousarray(indptr, dtype=np.int32)
+        ix_ = np.ascontiguousarray(indices, dtype=np.int32)
+        dt_ = np.ascontiguousarray(data, dtype=np.float64)
+        return cls(lib().rs_from_csr(n, _ip(ip_), _ip(ix_), _dp(dt_)))
+
+    @property
+    def size(self):
+        return lib().rs_size(self.ptr)
+
+    def to_csr(self):
+        n = self.size
+        nnz = lib().rs_nnz(self.ptr)
+        indptr = np.zeros(n + 1, dtype=np.int32)
+        indices = np.zeros(max(nnz, 1), dtype=np.int32)
+        data = np.zeros(max(nnz, 1), dtype=np.float64)
+        lib().rs_to_csr(self.ptr, _ip(indptr), _ip(indices), _dp(data))
+        return indptr, indices[:nnz], data[:nnz]
+
+    def __del__(self):
+        if self.owned and self.ptr and _lib is not None:
+            _lib.rs_free(self.ptr)
+            self.ptr = None
+
+
+@dataclass
+class RefLevel:
+    A: tuple            # (indptr, indices, data)
+    labels: np.ndarray | None
+    P: tuple | None
+    R: tuple | None
+
+
+class RefAMG:
+    """AMG_setup (LinA/Multigrid.c:1613) on a CSR matrix, hierarchy read back as CSR."""
+
+    def __init__(self, sysm, depth, sm=2, aggr_sm=2, coarsening=AGGRESSIVE, quiet=True):
+        self.A = RefMatrix.from_csr(sysm.n, sysm.indptr, sysm.indices, sysm.data)
+        if quiet:
+            lib().rs_silence(1)
+        try:
+            self.ptr = lib().rs_amg_setup(self.A.ptr, int(sysm.dof), depth, sm, aggr_sm, coarsening)
+        finally:
+            if quiet:
+                lib().rs_silence(0)
+        self.depth = depth
+        self.n = sysm.n
+
+    def level(self, lv) -> RefLevel:
+        L = lib()
+        A = RefMatrix(L.rs_amg_A(self.ptr, lv), owned=False).to_csr()
+        if lv == 0:
+            return RefLevel(A, None, None, None)
+        n = L.rs_amg_fine_size(self.ptr, lv)
+        labels = np.ctypeslib.as_array(L.rs_amg_labels(self.ptr, lv), shape=(n,)).copy()
+        P = RefMatrix(L.rs_amg_P(self.ptr, lv), owned=False).to_csr()
+        R = RefMatrix(L.rs_amg_R(self.ptr, lv), owned=False).to_csr()
+        return RefLevel(A, labels, P, R)
+
+    def sizes(self):
+        return [lib().rs_amg_fine_size(self.ptr, lv) for lv in range(self.depth)]
+
+    def pcg(self, b, tol=1e-8, max_iter=1000, smoother=SMOOTHER_REF_SOR, omega=1.0, x0=None):
+        """pcg with a one-V-cycle zero-guess preconditioner; returns (x, iterations, pcg_residuum)."""
+        x = np.zeros(self.n) if x0 is None else np.array(x0, dtype=np.float64)
+        bb = np.array(b, dtype=np.float64)
+        res = C.c_double(0.0)
+        lib().rs_set_smoother(smoother, omega)
+        lib().rs_forget_colouring()
+        lib().rs_silence(1)
+        try:
+            it = lib().rs_pcg_amg(self.ptr, self.A.ptr, _dp(x), _dp(bb), tol, max_iter, C.byref(res))
+        finally:
+            lib().rs_silence(0)
+        return x, it, res.value
+
+    def vcycle(self, r, smoother=SMOOTHER_REF_SOR, omega=1.0):
+        z = np.zeros(self.n)
+        rr = np.array(r, dtype=np.float64)
+        lib().rs_set_smoother(smoother, omega)
+        lib().rs_forget_colouring()
+        lib().rs_silence(1)
+        try:
+            lib().rs_vcycle_zero(self.ptr, _dp(rr), _dp(z))
+        finally:
+            lib().rs_silence(0)
+        return z
+
+    def __del__(self):
+        if getattr(self, "ptr", None) and _lib is not None:
+            _lib.rs_amg_free(self.ptr)
+            self.ptr = None
+
+
+def greedy_colouring(n, indptr, indices, data):
+    M = RefMatrix.from_csr(n, indptr, indices, data)
+    col = np.zeros(n, dtype=np.int32)
+    nc = lib().rs_greedy_colouring(M.ptr, _ip(col))
+    return nc, col

@@ -1,0 +1,319 @@
+/*
+ * ref_shim.c - test-infrastructure driver around the reference LinA library.
+ *
+ * This file is ORACLE code: it is compiled together with the reference's own
+ * LinA sources (LinA/*.c, built unmodified from where they lie) into
+ * oracle/_ref/libLinA_ref.so by oracle/Makefile.  Only tests and the CPU
+ * baseline leg of bench.py load it, and only to produce the values the GPU
+ * library is checked against.  It calls the reference exclusively through its
+ * public API (linear_algebra.h, Multigrid.h, PCGS.h, BiCGStab.h).
+ *
+ * What it adds:
+ *  - CSR <-> row-list conversion (the reference's matrix type is
+ *    LinA/linear_algebra.h:29-34);
+ *  - accessors for the AMG hierarchy (LinA/Multigrid.h:45-70);
+ *  - a PCG driver whose preconditioner is exactly one V-cycle from a zero
+ *    guess (AMG_solve with max_iter 1, LinA/Multigrid.c:1863-1931);
+ *  - two smoothers installed through the reference's own plug-in
+ *    AMG_set_smoother (LinA/Multigrid.c:1967): damped Jacobi and multicolour
+ *    SOR (greedy first-fit colouring of the symmetric nonzero graph), which
+ *    are the GPU smoothers' algorithms;
+ *  - a switch that makes malloc return zero-filled memory (glibc M_PERTURB),
+ *    so that the reference's read of an uninitialised array
+ *    (Importance_2nd, LinA/Multigrid.c:566) is deterministic.
+ */
+#include <fcntl.h>
+#include <malloc.h>
+#include <string.h>
+#include <unistd.h>
+
+#include "BiCGStab.h"
+#include "Multigrid.h"
+#include "PCGS.h"
+#include "linear_algebra.h"
+
+/* ---------------------------------------------------------------- stdout */
+static int saved_stdout = -1;
+
+void rs_silence(int on) {
+    fflush(stdout);
+    if (on && saved_stdout < 0) {
+        saved_stdout = dup(1);
+        int fd = open("/dev/null", O_WRONLY);
+        dup2(fd, 1);
+        close(fd);
+    } else if (!on && saved_stdout >= 0) {
+        dup2(saved_stdout, 1);
+        close(saved_stdout);
+        saved_stdout = -1;
+    }
+}
+
+void rs_malloc_zero(void) { mallopt(M_PERTURB, 255); }
+
+/* ------------------------------------------------------------ conversions */
+sparse_matrix* rs_from_csr(int n, const int* indptr, const int* indices, const double* data) {
+    sparse_matrix* A = (sparse_matrix*)malloc(sizeof(sparse_matrix));
+    A->size = n;
+    A->Len = (int*)malloc(n * sizeof(int));
+    A->Values = (double**)malloc(n * sizeof(double*));
+    A->Indices = (int**)malloc(n * sizeof(int*));
+    for (int i = 0; i < n; i++) {
+        int len = indptr[i + 1] - indptr[i];
+        if (len == 0) { /* the reference's empty row holds one explicit (i, 0.0) */
+            A->Len[i] = 1;
+            A->Values[i] = (double*)malloc(sizeof(double));
+            A->Indices[i] = (int*)malloc(sizeof(int));
+            A->Values[i][0] = 0.0;
+            A->Indices[i][0] = i;
+            continue;
+        }
+        A->Len[i] = len;
+        A->Values[i] = (double*)malloc(len * sizeof(double));
+        A->Indices[i] = (int*)malloc(len * sizeof(int));
+        memcpy(A->Values[i], data + indptr[i], len * sizeof(double));
+        memcpy(A->Indices[i], indices + indptr[i], len * sizeof(int));
+    }
+    return A;
+}
+
+void rs_free(sparse_matrix* A) {
+    if (A) { free_sparse(A); }
+}
+
+int rs_size(const sparse_matrix* A) { return A ? A->size : 0; }
+
+long rs_nnz(const sparse_matrix* A) {
+    long s = 0;
+    if (!A) return 0;
+    for (int i = 0; i < A->size; i++) s += A->Len[i];
+    return s;
+}
+
+void rs_to_csr(const sparse_matrix* A, int* indptr, int* indices, double* data) {
+    long p = 0;
+    indptr[0] = 0;
+    for (int i = 0; i < A->size; i++) {
+        memcpy(indices + p, A->Indices[i], A->Len[i] * sizeof(int));
+        memcpy(data + p, A->Values[i], A->Len[i] * sizeof(double));
+        p += A->Len[i];
+        indptr[i + 1] = (int)p;
+    }
+}
+
+/* ---------------------------------------------------------------- AMG */
+amg_system_info* rs_amg_setup(sparse_matrix* A, int dof, int depth, int sm, int aggr_sm, int coarsening) {
+    AMG_print_info(NO);
+    return AMG_setup(A, dof, depth, sm, aggr_sm, coarsening, STAND_ALONE, DIRECT, NULL, NULL);
+}
+
+int rs_amg_depth(const amg_system_info* I) { return I->depth; }
+int rs_amg_fine_size(const amg_system_info* I, int level) { return I->Fine_sizes[level]; }
+int rs_amg_coarse_size(const amg_system_info* I, int level) { return I->Coarse_sizes[level]; }
+sparse_matrix* rs_amg_A(amg_system_info* I, int level) { return I->Coarse_A[level]; }
+sparse_matrix* rs_amg_P(amg_system_info* I, int level) { return I->Prolongation[level]; }
+sparse_matrix* rs_amg_R(amg_system_info* I, int level) { return I->Restriction[level]; }
+sparse_matrix* rs_amg_L(amg_system_info* I, int level) { return I->L[level]; }
+sparse_matrix* rs_amg_U(amg_system_info* I, int level) { return I->U[level]; }
+sparse_matrix* rs_amg_signs(amg_system_info* I) { return I->Signs; }
+const int* rs_amg_labels(const amg_system_info* I, int level) { return I->Coarsening[level]; }
+
+void rs_amg_free(amg_system_info* I) {
+    if (I) {
+        AMG_free_data(I);
+        free(I);
+    }
+}
+
+void rs_amg_recompute(amg_system_info* I, sparse_matrix* A) { AMG_recompute_coarse_matrices(I, A); }
+
+/* --------------------------------------------------------- smoothers (oracle) */
+/* greedy first-fit colouring of the symmetric graph {(i,j): a_ij != 0 or a_ji != 0, i != j} */
+static const sparse_matrix* col_key = NULL;
+static int col_n = 0;
+static int* col_of = NULL;
+static int col_count = 0;
+static int* col_rows = NULL;   /* rows grouped by colour, increasing row index inside a colour */
+static int* col_ptr = NULL;
+
+int rs_greedy_colouring(const sparse_matrix* A, int* colour) {
+    int n = A->size;
+    /* transpose adjacency (nonzero off-diagonal entries) */
+    int* tcount = (int*)calloc(n + 1, sizeof(int));
+    for (int i = 0; i < n; i++)
+        for (int k = 0; k < A->Len[i]; k++) {
+            int j = A->Indices[i][k];
+            if (j != i && j < n && A->Values[i][k] != 0.0) tcount[j + 1]++;
+        }
+    for (int i = 0; i < n; i++) tcount[i + 1] += tcount[i];
+    int* tadj = (int*)malloc((tcount[n] + 1) * sizeof(int));
+    int* fill = (int*)calloc(n, sizeof(int));
+    for (int i = 0; i < n; i++)
+        for (int k = 0; k < A->Len[i]; k++) {
+            int j = A->Indices[i][k];
+            if (j != i && j < n && A->Values[i][k] != 0.0) tadj[tcount[j] + fill[j]++] = i;
+        }
+    int ncol = 0;
+    int* mark = (int*)malloc((n + 2) * sizeof(int));
+    for (int i = 0; i < n + 2; i++) mark[i] = -1;
+    for (int i = 0; i < n; i++) colour[i] = -1;
+    for (int i = 0; i < n; i++) {
+        for (int k = 0; k < A->Len[i]; k++) {
+            int j = A->Indices[i][k];
+            if (j != i && j < n && A->Values[i][k] != 0.0 && colour[j] >= 0) mark[colour[j]] = i;
+        }
+        for (int k = tcount[i]; k < tcount[i + 1]; k++) {
+            int j = tadj[k];
+            if (colour[j] >= 0) mark[colour[j]] = i;
+        }
+        int c = 0;
+        while (mark[c] == i) c++;
+        colour[i] = c;
+        if (c + 1 > ncol) ncol = c + 1;
+    }
+    free(mark);
+    free(fill);
+    free(tadj);
+    free(tcount);
+    return ncol;
+}
+
+static void ensure_colouring(const sparse_matrix* A) {
+    if (col_key == A && col_n == A->size) return;
+    free(col_of);
+    free(col_rows);
+    free(col_ptr);
+    col_n = A->size;
+    col_key = A;
+    col_of = (int*)malloc(col_n * sizeof(int));
+    col_count = rs_greedy_colouring(A, col_of);
+    col_ptr = (int*)calloc(col_count + 1, sizeof(int));
+    col_rows = (int*)malloc(col_n * sizeof(int));
+    for (int i = 0; i < col_n; i++) col_ptr[col_of[i] + 1]++;
+    for (int c = 0; c < col_count; c++) col_ptr[c + 1] += col_ptr[c];
+    int* fill = (int*)calloc(col_count, sizeof(int));
+    for (int i = 0; i < col_n; i++) col_rows[col_ptr[col_of[i]] + fill[col_of[i]]++] = i;
+    free(fill);
+}
+
+void rs_forget_colouring(void) { col_key = NULL; }
+
+static double smoother_omega = 1.0;
+
+/* multicolour SOR: colours in increasing order, SOR update of Multigrid.c:1345-1364 per row */
+static void rs_multicolour_sor(sparse_matrix* A, double* F, double* Sol, int* Label, double alpha, int fix,
+                               int iter, int deg_freedom) {
+    (void)alpha;
+    (void)deg_freedom;
+    ensure_colouring(A);
+    double w = smoother_omega;
+    for (int k = 0; k < iter; k++)
+        for (int c = 0; c < col_count; c++)
+            for (int p = col_ptr[c]; p < col_ptr[c + 1]; p++) {
+                int i = col_rows[p];
+                if (Label[i] == fix) continue;
+                double sum = F[i], diag = 0.0;
+                for (int j = 0; j < A->Len[i]; j++) {
+                    int ind = A->Indices[i][j];
+                    if (ind != i) sum -= A->Values[i][j] * Sol[ind];
+                    else diag = A->Values[i][j];
+                }
+                Sol[i] = (1.0 - w) * Sol[i] + w * sum / diag;
+            }
+}
+
+/* damped Jacobi with the same per-row update */
+static void rs_damped_jacobi(sparse_matrix* A, double* F, double* Sol, int* Label, double alpha, int fix, int iter,
+                             int deg_freedom) {
+    (void)alpha;
+    (void)deg_freedom;
+    int n = A->size;
+    double w = smoother_omega;
+    double* Old = (double*)malloc(n * sizeof(double));
+    for (int k = 0; k < iter; k++) {
+        memcpy(Old, Sol, n * sizeof(double));
+        for (int i = 0; i < n; i++) {
+            if (Label[i] == fix) continue;
+            double sum = F[i], diag = 0.0;
+            for (int j = 0; j < A->Len[i]; j++) {
+                int ind = A->Indices[i][j];
+                if (ind != i) sum -= A->Values[i][j] * Old[ind];
+                else diag = A->Values[i][j];
+            }
+            Sol[i] = (1.0 - w) * Old[i] + w * sum / diag;
+        }
+    }
+    free(Old);
+}
+
+/* kind: 0 reference lexicographic SOR, 1 reference parallel Jacobi, 2 damped Jacobi, 3 multicolour SOR */
+void rs_set_smoother(int kind, double omega) {
+    smoother_omega = omega;
+    AMG_set_SOR_relaxation_coeff(omega);
+    switch (kind) {
+        case 1: AMG_set_smoother(AMG_parallel_Jacobi_smoother); break;
+        case 2: AMG_set_smoother(rs_damped_jacobi); break;
+        case 3: AMG_set_smoother(rs_multicolour_sor); break;
+        default: AMG_set_smoother(AMG_SOR_smoother);
+    }
+}
+
+/* ------------------------------------------------------------------ PCG */
+static amg_system_info* pcg_amg = NULL;
+
+static int rs_precon_one_vcycle(int n, double* R, double* Z) {
+    memset(Z, 0, n * sizeof(double));
+    AMG_solve(pcg_amg, R, Z, NULL);
+    return 1;
+}
+
+/* pcg (LinA/PCGS.c:163-233) on A with a one-V-cycle zero-guess AMG preconditioner */
+int rs_pcg_amg(amg_system_info* I, sparse_matrix* A, double* x, double* b, double tol, int max_iter, double* pcg_res) {
+    pcg_amg = I;
+    AMG_print_info(NO);
+    AMG_set_max_iter(1);
+    AMG_set_eps(0.0);
+    PCG_default(A, NULL, NULL);
+    PCG_set_precon(rs_precon_one_vcycle);
+    int it = pcg(x, b, A->size, tol, max_iter);
+    if (pcg_res) *pcg_res = get_pcg_residuum();
+    return it;
+}
+
+/* AMG_solve as the reference runs it (V-cycles until eps or max_iter) */
+int rs_amg_solve(amg_system_info* I, double* F, double* X, double eps, int max_iter) {
+    AMG_print_info(NO);
+    AMG_set_eps(eps);
+    AMG_set_max_iter(max_iter);
+    return AMG_solve(I, F, X, NULL);
+}
+
+/* one V-cycle from a zero guess (the preconditioner application) */
+void rs_vcycle_zero(amg_system_info* I, double* R, double* Z) {
+    pcg_amg = I;
+    AMG_print_info(NO);
+    AMG_set_max_iter(1);
+    AMG_set_eps(0.0);
+    rs_precon_one_vcycle(I->Fine_sizes[I->depth - 1], R, Z);
+}
+
+/* ------------------------------------------------------------ elementary */
+void rs_spmv(sparse_matrix* A, const double* x, double* y) {
+    double* r = sparse_mult(A, (double*)x);
+    memcpy(y, r, A->size * sizeof(double));
+    free(r);
+}
+
+sparse_matrix* rs_product(sparse_matrix* A, sparse_matrix* B) { return sparse_product(A, B); }
+sparse_matrix* rs_transpose(sparse_matrix* A, int new_size) { return get_transpose(A, new_size); }
+
+int rs_ilu(sparse_matrix* A, sparse_matrix** L, sparse_matrix** U) {
+    *L = sparse_zero(A->size);
+    *U = sparse_zero(A->size);
+    return incomplete_LU_factorization(A, *L, *U);
+}
+
+void rs_ilu_apply(sparse_matrix* L, sparse_matrix* U, double* x) {
+    L_triang_invert(L, x);
+    U_triang_invert(U, x);
+}
