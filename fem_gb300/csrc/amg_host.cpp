@@ -10,8 +10,10 @@
 #include "amg_host.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <queue>
 
 namespace lina {
@@ -424,9 +426,58 @@ int coarse_map(const std::vector<int>& label, std::vector<int>& map) {
 // AMG_simple_standard_interpolation (Multigrid.c:989-1079) followed by
 // sparse_approximate (linear_algebra.c:1418-1442) and normalize_row_sum
 // (:455-464).  Returns false if a zero diagonal makes the reference abort.
+// Sparse accumulator for one row: mark[c] == id means column c is present.
+// A removal clears the mark; a later insertion of the same column starts from
+// the inserted value, exactly like remove_element followed by insert_sparse.
+struct RowAcc {
+    std::vector<double> val;
+    std::vector<int> mark;
+    std::vector<int> touched;
+    int id = 0;
+    explicit RowAcc(int n) : val(n, 0.0), mark(n, -1) {}
+    void begin() {
+        id++;
+        touched.clear();
+    }
+    void add(int c, double a) {
+        if (mark[c] == id) {
+            val[c] += a;
+        } else {
+            mark[c] = id;
+            val[c] = a;
+            touched.push_back(c);
+        }
+    }
+    void remove(int c) {
+        if (mark[c] == id) mark[c] = -1;
+    }
+    // present columns in increasing order with their values
+    void collect(std::vector<int>& cols, std::vector<double>& vals) {
+        std::sort(touched.begin(), touched.end());
+        cols.clear();
+        vals.clear();
+        int prev = -1;
+        for (int c : touched) {
+            if (c == prev) continue;
+            prev = c;
+            if (mark[c] == id) {
+                cols.push_back(c);
+                vals.push_back(val[c]);
+            }
+        }
+    }
+};
+
+// AMG_simple_standard_interpolation (Multigrid.c:989-1079) followed by
+// sparse_approximate (linear_algebra.c:1418-1442) and normalize_row_sum
+// (:455-464).  Rows are independent, so they are built in parallel; the
+// reference leaves its row loop at the first fine row without coarse
+// neighbours (Multigrid.c:1057-1059), so every row after that one keeps only
+// its initial (i, 0.0) entry.  Returns false if a zero diagonal makes the
+// reference abort.
 bool interpolation(const Csr& A, const std::vector<int>& label, const std::vector<int>& lev,
                    const std::vector<int>& map, int iter, double tol, Csr& P, std::string& err, bool& broke) {
-    int n = A.n;
+    const int n = A.n;
     std::vector<double> D(n);
     for (int i = 0; i < n; i++) {
         D[i] = csr_diag(A, i);
@@ -437,112 +488,147 @@ bool interpolation(const Csr& A, const std::vector<int>& label, const std::vecto
             return false;
         }
     }
-    std::vector<Row> Prow(n);
-    for (int i = 0; i < n; i++) {  // sparse_zero: every row starts as (i, 0.0)
-        Prow[i].c.assign(1, i);
-        Prow[i].v.assign(1, 0.0);
-    }
-    broke = false;
-    Row q, snap;
-    for (int i = 0; i < n && !broke; i++) {
-        if (label[i] != kFine) {
-            row_insert(Prow[i], 1.0, map[i]);
-            continue;
-        }
-        q.c.assign(A.col.begin() + A.ptr[i], A.col.begin() + A.ptr[i + 1]);
-        q.v.resize(q.c.size());
-        for (int p = A.ptr[i], k = 0; p < A.ptr[i + 1]; p++, k++) q.v[k] = A.val[p] / D[i];
-        for (int pass = 0; pass < iter; pass++) {
-            snap = q;
-            for (size_t j = 0; j < snap.c.size(); j++) {
-                int J = snap.c[j];
-                double qv = snap.v[j];
-                if (J != i && label[J] == kFine && qv != 0.0) {
-                    row_remove(q, J);
-                    for (int r = A.ptr[J]; r < A.ptr[J + 1]; r++) {
-                        int L = A.col[r];
-                        double a = A.val[r] / D[J];
-                        if (L != J && a != 0.0) row_insert(q, -a * qv, L);
+    int ncols = 0;
+    for (int c : A.col) ncols = std::max(ncols, c + 1);
+    ncols = std::max(ncols, n);
+    std::vector<std::vector<int>> rc(n);
+    std::vector<std::vector<double>> rv(n);
+    std::vector<char> fail(n, 0);
+#pragma omp parallel
+    {
+        RowAcc acc(ncols);
+        std::vector<int> qc, sc;
+        std::vector<double> qv, sv;
+#pragma omp for schedule(dynamic, 256)
+        for (int i = 0; i < n; i++) {
+            std::vector<int>& pc = rc[i];
+            std::vector<double>& pv = rv[i];
+            pc.assign(1, i);  // sparse_zero: every row starts as (i, 0.0)
+            pv.assign(1, 0.0);
+            if (label[i] != kFine) {
+                Row r{pc, pv};
+                row_insert(r, 1.0, map[i]);
+                pc.swap(r.c);
+                pv.swap(r.v);
+                continue;
+            }
+            qc.assign(A.col.begin() + A.ptr[i], A.col.begin() + A.ptr[i + 1]);
+            qv.resize(qc.size());
+            for (int p = A.ptr[i], k = 0; p < A.ptr[i + 1]; p++, k++) qv[k] = A.val[p] / D[i];
+            for (int pass = 0; pass < iter; pass++) {
+                sc = qc;
+                sv = qv;
+                acc.begin();
+                for (size_t k = 0; k < qc.size(); k++) acc.add(qc[k], qv[k]);
+                for (size_t j = 0; j < sc.size(); j++) {
+                    int J = sc[j];
+                    double q = sv[j];
+                    if (J != i && label[J] == kFine && q != 0.0) {
+                        acc.remove(J);
+                        for (int r = A.ptr[J]; r < A.ptr[J + 1]; r++) {
+                            int L = A.col[r];
+                            double a = A.val[r] / D[J];
+                            if (L != J && a != 0.0) acc.add(L, -a * q);
+                        }
                     }
                 }
+                acc.collect(qc, qv);
             }
-        }
-        // drop couplings to other unknowns (order preserving)
-        {
+            // drop couplings to other unknowns (order preserving)
             size_t w = 0;
-            for (size_t k = 0; k < q.c.size(); k++)
-                if (lev[q.c[k]] == lev[i]) {
-                    q.c[w] = q.c[k];
-                    q.v[w] = q.v[k];
+            for (size_t k = 0; k < qc.size(); k++)
+                if (lev[qc[k]] == lev[i]) {
+                    qc[w] = qc[k];
+                    qv[w] = qv[k];
                     w++;
                 }
-            q.c.resize(w);
-            q.v.resize(w);
-        }
-        double s_p = 0, c_p = 0, s_m = 0, c_m = 0;
-        double Di = D[i];
-        for (size_t k = 0; k < q.c.size(); k++) {
-            int J = q.c[k];
-            double qv = q.v[k];
-            if (J != i) {
-                if (qv < 0) {
-                    s_m += qv;
-                    if (label[J] == kCoarse) c_m += qv;
+            qc.resize(w);
+            qv.resize(w);
+            double s_p = 0, c_p = 0, s_m = 0, c_m = 0;
+            double Di = D[i];
+            for (size_t k = 0; k < qc.size(); k++) {
+                int J = qc[k];
+                double q = qv[k];
+                if (J != i) {
+                    if (q < 0) {
+                        s_m += q;
+                        if (label[J] == kCoarse) c_m += q;
+                    } else {
+                        s_p += q;
+                        if (label[J] == kCoarse) c_p += q;
+                    }
                 } else {
-                    s_p += qv;
-                    if (label[J] == kCoarse) c_p += qv;
+                    Di = q;
                 }
-            } else {
-                Di = qv;
             }
+            double alpha = 0, beta = 0;
+            if (c_m != 0) alpha = -s_m / c_m; else Di += s_m;
+            if (c_p != 0) beta = -s_p / c_p; else Di += s_p;
+            if (alpha == 0 && beta == 0) {
+                fail[i] = 1;
+                continue;
+            }
+            alpha /= Di;
+            beta /= Di;
+            Row r{pc, pv};
+            for (size_t k = 0; k < qc.size(); k++) {
+                int J = qc[k];
+                double q = qv[k];
+                if (J != i && label[J] == kCoarse) {
+                    if (q < 0 && alpha != 0) row_insert(r, alpha * q, map[J]);
+                    if (q > 0 && beta != 0) row_insert(r, beta * q, map[J]);
+                }
+            }
+            pc.swap(r.c);
+            pv.swap(r.v);
         }
-        double alpha = 0, beta = 0;
-        if (c_m != 0) alpha = -s_m / c_m; else Di += s_m;
-        if (c_p != 0) beta = -s_p / c_p; else Di += s_p;
-        if (alpha == 0 && beta == 0) {
-            // the reference prints and leaves the row loop here (Multigrid.c:1057-1059)
+    }
+    broke = false;
+    for (int i = 0; i < n; i++) {
+        if (broke) {
+            rc[i].assign(1, i);
+            rv[i].assign(1, 0.0);
+        } else if (fail[i]) {
             broke = true;
-            break;
-        }
-        alpha /= Di;
-        beta /= Di;
-        for (size_t k = 0; k < q.c.size(); k++) {
-            int J = q.c[k];
-            double qv = q.v[k];
-            if (J != i && label[J] == kCoarse) {
-                if (qv < 0 && alpha != 0) row_insert(Prow[i], alpha * qv, map[J]);
-                if (qv > 0 && beta != 0) row_insert(Prow[i], beta * qv, map[J]);
-            }
+            rc[i].assign(1, i);
+            rv[i].assign(1, 0.0);
         }
     }
     // delete_zeros, sparse_approximate, normalize_row_sum
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; i++) {
+        std::vector<int>& c = rc[i];
+        std::vector<double>& v = rv[i];
+        row_delete_zeros(c, v, i);
+        double mx = 0;
+        for (size_t k = 0; k < c.size(); k++) {
+            double a = std::fabs(v[k]);
+            if (c[k] != i && a > mx) mx = a;
+        }
+        size_t w = 0;
+        for (size_t k = 0; k < c.size(); k++) {
+            if (c[k] != i && std::fabs(v[k]) < mx * tol) continue;
+            c[w] = c[k];
+            v[w] = v[k];
+            w++;
+        }
+        c.resize(w);
+        v.resize(w);
+        double sum = 0;
+        for (double x : v) sum += x;
+        if (sum != 0)
+            for (double& x : v) x *= 1.0 / sum;
+    }
     P = Csr();
     P.n = n;
     P.ptr.assign(n + 1, 0);
+    for (int i = 0; i < n; i++) P.ptr[i + 1] = P.ptr[i] + (int)rc[i].size();
+    P.col.resize(P.ptr[n]);
+    P.val.resize(P.ptr[n]);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < n; i++) {
-        Row& r = Prow[i];
-        row_delete_zeros(r.c, r.v, i);
-        double mx = 0;
-        for (size_t k = 0; k < r.c.size(); k++) {
-            double a = std::fabs(r.v[k]);
-            if (r.c[k] != i && a > mx) mx = a;
-        }
-        size_t w = 0;
-        for (size_t k = 0; k < r.c.size(); k++) {
-            if (r.c[k] != i && std::fabs(r.v[k]) < mx * tol) continue;
-            r.c[w] = r.c[k];
-            r.v[w] = r.v[k];
-            w++;
-        }
-        r.c.resize(w);
-        r.v.resize(w);
-        double sum = 0;
-        for (double x : r.v) sum += x;
-        if (sum != 0)
-            for (double& x : r.v) x *= 1.0 / sum;
-        P.col.insert(P.col.end(), r.c.begin(), r.c.end());
-        P.val.insert(P.val.end(), r.v.begin(), r.v.end());
-        P.ptr[i + 1] = (int)P.col.size();
+        std::copy(rc[i].begin(), rc[i].end(), P.col.begin() + P.ptr[i]);
+        std::copy(rv[i].begin(), rv[i].end(), P.val.begin() + P.ptr[i]);
     }
     return true;
 }
@@ -701,44 +787,68 @@ Csr spgemm_ref(const Csr& A, const Csr& B) {
     Csr C;
     C.n = A.n;
     C.ncols = B.ncols;
-    C.ptr.assign(A.n + 1, 0);
     int width = std::max(B.ncols, A.n) + 1;
     for (int c : B.col) width = std::max(width, c + 1);
-    std::vector<double> acc(width, 0.0);
-    std::vector<int> mark(width, -1);
-    std::vector<int> cols;
-    std::vector<double> vals;
-    C.col.reserve(A.col.size() * 2);
-    C.val.reserve(A.col.size() * 2);
-    for (int i = 0; i < A.n; i++) {
-        cols.clear();
-        mark[i] = i;
-        acc[i] = 0.0;
-        cols.push_back(i);
-        for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
-            double a = A.val[p];
-            if (a == 0.0) continue;
-            int k = A.col[p];
-            for (int r = B.ptr[k]; r < B.ptr[k + 1]; r++) {
-                double b = B.val[r];
-                if (b == 0.0) continue;
-                int j = B.col[r];
-                if (mark[j] != i) {
-                    mark[j] = i;
-                    acc[j] = a * b;
-                    cols.push_back(j);
-                } else {
-                    acc[j] += a * b;
+    const int n = A.n;
+    const int chunk = 4096;
+    const int nchunks = (n + chunk - 1) / chunk;
+    std::vector<std::vector<int>> ccol(nchunks);
+    std::vector<std::vector<double>> cval(nchunks);
+    std::vector<std::vector<int>> clen(nchunks);
+#pragma omp parallel
+    {
+        std::vector<double> acc(width, 0.0);
+        std::vector<int> mark(width, -1);
+        std::vector<int> cols;
+        std::vector<double> vals;
+#pragma omp for schedule(dynamic, 1)
+        for (int ch = 0; ch < nchunks; ch++) {
+            const int i0 = ch * chunk, i1 = std::min(n, i0 + chunk);
+            for (int i = i0; i < i1; i++) {
+                cols.clear();
+                mark[i] = i;
+                acc[i] = 0.0;
+                cols.push_back(i);
+                for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
+                    double a = A.val[p];
+                    if (a == 0.0) continue;
+                    int k = A.col[p];
+                    for (int r = B.ptr[k]; r < B.ptr[k + 1]; r++) {
+                        double b = B.val[r];
+                        if (b == 0.0) continue;
+                        int j = B.col[r];
+                        if (mark[j] != i) {
+                            mark[j] = i;
+                            acc[j] = a * b;
+                            cols.push_back(j);
+                        } else {
+                            acc[j] += a * b;
+                        }
+                    }
                 }
+                std::sort(cols.begin(), cols.end());
+                vals.resize(cols.size());
+                for (size_t k = 0; k < cols.size(); k++) vals[k] = acc[cols[k]];
+                row_delete_zeros(cols, vals, i);
+                ccol[ch].insert(ccol[ch].end(), cols.begin(), cols.end());
+                cval[ch].insert(cval[ch].end(), vals.begin(), vals.end());
+                clen[ch].push_back((int)cols.size());
             }
         }
-        std::sort(cols.begin(), cols.end());
-        vals.resize(cols.size());
-        for (size_t k = 0; k < cols.size(); k++) vals[k] = acc[cols[k]];
-        row_delete_zeros(cols, vals, i);
-        C.col.insert(C.col.end(), cols.begin(), cols.end());
-        C.val.insert(C.val.end(), vals.begin(), vals.end());
-        C.ptr[i + 1] = (int)C.col.size();
+    }
+    C.ptr.assign(n + 1, 0);
+    for (int ch = 0, i = 0; ch < nchunks; ch++)
+        for (int len : clen[ch]) {
+            C.ptr[i + 1] = C.ptr[i] + len;
+            i++;
+        }
+    C.col.resize(C.ptr[n]);
+    C.val.resize(C.ptr[n]);
+#pragma omp parallel for schedule(static)
+    for (int ch = 0; ch < nchunks; ch++) {
+        int base = C.ptr[ch * chunk];
+        std::copy(ccol[ch].begin(), ccol[ch].end(), C.col.begin() + base);
+        std::copy(cval[ch].begin(), cval[ch].end(), C.val.begin() + base);
     }
     return C;
 }
@@ -804,17 +914,23 @@ bool amg_setup_host(const Csr& Ain, const AmgParams& p, HostHierarchy& h) {
         fine.dof_level.assign(n, 0);
         for (int k = 0; k < n; k++) fine.dof_level[k] = (mesh > 0) ? std::min(k / mesh, p.dof - 1) : 0;
     }
+    const bool timing = std::getenv("LINA_SETUP_TIMING") != nullptr;
+    auto now = [] { return std::chrono::steady_clock::now(); };
+    auto secs = [](auto a, auto b) { return std::chrono::duration<double>(b - a).count(); };
     for (int i = depth - 1; i > 0; i--) {
+        auto t0 = now();
         HostLevel& L = h.lv[i];
         HostLevel& C = h.lv[i - 1];
         const std::vector<int>& lev = L.dof_level;
         Lists S = strong_connections(L.A, lev, p.eps_minus, p.eps_plus);
         Lists T = transpose_lists(S, L.A.n);
+        auto t1 = now();
         bool aggressive = (p.coarsening == kAggressive && i == depth - 1);
         if (aggressive)
             L.coarse_size = aggressive_coarsening(L.A, lev, p.dof, S, T, p.eps_minus, p.eps_plus, L.labels);
         else
             L.coarse_size = standard_coarsening(L.A, lev, p.dof, S, T, L.labels, true);
+        auto t2 = now();
         std::vector<int> map;
         int nc = coarse_map(L.labels, map);
         if (nc != L.coarse_size) {
@@ -829,6 +945,7 @@ bool amg_setup_host(const Csr& Ain, const AmgParams& p, HostHierarchy& h) {
             return false;
         L.P.ncols = nc;
         if (broke) fprintf(stderr, "LinA-GB300 warning: AMG level %d has a fine row without coarse interpolation\n", i);
+        auto t3 = now();
         L.R = amg_transpose(L.P, nc);
         Csr AP = spgemm_ref(L.A, L.P);
         AP.ncols = nc;
@@ -838,8 +955,15 @@ bool amg_setup_host(const Csr& Ain, const AmgParams& p, HostHierarchy& h) {
             h.error = "erroneous coarse matrix";
             return false;
         }
+        auto t4 = now();
+        if (timing)
+            fprintf(stderr, "level %d n=%d nnz=%lld: strength %.2fs coarsen %.2fs interp %.2fs galerkin %.2fs\n", i,
+                    L.A.n, (long long)L.A.nnz(), secs(t0, t1), secs(t1, t2), secs(t2, t3), secs(t3, t4));
     }
-    return coarse_factor(h.lv[0].A, h.coarse, h.error);
+    auto tc = now();
+    bool ok = coarse_factor(h.lv[0].A, h.coarse, h.error);
+    if (timing) fprintf(stderr, "coarsest n=%d block=%zu: %.2fs\n", h.lv[0].A.n, h.coarse.block_rows.size(), secs(tc, now()));
+    return ok;
 }
 
 bool amg_recompute_host(HostHierarchy& h, const Csr& A) {

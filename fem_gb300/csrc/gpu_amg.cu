@@ -27,6 +27,7 @@
 namespace {
 
 std::string g_err;
+unsigned long long g_launches = 0;  // kernels launched by this library (all handles)
 
 void set_err(const char* fmt, ...) {
     char buf[512];
@@ -330,6 +331,14 @@ struct DLevel {
     float *x32 = nullptr, *t32 = nullptr, *b32 = nullptr, *r32 = nullptr;
 };
 
+// every non-CSR launch goes through here so that the library can report how many
+// kernels it issued
+template <typename... KA, typename... A>
+void go(void (*k)(KA...), int grid, cudaStream_t st, A... a) {
+    g_launches++;
+    k<<<grid, kThreads, 0, st>>>(a...);
+}
+
 int lanes_for(long nnz, int n) {
     double avg = n > 0 ? double(nnz) / n : 1.0;
     if (avg <= 6.0) return 4;
@@ -373,6 +382,7 @@ struct lina_gpu_amg {
     double* signs = nullptr;   // only when make_positive_diag flipped a row
     DCsr Aorig;                // unflipped finest matrix when signs exist (Krylov SpMV)
     bool has_signs = false;
+    bool host_only = false;
     // Krylov work
     double *kr = nullptr, *kz = nullptr, *kp = nullptr, *kq = nullptr, *kx = nullptr, *kb = nullptr,
            *kt = nullptr;
@@ -386,6 +396,7 @@ struct lina_gpu_amg {
     long dev_bytes = 0;
     std::vector<void*> allocations;
     // smoother timing
+    cudaEvent_t tm0 = nullptr, tm1 = nullptr;
     bool timing = false;
     std::vector<cudaEvent_t> ev_pool;
     int ev_used = 0;
@@ -394,6 +405,8 @@ struct lina_gpu_amg {
         for (void* p : allocations) cudaFree(p);
         if (sc_host) cudaFreeHost(sc_host);
         for (auto e : ev_pool) cudaEventDestroy(e);
+        if (tm0) cudaEventDestroy(tm0);
+        if (tm1) cudaEventDestroy(tm1);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -456,6 +469,7 @@ struct lina_gpu_amg {
                       const TX* dinv, TX w, const TX* z) {
         const int S = m.lanes;
         const int groups = kThreads / S;
+        g_launches++;
         int grid = (MODE == M_DOT) ? grid_red((long)nrows * S) : grid_for(nrows, groups);
         if (MODE == M_DOT) grid = std::min(grid, kMaxBlocks);
 #define LINA_CSR_CASE(SS)                                                                                     \
@@ -504,9 +518,9 @@ struct lina_gpu_amg {
     template <typename TX>
     void coarse_solve(const TX* b, TX* x) {
         const int n = lv[0].n;
-        coarse_gather_kernel<TX><<<grid_for(n, kThreads), kThreads, 0, stream>>>(n, b, c_inblock, c_blockpos,
+        go(coarse_gather_kernel<TX>, grid_for(n, kThreads), stream, n, b, c_inblock, c_blockpos,
                                                                                  c_dginv, c_bblk, x);
-        if (cm > 0) coarse_gemv_kernel<TX><<<grid_for((long)cm * 32, kThreads), kThreads, 0, stream>>>(
+        if (cm > 0) go(coarse_gemv_kernel<TX>, grid_for((long)cm * 32, kThreads), stream, 
             cm, c_inv, c_bblk, c_brows, x);
     }
 
@@ -520,7 +534,7 @@ struct lina_gpu_amg {
         TX* bout = ((const void*)bin == (const void*)b) ? nullptr : b;
         if (opt.smoother == LINA_SMOOTHER_JACOBI && nu > 0) {
             TX* cur = ((nu - 1) % 2 == 0) ? x : t;
-            jacobi_first_kernel<TB, TX><<<grid_for(L.n, kThreads), kThreads, 0, stream>>>(L.n, bin, sign, dinv,
+            go(jacobi_first_kernel<TB, TX>, grid_for(L.n, kThreads), stream, L.n, bin, sign, dinv,
                                                                                            iso, w, cur, bout);
             for (int k = 1; k < nu; k++) {
                 TX* nxt = (cur == x) ? t : x;
@@ -531,7 +545,7 @@ struct lina_gpu_amg {
                 cur = nxt;
             }
         } else {
-            init_x_kernel<TB, TX><<<grid_for(L.n, kThreads), kThreads, 0, stream>>>(L.n, bin, sign, iso, x, bout);
+            go(init_x_kernel<TB, TX>, grid_for(L.n, kThreads), stream, L.n, bin, sign, iso, x, bout);
             for (int k = 0; k < nu; k++) sor_sweep(L, b, x, time_it);
         }
     }
@@ -605,7 +619,7 @@ struct lina_gpu_amg {
         DLevel& L = lv[l];
         if (depth == 1) {
             if (opt.precision == LINA_PREC_MIXED) {
-                convert_kernel<double, float><<<grid_for(L.n, kThreads), kThreads, 0, stream>>>(L.n, r, L.b32);
+                go(convert_kernel<double, float>, grid_for(L.n, kThreads), stream, L.n, r, L.b32);
                 coarse_solve<float>(L.b32, kz32);
             } else {
                 coarse_solve<double>(r, z);
@@ -754,7 +768,7 @@ bool valid_csr(int n, const int* rowptr, const int* col) {
 int true_residual(lina_gpu_amg* h, const double* b, const double* x) {
     const DCsr& A = h->krylov_matrix();
     h->csr<double, M_RESID>(A, A.n, nullptr, x, h->kt, b);
-    norm2_kernel<double><<<grid_red(A.n), kThreads, 0, h->stream>>>(A.n, h->kt, h->partials, h->ticket, h->sc);
+    go(norm2_kernel<double>, grid_red(A.n), h->stream, A.n, h->kt, h->partials, h->ticket, h->sc);
     return 0;
 }
 
@@ -823,6 +837,7 @@ static int amg_create_impl(int n, const int* rowptr, const int* col, const doubl
         return LINA_GPU_ESETUP;
     }
     if (host_only) {
+        h->host_only = true;
         *out = h;
         return 0;
     }
@@ -867,16 +882,13 @@ int lina_gpu_amg_recompute(lina_gpu_amg* h, int n, const int* rowptr, const int*
         return LINA_GPU_ESETUP;
     }
     // the reference keeps the setup's signs and does not flip the new matrix
-    bool had_signs = h->has_signs;
-    std::vector<double> keep_signs = h->host.signs;
+    if (h->host_only) return 0;
     for (void* p : h->allocations) cudaFree(p);
     h->allocations.clear();
     h->dev_bytes = 0;
     h->Aorig = DCsr();
     int rc = upload_hierarchy(h);
     if (rc) return rc;
-    (void)had_signs;
-    (void)keep_signs;
     if (h->has_signs) rc = h->upload_csr(h->Aorig, csr_from(n, rowptr, col, val));
     return rc;
 }
@@ -899,21 +911,21 @@ int lina_gpu_amg_set_smoother(lina_gpu_amg* h, int smoother, double omega, int p
 }
 
 int lina_gpu_vcycle(lina_gpu_amg* h, const double* r_dev, double* z_dev) {
-    if (!h || !r_dev || !z_dev) {
+    if (!h || h->host_only || !r_dev || !z_dev) {
         set_err("lina_gpu_vcycle: invalid argument");
         return LINA_GPU_EINVAL;
     }
     const int n = h->lv[h->depth - 1].n;
     h->precondition(r_dev, z_dev, false);
     if (h->opt.precision == LINA_PREC_MIXED)
-        convert_kernel<float, double><<<grid_for(n, kThreads), kThreads, 0, h->stream>>>(n, h->kz32, z_dev);
+        go(convert_kernel<float, double>, grid_for(n, kThreads), h->stream, n, h->kz32, z_dev);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(h->stream));
     return 0;
 }
 
 int lina_gpu_spmv(lina_gpu_amg* h, int level, const double* x_dev, double* y_dev) {
-    if (!h || level < 0 || level >= h->depth || !x_dev || !y_dev) {
+    if (!h || h->host_only || level < 0 || level >= h->depth || !x_dev || !y_dev) {
         set_err("lina_gpu_spmv: invalid argument");
         return LINA_GPU_EINVAL;
     }
@@ -926,7 +938,7 @@ int lina_gpu_spmv(lina_gpu_amg* h, int level, const double* x_dev, double* y_dev
 
 int lina_gpu_pcg(lina_gpu_amg* h, const double* b_in, double* x_out, double tol, int max_iter, int stop_rule,
                  int flags, lina_gpu_solve_info* info) {
-    if (!h || !b_in || !x_out || max_iter < 1 ||
+    if (!h || h->host_only || !b_in || !x_out || max_iter < 1 ||
         (stop_rule != LINA_STOP_REFERENCE && stop_rule != LINA_STOP_RELATIVE)) {
         set_err("lina_gpu_pcg: invalid argument");
         return LINA_GPU_EINVAL;
@@ -957,7 +969,7 @@ int lina_gpu_pcg(lina_gpu_amg* h, const double* b_in, double* x_out, double tol,
     const int gv = grid_for(n, kThreads);
     const int gr = grid_red(n);
     // ||b||
-    norm2_kernel<double><<<gr, kThreads, 0, st>>>(n, b, h->partials, h->ticket, h->sc);
+    go(norm2_kernel<double>, gr, st, n, b, h->partials, h->ticket, h->sc);
     if (read_scalars(h)) return LINA_GPU_ECUDA;
     double bnorm = std::sqrt(h->sc_host->norm2);
     double hscale = 1.0;
@@ -965,8 +977,8 @@ int lina_gpu_pcg(lina_gpu_amg* h, const double* b_in, double* x_out, double tol,
         hscale = (bnorm == 0.0) ? 1.0 : bnorm;
         double inv = 1.0 / hscale;
         CK(cudaMemcpyAsync(h->hscal, &inv, sizeof(double), cudaMemcpyHostToDevice, st));
-        scale_kernel<<<gv, kThreads, 0, st>>>(n, b, h->hscal, 0);
-        scale_kernel<<<gv, kThreads, 0, st>>>(n, x, h->hscal, 0);
+        go(scale_kernel, gv, st, n, b, h->hscal, 0);
+        go(scale_kernel, gv, st, n, x, h->hscal, 0);
         bnorm *= inv;
     }
     // r = b - A x
@@ -975,9 +987,9 @@ int lina_gpu_pcg(lina_gpu_amg* h, const double* b_in, double* x_out, double tol,
     // w = M^-1 r (kept as the first z)
     auto zptr_norm = [&]() {
         if (mixed)
-            norm2_kernel<float><<<gr, kThreads, 0, st>>>(n, h->kz32, h->partials, h->ticket, h->sc);
+            go(norm2_kernel<float>, gr, st, n, h->kz32, h->partials, h->ticket, h->sc);
         else
-            norm2_kernel<double><<<gr, kThreads, 0, st>>>(n, z, h->partials, h->ticket, h->sc);
+            go(norm2_kernel<double>, gr, st, n, z, h->partials, h->ticket, h->sc);
     };
     double r0 = 0.0;
     bool have_z = false;
@@ -1008,16 +1020,16 @@ int lina_gpu_pcg(lina_gpu_amg* h, const double* b_in, double* x_out, double tol,
             if (!have_z) h->precondition(r, z, time_it);
             have_z = false;
             if (mixed)
-                dot_rz_kernel<float><<<gr, kThreads, 0, st>>>(n, r, h->kz32, q, flexible, h->partials, h->ticket,
+                go(dot_rz_kernel<float>, gr, st, n, r, h->kz32, q, flexible, h->partials, h->ticket,
                                                                h->sc);
             else
-                dot_rz_kernel<double><<<gr, kThreads, 0, st>>>(n, r, z, q, flexible, h->partials, h->ticket, h->sc);
+                go(dot_rz_kernel<double>, gr, st, n, r, z, q, flexible, h->partials, h->ticket, h->sc);
             if (mixed)
-                update_p_kernel<float><<<gv, kThreads, 0, st>>>(n, h->kz32, p, flexible, h->sc);
+                go(update_p_kernel<float>, gv, st, n, h->kz32, p, flexible, h->sc);
             else
-                update_p_kernel<double><<<gv, kThreads, 0, st>>>(n, z, p, flexible, h->sc);
+                go(update_p_kernel<double>, gv, st, n, z, p, flexible, h->sc);
             h->csr<double, M_DOT>(A, n, nullptr, p, q);
-            update_xr_kernel<<<gr, kThreads, 0, st>>>(n, x, r, p, q, h->partials, h->ticket, h->sc);
+            go(update_xr_kernel, gr, st, n, x, r, p, q, h->partials, h->ticket, h->sc);
             CK(cudaGetLastError());
             if (read_scalars(h)) return LINA_GPU_ECUDA;
             it++;
@@ -1059,7 +1071,7 @@ finish:
     inf->true_rel_residual = (bnorm > 0) ? std::sqrt(h->sc_host->norm2) / bnorm : 0.0;
     if (flags & LINA_PCG_NORMALIZE) {
         CK(cudaMemcpyAsync(h->hscal, &hscale, sizeof(double), cudaMemcpyHostToDevice, st));
-        scale_kernel<<<gv, kThreads, 0, st>>>(n, x, h->hscal, 0);
+        go(scale_kernel, gv, st, n, x, h->hscal, 0);
     }
     if (dev)
         CK(cudaMemcpyAsync(x_out, x, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
@@ -1084,6 +1096,42 @@ finish:
                 (mixed ? (8 * nnz + 4 * (nn + 1) + 16 * nn) : (12 * nnz + 4 * (nn + 1) + 32 * nn)) / L.ncolours;
     }
     return inf->status;
+}
+
+int lina_gpu_timer_begin(lina_gpu_amg* h) {
+    if (!h || h->host_only) return LINA_GPU_EINVAL;
+    if (!h->tm0) {
+        CK(cudaEventCreate(&h->tm0));
+        CK(cudaEventCreate(&h->tm1));
+    }
+    CK(cudaEventRecord(h->tm0, h->stream));
+    return 0;
+}
+
+int lina_gpu_timer_end(lina_gpu_amg* h, double* ms) {
+    if (!h || h->host_only || !h->tm0 || !ms) return LINA_GPU_EINVAL;
+    CK(cudaEventRecord(h->tm1, h->stream));
+    CK(cudaEventSynchronize(h->tm1));
+    float f = 0.f;
+    CK(cudaEventElapsedTime(&f, h->tm0, h->tm1));
+    *ms = f;
+    return 0;
+}
+
+unsigned long long lina_gpu_launches(void) { return g_launches; }
+
+void* lina_gpu_malloc_host(size_t bytes) {
+    void* p = nullptr;
+    if (cudaMallocHost(&p, bytes ? bytes : 1) != cudaSuccess) {
+        set_err("cudaMallocHost(%zu) failed", bytes);
+        return nullptr;
+    }
+    return p;
+}
+
+int lina_gpu_free_host(void* p) {
+    CK(cudaFreeHost(p));
+    return 0;
 }
 
 int lina_gpu_amg_depth(const lina_gpu_amg* h) { return h ? h->depth : 0; }
@@ -1126,7 +1174,7 @@ int lina_gpu_level_colours(const lina_gpu_amg* h, int level, int* colour) {
     return 0;
 }
 
-int lina_gpu_coarse_block_size(const lina_gpu_amg* h) { return h ? h->cm : 0; }
+int lina_gpu_coarse_block_size(const lina_gpu_amg* h) { return h ? (int)h->host.coarse.block_rows.size() : 0; }
 
 long lina_gpu_amg_device_bytes(const lina_gpu_amg* h) { return h ? h->dev_bytes : 0; }
 

@@ -92,6 +92,11 @@ def lib():
         "lina_gpu_synchronize": (C.c_int, []),
         "lina_gpu_device_count": (C.c_int, []),
         "lina_gpu_last_error": (C.c_char_p, []),
+        "lina_gpu_timer_begin": (C.c_int, [vp]),
+        "lina_gpu_timer_end": (C.c_int, [vp, dp]),
+        "lina_gpu_launches": (C.c_ulonglong, []),
+        "lina_gpu_malloc_host": (vp, [C.c_size_t]),
+        "lina_gpu_free_host": (C.c_int, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -169,6 +174,35 @@ class DeviceArray:
             self.free()
         except Exception:
             pass
+
+
+class PinnedArray:
+    """Page-locked host memory (cudaMallocHost) viewed as a numpy array."""
+
+    def __init__(self, n, dtype=np.float64):
+        self.dtype = np.dtype(dtype)
+        self.nbytes = int(n) * self.dtype.itemsize
+        self.ptr = lib().lina_gpu_malloc_host(max(self.nbytes, 1))
+        if not self.ptr:
+            raise LinaError(f"pinned allocation failed: {last_error()}")
+        buf = (C.c_char * max(self.nbytes, 1)).from_address(self.ptr)
+        self.array = np.frombuffer(buf, dtype=self.dtype, count=int(n))
+
+    def free(self):
+        if self.ptr:
+            self.array = None
+            lib().lina_gpu_free_host(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def launches() -> int:
+    return int(lib().lina_gpu_launches())
 
 
 class AMG:
@@ -275,6 +309,14 @@ class AMG:
         yd = DeviceArray(n)
         _check(lib().lina_gpu_spmv(self.h, lv, xd.ptr, yd.ptr), "spmv")
         return yd.to_host()
+
+    def timer_begin(self):
+        _check(lib().lina_gpu_timer_begin(self.h), "timer begin")
+
+    def timer_end(self) -> float:
+        ms = C.c_double()
+        _check(lib().lina_gpu_timer_end(self.h, C.byref(ms)), "timer end")
+        return ms.value
 
     @property
     def device_bytes(self):

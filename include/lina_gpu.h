@@ -102,6 +102,12 @@ int lina_gpu_vcycle(lina_gpu_amg* h, const double* r_dev, double* z_dev);
 /* y = A_level x on the device (level = depth-1 is the finest) */
 int lina_gpu_spmv(lina_gpu_amg* h, int level, const double* x_dev, double* y_dev);
 
+/* CUDA-event timing on the hierarchy's stream: elapsed milliseconds between begin and end */
+int lina_gpu_timer_begin(lina_gpu_amg* h);
+int lina_gpu_timer_end(lina_gpu_amg* h, double* ms);
+/* number of kernels this library has launched since it was loaded */
+unsigned long long lina_gpu_launches(void);
+
 /* hierarchy inspection (host copies of what the GPU holds) */
 int lina_gpu_amg_depth(const lina_gpu_amg* h);
 int lina_gpu_level_sizes(const lina_gpu_amg* h, int level, int* n, long* nnz_A, long* nnz_P, long* nnz_R,
@@ -119,6 +125,8 @@ int lina_gpu_free(void* p);
 int lina_gpu_memcpy_h2d(void* dst, const void* src, size_t bytes);
 int lina_gpu_memcpy_d2h(void* dst, const void* src, size_t bytes);
 int lina_gpu_synchronize(void);
+void* lina_gpu_malloc_host(size_t bytes);   /* pinned host memory */
+int lina_gpu_free_host(void* p);
 int lina_gpu_device_count(void);
 
 const char* lina_gpu_last_error(void);

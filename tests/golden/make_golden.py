@@ -1,0 +1,133 @@
+"""Generate the committed golden fixtures from the reference LinA itself.
+
+Run in a checkout where the reference tree is available (``make -C oracle ref``
+builds oracle/_ref/libLinA_ref.so from it):
+
+    python tests/golden/make_golden.py
+
+For each small seeded system it records what the reference computes:
+the AMG hierarchy of AMG_setup (LinA/Multigrid.c:1613) level by level (C/F
+labels, A, P, R), the greedy colouring of each level, one preconditioner
+application (a V-cycle from the zero guess) for a seeded residual, and full
+pcg solves (LinA/PCGS.c:163) with the smoothers the GPU library implements
+(installed into the reference through AMG_set_smoother) and with the
+reference's own lexicographic SOR.  Tests compare the GPU library against
+these files on machines where the reference is absent.
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from fem_gb300 import problems  # noqa: E402
+from oracle import ref  # noqa: E402
+
+# name -> (system factory, depth, coarsening)
+CASES = {
+    "poisson33_aggr": (lambda: problems.poisson_p1(33, seed=0), 4, ref.AGGRESSIVE),
+    "poisson33_std": (lambda: problems.poisson_p1(33, seed=0), 4, ref.STANDARD),
+    "elast17_aggr": (lambda: problems.elasticity_p1(17), 3, ref.AGGRESSIVE),
+    "elast17_std": (lambda: problems.elasticity_p1(17), 3, ref.STANDARD),
+}
+# larger systems for which only the solves are stored (the input is regenerated
+# by fem_gb300.problems and checked against the stored digest)
+SOLVE_CASES = {
+    "poisson129_aggr_solve": (lambda: problems.poisson_p1(129, seed=0), 5, ref.AGGRESSIVE),
+    "elast65_std_solve": (lambda: problems.elasticity_p1(65), 5, ref.STANDARD),
+}
+# smoother configurations: name -> (reference smoother kind, omega)
+SMOOTHERS = {
+    "jacobi": (ref.SMOOTHER_DAMPED_JACOBI, 0.6),
+    "mcsor": (ref.SMOOTHER_MC_SOR, 1.0),
+    "refsor": (ref.SMOOTHER_REF_SOR, 1.0),
+}
+TOL = 1e-8
+MAX_IT = 500
+
+
+def system_digest(s) -> str:
+    h = hashlib.sha256()
+    for a in (s.indptr, s.indices, s.data, s.b):
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def make_case(name):
+    factory, depth, coarsening = CASES[name]
+    s = factory()
+    amg = ref.RefAMG(s, depth, 2, 2, coarsening)
+    out = {
+        "n": np.int64(s.n), "dof": np.int64(s.dof), "depth": np.int64(depth),
+        "coarsening": np.int64(coarsening), "digest": np.array(system_digest(s)),
+        "indptr": s.indptr, "indices": s.indices, "data": s.data, "b": s.b,
+        "sizes": np.array(amg.sizes(), dtype=np.int64),
+    }
+    for lv in range(depth):
+        L = amg.level(lv)
+        out[f"L{lv}_A_ptr"], out[f"L{lv}_A_col"], out[f"L{lv}_A_val"] = L.A
+        if lv > 0:
+            out[f"L{lv}_labels"] = L.labels
+            out[f"L{lv}_P_ptr"], out[f"L{lv}_P_col"], out[f"L{lv}_P_val"] = L.P
+            out[f"L{lv}_R_ptr"], out[f"L{lv}_R_col"], out[f"L{lv}_R_val"] = L.R
+            nc, col = ref.greedy_colouring(len(L.A[0]) - 1, *L.A)
+            out[f"L{lv}_colour"] = col
+    rng = np.random.default_rng(1)
+    r = rng.uniform(-1.0, 1.0, s.n)
+    out["vcycle_r"] = r
+    for sname, (kind, omega) in SMOOTHERS.items():
+        out[f"vcycle_{sname}"] = amg.vcycle(r, kind, omega)
+        x, it, res = amg.pcg(s.b, TOL, MAX_IT, kind, omega)
+        out[f"pcg_{sname}_x"] = x
+        out[f"pcg_{sname}_it"] = np.int64(it)
+        out[f"pcg_{sname}_res"] = np.float64(res)
+    # an accurate FP64 solution (reference pcg to a tight tolerance) for error bars
+    x, it, res = amg.pcg(s.b, 1e-13, 2000, ref.SMOOTHER_MC_SOR, 1.0)
+    out["x_tight"] = x
+    return out
+
+
+def make_solve_case(name):
+    factory, depth, coarsening = SOLVE_CASES[name]
+    s = factory()
+    amg = ref.RefAMG(s, depth, 2, 2, coarsening)
+    out = {"n": np.int64(s.n), "dof": np.int64(s.dof), "depth": np.int64(depth),
+           "coarsening": np.int64(coarsening), "digest": np.array(system_digest(s)),
+           "sizes": np.array(amg.sizes(), dtype=np.int64)}
+    for sname, (kind, omega) in SMOOTHERS.items():
+        if sname == "refsor":
+            continue
+        x, it, res = amg.pcg(s.b, TOL, MAX_IT, kind, omega)
+        out[f"pcg_{sname}_x"] = x
+        out[f"pcg_{sname}_it"] = np.int64(it)
+        out[f"pcg_{sname}_res"] = np.float64(res)
+    x, it, res = amg.pcg(s.b, 1e-13, 2000, ref.SMOOTHER_MC_SOR, 1.0)
+    out["x_tight"] = x
+    return out
+
+
+def main():
+    if not ref.available():
+        sys.exit("oracle/_ref/libLinA_ref.so is missing: run `make -C oracle ref` where the reference tree exists")
+    for name in CASES:
+        data = make_case(name)
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **data)
+        print(f"{path}: sizes {list(data['sizes'])}, pcg iterations "
+              + ", ".join(f"{k}={int(data[f'pcg_{k}_it'])}" for k in SMOOTHERS))
+    for name in SOLVE_CASES:
+        data = make_solve_case(name)
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **data)
+        print(f"{path}: sizes {list(data['sizes'])}, pcg iterations "
+              + ", ".join(f"{k}={int(data[f'pcg_{k}_it'])}" for k in ("jacobi", "mcsor")))
+
+
+if __name__ == "__main__":
+    main()
