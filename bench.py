@@ -1,0 +1,355 @@
+"""Benchmark of the LinA sparse solve path on one GB300.
+
+Workload (the configuration the headline metric is quoted on): plane-strain
+P1 elasticity on a 1025 x 1025 node grid of the unit square, 2,101,250
+unknowns (block ordering [u_x, u_y]), ~29.3M stored nonzeros, E = 210,
+nu = 0.3, stiffness degraded by (1-d)^2 + 1e-6 around a notch from (0, 0.5)
+to (0.5, 0.5) with d = exp(-dist / 2h); bottom edge clamped, top edge
+u_y = 1e-3.  AMG setup as the reference's AMG_setup with standard coarsening
+and dof = 2; one V-cycle per iteration (2 pre + 2 post sweeps) inside CG.
+
+A step is one complete solve to the true relative residual 1e-8 with the
+mixed-precision preconditioner (FP32 V-cycle, FP64 coarse solve, FP64
+flexible CG).  ``value`` is solves/s with the matrix hierarchy and the
+right-hand side already in HBM; ``e2e`` is the same solve through the C-ABI
+with host buffers (pinned), so the H2D copy of b and the D2H copy of x are in
+the timed region.  The same GPU's plain FP64 path and the CPU baseline are
+measured in the same run.  The finest-level matrix (~235 MB FP32 values and
+indices, ~352 MB FP64) exceeds the 129 MB L2, so no L2 flush is needed
+between steps.
+
+``--impl reference`` times the CPU implementation of the reference's solve
+(the CPU restatement in oracle/, bit-exact to the reference on its golden
+vectors, or the reference itself where it was built here) on the same
+workload and prints the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "AMG-PCG solves/s at 2.1M dofs to rel-res 1e-8: mixed vs FP64 GPU; HBM GB/s"
+DEFAULT_DEPTH = {65: 5, 129: 6, 257: 8, 513: 9, 1025: 10}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--m", type=int, default=1025, help="grid nodes per side")
+    p.add_argument("--depth", type=int, default=0)
+    p.add_argument("--smoother", default="jacobi", choices=["jacobi", "mcsor"])
+    p.add_argument("--omega", type=float, default=0.0)
+    p.add_argument("--tol", type=float, default=1e-8)
+    p.add_argument("--cpu-seconds", type=float, default=20.0, help="bound of the CPU baseline sample")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-fp64", action="store_true")
+    return p.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock and throttle-reason samples every 200 ms while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "", 1).isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "", 1).isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[3 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            if line.startswith("dram_bytes_per_launch_full_size:"):
+                return float(line.split(":", 1)[1])
+    return None
+
+
+def build_system(m):
+    from fem_gb300 import problems
+    return problems.elasticity_p1(m)
+
+
+def cpu_baseline(amg, s, smoother, omega, full_iterations, tol, seconds):
+    """CPU restatement (oracle) of the same solve on the same hierarchy, bounded sample."""
+    from oracle import port
+    kind = port.JACOBI if smoother == "jacobi" else port.MC_SOR
+    P = port.PortAMG(port.levels_from_amg(amg), kind, omega, 2, 2)
+    t0 = time.perf_counter()
+    x, it, _ = P.pcg(s.b, tol, 100000, 1, seconds)
+    dt = time.perf_counter() - t0
+    per_it = dt / max(it, 1)
+    value = 1.0 / (per_it * full_iterations)
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
+            "sample": f"{it} PCG iterations ({dt:.1f} s) of the same FP64 solve on the same hierarchy, "
+                      f"scaled to a full solve of {full_iterations} iterations"}
+
+
+def run_gb300(args, rank, world, local):
+    from fem_gb300 import lina
+    m = args.m
+    depth = args.depth or DEFAULT_DEPTH.get(m, 8)
+    smoother = lina.SMOOTHER_JACOBI if args.smoother == "jacobi" else lina.SMOOTHER_MC_SOR
+    omega = args.omega or (0.6 if args.smoother == "jacobi" else 1.0)
+    if lina.lib().lina_gpu_device_count() < 1:
+        raise SystemExit("no CUDA device")
+    s = build_system(m)
+    t0 = time.perf_counter()
+    amg = lina.AMG.from_system(s, depth=depth, coarsening=lina.STANDARD, smoother=smoother, omega=omega,
+                               precision=lina.PREC_MIXED)
+    setup_s = time.perf_counter() - t0
+    n = s.n
+    b_dev = lina.DeviceArray.from_host(s.b)
+    x_dev = lina.DeviceArray(n)
+
+    def solve_dev(flags=0):
+        return amg.pcg_device(b_dev, x_dev, tol=args.tol, max_iter=2000, stop=lina.STOP_RELATIVE, flags=flags)
+
+    for _ in range(args.warmup):
+        solve_dev()
+    barrier(world)
+    clocks = ClockSampler(local)
+    clocks.start()
+    lina.lib().lina_gpu_synchronize()
+    launches0 = lina.launches()
+    amg.timer_begin()
+    infos = [solve_dev(lina.PCG_TIME_KERNELS) for _ in range(args.steps)]
+    ms = amg.timer_end()
+    launches = lina.launches() - launches0
+    clocks.stop()
+    ms = max_over_ranks(ms, world)
+    value = world * args.steps / (ms / 1e3)
+    it_mixed = [i.iterations for i in infos]
+    trr = max(i.true_rel_residual for i in infos)
+    sm_ms = sum(i.smoother_ms for i in infos)
+    sm_n = sum(i.smoother_launches for i in infos)
+    sm_bytes = infos[0].smoother_bytes
+    peak, peak_kind = measured_peaks()
+    achieved = sm_bytes / (sm_ms / sm_n / 1e3) / 1e9 if sm_n else None
+
+    # end to end through the C-ABI with pinned host buffers
+    hb = lina.PinnedArray(n)
+    hx = lina.PinnedArray(n)
+    hb.array[:] = s.b
+    e2e_ms = []
+    for k in range(args.warmup + args.steps):
+        info = lina.SolveInfo()
+        amg.timer_begin()
+        rc = lina.lib().lina_gpu_pcg(amg.h, hb.ptr, hx.ptr, args.tol, 2000, lina.STOP_RELATIVE, 0,
+                                     ctypes.byref(info))
+        t = amg.timer_end()
+        if rc not in (0, -5):
+            raise RuntimeError(lina.last_error())
+        if k >= args.warmup:
+            e2e_ms.append(t)
+    e2e_value = world * len(e2e_ms) / (max_over_ranks(sum(e2e_ms), world) / 1e3)
+
+    # the same GPU's plain FP64 path on the same hierarchy
+    fp64 = None
+    if not args.no_fp64:
+        amg.set_smoother(smoother, omega, lina.PREC_FP64)
+        for _ in range(max(1, args.warmup)):
+            solve_dev()
+        amg.timer_begin()
+        i64 = [solve_dev(lina.PCG_TIME_KERNELS) for _ in range(args.steps)]
+        ms64 = max_over_ranks(amg.timer_end(), world)
+        sm64 = sum(i.smoother_ms for i in i64) / max(1, sum(i.smoother_launches for i in i64))
+        fp64 = {"value": world * args.steps / (ms64 / 1e3), "unit": "solves/s",
+                "iterations": [i.iterations for i in i64],
+                "true_rel_residual": max(i.true_rel_residual for i in i64),
+                "smoother_gbs": i64[0].smoother_bytes / (sm64 / 1e3) / 1e9 if sm64 else None}
+        amg.set_smoother(smoother, omega, lina.PREC_MIXED)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        full_it = fp64["iterations"][0] if fp64 else it_mixed[0]
+        cpu = cpu_baseline(amg, s, args.smoother, omega, full_it, args.tol, args.cpu_seconds)
+
+    traffic = profiled_traffic()
+    sizes = amg.sizes()
+    out = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 preconditioner / f64 Krylov",
+        "data": "synthetic (seeded structured P1 mesh, notch damage field)",
+        "config": {"workload": f"degraded plane-strain P1 elasticity {m}x{m} nodes, {n} dofs, "
+                               f"AMG-PCG mixed precision to true rel-res {args.tol:g}",
+                   "dofs": n, "nnz": int(s.nnz), "amg_depth": depth, "level_sizes": sizes,
+                   "coarsening": "standard", "smoother": args.smoother, "omega": omega, "sweeps": "2+2",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "inputs exceed L2 (finest matrix > 129 MB), no flush"},
+        "iterations": it_mixed, "true_rel_residual": trr, "dofs_per_s": value * n, "setup_s": setup_s,
+        "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},
+        "gpu_launches": int(launches),
+        "fp64_gpu": fp64,
+        "mixed_vs_fp64": (value / fp64["value"]) if fp64 else None,
+        "roofline": {"bound": "hbm", "kernel": "finest-level FP32 Jacobi sweep (csr_kernel M_JACOBI)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,
+                     "traffic": traffic, "bytes_per_launch": sm_bytes,
+                     "avg_launch_us": (sm_ms / sm_n * 1e3) if sm_n else None},
+        "cpu_baseline": cpu,
+        "clocks": clocks.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(out))
+
+
+def run_reference(args, rank, world):
+    """CPU implementation of the reference solve on the same workload (rank 0 only)."""
+    if rank != 0:
+        return
+    from fem_gb300 import lina
+    from oracle import port
+    m = args.m
+    depth = args.depth or DEFAULT_DEPTH.get(m, 8)
+    omega = args.omega or (0.6 if args.smoother == "jacobi" else 1.0)
+    s = build_system(m)
+    # hierarchy: the library's host setup, identical to the reference's AMG_setup (pinned by tests)
+    amg = lina.AMG.from_system(s, host_only=True, depth=depth, coarsening=lina.STANDARD)
+    kind = port.JACOBI if args.smoother == "jacobi" else port.MC_SOR
+    P = port.PortAMG(port.levels_from_amg(amg), kind, omega, 2, 2)
+    # one full solve fixes the iteration count of the workload
+    t0 = time.perf_counter()
+    _, it_full, _ = P.pcg(s.b, args.tol, 2000, 1, 600.0)
+    t_full = time.perf_counter() - t0
+    per_it = [t_full / max(it_full, 1)]
+    sample_it = 2
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        _, it, _ = P.pcg(s.b, 0.0, sample_it, 1)
+        if k >= args.warmup:
+            per_it.append((time.perf_counter() - t0) / max(it, 1))
+    value = 1.0 / (statistics.median(per_it) * it_full)
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    sample = (f"one full solve ({it_full} iterations, {t_full:.1f} s) plus {args.steps} samples of {sample_it} "
+              f"iterations, scaled to a full solve")
+    out = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded structured P1 mesh, notch damage field)",
+           "impl": "reference",
+           "config": {"workload": f"degraded plane-strain P1 elasticity {m}x{m} nodes, {s.n} dofs, "
+                                  f"AMG-PCG to true rel-res {args.tol:g}", "dofs": s.n, "amg_depth": depth,
+                      "smoother": args.smoother, "omega": omega},
+           "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+_pg = None
+
+
+def init_dist(world):
+    global _pg
+    if world > 1 and _pg is None:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        _pg = dist
+
+
+def barrier(world):
+    if world > 1:
+        _pg.barrier()
+
+
+def max_over_ranks(v, world):
+    if world <= 1:
+        return v
+    import torch
+    t = torch.tensor([float(v)])
+    _pg.all_reduce(t, op=_pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    init_dist(world)
+    if world > 1:
+        from fem_gb300 import lina
+        lina.set_device(local)
+    run_gb300(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

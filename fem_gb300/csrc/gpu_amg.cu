@@ -800,6 +800,11 @@ void lina_gpu_default_options(lina_gpu_amg_options* o) {
 
 const char* lina_gpu_last_error(void) { return g_err.c_str(); }
 
+int lina_gpu_set_device(int device) {
+    CK(cudaSetDevice(device));
+    return 0;
+}
+
 int lina_gpu_device_count(void) {
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;

@@ -91,6 +91,7 @@ def lib():
         "lina_gpu_memcpy_d2h": (C.c_int, [vp, vp, C.c_size_t]),
         "lina_gpu_synchronize": (C.c_int, []),
         "lina_gpu_device_count": (C.c_int, []),
+        "lina_gpu_set_device": (C.c_int, [C.c_int]),
         "lina_gpu_last_error": (C.c_char_p, []),
         "lina_gpu_timer_begin": (C.c_int, [vp]),
         "lina_gpu_timer_end": (C.c_int, [vp, dp]),
@@ -199,6 +200,10 @@ class PinnedArray:
             self.free()
         except Exception:
             pass
+
+
+def set_device(device: int):
+    _check(lib().lina_gpu_set_device(int(device)), "set device")
 
 
 def launches() -> int:

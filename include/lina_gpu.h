@@ -128,6 +128,7 @@ int lina_gpu_synchronize(void);
 void* lina_gpu_malloc_host(size_t bytes);   /* pinned host memory */
 int lina_gpu_free_host(void* p);
 int lina_gpu_device_count(void);
+int lina_gpu_set_device(int device);   /* select the GPU for hierarchies created afterwards */
 
 const char* lina_gpu_last_error(void);
 
