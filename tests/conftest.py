@@ -51,11 +51,20 @@ def load_golden(name):
 
 
 def system_for(name):
-    """Regenerate the input system of a golden case (and check it against the stored digest)."""
+    """The exact input system of a golden case, as the reference received it.
+
+    The stored arrays are used rather than a regeneration because numpy's
+    transcendental functions may differ in the last bit between x86 and Arm
+    hosts (the damage field uses exp); tests/test_problems.py checks that the
+    generator reproduces the stored input.
+    """
     from fem_gb300 import problems
-    from tests.golden.make_golden import CASES, SOLVE_CASES, system_digest
-    factory = (CASES.get(name) or SOLVE_CASES.get(name))[0]
-    s = factory()
     g = load_golden(name)
-    assert str(g["digest"]) == system_digest(s), f"generator output changed for {name}"
-    return s
+    return problems.CSRSystem(int(g["n"]), g["indptr"], g["indices"], g["data"], g["b"], dof=int(g["dof"]),
+                              meta={"golden": name})
+
+
+def regenerate(name):
+    from tests.golden.make_golden import CASES, SOLVE_CASES
+    factory = (CASES.get(name) or SOLVE_CASES.get(name))[0]
+    return factory()

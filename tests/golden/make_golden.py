@@ -99,6 +99,7 @@ def make_solve_case(name):
     amg = ref.RefAMG(s, depth, 2, 2, coarsening)
     out = {"n": np.int64(s.n), "dof": np.int64(s.dof), "depth": np.int64(depth),
            "coarsening": np.int64(coarsening), "digest": np.array(system_digest(s)),
+           "indptr": s.indptr, "indices": s.indices, "data": s.data, "b": s.b,
            "sizes": np.array(amg.sizes(), dtype=np.int64)}
     for sname, (kind, omega) in SMOOTHERS.items():
         if sname == "refsor":
