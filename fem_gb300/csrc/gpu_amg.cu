@@ -48,7 +48,7 @@ void set_err(const char* fmt, ...) {
     } while (0)
 
 constexpr int kThreads = 256;
-constexpr int kMaxBlocks = 2048;      // partials per reduction value
+constexpr int kMaxBlocks = 16384;     // partials per reduction value
 constexpr int kGridCap = 152 * 12;    // grid-stride cap: 152 SMs x 12 blocks of 256
 
 // ---------------------------------------------------------------- reductions
@@ -115,54 +115,60 @@ struct KScalars {
 // ---------------------------------------------------------------- CSR kernels
 enum { M_SPMV = 0, M_RESID = 1, M_JACOBI = 2, M_SOR = 3, M_ADD = 4, M_DOT = 5 };
 
-// One group of S lanes per row; the warp walks rows in grid-stride steps.
+// SELL-32 layout: rows are cut into slices of 32 consecutive rows (of the
+// natural order, or of a colour class); slice s holds its rows' entries
+// column-major, entry k of the row in lane l at sptr[s] + 32 k + l, padded to
+// the longest row of the slice with (own row, 0.0).  One thread per row: the
+// warp's loads of values and column indices are 128-byte coalesced and every
+// load of a row is independent of the others, so many are in flight.  Entries
+// of a row are summed in stored (column) order.
 //  M_SPMV : y = A x
 //  M_RESID: y = b - A x
 //  M_JACOBI: y = x + w dinv (b - A x)              (y != x)
-//  M_SOR  : x = x + w dinv (b - A x) on rows[]      (in place, one colour)
+//  M_SOR  : x = x + w dinv (b - A x) for the rows of one colour (in place)
 //  M_ADD  : y = z + A x                             (z may alias y)
 //  M_DOT  : y = A x, and sum_i x_i y_i -> sc->pq
-template <typename TV, typename TX, int S, int MODE>
-__global__ void __launch_bounds__(kThreads) csr_kernel(int nrows, const int* __restrict__ rows,
-                                                       const int* __restrict__ ptr, const int* __restrict__ col,
-                                                       const TV* __restrict__ val, const TX* x, TX* y,
-                                                       const TX* __restrict__ b, const TX* __restrict__ dinv, TX w,
-                                                       const TX* z, double* partials, unsigned* ticket,
-                                                       KScalars* sc) {
-    const int lane = threadIdx.x & 31;
-    const int sub = lane & (S - 1);
-    const int groups_per_warp = 32 / S;
-    const long warp_global = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const long nwarps = ((long)gridDim.x * blockDim.x) >> 5;
+template <typename TV, typename TX, int MODE>
+__global__ void __launch_bounds__(kThreads) sell_kernel(int npos, const int* __restrict__ rowmap,
+                                                        const int* __restrict__ sptr, const int* __restrict__ col,
+                                                        const TV* __restrict__ val, const TX* x, TX* y,
+                                                        const TX* __restrict__ b, const TX* __restrict__ dinv, TX w,
+                                                        const TX* z, double* partials, unsigned* ticket,
+                                                        KScalars* sc) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     double dot = 0.0;
-    for (long gb = warp_global * groups_per_warp; gb < nrows; gb += nwarps * groups_per_warp) {
-        const long g = gb + lane / S;
-        const bool valid = g < nrows;
-        int i = 0, s = 0, e = 0;
-        if (valid) {
-            i = rows ? rows[g] : (int)g;
-            s = ptr[i];
-            e = ptr[i + 1];
-        }
+    int i = -1;
+    if (t < npos) i = rowmap ? rowmap[t] : t;
+    if (i >= 0) {
+        const int sl = t >> 5, lane = t & 31;
+        const int p0 = sptr[sl];
+        const int len = (sptr[sl + 1] - p0) >> 5;
+        const int* cp = col + p0 + lane;
+        const TV* vp = val + p0 + lane;
         TX sum = TX(0);
-        for (int k = s + sub; k < e; k += S) sum += TX(val[k]) * x[col[k]];
-#pragma unroll
-        for (int o = S / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, S);
-        if (valid && sub == 0) {
-            if constexpr (MODE == M_SPMV) {
-                y[i] = sum;
-            } else if constexpr (MODE == M_RESID) {
-                y[i] = b[i] - sum;
-            } else if constexpr (MODE == M_JACOBI) {
-                y[i] = x[i] + w * dinv[i] * (b[i] - sum);
-            } else if constexpr (MODE == M_SOR) {
-                y[i] = x[i] + w * dinv[i] * (b[i] - sum);
-            } else if constexpr (MODE == M_ADD) {
-                y[i] = z[i] + sum;
-            } else if constexpr (MODE == M_DOT) {
-                y[i] = sum;
-                dot += double(x[i]) * double(sum);
-            }
+        int k = 0;
+        for (; k + 4 <= len; k += 4) {
+            const int c0 = cp[32 * k], c1 = cp[32 * (k + 1)], c2 = cp[32 * (k + 2)], c3 = cp[32 * (k + 3)];
+            const TX v0 = TX(vp[32 * k]), v1 = TX(vp[32 * (k + 1)]), v2 = TX(vp[32 * (k + 2)]),
+                     v3 = TX(vp[32 * (k + 3)]);
+            const TX x0 = x[c0], x1 = x[c1], x2 = x[c2], x3 = x[c3];
+            sum += v0 * x0;
+            sum += v1 * x1;
+            sum += v2 * x2;
+            sum += v3 * x3;
+        }
+        for (; k < len; k++) sum += TX(vp[32 * k]) * x[cp[32 * k]];
+        if constexpr (MODE == M_SPMV) {
+            y[i] = sum;
+        } else if constexpr (MODE == M_RESID) {
+            y[i] = b[i] - sum;
+        } else if constexpr (MODE == M_JACOBI || MODE == M_SOR) {
+            y[i] = x[i] + w * dinv[i] * (b[i] - sum);
+        } else if constexpr (MODE == M_ADD) {
+            y[i] = z[i] + sum;
+        } else if constexpr (MODE == M_DOT) {
+            y[i] = sum;
+            dot = double(x[i]) * double(sum);
         }
     }
     if constexpr (MODE == M_DOT) {
@@ -309,24 +315,76 @@ __global__ void __launch_bounds__(kThreads) norm2_kernel(int n, const T* __restr
 // ======================================================================= host
 namespace {
 
+// a matrix on the device in SELL-32 layout (see sell_kernel)
 struct DCsr {
     int n = 0, ncols = 0;
-    long nnz = 0;
-    int* ptr = nullptr;
+    long nnz = 0;        // stored entries of the CSR source
+    long padded = 0;     // entries including slice padding
+    int npos = 0;        // slice positions (multiple of 32)
+    int* sptr = nullptr;
     int* col = nullptr;
     double* v64 = nullptr;
     float* v32 = nullptr;
-    int lanes = 8;
+    int* rowmap = nullptr;          // row of each position (-1 = padding), null = natural order
+    std::vector<int> group_slice;   // colour c occupies slices [group_slice[c], group_slice[c+1])
 };
+
+// Host-side SELL-32 construction; `order` lists the rows per group (colour)
+// and each group starts on a slice boundary.  Without groups the natural row
+// order is used.
+struct SellHost {
+    std::vector<int> sptr{0}, col, rowmap;
+    std::vector<double> val;
+    std::vector<int> group_slice{0};
+};
+
+SellHost make_sell(const lina::Csr& A, const std::vector<std::vector<int>>* groups) {
+    SellHost S;
+    auto add_group = [&](const int* rows, int nr) {
+        for (int base = 0; base < nr; base += 32) {
+            int len = 0;
+            for (int l = 0; l < 32 && base + l < nr; l++) {
+                int r = rows ? rows[base + l] : base + l;
+                len = std::max(len, A.ptr[r + 1] - A.ptr[r]);
+            }
+            const size_t off = S.col.size();
+            S.col.resize(off + 32 * (size_t)len);
+            S.val.resize(off + 32 * (size_t)len);
+            for (int l = 0; l < 32; l++) {
+                const bool valid = base + l < nr;
+                const int r = valid ? (rows ? rows[base + l] : base + l) : -1;
+                const int rl = valid ? A.ptr[r + 1] - A.ptr[r] : 0;
+                for (int k = 0; k < len; k++) {
+                    const size_t q = off + 32 * (size_t)k + l;
+                    if (k < rl) {
+                        S.col[q] = A.col[A.ptr[r] + k];
+                        S.val[q] = A.val[A.ptr[r] + k];
+                    } else {
+                        S.col[q] = valid ? r : 0;
+                        S.val[q] = 0.0;
+                    }
+                }
+                S.rowmap.push_back(r);
+            }
+            S.sptr.push_back((int)S.col.size());
+        }
+        S.group_slice.push_back((int)S.sptr.size() - 1);
+    };
+    if (groups) {
+        for (const auto& g : *groups) add_group(g.data(), (int)g.size());
+    } else {
+        add_group(nullptr, A.n);
+    }
+    return S;
+}
 
 struct DLevel {
     int n = 0;
     DCsr A, P, R;
+    DCsr Acol;  // rows grouped by colour (multicolour SOR)
     double* dinv64 = nullptr;
     float* dinv32 = nullptr;
     int ncolours = 0;
-    std::vector<int> cptr;
-    int* crows = nullptr;
     double *x64 = nullptr, *t64 = nullptr, *b64 = nullptr, *r64 = nullptr;
     float *x32 = nullptr, *t32 = nullptr, *b32 = nullptr, *r32 = nullptr;
 };
@@ -337,14 +395,6 @@ template <typename... KA, typename... A>
 void go(void (*k)(KA...), int grid, cudaStream_t st, A... a) {
     g_launches++;
     k<<<grid, kThreads, 0, st>>>(a...);
-}
-
-int lanes_for(long nnz, int n) {
-    double avg = n > 0 ? double(nnz) / n : 1.0;
-    if (avg <= 6.0) return 4;
-    if (avg <= 12.0) return 8;
-    if (avg <= 24.0) return 16;
-    return 32;
 }
 
 int grid_for(long items, int per_block) {
@@ -430,18 +480,33 @@ struct lina_gpu_amg {
         if (count) CK(cudaMemcpyAsync(*p, src, count * sizeof(T), cudaMemcpyHostToDevice, stream));
         return 0;
     }
-    int upload_csr(DCsr& d, const lina::Csr& c) {
+    int upload_csr(DCsr& d, const lina::Csr& c, const std::vector<std::vector<int>>* groups = nullptr) {
+        d = DCsr();
         d.n = c.n;
         d.ncols = c.ncols;
         d.nnz = c.nnz();
-        d.lanes = lanes_for(d.nnz, d.n);
-        std::vector<float> v32(c.val.begin(), c.val.end());
+        if (c.nnz() > (long)INT_MAX / 2) {
+            set_err("matrix too large for 32-bit SELL offsets");
+            return LINA_GPU_EINVAL;
+        }
+        SellHost S = make_sell(c, groups);
+        if (S.col.size() > (size_t)INT_MAX) {
+            set_err("padded matrix too large for 32-bit SELL offsets");
+            return LINA_GPU_EINVAL;
+        }
+        d.padded = (long)S.col.size();
+        d.npos = (int)S.rowmap.size();
+        d.group_slice = S.group_slice;
+        std::vector<float> v32(S.val.begin(), S.val.end());
         int rc;
-        if ((rc = upload(&d.ptr, c.ptr.data(), c.ptr.size()))) return rc;
-        if ((rc = upload(&d.col, c.col.data(), c.col.size()))) return rc;
-        if ((rc = upload(&d.v64, c.val.data(), c.val.size()))) return rc;
+        if ((rc = upload(&d.sptr, S.sptr.data(), S.sptr.size()))) return rc;
+        if ((rc = upload(&d.col, S.col.data(), S.col.size()))) return rc;
+        if ((rc = upload(&d.v64, S.val.data(), S.val.size()))) return rc;
         if ((rc = upload(&d.v32, v32.data(), v32.size()))) return rc;
-        // the float copy must outlive the async copy
+        if (groups) {
+            if ((rc = upload(&d.rowmap, S.rowmap.data(), S.rowmap.size()))) return rc;
+        }
+        // the host copies must outlive the asynchronous uploads
         return cudaStreamSynchronize(stream) == cudaSuccess ? 0 : LINA_GPU_ECUDA;
     }
 
@@ -465,35 +530,37 @@ struct lina_gpu_amg {
 
     // ------------------------------------------------------------ kernels
     template <typename TV, typename TX, int MODE>
-    void launch_csr_t(const DCsr& m, const TV* val, int nrows, const int* rows, const TX* x, TX* y, const TX* b,
-                      const TX* dinv, TX w, const TX* z) {
-        const int S = m.lanes;
-        const int groups = kThreads / S;
+    void launch_sell_t(const DCsr& m, const TV* val, int slice0, int slice1, const TX* x, TX* y, const TX* b,
+                       const TX* dinv, TX w, const TX* z) {
+        const int npos = (slice1 - slice0) * 32;
+        if (npos <= 0) return;
+        const int grid = (npos + kThreads - 1) / kThreads;
         g_launches++;
-        int grid = (MODE == M_DOT) ? grid_red((long)nrows * S) : grid_for(nrows, groups);
-        if (MODE == M_DOT) grid = std::min(grid, kMaxBlocks);
-#define LINA_CSR_CASE(SS)                                                                                     \
-    case SS:                                                                                                  \
-        csr_kernel<TV, TX, SS, MODE><<<grid, kThreads, 0, stream>>>(nrows, rows, m.ptr, m.col, val, x, y, b, \
-                                                                    dinv, w, z, partials, ticket, sc);       \
-        break;
-        switch (S) {
-            LINA_CSR_CASE(4)
-            LINA_CSR_CASE(8)
-            LINA_CSR_CASE(16)
-            default:
-                LINA_CSR_CASE(32)
-        }
-#undef LINA_CSR_CASE
+        sell_kernel<TV, TX, MODE><<<grid, kThreads, 0, stream>>>(
+            npos, m.rowmap ? m.rowmap + (size_t)slice0 * 32 : nullptr, m.sptr + slice0, m.col, val, x, y, b, dinv,
+            w, z, partials, ticket, sc);
     }
 
+    // all rows of m (natural order)
     template <typename TX, int MODE>
-    void csr(const DCsr& m, int nrows, const int* rows, const TX* x, TX* y, const TX* b = nullptr,
-             const TX* dinv = nullptr, TX w = TX(0), const TX* z = nullptr) {
+    void csr(const DCsr& m, const TX* x, TX* y, const TX* b = nullptr, const TX* dinv = nullptr, TX w = TX(0),
+             const TX* z = nullptr) {
+        const int ns = (int)m.group_slice.back();
         if constexpr (sizeof(TX) == 8)
-            launch_csr_t<double, TX, MODE>(m, m.v64, nrows, rows, x, y, b, dinv, w, z);
+            launch_sell_t<double, TX, MODE>(m, m.v64, 0, ns, x, y, b, dinv, w, z);
         else
-            launch_csr_t<float, TX, MODE>(m, m.v32, nrows, rows, x, y, b, dinv, w, z);
+            launch_sell_t<float, TX, MODE>(m, m.v32, 0, ns, x, y, b, dinv, w, z);
+    }
+
+    // the rows of colour c of a colour-grouped matrix
+    template <typename TX, int MODE>
+    void csr_group(const DCsr& m, int c, const TX* x, TX* y, const TX* b, const TX* dinv, TX w) {
+        if constexpr (sizeof(TX) == 8)
+            launch_sell_t<double, TX, MODE>(m, m.v64, m.group_slice[c], m.group_slice[c + 1], x, y, b, dinv, w,
+                                            nullptr);
+        else
+            launch_sell_t<float, TX, MODE>(m, m.v32, m.group_slice[c], m.group_slice[c + 1], x, y, b, dinv, w,
+                                           nullptr);
     }
 
     // ------------------------------------------------------------ V-cycle
@@ -540,7 +607,7 @@ struct lina_gpu_amg {
                 TX* nxt = (cur == x) ? t : x;
                 cudaEvent_t e0;
                 if (time_it) ev_record_pair_start(&e0);
-                csr<TX, M_JACOBI>(L.A, L.n, nullptr, cur, nxt, b, dinv, w);
+                csr<TX, M_JACOBI>(L.A, cur, nxt, b, dinv, w);
                 if (time_it) ev_record_pair_end();
                 cur = nxt;
             }
@@ -554,11 +621,9 @@ struct lina_gpu_amg {
     void sor_sweep(DLevel& L, const TX* b, TX* x, bool time_it) {
         const TX w = TX(opt.omega);
         for (int c = 0; c < L.ncolours; c++) {
-            int cnt = L.cptr[c + 1] - L.cptr[c];
-            if (cnt == 0) continue;
             cudaEvent_t e0;
             if (time_it) ev_record_pair_start(&e0);
-            csr<TX, M_SOR>(L.A, cnt, L.crows + L.cptr[c], x, x, b, lvdinv<TX>(L), w);
+            csr_group<TX, M_SOR>(L.Acol, c, x, x, b, lvdinv<TX>(L), w);
             if (time_it) ev_record_pair_end();
         }
     }
@@ -571,17 +636,17 @@ struct lina_gpu_amg {
         TX* t = lvx<TX>(L, 1);
         if (opt.smoother == LINA_SMOOTHER_JACOBI) {
             TX* cur = (nu % 2 == 0) ? x : t;
-            csr<TX, M_ADD>(L.P, L.n, nullptr, e, cur, nullptr, nullptr, TX(0), x);
+            csr<TX, M_ADD>(L.P, e, cur, nullptr, nullptr, TX(0), x);
             for (int k = 0; k < nu; k++) {
                 TX* nxt = (cur == x) ? t : x;
                 cudaEvent_t e0;
                 if (time_it) ev_record_pair_start(&e0);
-                csr<TX, M_JACOBI>(L.A, L.n, nullptr, cur, nxt, b, dinv, w);
+                csr<TX, M_JACOBI>(L.A, cur, nxt, b, dinv, w);
                 if (time_it) ev_record_pair_end();
                 cur = nxt;
             }
         } else {
-            csr<TX, M_ADD>(L.P, L.n, nullptr, e, x, nullptr, nullptr, TX(0), x);
+            csr<TX, M_ADD>(L.P, e, x, nullptr, nullptr, TX(0), x);
             for (int k = 0; k < nu; k++) sor_sweep(L, b, x, time_it);
         }
         (void)l;
@@ -606,8 +671,8 @@ struct lina_gpu_amg {
         DLevel& C = lv[l - 1];
         TX* cb = lvx<TX>(C, 2);
         TX* cx = lvx<TX>(C, 0);
-        csr<TX, M_RESID>(L.A, L.n, nullptr, x, r, b);
-        csr<TX, M_SPMV>(L.R, C.n, nullptr, r, cb);
+        csr<TX, M_RESID>(L.A, x, r, b);
+        csr<TX, M_SPMV>(L.R, r, cb);
         vcycle_level<TX>(l - 1, cb, cx, false);
         correct_and_postsmooth<TX>(l, L, nu, b, x, cx, time_it);
     }
@@ -670,14 +735,9 @@ int upload_hierarchy(lina_gpu_amg* h) {
             if ((rc = h->upload_csr(L.R, hl.R))) return rc;
             std::vector<int> colour;
             L.ncolours = lina::greedy_colouring(hl.A, colour);
-            L.cptr.assign(L.ncolours + 1, 0);
-            for (int c : colour) L.cptr[c + 1]++;
-            for (int c = 0; c < L.ncolours; c++) L.cptr[c + 1] += L.cptr[c];
-            std::vector<int> rows(L.n);
-            std::vector<int> fill(L.cptr.begin(), L.cptr.end() - 1);
-            for (int i = 0; i < L.n; i++) rows[fill[colour[i]]++] = i;
-            if ((rc = h->upload(&L.crows, rows.data(), rows.size()))) return rc;
-            CK(cudaStreamSynchronize(h->stream));
+            std::vector<std::vector<int>> groups(L.ncolours);
+            for (int i = 0; i < L.n; i++) groups[colour[i]].push_back(i);
+            if ((rc = h->upload_csr(L.Acol, hl.A, &groups))) return rc;
         }
         // work vectors
         if ((rc = h->alloc(&L.x64, L.n))) return rc;
@@ -767,7 +827,7 @@ bool valid_csr(int n, const int* rowptr, const int* col) {
 // true residual b - A x (FP64), norm into sc->norm2; result left in kt
 int true_residual(lina_gpu_amg* h, const double* b, const double* x) {
     const DCsr& A = h->krylov_matrix();
-    h->csr<double, M_RESID>(A, A.n, nullptr, x, h->kt, b);
+    h->csr<double, M_RESID>(A, x, h->kt, b);
     go(norm2_kernel<double>, grid_red(A.n), h->stream, A.n, h->kt, h->partials, h->ticket, h->sc);
     return 0;
 }
@@ -935,7 +995,7 @@ int lina_gpu_spmv(lina_gpu_amg* h, int level, const double* x_dev, double* y_dev
         return LINA_GPU_EINVAL;
     }
     const DCsr& A = h->lv[level].A;
-    h->csr<double, M_SPMV>(A, A.n, nullptr, x_dev, y_dev);
+    h->csr<double, M_SPMV>(A, x_dev, y_dev);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(h->stream));
     return 0;
@@ -988,7 +1048,7 @@ int lina_gpu_pcg(lina_gpu_amg* h, const double* b_in, double* x_out, double tol,
     }
     // r = b - A x
     const DCsr& A = h->krylov_matrix();
-    h->csr<double, M_RESID>(A, n, nullptr, x, r, b);
+    h->csr<double, M_RESID>(A, x, r, b);
     // w = M^-1 r (kept as the first z)
     auto zptr_norm = [&]() {
         if (mixed)
@@ -1033,7 +1093,7 @@ int lina_gpu_pcg(lina_gpu_amg* h, const double* b_in, double* x_out, double tol,
                 go(update_p_kernel<float>, gv, st, n, h->kz32, p, flexible, h->sc);
             else
                 go(update_p_kernel<double>, gv, st, n, z, p, flexible, h->sc);
-            h->csr<double, M_DOT>(A, n, nullptr, p, q);
+            h->csr<double, M_DOT>(A, p, q);
             go(update_xr_kernel, gr, st, n, x, r, p, q, h->partials, h->ticket, h->sc);
             CK(cudaGetLastError());
             if (read_scalars(h)) return LINA_GPU_ECUDA;

@@ -75,8 +75,11 @@ def test_pcg_mixed_precision(name, smoother):
     amg.set_smoother(SMOOTHERS[smoother][0], SMOOTHERS[smoother][1], lina.PREC_FP64)
     x64, info64 = amg.pcg(s.b, tol=1e-8, max_iter=1000, stop=lina.STOP_RELATIVE)
     assert info.iterations <= max(int(1.1 * info64.iterations) + 1, info64.iterations + 2)
+    # error against the accurate reference solution: 1e-7, or within 10x of what the FP64
+    # path reaches at the same residual where the system's conditioning allows no better
     xt = g["x_tight"]
-    assert rel(x, xt) < 1e-7 * max(1.0, 10 * rel(x64, xt) / 1e-7) if rel(x64, xt) > 1e-7 else rel(x, xt) < 1e-7
+    err, err64 = rel(x, xt), rel(x64, xt)
+    assert err <= max(1e-7, 10 * err64), (err, err64)
 
 
 @pytest.mark.parametrize("name", golden_cases("hierarchy"))
