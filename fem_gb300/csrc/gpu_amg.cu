@@ -338,7 +338,9 @@ struct SellHost {
     std::vector<int> group_slice{0};
 };
 
-SellHost make_sell(const lina::Csr& A, const std::vector<std::vector<int>>* groups) {
+// Padding entries repeat a column the row already uses (or column 0 for an
+// empty row), so every gathered index lies inside the input vector.
+SellHost make_sell(const lina::Csr& A, int ncols, const std::vector<std::vector<int>>* groups) {
     SellHost S;
     auto add_group = [&](const int* rows, int nr) {
         for (int base = 0; base < nr; base += 32) {
@@ -354,13 +356,21 @@ SellHost make_sell(const lina::Csr& A, const std::vector<std::vector<int>>* grou
                 const bool valid = base + l < nr;
                 const int r = valid ? (rows ? rows[base + l] : base + l) : -1;
                 const int rl = valid ? A.ptr[r + 1] - A.ptr[r] : 0;
+                int pad_col = 0;
+                for (int k = 0; k < rl; k++)
+                    if (A.col[A.ptr[r] + k] < ncols) {
+                        pad_col = A.col[A.ptr[r] + k];
+                        break;
+                    }
                 for (int k = 0; k < len; k++) {
                     const size_t q = off + 32 * (size_t)k + l;
-                    if (k < rl) {
+                    if (k < rl && A.col[A.ptr[r] + k] < ncols) {
                         S.col[q] = A.col[A.ptr[r] + k];
                         S.val[q] = A.val[A.ptr[r] + k];
                     } else {
-                        S.col[q] = valid ? r : 0;
+                        // padding, or an explicit zero whose column lies outside the
+                        // operand (the reference's (i, 0.0) placeholder of an empty row)
+                        S.col[q] = pad_col;
                         S.val[q] = 0.0;
                     }
                 }
@@ -489,7 +499,13 @@ struct lina_gpu_amg {
             set_err("matrix too large for 32-bit SELL offsets");
             return LINA_GPU_EINVAL;
         }
-        SellHost S = make_sell(c, groups);
+        const int ncols = c.ncols > 0 ? c.ncols : c.n;
+        for (size_t k = 0; k < c.col.size(); k++)
+            if (c.col[k] < 0 || (c.col[k] >= ncols && c.val[k] != 0.0)) {
+                set_err("matrix entry with column %d outside [0, %d)", c.col[k], ncols);
+                return LINA_GPU_EINVAL;
+            }
+        SellHost S = make_sell(c, ncols, groups);
         if (S.col.size() > (size_t)INT_MAX) {
             set_err("padded matrix too large for 32-bit SELL offsets");
             return LINA_GPU_EINVAL;
