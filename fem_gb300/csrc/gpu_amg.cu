@@ -1215,6 +1215,113 @@ int lina_gpu_free_host(void* p) {
     return 0;
 }
 
+// ------------------------------------------------------------ single matrices
+// A standalone matrix on the device (SELL-32, FP64 and FP32 values) with the
+// same kernels as the hierarchy levels; it reuses the hierarchy machinery with
+// a one-level, setup-free handle.
+struct lina_gpu_matrix {
+    lina_gpu_amg* h = nullptr;
+    DCsr A;
+    double* dinv64 = nullptr;
+    float* dinv32 = nullptr;
+};
+
+int lina_gpu_matrix_create(int n, int ncols, const int* rowptr, const int* col, const double* val,
+                           lina_gpu_matrix** out) {
+    if (!out || n <= 0 || ncols <= 0 || !rowptr || !col || !val || rowptr[0] != 0) {
+        set_err("lina_gpu_matrix_create: invalid argument");
+        return LINA_GPU_EINVAL;
+    }
+    for (int i = 0; i < n; i++)
+        if (rowptr[i + 1] < rowptr[i]) {
+            set_err("lina_gpu_matrix_create: row pointers decrease at row %d", i);
+            return LINA_GPU_EINVAL;
+        }
+    *out = nullptr;
+    lina_gpu_matrix* m = new lina_gpu_matrix();
+    m->h = new lina_gpu_amg();
+    lina_gpu_amg* h = m->h;
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        set_err("cudaStreamCreate failed");
+        delete h;
+        delete m;
+        return LINA_GPU_ECUDA;
+    }
+    lina::Csr c;
+    c.n = n;
+    c.ncols = ncols;
+    c.ptr.assign(rowptr, rowptr + n + 1);
+    c.col.assign(col, col + rowptr[n]);
+    c.val.assign(val, val + rowptr[n]);
+    std::vector<double> dinv(n, 0.0);
+    for (int i = 0; i < n; i++)
+        for (int p = c.ptr[i]; p < c.ptr[i + 1]; p++)
+            if (c.col[p] == i && c.val[p] != 0.0) dinv[i] = 1.0 / c.val[p];
+    std::vector<float> dinv32(dinv.begin(), dinv.end());
+    int rc = h->upload_csr(m->A, c);
+    if (!rc) rc = h->upload(&m->dinv64, dinv.data(), dinv.size());
+    if (!rc) rc = h->upload(&m->dinv32, dinv32.data(), dinv32.size());
+    if (!rc) rc = h->alloc(&h->partials, 2 * kMaxBlocks);
+    if (!rc) rc = h->alloc(&h->ticket, 4);
+    if (!rc) rc = h->alloc(&h->sc, 1);
+    if (!rc && cudaMemsetAsync(h->ticket, 0, 4 * sizeof(unsigned), h->stream) != cudaSuccess) rc = LINA_GPU_ECUDA;
+    if (!rc && cudaStreamSynchronize(h->stream) != cudaSuccess) rc = LINA_GPU_ECUDA;
+    if (rc) {
+        delete h;
+        delete m;
+        return rc;
+    }
+    *out = m;
+    return 0;
+}
+
+int lina_gpu_matrix_destroy(lina_gpu_matrix* m) {
+    if (m) {
+        delete m->h;
+        delete m;
+    }
+    return 0;
+}
+
+int lina_gpu_matrix_spmv(lina_gpu_matrix* m, int precision, const void* x_dev, void* y_dev) {
+    if (!m || !x_dev || !y_dev) {
+        set_err("lina_gpu_matrix_spmv: invalid argument");
+        return LINA_GPU_EINVAL;
+    }
+    if (precision == LINA_PREC_MIXED)
+        m->h->csr<float, M_SPMV>(m->A, (const float*)x_dev, (float*)y_dev);
+    else
+        m->h->csr<double, M_SPMV>(m->A, (const double*)x_dev, (double*)y_dev);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(m->h->stream));
+    return 0;
+}
+
+int lina_gpu_matrix_jacobi(lina_gpu_matrix* m, int precision, double omega, int sweeps, const void* b_dev,
+                           void* x_dev, void* tmp_dev) {
+    if (!m || !b_dev || !x_dev || !tmp_dev || sweeps < 0) {
+        set_err("lina_gpu_matrix_jacobi: invalid argument");
+        return LINA_GPU_EINVAL;
+    }
+    for (int k = 0; k < sweeps; k++) {
+        const bool even = (k % 2 == 0);
+        if (precision == LINA_PREC_MIXED) {
+            const float* xi = (const float*)(even ? x_dev : tmp_dev);
+            float* xo = (float*)(even ? tmp_dev : x_dev);
+            m->h->csr<float, M_JACOBI>(m->A, xi, xo, (const float*)b_dev, m->dinv32, (float)omega);
+        } else {
+            const double* xi = (const double*)(even ? x_dev : tmp_dev);
+            double* xo = (double*)(even ? tmp_dev : x_dev);
+            m->h->csr<double, M_JACOBI>(m->A, xi, xo, (const double*)b_dev, m->dinv64, omega);
+        }
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(m->h->stream));
+    return 0;
+}
+
+long lina_gpu_matrix_padded_entries(const lina_gpu_matrix* m) { return m ? m->A.padded : 0; }
+
 int lina_gpu_amg_depth(const lina_gpu_amg* h) { return h ? h->depth : 0; }
 
 int lina_gpu_level_sizes(const lina_gpu_amg* h, int level, int* n, long* nnz_A, long* nnz_P, long* nnz_R,

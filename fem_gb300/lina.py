@@ -97,6 +97,11 @@ def lib():
         "lina_gpu_timer_end": (C.c_int, [vp, dp]),
         "lina_gpu_launches": (C.c_ulonglong, []),
         "lina_gpu_malloc_host": (vp, [C.c_size_t]),
+        "lina_gpu_matrix_create": (C.c_int, [C.c_int, C.c_int, ip, ip, dp, C.POINTER(vp)]),
+        "lina_gpu_matrix_destroy": (C.c_int, [vp]),
+        "lina_gpu_matrix_spmv": (C.c_int, [vp, C.c_int, vp, vp]),
+        "lina_gpu_matrix_jacobi": (C.c_int, [vp, C.c_int, C.c_double, C.c_int, vp, vp, vp]),
+        "lina_gpu_matrix_padded_entries": (C.c_long, [vp]),
         "lina_gpu_free_host": (C.c_int, [vp]),
     }
     for name, (res, args) in sig.items():
@@ -208,6 +213,57 @@ def set_device(device: int):
 
 def launches() -> int:
     return int(lib().lina_gpu_launches())
+
+
+class Matrix:
+    """A single device matrix (SELL-32) with the library's SpMV and Jacobi kernels."""
+
+    def __init__(self, n, indptr, indices, data, ncols=None):
+        self.n = int(n)
+        self.ncols = int(ncols or n)
+        ip_ = np.ascontiguousarray(indptr, dtype=np.int32)
+        ix_ = np.ascontiguousarray(indices, dtype=np.int32)
+        dv_ = np.ascontiguousarray(data, dtype=np.float64)
+        h = C.c_void_p()
+        _check(lib().lina_gpu_matrix_create(self.n, self.ncols, _ip(ip_), _ip(ix_), _dp(dv_), C.byref(h)),
+               "matrix create")
+        self.h = h
+
+    @property
+    def padded_entries(self):
+        return lib().lina_gpu_matrix_padded_entries(self.h)
+
+    def spmv_device(self, x: DeviceArray, y: DeviceArray, precision=PREC_FP64):
+        _check(lib().lina_gpu_matrix_spmv(self.h, precision, x.ptr, y.ptr), "matrix spmv")
+
+    def spmv(self, x, precision=PREC_FP64):
+        dt = np.float32 if precision == PREC_MIXED else np.float64
+        xd = DeviceArray.from_host(np.asarray(x, dtype=dt))
+        yd = DeviceArray(self.n, dt)
+        self.spmv_device(xd, yd, precision)
+        return yd.to_host()
+
+    def jacobi_device(self, b: DeviceArray, x: DeviceArray, tmp: DeviceArray, omega, sweeps, precision=PREC_FP64):
+        _check(lib().lina_gpu_matrix_jacobi(self.h, precision, omega, sweeps, b.ptr, x.ptr, tmp.ptr), "jacobi")
+
+    def jacobi(self, b, x0, omega, sweeps, precision=PREC_FP64):
+        dt = np.float32 if precision == PREC_MIXED else np.float64
+        bd = DeviceArray.from_host(np.asarray(b, dtype=dt))
+        xd = DeviceArray.from_host(np.asarray(x0, dtype=dt))
+        td = DeviceArray(self.n, dt)
+        self.jacobi_device(bd, xd, td, omega, sweeps, precision)
+        return (td if sweeps % 2 else xd).to_host()
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().lina_gpu_matrix_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class AMG:

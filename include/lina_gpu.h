@@ -102,6 +102,21 @@ int lina_gpu_vcycle(lina_gpu_amg* h, const double* r_dev, double* z_dev);
 /* y = A_level x on the device (level = depth-1 is the finest) */
 int lina_gpu_spmv(lina_gpu_amg* h, int level, const double* x_dev, double* y_dev);
 
+/* A single matrix on the device (the SpMV and smoother kernels without a hierarchy).
+   Vectors are device pointers of FP64 (LINA_PREC_FP64) or FP32 (LINA_PREC_MIXED) elements. */
+typedef struct lina_gpu_matrix lina_gpu_matrix;
+int lina_gpu_matrix_create(int n, int ncols, const int* rowptr, const int* col, const double* val,
+                           lina_gpu_matrix** out);
+int lina_gpu_matrix_destroy(lina_gpu_matrix* m);
+/* y = A x */
+int lina_gpu_matrix_spmv(lina_gpu_matrix* m, int precision, const void* x_dev, void* y_dev);
+/* `sweeps` damped Jacobi sweeps x <- x + w D^-1 (b - A x); tmp is a work vector; after an odd
+   number of sweeps the result is in tmp, after an even number in x */
+int lina_gpu_matrix_jacobi(lina_gpu_matrix* m, int precision, double omega, int sweeps, const void* b_dev,
+                           void* x_dev, void* tmp_dev);
+/* stored entries including the SELL-32 slice padding */
+long lina_gpu_matrix_padded_entries(const lina_gpu_matrix* m);
+
 /* CUDA-event timing on the hierarchy's stream: elapsed milliseconds between begin and end */
 int lina_gpu_timer_begin(lina_gpu_amg* h);
 int lina_gpu_timer_end(lina_gpu_amg* h, double* ms);

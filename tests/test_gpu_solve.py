@@ -104,3 +104,36 @@ def test_device_pointer_solve_equals_host_solve():
     idev = amg.pcg_device(bd, xd, tol=1e-8, stop=lina.STOP_RELATIVE)
     assert idev.iterations == ih.iterations
     assert np.array_equal(xd.to_host(), xh)  # deterministic reductions
+
+
+@pytest.mark.parametrize("prec", [lina.PREC_FP64, lina.PREC_MIXED])
+def test_matrix_spmv_and_jacobi(prec):
+    from fem_gb300 import problems
+    s = problems.elasticity_p1(33)
+    A = sp.csr_matrix((s.data, s.indices, s.indptr), shape=(s.n, s.n))
+    M = lina.Matrix(s.n, s.indptr, s.indices, s.data)
+    rng = np.random.default_rng(2)
+    x = rng.uniform(-1, 1, s.n)
+    tol = 1e-14 if prec == lina.PREC_FP64 else 1e-6
+    assert rel(M.spmv(x, prec), A @ x) < tol
+    # two damped Jacobi sweeps against the plain formula x <- x + w D^-1 (b - A x)
+    d = A.diagonal()
+    y = x.copy()
+    for _ in range(2):
+        y = y + 0.6 * (s.b - A @ y) / d
+    assert rel(M.jacobi(s.b, x, 0.6, 2, prec), y) < (1e-13 if prec == lina.PREC_FP64 else 1e-5)
+
+
+def test_rectangular_prolongation_stays_in_bounds():
+    """P (fine x coarse) with rows of different lengths: the padded SELL entries must only
+    gather coarse-vector entries (checked through the result on a coarse vector of ones)."""
+    s, g, amg = _amg("elast17_std")
+    l = int(g["depth"]) - 1
+    ptr, col, val = g[f"L{l}_P_ptr"], g[f"L{l}_P_col"], g[f"L{l}_P_val"]
+    nc = len(g[f"L{l}_R_ptr"]) - 1
+    M = lina.Matrix(len(ptr) - 1, ptr, col, val, ncols=nc)
+    e = np.ones(nc)
+    keep = col < nc
+    assert np.all(val[~keep] == 0.0)
+    P = sp.csr_matrix((np.where(keep, val, 0.0), np.where(keep, col, 0), ptr), shape=(len(ptr) - 1, nc))
+    assert rel(M.spmv(e), P @ e) < 1e-14
