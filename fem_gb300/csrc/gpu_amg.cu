@@ -28,6 +28,7 @@ namespace {
 
 std::string g_err;
 unsigned long long g_launches = 0;  // kernels launched by this library (all handles)
+int g_layout = 0;                   // 0 automatic, 1 SELL-32 everywhere, 2 CSR-vector everywhere
 
 void set_err(const char* fmt, ...) {
     char buf[512];
@@ -169,6 +170,56 @@ __global__ void __launch_bounds__(kThreads) sell_kernel(int npos, const int* __r
         } else if constexpr (MODE == M_DOT) {
             y[i] = sum;
             dot = double(x[i]) * double(sum);
+        }
+    }
+    if constexpr (MODE == M_DOT) {
+        double v[1] = {dot};
+        grid_reduce<1>(v, partials, ticket, [sc](double* t) { sc->pq = t[0]; });
+    }
+}
+
+// CSR with a group of S lanes per row, for levels whose rows are long (dense
+// coarse operators) or too few to fill the GPU one thread per row.  Lanes of a
+// group read consecutive entries of their row (coalesced); `rows` lists the
+// rows of one colour class, or is null for all rows in order.
+template <typename TV, typename TX, int S, int MODE>
+__global__ void __launch_bounds__(kThreads) csrv_kernel(int nrows, const int* __restrict__ rows,
+                                                        const int* __restrict__ ptr, const int* __restrict__ col,
+                                                        const TV* __restrict__ val, const TX* x, TX* y,
+                                                        const TX* __restrict__ b, const TX* __restrict__ dinv, TX w,
+                                                        const TX* z, double* partials, unsigned* ticket,
+                                                        KScalars* sc) {
+    const int lane = threadIdx.x & 31;
+    const int sub = lane & (S - 1);
+    const long warp_global = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long nwarps = ((long)gridDim.x * blockDim.x) >> 5;
+    double dot = 0.0;
+    for (long gb = warp_global * (32 / S); gb < nrows; gb += nwarps * (32 / S)) {
+        const long g = gb + lane / S;
+        const bool valid = g < nrows;
+        int i = 0, s0 = 0, e0 = 0;
+        if (valid) {
+            i = rows ? rows[g] : (int)g;
+            s0 = ptr[i];
+            e0 = ptr[i + 1];
+        }
+        TX sum = TX(0);
+        for (int k = s0 + sub; k < e0; k += S) sum += TX(val[k]) * x[col[k]];
+#pragma unroll
+        for (int o = S / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, S);
+        if (valid && sub == 0) {
+            if constexpr (MODE == M_SPMV) {
+                y[i] = sum;
+            } else if constexpr (MODE == M_RESID) {
+                y[i] = b[i] - sum;
+            } else if constexpr (MODE == M_JACOBI || MODE == M_SOR) {
+                y[i] = x[i] + w * dinv[i] * (b[i] - sum);
+            } else if constexpr (MODE == M_ADD) {
+                y[i] = z[i] + sum;
+            } else if constexpr (MODE == M_DOT) {
+                y[i] = sum;
+                dot += double(x[i]) * double(sum);
+            }
         }
     }
     if constexpr (MODE == M_DOT) {
@@ -327,7 +378,24 @@ struct DCsr {
     float* v32 = nullptr;
     int* rowmap = nullptr;          // row of each position (-1 = padding), null = natural order
     std::vector<int> group_slice;   // colour c occupies slices [group_slice[c], group_slice[c+1])
+    // CSR-vector layout (lanes > 0): CSR arrays and, for colour groups, the rows of each colour
+    int lanes = 0;
+    int* ptr = nullptr;
+    int* rows = nullptr;
+    std::vector<int> group_row;     // colour c: rows[group_row[c] .. group_row[c+1])
 };
+
+// Layout choice: one thread per row (SELL-32) when rows are short and there
+// are enough of them to keep every SM busy; otherwise a group of lanes per row.
+int csrv_lanes_for(const lina::Csr& c) {
+    const double avg = c.n > 0 ? double(c.nnz()) / c.n : 0.0;
+    if (g_layout == 1) return 0;
+    if (g_layout == 0 && c.n >= 152 * 16 * 32 && avg <= 64.0) return 0;
+    if (avg >= 64.0) return 32;
+    if (avg >= 24.0) return 16;
+    if (avg >= 8.0) return 8;
+    return 4;
+}
 
 // Host-side SELL-32 construction; `order` lists the rows per group (colour)
 // and each group starts on a slice boundary.  Without groups the natural row
@@ -505,6 +573,33 @@ struct lina_gpu_amg {
                 set_err("matrix entry with column %d outside [0, %d)", c.col[k], ncols);
                 return LINA_GPU_EINVAL;
             }
+        d.lanes = csrv_lanes_for(c);
+        if (d.lanes > 0) {
+            // CSR-vector: sanitise placeholder columns outside the operand, keep the CSR arrays
+            std::vector<int> colc(c.col);
+            for (size_t k = 0; k < colc.size(); k++)
+                if (colc[k] >= ncols) colc[k] = 0;  // value is 0.0 (checked above)
+            std::vector<float> v32(c.val.begin(), c.val.end());
+            int rc;
+            if ((rc = upload(&d.ptr, c.ptr.data(), c.ptr.size()))) return rc;
+            if ((rc = upload(&d.col, colc.data(), colc.size()))) return rc;
+            if ((rc = upload(&d.v64, c.val.data(), c.val.size()))) return rc;
+            if ((rc = upload(&d.v32, v32.data(), v32.size()))) return rc;
+            d.padded = c.nnz();
+            d.group_row.assign(1, 0);
+            if (groups) {
+                std::vector<int> all;
+                for (const auto& g : *groups) {
+                    all.insert(all.end(), g.begin(), g.end());
+                    d.group_row.push_back((int)all.size());
+                }
+                if ((rc = upload(&d.rows, all.data(), all.size()))) return rc;
+            } else {
+                d.group_row.push_back(c.n);
+            }
+            d.group_slice.assign(1, 0);
+            return cudaStreamSynchronize(stream) == cudaSuccess ? 0 : LINA_GPU_ECUDA;
+        }
         SellHost S = make_sell(c, ncols, groups);
         if (S.col.size() > (size_t)INT_MAX) {
             set_err("padded matrix too large for 32-bit SELL offsets");
@@ -557,10 +652,43 @@ struct lina_gpu_amg {
             w, z, partials, ticket, sc);
     }
 
+    template <typename TV, typename TX, int MODE>
+    void launch_csrv_t(const DCsr& m, const TV* val, int r0, int r1, const TX* x, TX* y, const TX* b,
+                       const TX* dinv, TX w, const TX* z) {
+        const int nrows = r1 - r0;
+        if (nrows <= 0) return;
+        const int S = m.lanes;
+        long grid = ((long)nrows * S + kThreads - 1) / kThreads;
+        if (MODE == M_DOT && grid > kMaxBlocks) grid = kMaxBlocks;
+        if (grid > (1L << 30)) grid = 1L << 30;
+        const int* rl = m.rows ? m.rows + r0 : nullptr;
+        g_launches++;
+#define LINA_CSRV_CASE(SS)                                                                                       \
+    case SS:                                                                                                     \
+        csrv_kernel<TV, TX, SS, MODE><<<(int)grid, kThreads, 0, stream>>>(nrows, rl, m.ptr, m.col, val, x, y, b, \
+                                                                          dinv, w, z, partials, ticket, sc);     \
+        break;
+        switch (S) {
+            LINA_CSRV_CASE(4)
+            LINA_CSRV_CASE(8)
+            LINA_CSRV_CASE(16)
+            default:
+                LINA_CSRV_CASE(32)
+        }
+#undef LINA_CSRV_CASE
+    }
+
     // all rows of m (natural order)
     template <typename TX, int MODE>
     void csr(const DCsr& m, const TX* x, TX* y, const TX* b = nullptr, const TX* dinv = nullptr, TX w = TX(0),
              const TX* z = nullptr) {
+        if (m.lanes > 0) {
+            if constexpr (sizeof(TX) == 8)
+                launch_csrv_t<double, TX, MODE>(m, m.v64, 0, m.n, x, y, b, dinv, w, z);
+            else
+                launch_csrv_t<float, TX, MODE>(m, m.v32, 0, m.n, x, y, b, dinv, w, z);
+            return;
+        }
         const int ns = (int)m.group_slice.back();
         if constexpr (sizeof(TX) == 8)
             launch_sell_t<double, TX, MODE>(m, m.v64, 0, ns, x, y, b, dinv, w, z);
@@ -571,6 +699,15 @@ struct lina_gpu_amg {
     // the rows of colour c of a colour-grouped matrix
     template <typename TX, int MODE>
     void csr_group(const DCsr& m, int c, const TX* x, TX* y, const TX* b, const TX* dinv, TX w) {
+        if (m.lanes > 0) {
+            if constexpr (sizeof(TX) == 8)
+                launch_csrv_t<double, TX, MODE>(m, m.v64, m.group_row[c], m.group_row[c + 1], x, y, b, dinv, w,
+                                                nullptr);
+            else
+                launch_csrv_t<float, TX, MODE>(m, m.v32, m.group_row[c], m.group_row[c + 1], x, y, b, dinv, w,
+                                               nullptr);
+            return;
+        }
         if constexpr (sizeof(TX) == 8)
             launch_sell_t<double, TX, MODE>(m, m.v64, m.group_slice[c], m.group_slice[c + 1], x, y, b, dinv, w,
                                             nullptr);
@@ -875,6 +1012,15 @@ void lina_gpu_default_options(lina_gpu_amg_options* o) {
 }
 
 const char* lina_gpu_last_error(void) { return g_err.c_str(); }
+
+int lina_gpu_set_layout(int layout) {
+    if (layout < 0 || layout > 2) {
+        set_err("lina_gpu_set_layout: layout must be 0, 1 or 2");
+        return LINA_GPU_EINVAL;
+    }
+    g_layout = layout;
+    return 0;
+}
 
 int lina_gpu_set_device(int device) {
     CK(cudaSetDevice(device));

@@ -92,6 +92,7 @@ def lib():
         "lina_gpu_synchronize": (C.c_int, []),
         "lina_gpu_device_count": (C.c_int, []),
         "lina_gpu_set_device": (C.c_int, [C.c_int]),
+        "lina_gpu_set_layout": (C.c_int, [C.c_int]),
         "lina_gpu_last_error": (C.c_char_p, []),
         "lina_gpu_timer_begin": (C.c_int, [vp]),
         "lina_gpu_timer_end": (C.c_int, [vp, dp]),
@@ -205,6 +206,13 @@ class PinnedArray:
             self.free()
         except Exception:
             pass
+
+
+LAYOUT_AUTO, LAYOUT_SELL, LAYOUT_CSRV = 0, 1, 2
+
+
+def set_layout(layout: int):
+    _check(lib().lina_gpu_set_layout(int(layout)), "set layout")
 
 
 def set_device(device: int):

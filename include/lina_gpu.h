@@ -144,6 +144,10 @@ void* lina_gpu_malloc_host(size_t bytes);   /* pinned host memory */
 int lina_gpu_free_host(void* p);
 int lina_gpu_device_count(void);
 int lina_gpu_set_device(int device);   /* select the GPU for hierarchies created afterwards */
+/* storage layout of matrices uploaded afterwards: 0 automatic (SELL-32 thread-per-row for large
+   levels with short rows, CSR with a lane group per row otherwise), 1 SELL-32 always,
+   2 CSR lane groups always */
+int lina_gpu_set_layout(int layout);
 
 const char* lina_gpu_last_error(void);
 

@@ -28,12 +28,19 @@ def _amg(name, smoother="jacobi", precision=lina.PREC_FP64):
                                       omega=om, precision=precision)
 
 
+@pytest.fixture(params=[lina.LAYOUT_AUTO, lina.LAYOUT_SELL, lina.LAYOUT_CSRV], ids=["auto", "sell", "csrv"])
+def layout(request):
+    lina.set_layout(request.param)
+    yield request.param
+    lina.set_layout(lina.LAYOUT_AUTO)
+
+
 def rel(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
 
 
 @pytest.mark.parametrize("name", golden_cases("hierarchy"))
-def test_spmv_every_level(name):
+def test_spmv_every_level(name, layout):
     s, g, amg = _amg(name)
     rng = np.random.default_rng(7)
     for l in range(amg.depth):
@@ -46,7 +53,7 @@ def test_spmv_every_level(name):
 
 @pytest.mark.parametrize("name", golden_cases("hierarchy"))
 @pytest.mark.parametrize("smoother", list(SMOOTHERS))
-def test_vcycle_matches_reference(name, smoother):
+def test_vcycle_matches_reference(name, smoother, layout):
     s, g, amg = _amg(name, smoother)
     z = amg.vcycle(g["vcycle_r"])
     assert rel(z, g[f"vcycle_{smoother}"]) < 1e-11
@@ -54,7 +61,7 @@ def test_vcycle_matches_reference(name, smoother):
 
 @pytest.mark.parametrize("name", golden_cases("hierarchy") + golden_cases("solve"))
 @pytest.mark.parametrize("smoother", list(SMOOTHERS))
-def test_pcg_fp64_matches_reference(name, smoother):
+def test_pcg_fp64_matches_reference(name, smoother, layout):
     s, g, amg = _amg(name, smoother)
     x, info = amg.pcg(s.b, tol=1e-8, max_iter=500, stop=lina.STOP_REFERENCE,
                       flags=lina.PCG_NORMALIZE | lina.PCG_FINAL_PRECON)
@@ -107,7 +114,7 @@ def test_device_pointer_solve_equals_host_solve():
 
 
 @pytest.mark.parametrize("prec", [lina.PREC_FP64, lina.PREC_MIXED])
-def test_matrix_spmv_and_jacobi(prec):
+def test_matrix_spmv_and_jacobi(prec, layout):
     from fem_gb300 import problems
     s = problems.elasticity_p1(33)
     A = sp.csr_matrix((s.data, s.indices, s.indptr), shape=(s.n, s.n))
@@ -124,7 +131,7 @@ def test_matrix_spmv_and_jacobi(prec):
     assert rel(M.jacobi(s.b, x, 0.6, 2, prec), y) < (1e-13 if prec == lina.PREC_FP64 else 1e-5)
 
 
-def test_rectangular_prolongation_stays_in_bounds():
+def test_rectangular_prolongation_stays_in_bounds(layout):
     """P (fine x coarse) with rows of different lengths: the padded SELL entries must only
     gather coarse-vector entries (checked through the result on a coarse vector of ones)."""
     s, g, amg = _amg("elast17_std")
