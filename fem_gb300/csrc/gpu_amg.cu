@@ -108,10 +108,18 @@ __device__ void grid_reduce(double (&v)[NV], double* partials, unsigned* ticket,
 
 // Krylov scalars kept on the device so that no host round trip sits between kernels.
 struct KScalars {
-    double s, s_old, pq, t, rr, alpha, beta, r0, norm2, aux;
+    double s, s_old, pq, t, rr, alpha, beta, r0, norm2, aux, tol;
     int iter;
-    int pad;
+    int maxit;
 };
+
+// last node of the graph-captured iteration: continue the device-side loop
+// while the residual test fails and the iteration budget lasts
+__global__ void loop_cond_kernel(cudaGraphConditionalHandle handle, const KScalars* sc) {
+    const double rel = sqrt(sc->rr) / sc->r0;
+    const bool more = isfinite(rel) && rel > sc->tol && sc->iter < sc->maxit;
+    cudaGraphSetConditional(handle, more ? 1u : 0u);
+}
 
 // ---------------------------------------------------------------- CSR kernels
 enum { M_SPMV = 0, M_RESID = 1, M_JACOBI = 2, M_SOR = 3, M_ADD = 4, M_DOT = 5 };
@@ -523,6 +531,16 @@ struct lina_gpu_amg {
     cudaStream_t stream = nullptr;
     long dev_bytes = 0;
     std::vector<void*> allocations;
+    // CUDA graph of one PCG iteration inside a device-side while loop
+    cudaGraphExec_t gexec = nullptr;
+    int g_prec = -1, g_smoother = -1;
+    double g_omega = 0.0;
+    long g_kernels = 0;  // kernels per captured iteration
+    void drop_graph() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        gexec = nullptr;
+        g_prec = -1;
+    }
     // smoother timing
     cudaEvent_t tm0 = nullptr, tm1 = nullptr;
     bool timing = false;
@@ -530,6 +548,7 @@ struct lina_gpu_amg {
     int ev_used = 0;
 
     ~lina_gpu_amg() {
+        drop_graph();
         for (void* p : allocations) cudaFree(p);
         if (sc_host) cudaFreeHost(sc_host);
         for (auto e : ev_pool) cudaEventDestroy(e);
@@ -858,6 +877,70 @@ struct lina_gpu_amg {
     }
 
     const DCsr& krylov_matrix() const { return has_signs ? Aorig : lv[depth - 1].A; }
+
+    // one PCG iteration: z = M^-1 r (unless reused), s = r.z, p = z + beta p, q = A p, x/r update
+    void issue_iteration(int n, bool precon, bool time_it) {
+        const bool mixed = (opt.precision == LINA_PREC_MIXED);
+        const int flexible = mixed ? 1 : 0;
+        const int gr = grid_red(n), gv = grid_for(n, kThreads);
+        if (precon) precondition(kr, kz, time_it);
+        if (mixed)
+            go(dot_rz_kernel<float>, gr, stream, n, (const double*)kr, (const float*)kz32, (const double*)kq, flexible,
+               partials, ticket, sc);
+        else
+            go(dot_rz_kernel<double>, gr, stream, n, (const double*)kr, (const double*)kz, (const double*)kq,
+               flexible, partials, ticket, sc);
+        if (mixed)
+            go(update_p_kernel<float>, gv, stream, n, (const float*)kz32, kp, flexible, sc);
+        else
+            go(update_p_kernel<double>, gv, stream, n, (const double*)kz, kp, flexible, sc);
+        csr<double, M_DOT>(krylov_matrix(), kp, kq);
+        go(update_xr_kernel, gr, stream, n, kx, kr, (const double*)kp, (const double*)kq, partials, ticket, sc);
+    }
+
+    // capture issue_iteration + the loop test into a while-loop graph (cached per configuration)
+    int ensure_graph(int n) {
+        if (gexec && g_prec == opt.precision && g_smoother == opt.smoother && g_omega == opt.omega) return 0;
+        drop_graph();
+        cudaGraph_t g = nullptr;
+        CK(cudaGraphCreate(&g, 0));
+        cudaGraphConditionalHandle hd;
+        cudaError_t e = cudaGraphConditionalHandleCreate(&hd, g, 1, cudaGraphCondAssignDefault);
+        cudaGraphNodeParams cp = {};
+        cudaGraphNode_t node;
+        if (e == cudaSuccess) {
+            cp.type = cudaGraphNodeTypeConditional;
+            cp.conditional.handle = hd;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp);
+        }
+        if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(stream, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                                               cudaStreamCaptureModeRelaxed);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(g);
+            set_err("graph construction failed: %s", cudaGetErrorString(e));
+            return LINA_GPU_ECUDA;
+        }
+        const unsigned long long before = g_launches;
+        issue_iteration(n, true, false);
+        loop_cond_kernel<<<1, 1, 0, stream>>>(hd, sc);
+        g_kernels = (long)(g_launches - before) + 1;
+        g_launches = before;
+        cudaGraph_t body = nullptr;
+        e = cudaStreamEndCapture(stream, &body);
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            gexec = nullptr;
+            set_err("graph capture/instantiation failed: %s", cudaGetErrorString(e));
+            return LINA_GPU_ECUDA;
+        }
+        g_prec = opt.precision;
+        g_smoother = opt.smoother;
+        g_omega = opt.omega;
+        return 0;
+    }
 };
 
 namespace {
@@ -1110,6 +1193,7 @@ int lina_gpu_amg_recompute(lina_gpu_amg* h, int n, const int* rowptr, const int*
     }
     // the reference keeps the setup's signs and does not flip the new matrix
     if (h->host_only) return 0;
+    h->drop_graph();
     for (void* p : h->allocations) cudaFree(p);
     h->allocations.clear();
     h->dev_bytes = 0;
@@ -1134,6 +1218,7 @@ int lina_gpu_amg_set_smoother(lina_gpu_amg* h, int smoother, double omega, int p
     h->opt.smoother = smoother;
     h->opt.omega = omega;
     h->opt.precision = precision;
+    h->drop_graph();
     return 0;
 }
 
@@ -1176,11 +1261,10 @@ int lina_gpu_pcg(lina_gpu_amg* h, const double* b_in, double* x_out, double tol,
     const int n = h->lv[h->depth - 1].n;
     const bool dev = (flags & LINA_PCG_DEVICE_PTRS) != 0;
     const bool mixed = (h->opt.precision == LINA_PREC_MIXED);
-    const int flexible = mixed ? 1 : 0;
     const bool time_it = (flags & LINA_PCG_TIME_KERNELS) != 0;
     h->ev_used = 0;
     cudaStream_t st = h->stream;
-    double *b = h->kb, *x = h->kx, *r = h->kr, *z = h->kz, *p = h->kp, *q = h->kq;
+    double *b = h->kb, *x = h->kx, *r = h->kr, *z = h->kz;
     // inputs
     if (dev)
         CK(cudaMemcpyAsync(b, b_in, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
@@ -1240,28 +1324,40 @@ int lina_gpu_pcg(lina_gpu_amg* h, const double* b_in, double* x_out, double tol,
         }
     }
     {
+        // Iterations run either one by one from the host (kernel timing requested)
+        // or as a captured CUDA graph whose while-loop node repeats the iteration
+        // on the device until the residual test passes.
+        const bool use_graph = !time_it && !(flags & LINA_PCG_HOST_LOOP);
         int it = 0;
         int restarts = 0;
+        int dev_iter = 0;  // the device's iteration counter (reset on restart)
         double rel = 0.0;
         for (;;) {
-            if (!have_z) h->precondition(r, z, time_it);
-            have_z = false;
-            if (mixed)
-                go(dot_rz_kernel<float>, gr, st, n, r, h->kz32, q, flexible, h->partials, h->ticket,
-                                                               h->sc);
-            else
-                go(dot_rz_kernel<double>, gr, st, n, r, z, q, flexible, h->partials, h->ticket, h->sc);
-            if (mixed)
-                go(update_p_kernel<float>, gv, st, n, h->kz32, p, flexible, h->sc);
-            else
-                go(update_p_kernel<double>, gv, st, n, z, p, flexible, h->sc);
-            h->csr<double, M_DOT>(A, p, q);
-            go(update_xr_kernel, gr, st, n, x, r, p, q, h->partials, h->ticket, h->sc);
-            CK(cudaGetLastError());
-            if (read_scalars(h)) return LINA_GPU_ECUDA;
-            it++;
-            double rr = h->sc_host->rr;
-            rel = std::sqrt(rr) / r0;
+            if (use_graph && !have_z) {
+                int rc = h->ensure_graph(n);
+                if (rc) return rc;
+                KScalars lim;
+                lim.r0 = r0;
+                lim.tol = tol;
+                CK(cudaMemcpyAsync(&h->sc->r0, &lim.r0, sizeof(double), cudaMemcpyHostToDevice, st));
+                CK(cudaMemcpyAsync(&h->sc->tol, &lim.tol, sizeof(double), cudaMemcpyHostToDevice, st));
+                int maxit = dev_iter + (max_iter - it);
+                CK(cudaMemcpyAsync(&h->sc->maxit, &maxit, sizeof(int), cudaMemcpyHostToDevice, st));
+                CK(cudaGraphLaunch(h->gexec, st));
+                if (read_scalars(h)) return LINA_GPU_ECUDA;
+                int done = h->sc_host->iter - dev_iter;
+                g_launches += (unsigned long long)done * (unsigned long long)h->g_kernels;
+                it += done;
+                dev_iter = h->sc_host->iter;
+            } else {
+                h->issue_iteration(n, !have_z, time_it);
+                have_z = false;
+                CK(cudaGetLastError());
+                if (read_scalars(h)) return LINA_GPU_ECUDA;
+                it++;
+                dev_iter = h->sc_host->iter;
+            }
+            rel = std::sqrt(h->sc_host->rr) / r0;
             if (!std::isfinite(rel)) {
                 inf->status = LINA_GPU_EBREAKDOWN;
                 break;
@@ -1276,6 +1372,7 @@ int lina_gpu_pcg(lina_gpu_amg* h, const double* b_in, double* x_out, double tol,
                     CK(cudaMemcpyAsync(r, h->kt, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
                     int zero = 0;
                     CK(cudaMemcpyAsync(&h->sc->iter, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
+                    dev_iter = 0;
                     restarts++;
                     converged = false;
                 }

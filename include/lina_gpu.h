@@ -52,6 +52,8 @@ extern "C" {
                                     pcg residuum (LinA/PCGS.c:217-218)                    */
 #define LINA_PCG_TIME_KERNELS 8  /* time the finest-level smoother launches with CUDA events */
 #define LINA_PCG_NORMALIZE 16    /* scale b and x by 1/||b|| during the solve, as pcg does */
+#define LINA_PCG_HOST_LOOP 32    /* drive every iteration from the host instead of the captured
+                                    CUDA graph with its device-side while loop              */
 
 typedef struct lina_gpu_amg lina_gpu_amg;
 

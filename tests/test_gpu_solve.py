@@ -144,3 +144,24 @@ def test_rectangular_prolongation_stays_in_bounds(layout):
     assert np.all(val[~keep] == 0.0)
     P = sp.csr_matrix((np.where(keep, val, 0.0), np.where(keep, col, 0), ptr), shape=(len(ptr) - 1, nc))
     assert rel(M.spmv(e), P @ e) < 1e-14
+
+
+@pytest.mark.parametrize("name", ["elast65_std_solve", "poisson129_aggr_solve"])
+@pytest.mark.parametrize("prec", [lina.PREC_FP64, lina.PREC_MIXED])
+def test_graph_loop_equals_host_loop(name, prec):
+    """The captured CUDA graph (device-side while loop) computes exactly what the host-driven
+    loop computes: same iterations, bitwise-equal solution (deterministic reductions)."""
+    s, g, amg = _amg(name, "jacobi", prec)
+    xg, ig = amg.pcg(s.b, tol=1e-8, stop=lina.STOP_RELATIVE)
+    xh, ih = amg.pcg(s.b, tol=1e-8, stop=lina.STOP_RELATIVE, flags=lina.PCG_HOST_LOOP)
+    assert ig.iterations == ih.iterations and ig.status == ih.status == 0
+    assert np.array_equal(xg, xh)
+    # a second graph launch reuses the cached graph
+    xg2, ig2 = amg.pcg(s.b, tol=1e-8, stop=lina.STOP_RELATIVE)
+    assert np.array_equal(xg2, xg)
+
+
+def test_graph_respects_iteration_limit():
+    s, g, amg = _amg("elast65_std_solve", "jacobi", lina.PREC_MIXED)
+    x, info = amg.pcg(s.b, tol=1e-14, max_iter=5, stop=lina.STOP_RELATIVE)
+    assert info.iterations == 5 and info.status == lina.ENOCONV
