@@ -267,7 +267,7 @@ def run_gb300(args, rank, world, local):
         "gpu_launches": int(launches),
         "fp64_gpu": fp64,
         "mixed_vs_fp64": (value / fp64["value"]) if fp64 else None,
-        "roofline": {"bound": "hbm", "kernel": "finest-level FP32 Jacobi sweep (csr_kernel M_JACOBI)",
+        "roofline": {"bound": "hbm", "kernel": "finest-level FP32 Jacobi sweep (sell_kernel<float,float,M_JACOBI>)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,
                      "traffic": traffic, "bytes_per_launch": sm_bytes,
