@@ -51,6 +51,7 @@ void set_err(const char* fmt, ...) {
 constexpr int kThreads = 256;
 constexpr int kMaxBlocks = 16384;     // partials per reduction value
 constexpr int kGridCap = 152 * 12;    // grid-stride cap: 152 SMs x 12 blocks of 256
+constexpr int kReduceGrid = 152 * 8;  // kernels that end in a grid reduction: one wave of blocks
 
 // ---------------------------------------------------------------- reductions
 __device__ __forceinline__ double warp_sum(double v) {
@@ -144,11 +145,11 @@ __global__ void __launch_bounds__(kThreads) sell_kernel(int npos, const int* __r
                                                         const TX* __restrict__ b, const TX* __restrict__ dinv, TX w,
                                                         const TX* z, double* partials, unsigned* ticket,
                                                         KScalars* sc) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     double dot = 0.0;
-    int i = -1;
-    if (t < npos) i = rowmap ? rowmap[t] : t;
-    if (i >= 0) {
+    // grid-stride over slice positions (npos is a multiple of 32, so warps stay whole)
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < npos; t += gridDim.x * blockDim.x) {
+        const int i = rowmap ? rowmap[t] : t;
+        if (i < 0) continue;
         const int sl = t >> 5, lane = t & 31;
         const int p0 = sptr[sl];
         const int len = (sptr[sl + 1] - p0) >> 5;
@@ -177,7 +178,7 @@ __global__ void __launch_bounds__(kThreads) sell_kernel(int npos, const int* __r
             y[i] = z[i] + sum;
         } else if constexpr (MODE == M_DOT) {
             y[i] = sum;
-            dot = double(x[i]) * double(sum);
+            dot += double(x[i]) * double(sum);
         }
     }
     if constexpr (MODE == M_DOT) {
@@ -306,6 +307,23 @@ __global__ void scale_kernel(long n, double* __restrict__ v, const double* __res
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) v[i] *= s;
 }
 
+// AMG_solve helpers: b = signs * F, the isolated-row fix x_i = b_i / a_i, x += z
+__global__ void mul_kernel(int n, double* __restrict__ b, const double* __restrict__ f) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) b[i] *= f[i];
+}
+
+__global__ void fix_isolated_kernel(int n, const double* __restrict__ b, const double* __restrict__ isoinv,
+                                    double* __restrict__ x) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        if (isoinv[i] != 0.0) x[i] = b[i] * isoinv[i];
+}
+
+template <typename TZ>
+__global__ void add_kernel(int n, double* __restrict__ x, const TZ* __restrict__ z) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        x[i] += double(z[i]);
+}
+
 // ------------------------------------------------------------ Krylov kernels
 // s_old = s; s = r.z; t = z.q (flexible CG)
 template <typename TZ>
@@ -314,6 +332,7 @@ __global__ void __launch_bounds__(kThreads) dot_rz_kernel(int n, const double* _
                                                           int flexible, double* partials, unsigned* ticket,
                                                           KScalars* sc) {
     double v[2] = {0.0, 0.0};
+#pragma unroll 4
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
         double zi = double(z[i]);
         v[0] += r[i] * zi;
@@ -345,6 +364,7 @@ __global__ void __launch_bounds__(kThreads) update_xr_kernel(int n, double* __re
                                                              unsigned* ticket, KScalars* sc) {
     const double alpha = sc->s / sc->pq;
     double v[1] = {0.0};
+#pragma unroll 4
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
         x[i] += alpha * p[i];
         double ri = r[i] - alpha * q[i];
@@ -362,6 +382,7 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads) norm2_kernel(int n, const T* __restrict__ v, double* partials,
                                                          unsigned* ticket, KScalars* sc) {
     double a[1] = {0.0};
+#pragma unroll 4
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
         double x = double(v[i]);
         a[0] += x * x;
@@ -398,7 +419,7 @@ struct DCsr {
 int csrv_lanes_for(const lina::Csr& c) {
     const double avg = c.n > 0 ? double(c.nnz()) / c.n : 0.0;
     if (g_layout == 1) return 0;
-    if (g_layout == 0 && c.n >= 152 * 16 * 32 && avg <= 64.0) return 0;
+    if (g_layout == 0 && c.n >= 300000 && avg <= 64.0) return 0;
     if (avg >= 64.0) return 32;
     if (avg >= 24.0) return 16;
     if (avg >= 8.0) return 8;
@@ -493,8 +514,7 @@ int grid_for(long items, int per_block) {
 int grid_red(long items) {
     long g = (items + kThreads - 1) / kThreads;
     if (g < 1) g = 1;
-    if (g > kMaxBlocks) g = kMaxBlocks;
-    if (g > kGridCap) g = kGridCap;
+    if (g > kReduceGrid) g = kReduceGrid;
     return (int)g;
 }
 
@@ -664,7 +684,8 @@ struct lina_gpu_amg {
                        const TX* dinv, TX w, const TX* z) {
         const int npos = (slice1 - slice0) * 32;
         if (npos <= 0) return;
-        const int grid = (npos + kThreads - 1) / kThreads;
+        int grid = (npos + kThreads - 1) / kThreads;
+        if (MODE == M_DOT && grid > kReduceGrid) grid = kReduceGrid;
         g_launches++;
         sell_kernel<TV, TX, MODE><<<grid, kThreads, 0, stream>>>(
             npos, m.rowmap ? m.rowmap + (size_t)slice0 * 32 : nullptr, m.sptr + slice0, m.col, val, x, y, b, dinv,
@@ -678,7 +699,7 @@ struct lina_gpu_amg {
         if (nrows <= 0) return;
         const int S = m.lanes;
         long grid = ((long)nrows * S + kThreads - 1) / kThreads;
-        if (MODE == M_DOT && grid > kMaxBlocks) grid = kMaxBlocks;
+        if (MODE == M_DOT && grid > kReduceGrid) grid = kReduceGrid;
         if (grid > (1L << 30)) grid = 1L << 30;
         const int* rl = m.rows ? m.rows + r0 : nullptr;
         g_launches++;
@@ -851,7 +872,7 @@ struct lina_gpu_amg {
 
     // z = M^-1 r on the finest level (r FP64 on the device); mixed precision
     // leaves the result in kz32 (FP32), FP64 in z.
-    void precondition(const double* r, double* z, bool time_it) {
+    void precondition(const double* r, double* z, bool time_it, bool apply_signs = true) {
         const int l = depth - 1;
         DLevel& L = lv[l];
         if (depth == 1) {
@@ -864,13 +885,13 @@ struct lina_gpu_amg {
             return;
         }
         const int nu = (opt.coarsening == LINA_AGGRESSIVE) ? opt.aggr_smoothing_iterations : opt.smoothing_iterations;
-        const double* sign = has_signs ? signs : nullptr;
+        const double* sign = (has_signs && apply_signs) ? signs : nullptr;
         if (opt.precision == LINA_PREC_MIXED) {
             presmooth<double, float>(L, nu, r, sign, isoinv, L.b32, kz32, time_it);
             run_rest<float>(l, L, nu, L.b32, kz32, time_it);
         } else {
             double* b = const_cast<double*>(r);
-            if (has_signs) b = L.b64;
+            if (sign) b = L.b64;
             presmooth<double, double>(L, nu, r, sign, isoinv, b, z, time_it);
             run_rest<double>(l, L, nu, b, z, time_it);
         }
@@ -1234,6 +1255,51 @@ int lina_gpu_vcycle(lina_gpu_amg* h, const double* r_dev, double* z_dev) {
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(h->stream));
     return 0;
+}
+
+int lina_gpu_amg_solve(lina_gpu_amg* h, const double* F, double* X, double eps, int max_iter, int flags,
+                       int* iterations, double* rel_residual) {
+    if (!h || h->host_only || !F || !X || max_iter < 0) {
+        set_err("lina_gpu_amg_solve: invalid argument");
+        return LINA_GPU_EINVAL;
+    }
+    const int n = h->lv[h->depth - 1].n;
+    const bool dev = (flags & LINA_PCG_DEVICE_PTRS) != 0;
+    cudaStream_t st = h->stream;
+    const int gv = grid_for(n, kThreads), gr = grid_red(n);
+    double *b = h->kb, *x = h->kx, *r = h->kr;
+    CK(cudaMemcpyAsync(b, F, n * sizeof(double), dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(x, X, n * sizeof(double), dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+    if (h->has_signs) go(mul_kernel, gv, st, n, b, (const double*)h->signs);
+    if (h->depth > 1) go(fix_isolated_kernel, gv, st, n, (const double*)b, (const double*)h->isoinv, x);
+    const DCsr& A = h->lv[h->depth - 1].A;
+    auto residual = [&]() -> double {
+        h->csr<double, M_RESID>(A, x, r, b);
+        go(norm2_kernel<double>, gr, st, n, (const double*)r, h->partials, h->ticket, h->sc);
+        if (read_scalars(h)) return -1.0;
+        return std::sqrt(h->sc_host->norm2);
+    };
+    const double r0 = residual();
+    if (r0 < 0) return LINA_GPU_ECUDA;
+    double rr = r0;
+    int it = 0;
+    // one V-cycle with initial guess x equals x + V(0, b - A x) for the linear smoothers used here
+    while (r0 != 0.0 && std::fabs(rr / r0) > eps && it < max_iter) {
+        h->precondition(r, h->kz, false, false);
+        if (h->opt.precision == LINA_PREC_MIXED)
+            go(add_kernel<float>, gv, st, n, x, (const float*)h->kz32);
+        else
+            go(add_kernel<double>, gv, st, n, x, (const double*)h->kz);
+        rr = residual();
+        if (rr < 0) return LINA_GPU_ECUDA;
+        it++;
+        if (!std::isfinite(rr)) break;
+    }
+    CK(cudaMemcpyAsync(X, x, n * sizeof(double), dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (iterations) *iterations = it;
+    if (rel_residual) *rel_residual = (r0 != 0.0) ? rr / r0 : 0.0;
+    return std::isfinite(rr) ? 0 : LINA_GPU_EBREAKDOWN;
 }
 
 int lina_gpu_spmv(lina_gpu_amg* h, int level, const double* x_dev, double* y_dev) {

@@ -99,6 +99,11 @@ int lina_gpu_amg_set_smoother(lina_gpu_amg* h, int smoother, double omega, int p
 /* AMG-preconditioned CG on the hierarchy's finest matrix (pcg, LinA/PCGS.c:163). */
 int lina_gpu_pcg(lina_gpu_amg* h, const double* b, double* x, double tol, int max_iter,
                  int stop_rule, int flags, lina_gpu_solve_info* info);
+/* AMG_solve (LinA/Multigrid.c:1863): V-cycles from the initial guess X until ||F - A X|| / ||F - A X0||
+   <= eps or max_iter cycles; flags may hold LINA_PCG_DEVICE_PTRS.  Returns the cycles done and the
+   final relative residual. */
+int lina_gpu_amg_solve(lina_gpu_amg* h, const double* F, double* X, double eps, int max_iter, int flags,
+                       int* iterations, double* rel_residual);
 /* one preconditioner application z = M^-1 r (device pointers), zero initial guess */
 int lina_gpu_vcycle(lina_gpu_amg* h, const double* r_dev, double* z_dev);
 /* y = A_level x on the device (level = depth-1 is the finest) */

@@ -72,6 +72,8 @@ def lib():
         "rs_transpose": (vp, [vp, C.c_int]),
         "rs_ilu": (C.c_int, [vp, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
         "rs_ilu_apply": (None, [vp, vp, dp]),
+        "rs_pcg_stock_amg": (C.c_int, [vp, C.c_int, C.c_int, C.c_double, dp, dp, C.c_double, C.c_int, dp]),
+        "rs_amg_solve_fresh": (C.c_int, [vp, dp, dp, C.c_double, C.c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -174,6 +176,19 @@ class RefAMG:
             lib().rs_silence(0)
         return x, it, res.value
 
+    def amg_solve(self, F, eps=1e-8, max_iter=200, smoother=SMOOTHER_REF_SOR, omega=1.0):
+        """AMG_solve from a zero guess; returns (x, V-cycles)."""
+        x = np.zeros(self.n)
+        f = np.array(F, dtype=np.float64)
+        lib().rs_set_smoother(smoother, omega)
+        lib().rs_forget_colouring()
+        lib().rs_silence(1)
+        try:
+            it = lib().rs_amg_solve_fresh(self.ptr, _dp(f), _dp(x), eps, max_iter)
+        finally:
+            lib().rs_silence(0)
+        return x, it
+
     def vcycle(self, r, smoother=SMOOTHER_REF_SOR, omega=1.0):
         z = np.zeros(self.n)
         rr = np.array(r, dtype=np.float64)
@@ -190,6 +205,22 @@ class RefAMG:
         if getattr(self, "ptr", None) and _lib is not None:
             _lib.rs_amg_free(self.ptr)
             self.ptr = None
+
+
+def pcg_stock(sysm, depth, smoother=SMOOTHER_MC_SOR, omega=1.6, tol=1e-8, max_iter=500):
+    """PCG_default + PCG_set_AMG_preconditioner + pcg on the reference; returns (x, iterations, residuum)."""
+    A = RefMatrix.from_csr(sysm.n, sysm.indptr, sysm.indices, sysm.data)
+    x = np.zeros(sysm.n)
+    b = np.array(sysm.b, dtype=np.float64)
+    res = C.c_double(0.0)
+    lib().rs_set_smoother(smoother, omega)
+    lib().rs_forget_colouring()
+    lib().rs_silence(1)
+    try:
+        it = lib().rs_pcg_stock_amg(A.ptr, int(sysm.dof), depth, omega, _dp(x), _dp(b), tol, max_iter, C.byref(res))
+    finally:
+        lib().rs_silence(0)
+    return x, it, res.value
 
 
 def greedy_colouring(n, indptr, indices, data):

@@ -317,3 +317,24 @@ void rs_ilu_apply(sparse_matrix* L, sparse_matrix* U, double* x) {
     L_triang_invert(L, x);
     U_triang_invert(U, x);
 }
+
+/* the reference's own AMG preconditioner path: PCG_default + PCG_set_AMG_preconditioner
+   (LinA/PCGS.c:29, :118-129) + pcg; the smoother installed by rs_set_smoother stays in place */
+int rs_pcg_stock_amg(sparse_matrix* A, int dof, int depth, double omega, double* x, double* b, double tol,
+                     int max_iter, double* pcg_res) {
+    PCG_default(A, NULL, NULL);
+    PCG_set_AMG_preconditioner(A, dof, depth);
+    AMG_set_SOR_relaxation_coeff(omega);
+    smoother_omega = omega;
+    int it = pcg(x, b, A->size, tol, max_iter);
+    if (pcg_res) *pcg_res = get_pcg_residuum();
+    return it;
+}
+
+/* AMG_solve from a zero guess to eps with at most max_iter V-cycles */
+int rs_amg_solve_fresh(amg_system_info* I, double* F, double* X, double eps, int max_iter) {
+    AMG_print_info(NO);
+    AMG_set_eps(eps);
+    AMG_set_max_iter(max_iter);
+    return AMG_solve(I, F, X, NULL);
+}

@@ -90,6 +90,16 @@ def make_case(name):
     # an accurate FP64 solution (reference pcg to a tight tolerance) for error bars
     x, it, res = amg.pcg(s.b, 1e-13, 2000, ref.SMOOTHER_MC_SOR, 1.0)
     out["x_tight"] = x
+    # AMG_solve alone (V-cycles to 1e-8) with damped Jacobi
+    x, it = amg.amg_solve(s.b, 1e-8, 200, ref.SMOOTHER_DAMPED_JACOBI, 0.6)
+    out["amgsolve_jacobi_x"] = x
+    out["amgsolve_jacobi_it"] = np.int64(it)
+    # the reference's stock AMG preconditioner (PCG_set_AMG_preconditioner: aggressive coarsening,
+    # 2+3 sweeps, up to 100 warm-started V-cycles to 1e-2) with multicolour SOR, omega 1.6
+    x, it, res = ref.pcg_stock(s, depth, ref.SMOOTHER_MC_SOR, 1.6)
+    out["stock_x"] = x
+    out["stock_it"] = np.int64(it)
+    out["stock_res"] = np.float64(res)
     return out
 
 

@@ -23,7 +23,8 @@ def declared_functions():
             before = text[max(0, m.start() - 80):m.start()]
             if "typedef" in before.split(";")[-1]:
                 continue
-            if name in {"if", "while", "for", "return", "sizeof"}:
+            if name in {"if", "while", "for", "return", "sizeof", "int", "void", "double", "float", "char", "long",
+                        "unsigned"}:
                 continue
             names.add(name)
     return names
