@@ -1631,6 +1631,8 @@ int lina_gpu_matrix_jacobi(lina_gpu_matrix* m, int precision, double omega, int 
 
 long lina_gpu_matrix_padded_entries(const lina_gpu_matrix* m) { return m ? m->A.padded : 0; }
 
+int lina_gpu_matrix_rows(const lina_gpu_matrix* m) { return m ? m->A.n : 0; }
+
 int lina_gpu_amg_depth(const lina_gpu_amg* h) { return h ? h->depth : 0; }
 
 int lina_gpu_level_sizes(const lina_gpu_amg* h, int level, int* n, long* nnz_A, long* nnz_P, long* nnz_R,

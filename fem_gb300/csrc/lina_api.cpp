@@ -25,6 +25,8 @@
 #include "BiCGStab.h"
 #include "Multigrid.h"
 #include "PCGS.h"
+#include <cuda_runtime.h>
+
 #include "gpu_ops.h"
 #include "lina_gpu.h"
 #include "linear_algebra.h"
@@ -1238,6 +1240,105 @@ int BiCGStab_solve(double* X, double* b, int n) {
     AMG_add_stat(&bi_stat, iter, fabs(r / r0));
     if (!lina::dev::d2h(X, x, n)) return -1;
     return iter;
+}
+
+}  // extern "C"
+
+// ============================================================ device BiCGStab and ILU(0) (C-ABI)
+extern "C" {
+
+int lina_gpu_ilu_create_from_matrix(int n, const int* rowptr, const int* col, const double* val,
+                                    lina_gpu_ilu** out) {
+    if (!out || n <= 0 || !rowptr || !col || !val) return LINA_GPU_EINVAL;
+    sparse_matrix* A = from_csr(n, rowptr, col, val);
+    sparse_matrix* L = sparse_zero(n);
+    sparse_matrix* U = sparse_zero(n);
+    int ok = incomplete_LU_factorization(A, L, U);
+    int rc = LINA_GPU_ESETUP;
+    if (ok) {
+        CsrCopy l = to_csr(L), u = to_csr(U);
+        rc = lina_gpu_ilu_create(n, l.ptr.data(), l.col.data(), l.val.data(), u.ptr.data(), u.col.data(),
+                                 u.val.data(), out);
+    }
+    free_sparse(A);
+    free_sparse(L);
+    free_sparse(U);
+    return rc;
+}
+
+int lina_gpu_bicgstab(lina_gpu_matrix* Am, lina_gpu_ilu* ilu, int ilu_precision, const double* b_in, double* x_out,
+                      double tol, int max_iter, int flags, lina_gpu_solve_info* info) {
+    if (!Am || !b_in || !x_out || max_iter < 0) return LINA_GPU_EINVAL;
+    lina_gpu_solve_info local{};
+    lina_gpu_solve_info* inf = info ? info : &local;
+    memset(inf, 0, sizeof *inf);
+    const bool dev = (flags & LINA_PCG_DEVICE_PTRS) != 0;
+    const int n = lina_gpu_matrix_rows(Am);
+    DevVecs d(10, n);
+    if (!d.ok()) return LINA_GPU_ECUDA;
+    double *x = d.v[0], *bb = d.v[1], *S = d.v[2], *PS = d.v[3], *PP = d.v[4], *APP = d.v[5], *APS = d.v[6],
+           *R = d.v[7], *R0 = d.v[8], *P = d.v[9];
+    bool ok = dev ? lina::dev::d2d(bb, b_in, n) : lina::dev::h2d(bb, b_in, n);
+    if (flags & LINA_PCG_USE_X0)
+        ok = ok && (dev ? lina::dev::d2d(x, x_out, n) : lina::dev::h2d(x, x_out, n));
+    else
+        ok = ok && lina::dev::zero(x, n);
+    auto matvec = [&](const double* in, double* out) {
+        lina::dev::sync();
+        return lina_gpu_matrix_spmv(Am, LINA_PREC_FP64, in, out) == 0;
+    };
+    auto precon = [&](const double* in, double* out) {
+        lina::dev::sync();
+        if (!ilu) return lina::dev::d2d(out, in, n);
+        return lina_gpu_ilu_apply(ilu, ilu_precision, in, out) == 0;
+    };
+    ok = ok && matvec(x, R);
+    ok = ok && lina::dev::axpy(R, -1., bb, n) && lina::dev::scal(R, -1., n) && lina::dev::d2d(R0, R, n) &&
+         lina::dev::d2d(P, R, n);
+    if (!ok) return LINA_GPU_ECUDA;
+    double r0 = sqrt(lina::dev::dot(R, R, n)), r = r0;
+    int iter = 0;
+    if (r0 != 0) {
+        do {
+            if (!precon(P, PP) || !matvec(PP, APP)) return LINA_GPU_ECUDA;
+            double h = lina::dev::dot(R, R0, n);
+            double t = lina::dev::dot(APP, R0, n);
+            if (t == 0) break;
+            double alpha = h / t;
+            lina::dev::d2d(S, R, n);
+            lina::dev::axpy(S, -alpha, APP, n);
+            if (!precon(S, PS) || !matvec(PS, APS)) return LINA_GPU_ECUDA;
+            double s = lina::dev::dot(APS, APS, n);
+            if (s == 0) break;
+            double omega = lina::dev::dot(APS, S, n) / s;
+            lina::dev::axpy(x, alpha, PP, n);
+            lina::dev::axpy(x, omega, PS, n);
+            lina::dev::d2d(R, S, n);
+            lina::dev::axpy(R, -omega, APS, n);
+            double beta = lina::dev::dot(R, R0, n) * alpha / (h * omega);
+            lina::dev::axpy(P, -omega, APP, n);
+            lina::dev::scal(P, beta, n);
+            lina::dev::axpy(P, 1., R, n);
+            r = sqrt(lina::dev::dot(R, R, n));
+            iter++;
+            if (!std::isfinite(r)) break;
+        } while (r / r0 > tol && iter <= max_iter);
+    }
+    inf->iterations = iter;
+    inf->rel_residual = (r0 != 0) ? r / r0 : 0.0;
+    if (!std::isfinite(inf->rel_residual))
+        inf->status = LINA_GPU_EBREAKDOWN;
+    else if (inf->rel_residual > tol)
+        inf->status = LINA_GPU_ENOCONV;
+    // true residual
+    if (!matvec(x, APP)) return LINA_GPU_ECUDA;
+    lina::dev::d2d(S, bb, n);
+    lina::dev::axpy(S, -1., APP, n);
+    double bn = sqrt(lina::dev::dot(bb, bb, n));
+    inf->true_rel_residual = bn > 0 ? sqrt(lina::dev::dot(S, S, n)) / bn : 0.0;
+    ok = dev ? lina::dev::d2d(x_out, x, n) : lina::dev::d2h(x_out, x, n);
+    lina::dev::sync();
+    return ok ? inf->status : LINA_GPU_ECUDA;
 }
 
 }  // extern "C"

@@ -121,8 +121,28 @@ int lina_gpu_matrix_spmv(lina_gpu_matrix* m, int precision, const void* x_dev, v
    number of sweeps the result is in tmp, after an even number in x */
 int lina_gpu_matrix_jacobi(lina_gpu_matrix* m, int precision, double omega, int sweeps, const void* b_dev,
                            void* x_dev, void* tmp_dev);
+int lina_gpu_matrix_rows(const lina_gpu_matrix* m);
 /* stored entries including the SELL-32 slice padding */
 long lina_gpu_matrix_padded_entries(const lina_gpu_matrix* m);
+
+/* ILU(0) preconditioner on the GPU: factors as incomplete_LU_factorization produces them
+   (LinA/linear_algebra.c:1952: L lower with diagonal, U upper with unit diagonal), applied by
+   level-scheduled forward and backward solves. */
+typedef struct lina_gpu_ilu lina_gpu_ilu;
+int lina_gpu_ilu_create(int n, const int* Lptr, const int* Lcol, const double* Lval, const int* Uptr,
+                        const int* Ucol, const double* Uval, lina_gpu_ilu** out);
+/* factorise A (CSR) with the reference's ILU(0) on the host, then upload; returns LINA_GPU_ESETUP on a zero pivot */
+int lina_gpu_ilu_create_from_matrix(int n, const int* rowptr, const int* col, const double* val, lina_gpu_ilu** out);
+int lina_gpu_ilu_destroy(lina_gpu_ilu* h);
+int lina_gpu_ilu_levels(const lina_gpu_ilu* h, int* nlev_L, int* nlev_U);
+/* z = U^-1 L^-1 r (device vectors, FP64); LINA_PREC_MIXED solves in FP32 */
+int lina_gpu_ilu_apply(lina_gpu_ilu* h, int precision, const double* r_dev, double* z_dev);
+
+/* BiCGStab (BiCGStab_solve, LinA/BiCGStab.c:115-198) on device vectors with A a device matrix and
+   the ILU(0) preconditioner (or none if ilu is NULL); stops when ||r|| / ||r0|| <= tol.
+   flags: LINA_PCG_DEVICE_PTRS, LINA_PCG_USE_X0; ilu_precision selects the precision of the ILU solves. */
+int lina_gpu_bicgstab(lina_gpu_matrix* A, lina_gpu_ilu* ilu, int ilu_precision, const double* b, double* x,
+                      double tol, int max_iter, int flags, lina_gpu_solve_info* info);
 
 /* CUDA-event timing on the hierarchy's stream: elapsed milliseconds between begin and end */
 int lina_gpu_timer_begin(lina_gpu_amg* h);
