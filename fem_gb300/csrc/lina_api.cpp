@@ -573,6 +573,33 @@ lina_gpu_matrix* device_matrix(const sparse_matrix* A) {
     return d.m;
 }
 
+// device ILU(0) of the factors given to PCG_default (PCG_preconlr on the GPU)
+struct DevIlu {
+    lina_gpu_ilu* h = nullptr;
+    uint64_t fpl = 0, fpu = 0;
+    const sparse_matrix *L = nullptr, *U = nullptr;
+} g_devilu;
+
+lina_gpu_ilu* device_ilu(const sparse_matrix* L, const sparse_matrix* U) {
+    uint64_t fl = fingerprint(L), fu = fingerprint(U);
+    if (g_devilu.h && g_devilu.L == L && g_devilu.U == U && g_devilu.fpl == fl && g_devilu.fpu == fu)
+        return g_devilu.h;
+    if (g_devilu.h) lina_gpu_ilu_destroy(g_devilu.h);
+    g_devilu = DevIlu();
+    CsrCopy l = to_csr(L), u = to_csr(U);
+    if (lina_gpu_ilu_create(l.n, l.ptr.data(), l.col.data(), l.val.data(), u.ptr.data(), u.col.data(), u.val.data(),
+                            &g_devilu.h) != 0) {
+        fprintf(stderr, "LinA-GB300: device ILU factors could not be created\n");
+        g_devilu.h = nullptr;
+        return nullptr;
+    }
+    g_devilu.L = L;
+    g_devilu.U = U;
+    g_devilu.fpl = fl;
+    g_devilu.fpu = fu;
+    return g_devilu.h;
+}
+
 // host staging buffers for callbacks
 struct Stage {
     std::vector<double> a, b;
@@ -969,6 +996,13 @@ int apply_precon(Precon f, int n, const double* r, double* z, amg_statistics* st
         if (stat) AMG_add_stat(stat, iters, fabs(rel));
         return iters;
     }
+    if (f == PCG_preconlr) {
+        if (!pcg_default_L || !pcg_default_U) return lina::dev::d2d(z, r, n) ? 1 : -1;
+        lina_gpu_ilu* ilu = device_ilu(pcg_default_L, pcg_default_U);
+        if (!ilu) return -1;
+        lina::dev::sync();
+        return lina_gpu_ilu_apply(ilu, LINA_PREC_FP64, r, z) == 0 ? 1 : -1;
+    }
     g_stage.ensure(n);
     if (!lina::dev::d2h(g_stage.a.data(), r, n) || !lina::dev::d2h(g_stage.b.data(), z, n)) return -1;
     int k = f(n, g_stage.a.data(), g_stage.b.data());
@@ -1041,10 +1075,14 @@ int PCG_preconlr(int n, double* z, double* w) {
         copy_vector_to(z, w, n);
         return 1;
     }
-    copy_vector_to(z, w, n);
-    L_triang_invert(pcg_default_L, w);
-    U_triang_invert(pcg_default_U, w);
-    return 1;
+    lina_gpu_ilu* ilu = device_ilu(pcg_default_L, pcg_default_U);
+    double* dz = lina::dev::alloc(n);
+    double* dw = lina::dev::alloc(n);
+    int ok = ilu && dz && dw && lina::dev::h2d(dz, z, n) && lina_gpu_ilu_apply(ilu, LINA_PREC_FP64, dz, dw) == 0 &&
+             lina::dev::d2h(w, dw, n);
+    lina::dev::release(dz);
+    lina::dev::release(dw);
+    return ok ? 1 : 0;
 }
 
 int PCG_AMG_precon(int n, double* Y, double* X) {

@@ -104,6 +104,12 @@ def lib():
         "lina_gpu_matrix_spmv": (C.c_int, [vp, C.c_int, vp, vp]),
         "lina_gpu_matrix_jacobi": (C.c_int, [vp, C.c_int, C.c_double, C.c_int, vp, vp, vp]),
         "lina_gpu_matrix_padded_entries": (C.c_long, [vp]),
+        "lina_gpu_matrix_rows": (C.c_int, [vp]),
+        "lina_gpu_ilu_create_from_matrix": (C.c_int, [C.c_int, ip, ip, dp, C.POINTER(vp)]),
+        "lina_gpu_ilu_destroy": (C.c_int, [vp]),
+        "lina_gpu_ilu_levels": (C.c_int, [vp, ip, ip]),
+        "lina_gpu_ilu_apply": (C.c_int, [vp, C.c_int, vp, vp]),
+        "lina_gpu_bicgstab": (C.c_int, [vp, vp, C.c_int, vp, vp, C.c_double, C.c_int, C.c_int, C.POINTER(SolveInfo)]),
         "lina_gpu_free_host": (C.c_int, [vp]),
     }
     for name, (res, args) in sig.items():
@@ -273,6 +279,54 @@ class Matrix:
             self.close()
         except Exception:
             pass
+
+
+class ILU:
+    """ILU(0) of a CSR matrix (the reference's factorisation) applied on the GPU."""
+
+    def __init__(self, n, indptr, indices, data):
+        self.n = int(n)
+        ip_ = np.ascontiguousarray(indptr, dtype=np.int32)
+        ix_ = np.ascontiguousarray(indices, dtype=np.int32)
+        dv_ = np.ascontiguousarray(data, dtype=np.float64)
+        h = C.c_void_p()
+        _check(lib().lina_gpu_ilu_create_from_matrix(self.n, _ip(ip_), _ip(ix_), _dp(dv_), C.byref(h)), "ILU")
+        self.h = h
+
+    def levels(self):
+        a, b = C.c_int(), C.c_int()
+        _check(lib().lina_gpu_ilu_levels(self.h, C.byref(a), C.byref(b)), "ILU levels")
+        return a.value, b.value
+
+    def apply(self, r, precision=PREC_FP64):
+        rd = DeviceArray.from_host(np.asarray(r, dtype=np.float64))
+        zd = DeviceArray(self.n)
+        _check(lib().lina_gpu_ilu_apply(self.h, precision, rd.ptr, zd.ptr), "ILU apply")
+        return zd.to_host()
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().lina_gpu_ilu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def bicgstab(M: "Matrix", b, ilu: "ILU | None" = None, ilu_precision=PREC_FP64, tol=1e-8, max_iter=1000, x0=None):
+    """BiCGStab_solve on the GPU; returns (x, SolveInfo)."""
+    bb = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros(M.n) if x0 is None else np.array(x0, dtype=np.float64)
+    info = SolveInfo()
+    flags = PCG_USE_X0 if x0 is not None else 0
+    rc = lib().lina_gpu_bicgstab(M.h, ilu.h if ilu else None, ilu_precision, bb.ctypes.data, x.ctypes.data, tol,
+                                 max_iter, flags, C.byref(info))
+    if rc not in (0, ENOCONV):
+        raise LinaError(f"bicgstab failed ({rc}): {last_error()}")
+    return x, info
 
 
 class AMG:

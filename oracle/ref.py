@@ -74,6 +74,7 @@ def lib():
         "rs_ilu_apply": (None, [vp, vp, dp]),
         "rs_pcg_stock_amg": (C.c_int, [vp, C.c_int, C.c_int, C.c_double, dp, dp, C.c_double, C.c_int, dp]),
         "rs_amg_solve_fresh": (C.c_int, [vp, dp, dp, C.c_double, C.c_int]),
+        "rs_bicgstab_ilu": (C.c_int, [vp, dp, dp, C.c_double, C.c_int, C.c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -221,6 +222,31 @@ def pcg_stock(sysm, depth, smoother=SMOOTHER_MC_SOR, omega=1.6, tol=1e-8, max_it
     finally:
         lib().rs_silence(0)
     return x, it, res.value
+
+
+def ilu_apply(sysm, r):
+    """z = U^-1 L^-1 r with the reference's ILU(0) of the system matrix."""
+    A = RefMatrix.from_csr(sysm.n, sysm.indptr, sysm.indices, sysm.data)
+    Lp, Up = C.c_void_p(), C.c_void_p()
+    if lib().rs_ilu(A.ptr, C.byref(Lp), C.byref(Up)) != 1:
+        raise RuntimeError("reference ILU(0) hit a zero pivot")
+    Lm, Um = RefMatrix(Lp.value), RefMatrix(Up.value)
+    z = np.array(r, dtype=np.float64)
+    lib().rs_ilu_apply(Lm.ptr, Um.ptr, _dp(z))
+    return z
+
+
+def bicgstab_ilu(sysm, eps=1e-8, max_iter=1000):
+    """BiCGStab_solve with the ILU(0) preconditioner; returns (x, iterations)."""
+    A = RefMatrix.from_csr(sysm.n, sysm.indptr, sysm.indices, sysm.data)
+    x = np.zeros(sysm.n)
+    b = np.array(sysm.b, dtype=np.float64)
+    lib().rs_silence(1)
+    try:
+        it = lib().rs_bicgstab_ilu(A.ptr, _dp(x), _dp(b), eps, max_iter, 1)
+    finally:
+        lib().rs_silence(0)
+    return x, it
 
 
 def greedy_colouring(n, indptr, indices, data):

@@ -338,3 +338,33 @@ int rs_amg_solve_fresh(amg_system_info* I, double* F, double* X, double eps, int
     AMG_set_max_iter(max_iter);
     return AMG_solve(I, F, X, NULL);
 }
+
+/* BiCGStab_solve (LinA/BiCGStab.c:115) with A as the product and ILU(0) of A as the preconditioner */
+static sparse_matrix *bi_A = NULL, *bi_L = NULL, *bi_U = NULL;
+static void bi_matvec(int n, double* y, double* x) {
+    double* r = sparse_mult(bi_A, y);
+    memcpy(x, r, n * sizeof(double));
+    free(r);
+}
+static int bi_ilu(int n, double* y, double* x) {
+    memcpy(x, y, n * sizeof(double));
+    L_triang_invert(bi_L, x);
+    U_triang_invert(bi_U, x);
+    return 1;
+}
+int rs_bicgstab_ilu(sparse_matrix* A, double* x, double* b, double eps, int max_iter, int use_ilu) {
+    bi_A = A;
+    bi_L = sparse_zero(A->size);
+    bi_U = sparse_zero(A->size);
+    if (!incomplete_LU_factorization(A, bi_L, bi_U)) return -1;
+    BI_set_mat_mult(bi_matvec);
+    BI_set_precon(use_ilu ? bi_ilu : NULL);
+    BI_set_eps(eps);
+    BI_set_max_iter(max_iter);
+    BI_print_info(NO);
+    BI_set_stat("", "");
+    int it = BiCGStab_solve(x, b, A->size);
+    free_sparse(bi_L);
+    free_sparse(bi_U);
+    return it;
+}

@@ -100,6 +100,11 @@ def make_case(name):
     out["stock_x"] = x
     out["stock_it"] = np.int64(it)
     out["stock_res"] = np.float64(res)
+    # ILU(0) preconditioner application and BiCGStab with it
+    out["ilu_z"] = ref.ilu_apply(s, r)
+    x, it = ref.bicgstab_ilu(s, 1e-8, 1000)
+    out["bicgstab_ilu_x"] = x
+    out["bicgstab_ilu_it"] = np.int64(it)
     return out
 
 

@@ -165,3 +165,28 @@ def test_graph_respects_iteration_limit():
     s, g, amg = _amg("elast65_std_solve", "jacobi", lina.PREC_MIXED)
     x, info = amg.pcg(s.b, tol=1e-14, max_iter=5, stop=lina.STOP_RELATIVE)
     assert info.iterations == 5 and info.status == lina.ENOCONV
+
+
+@pytest.mark.parametrize("name", golden_cases("hierarchy"))
+@pytest.mark.parametrize("prec", [lina.PREC_FP64, lina.PREC_MIXED])
+def test_ilu_apply_matches_reference(name, prec):
+    g = load_golden(name)
+    s = system_for(name)
+    ilu = lina.ILU(s.n, s.indptr, s.indices, s.data)
+    z = ilu.apply(g["vcycle_r"], prec)
+    assert rel(z, g["ilu_z"]) < (1e-12 if prec == lina.PREC_FP64 else 1e-5)
+
+
+@pytest.mark.parametrize("name", golden_cases("hierarchy"))
+def test_bicgstab_ilu_matches_reference(name):
+    g = load_golden(name)
+    s = system_for(name)
+    M = lina.Matrix(s.n, s.indptr, s.indices, s.data)
+    ilu = lina.ILU(s.n, s.indptr, s.indices, s.data)
+    x, info = lina.bicgstab(M, s.b, ilu, lina.PREC_FP64, tol=1e-8)
+    it_ref = int(g["bicgstab_ilu_it"])
+    assert info.status == 0 and abs(info.iterations - it_ref) <= max(1, it_ref // 10)
+    assert rel(x, g["bicgstab_ilu_x"]) < 1e-6
+    # FP32 ILU solves inside the FP64 BiCGStab reach the same tolerance
+    x32, i32 = lina.bicgstab(M, s.b, ilu, lina.PREC_MIXED, tol=1e-8)
+    assert i32.status == 0 and i32.true_rel_residual < 1e-7
