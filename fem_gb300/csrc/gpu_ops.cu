@@ -154,3 +154,14 @@ void* stream() {
 
 }  // namespace dev
 }  // namespace lina
+
+#include "lina_gpu.h"
+
+extern "C" int lina_gpu_dot(const double* a_dev, const double* b_dev, long n, double* result) {
+    if (!a_dev || !b_dev || !result || n < 0) return LINA_GPU_EINVAL;
+    if (!lina::dev::ready()) return LINA_GPU_ECUDA;
+    double r = lina::dev::dot(a_dev, b_dev, n);
+    if (std::isnan(r) && cudaGetLastError() != cudaSuccess) return LINA_GPU_ECUDA;
+    *result = r;
+    return 0;
+}

@@ -109,6 +109,7 @@ def lib():
         "lina_gpu_ilu_destroy": (C.c_int, [vp]),
         "lina_gpu_ilu_levels": (C.c_int, [vp, ip, ip]),
         "lina_gpu_ilu_apply": (C.c_int, [vp, C.c_int, vp, vp]),
+        "lina_gpu_dot": (C.c_int, [vp, vp, C.c_long, dp]),
         "lina_gpu_bicgstab": (C.c_int, [vp, vp, C.c_int, vp, vp, C.c_double, C.c_int, C.c_int, C.POINTER(SolveInfo)]),
         "lina_gpu_free_host": (C.c_int, [vp]),
     }
@@ -220,6 +221,12 @@ LAYOUT_AUTO, LAYOUT_SELL, LAYOUT_CSRV = 0, 1, 2
 
 def set_layout(layout: int):
     _check(lib().lina_gpu_set_layout(int(layout)), "set layout")
+
+
+def dot(a: "DeviceArray", b: "DeviceArray") -> float:
+    r = C.c_double()
+    _check(lib().lina_gpu_dot(a.ptr, b.ptr, a.n, C.byref(r)), "dot")
+    return r.value
 
 
 def set_device(device: int):

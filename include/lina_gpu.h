@@ -161,6 +161,10 @@ int lina_gpu_coarse_block_size(const lina_gpu_amg* h);
 /* bytes held on the device by the hierarchy */
 long lina_gpu_amg_device_bytes(const lina_gpu_amg* h);
 
+/* result = a . b for device vectors of n FP64 values: single-pass grid reduction (block partial
+   sums in device scratch memory, the last block adds them in a fixed order) */
+int lina_gpu_dot(const double* a_dev, const double* b_dev, long n, double* result);
+
 /* device memory helpers so that callers need no CUDA runtime of their own */
 void* lina_gpu_malloc(size_t bytes);
 int lina_gpu_free(void* p);

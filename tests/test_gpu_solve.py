@@ -190,3 +190,12 @@ def test_bicgstab_ilu_matches_reference(name):
     # FP32 ILU solves inside the FP64 BiCGStab reach the same tolerance
     x32, i32 = lina.bicgstab(M, s.b, ilu, lina.PREC_MIXED, tol=1e-8)
     assert i32.status == 0 and i32.true_rel_residual < 1e-7
+
+
+@pytest.mark.parametrize("n", [0, 1, 1000, 1 << 20, 3 * (1 << 20) + 7])
+def test_device_dot(n):
+    rng = np.random.default_rng(n)
+    a, b = rng.standard_normal(n), rng.standard_normal(n)
+    got = lina.dot(lina.DeviceArray.from_host(a), lina.DeviceArray.from_host(b))
+    want = float(np.dot(a, b))
+    assert abs(got - want) <= 1e-13 * max(1.0, np.abs(a) @ np.abs(b))
