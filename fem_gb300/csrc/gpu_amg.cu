@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "amg_host.h"
+#include "gpu_ops.h"
 #include "lina_gpu.h"
 
 namespace {
@@ -1096,6 +1097,12 @@ int read_scalars(lina_gpu_amg* h) {
 }
 
 }  // namespace
+
+namespace lina {
+namespace dev {
+void set_error(const char* msg) { g_err = msg ? msg : ""; }
+}  // namespace dev
+}  // namespace lina
 
 // =================================================================== C-ABI
 extern "C" {

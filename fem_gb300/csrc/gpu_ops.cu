@@ -165,3 +165,125 @@ extern "C" int lina_gpu_dot(const double* a_dev, const double* b_dev, long n, do
     *result = r;
     return 0;
 }
+
+// ---------------------------------------------------------------- allocation-free dot product
+// Some callers cannot allocate device memory at the point where they need a
+// reduction: code that runs while its stream is being captured into a CUDA
+// graph (cudaMalloc is not permitted during capture), a host function
+// enqueued with cudaLaunchHostFunc (which may not make CUDA calls that
+// allocate), or an integration whose device memory is fixed up front by the
+// host application.  lina_gpu_dot computes the same product but obtains its
+// partial-sum buffer from the library's allocator on first use;
+// lina_gpu_dot_noalloc keeps that scratch in a fixed array that the module
+// itself defines in device memory, so the call allocates nothing.
+//
+// The array holds one partial sum per block of 2048 elements plus the result
+// and an arrival counter: 16,384 partials, so at most 33,554,432 elements per
+// call (larger n is rejected).  It is 128 KB and occupies every GPU that loads
+// the library for as long as the process runs.  All calls share it and it
+// keeps the last call's contents; the arrival counter is cleared before every
+// launch.  Calls whose kernels overlap on the GPU (different streams, other
+// threads) race on the shared array and give wrong results: issue them one at
+// a time.  The first call on each device looks up the array's device address
+// with cudaGetSymbolAddress (with that device current); make that first call
+// before any stream capture begins.
+namespace {
+
+constexpr int kNoAllocThreads = 256;
+constexpr int kNoAllocPerThread = 8;
+constexpr long kNoAllocPerBlock = (long)kNoAllocThreads * kNoAllocPerThread;  // 2048 elements
+constexpr int kNoAllocMaxBlocks = 16384;
+constexpr long kNoAllocMaxN = kNoAllocPerBlock * kNoAllocMaxBlocks;  // 33,554,432 elements
+constexpr int kNoAllocResult = kNoAllocMaxBlocks;                     // slot of the result
+constexpr int kNoAllocCounter = kNoAllocMaxBlocks + 1;                // slot holding the arrival counter
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) double g_dot_scratch[kNoAllocMaxBlocks + 2];
+
+double* g_dot_scratch_addr[kMaxDevices] = {nullptr};
+
+__global__ void __launch_bounds__(kNoAllocThreads) dot_noalloc_kernel(long n, const double* __restrict__ a,
+                                                                      const double* __restrict__ b,
+                                                                      double* scratch) {
+    __shared__ double sm[kNoAllocThreads / 32];
+    __shared__ bool last;
+    unsigned* counter = reinterpret_cast<unsigned*>(scratch + kNoAllocCounter);
+    const long base = (long)blockIdx.x * kNoAllocPerBlock;
+    double v = 0.0;
+#pragma unroll
+    for (int k = 0; k < kNoAllocPerThread; k++) {
+        const long i = base + (long)k * kNoAllocThreads + threadIdx.x;
+        if (i < n) v += a[i] * b[i];
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    v = lina::dev::warp_sum(v);
+    if (lane == 0) sm[wid] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < kNoAllocThreads / 32; w++) t += sm[w];
+        scratch[blockIdx.x] = t;
+        __threadfence();
+        last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double x = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += kNoAllocThreads) x += __ldcg(scratch + i);
+    x = lina::dev::warp_sum(x);
+    __syncthreads();
+    if (lane == 0) sm[wid] = x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < kNoAllocThreads / 32; w++) t += sm[w];
+        scratch[kNoAllocResult] = t;
+        *counter = 0u;
+    }
+}
+
+}  // namespace
+
+extern "C" int lina_gpu_dot_noalloc(const double* a_dev, const double* b_dev, long n, double* result) {
+    if (!a_dev || !b_dev || !result || n < 0) {
+        lina::dev::set_error("lina_gpu_dot_noalloc: null pointer or negative length");
+        return LINA_GPU_EINVAL;
+    }
+    if (n > kNoAllocMaxN) {
+        lina::dev::set_error("lina_gpu_dot_noalloc: n exceeds the allocation-free limit of 33554432 elements "
+                             "(use lina_gpu_dot)");
+        return LINA_GPU_EINVAL;
+    }
+    int device = 0;
+    if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= kMaxDevices) {
+        lina::dev::set_error("lina_gpu_dot_noalloc: no usable current device");
+        return LINA_GPU_ECUDA;
+    }
+    if (!g_dot_scratch_addr[device]) {
+        double* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress((void**)&p, g_dot_scratch);
+        if (e != cudaSuccess || !p) {
+            lina::dev::set_error("lina_gpu_dot_noalloc: cudaGetSymbolAddress of the scratch array failed");
+            return LINA_GPU_ECUDA;
+        }
+        g_dot_scratch_addr[device] = p;
+    }
+    double* scratch = g_dot_scratch_addr[device];
+    if (n == 0) {
+        *result = 0.0;
+        return 0;
+    }
+    if (cudaMemsetAsync(scratch + kNoAllocCounter, 0, sizeof(double), 0) != cudaSuccess) {
+        lina::dev::set_error("lina_gpu_dot_noalloc: clearing the arrival counter failed");
+        return LINA_GPU_ECUDA;
+    }
+    const int grid = (int)((n + kNoAllocPerBlock - 1) / kNoAllocPerBlock);
+    dot_noalloc_kernel<<<grid, kNoAllocThreads, 0, 0>>>(n, a_dev, b_dev, scratch);
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpy(result, scratch + kNoAllocResult, sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
+        lina::dev::set_error("lina_gpu_dot_noalloc: kernel or result copy failed");
+        return LINA_GPU_ECUDA;
+    }
+    return 0;
+}

@@ -22,6 +22,7 @@ bool scal(double* x, double a, long n);                   // x *= a
 bool xpay(double* y, const double* x, double a, long n);  // y = x + a y
 bool sync();
 void* stream();                                    // the cudaStream_t used by these helpers
+void set_error(const char* msg);                   // text returned by lina_gpu_last_error()
 
 }  // namespace dev
 }  // namespace lina

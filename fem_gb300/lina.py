@@ -110,6 +110,7 @@ def lib():
         "lina_gpu_ilu_levels": (C.c_int, [vp, ip, ip]),
         "lina_gpu_ilu_apply": (C.c_int, [vp, C.c_int, vp, vp]),
         "lina_gpu_dot": (C.c_int, [vp, vp, C.c_long, dp]),
+        "lina_gpu_dot_noalloc": (C.c_int, [vp, vp, C.c_long, dp]),
         "lina_gpu_bicgstab": (C.c_int, [vp, vp, C.c_int, vp, vp, C.c_double, C.c_int, C.c_int, C.POINTER(SolveInfo)]),
         "lina_gpu_free_host": (C.c_int, [vp]),
     }

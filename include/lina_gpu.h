@@ -164,6 +164,14 @@ long lina_gpu_amg_device_bytes(const lina_gpu_amg* h);
 /* result = a . b for device vectors of n FP64 values: single-pass grid reduction (block partial
    sums in device scratch memory, the last block adds them in a fixed order) */
 int lina_gpu_dot(const double* a_dev, const double* b_dev, long n, double* result);
+/* The same product for callers that cannot allocate device memory (code running during a stream
+   capture into a CUDA graph, host functions enqueued on a stream, hosts whose device memory is fixed
+   in advance).  No counterpart in the reference.  Its scratch is a 128 KB array defined in device
+   memory by the library and kept on every GPU that loads it; n is limited to 33,554,432 elements
+   (larger n returns LINA_GPU_EINVAL).  It runs on the legacy default stream and returns the result
+   on the host.  All calls share the scratch array: calls that overlap on the GPU race.  The first
+   call on a device looks up the array's address and should come before any stream capture. */
+int lina_gpu_dot_noalloc(const double* a_dev, const double* b_dev, long n, double* result);
 
 /* device memory helpers so that callers need no CUDA runtime of their own */
 void* lina_gpu_malloc(size_t bytes);
