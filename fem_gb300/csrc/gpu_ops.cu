@@ -111,6 +111,11 @@ bool h2d(double* d, const double* h, long n) {
            cudaStreamSynchronize(g_stream) == cudaSuccess;
 }
 
+bool h2d_bytes(void* d, const void* h, long bytes) {
+    return cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, g_stream) == cudaSuccess &&
+           cudaStreamSynchronize(g_stream) == cudaSuccess;
+}
+
 bool d2h(double* h, const double* d, long n) {
     return cudaMemcpyAsync(h, d, n * sizeof(double), cudaMemcpyDeviceToHost, g_stream) == cudaSuccess &&
            cudaStreamSynchronize(g_stream) == cudaSuccess;

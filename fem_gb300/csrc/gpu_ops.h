@@ -13,6 +13,7 @@ bool ready();                                      // context created (creates o
 double* alloc(long n);                             // FP64 device vector, nullptr on failure
 void release(void* p);
 bool h2d(double* d, const double* h, long n);
+bool h2d_bytes(void* d, const void* h, long bytes);
 bool d2h(double* h, const double* d, long n);
 bool d2d(double* d, const double* s, long n);
 bool zero(double* d, long n);

@@ -25,10 +25,12 @@
 #include "BiCGStab.h"
 #include "Multigrid.h"
 #include "PCGS.h"
+#include "reflective_newton.h"
 #include <cuda_runtime.h>
 
 #include "gpu_ops.h"
 #include "lina_gpu.h"
+#include "lina_internal.h"
 #include "linear_algebra.h"
 
 // ============================================================ row-list helpers
@@ -124,6 +126,7 @@ sparse_matrix* clone(sparse_matrix* A) {
 }
 
 void Free_sparse(sparse_matrix* A) {
+    lina::api::forget_device_matrix(A);  // a device copy cached for this matrix goes with it
     for (int i = 0; i < A->size; i++) {
         free(A->Values[i]);
         free(A->Indices[i]);
@@ -483,13 +486,8 @@ double ILU_residuum(sparse_matrix* A, sparse_matrix* L, sparse_matrix* U, double
 }  // extern "C"
 
 // ============================================================ row list <-> CSR
-namespace {
-
-struct CsrCopy {
-    int n = 0;
-    std::vector<int> ptr, col;
-    std::vector<double> val;
-};
+namespace lina {
+namespace api {
 
 CsrCopy to_csr(const sparse_matrix* A) {
     CsrCopy c;
@@ -546,6 +544,12 @@ uint64_t fingerprint(const sparse_matrix* A) {
     return h;
 }
 
+}  // namespace api
+}  // namespace lina
+
+namespace {
+using namespace lina::api;
+
 // device copies of caller matrices used as operators (PCG_mult, BiCGStab products)
 struct DevMat {
     lina_gpu_matrix* m = nullptr;
@@ -554,7 +558,16 @@ struct DevMat {
 };
 std::unordered_map<const sparse_matrix*, DevMat> g_devmats;
 
-lina_gpu_matrix* device_matrix(const sparse_matrix* A) {
+}  // namespace
+
+void lina::api::forget_device_matrix(const sparse_matrix* A) {
+    auto it = g_devmats.find(A);
+    if (it == g_devmats.end()) return;
+    if (it->second.m) lina_gpu_matrix_destroy(it->second.m);
+    g_devmats.erase(it);
+}
+
+lina_gpu_matrix* lina::api::device_matrix(const sparse_matrix* A) {
     uint64_t fp = fingerprint(A);
     DevMat& d = g_devmats[A];
     if (d.m && d.fp == fp && d.n == A->size) return d.m;
@@ -574,13 +587,15 @@ lina_gpu_matrix* device_matrix(const sparse_matrix* A) {
 }
 
 // device ILU(0) of the factors given to PCG_default (PCG_preconlr on the GPU)
+namespace {
 struct DevIlu {
     lina_gpu_ilu* h = nullptr;
     uint64_t fpl = 0, fpu = 0;
     const sparse_matrix *L = nullptr, *U = nullptr;
 } g_devilu;
+}  // namespace
 
-lina_gpu_ilu* device_ilu(const sparse_matrix* L, const sparse_matrix* U) {
+lina_gpu_ilu* lina::api::device_ilu(const sparse_matrix* L, const sparse_matrix* U) {
     uint64_t fl = fingerprint(L), fu = fingerprint(U);
     if (g_devilu.h && g_devilu.L == L && g_devilu.U == U && g_devilu.fpl == fl && g_devilu.fpu == fu)
         return g_devilu.h;
@@ -599,6 +614,8 @@ lina_gpu_ilu* device_ilu(const sparse_matrix* L, const sparse_matrix* U) {
     g_devilu.fpu = fu;
     return g_devilu.h;
 }
+
+namespace {
 
 // host staging buffers for callbacks
 struct Stage {
@@ -960,7 +977,8 @@ amg_statistics bi_stat;
 // y = A x on device vectors: the library's own product runs on the GPU, a
 // caller's callback runs on host copies
 bool apply_matmult(MatMult f, sparse_matrix* own, int n, const double* x, double* y) {
-    if (f == PCG_mult && own) {
+    if (f == RN_default_mat_mult) own = lina::api::rn_default_matrix();
+    if ((f == PCG_mult || f == RN_default_mat_mult) && own) {
         lina_gpu_matrix* m = device_matrix(own);
         if (!m) return false;
         lina::dev::sync();
@@ -1165,6 +1183,9 @@ void BI_set_mat_mult(void (*Matrix_multiplication)(int n, double* Y, double* X))
 amg_system_info* BI_get_AMG_setup_data(void) { return bi_amg_data; }
 void BI_set_AMG_setup_data(amg_system_info* AMG_data) { bi_amg_data = AMG_data; }
 void BI_set_eps(double eps) { bi_eps = eps; }
+}  // extern "C"
+double lina::api::bi_eps_value() { return bi_eps; }
+extern "C" {
 void BI_set_max_iter(int max_iter) { bi_max_iter = max_iter; }
 int BI_get_max_iter(void) { return bi_max_iter; }
 void BI_set_stat(char* Out_AMG, char* Out_BiCGStab) {

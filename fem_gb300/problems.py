@@ -230,3 +230,54 @@ def elasticity_p1(m: int, E: float = 210.0, nu: float = 0.3, degraded: bool = Tr
     return CSRSystem(2 * nn, indptr, indices, data, b, dof=2,
                      meta={"kind": "elasticity_p1", "m": m, "E": E, "nu": nu,
                            "degraded": degraded, "top_uy": top_uy, "n_fixed": len(fixed)})
+
+
+def _mass_element(tri, h):
+    """3x3 lumped P1 mass: |T|/3 on the diagonal."""
+    _, _, area = _tri_geometry(tri, h)
+    return np.eye(3) * (area / 3.0)
+
+
+def damage_qp(m: int, gc: float = 1.0, ell: float = 0.03, drive: float = 100.0,
+              lower_scale: float = 0.5) -> CSRSystem:
+    """Bound-constrained quadratic of phase-field (AT2) damage type on an m x m grid.
+
+    Minimise ``q(d) = d.H.d/2 + d.b`` subject to ``lower <= d <= upper`` with
+    ``H = gc*ell*K + (gc/ell)*M + 2*psi*M`` and ``b = -(2*psi + drive*psi)*M*1``:
+    K the P1 Laplacian (natural boundary), M the lumped mass and ``psi`` a
+    per-element driving energy peaked at the notch tip (0.5, 0.5).  The extra
+    ``drive`` term pushes the unconstrained minimiser above 1 around the tip, so
+    both bounds are active somewhere: ``upper = 1`` and ``lower`` = the nodal
+    notch damage times ``lower_scale`` (irreversibility against a previous
+    state).  The start ``x0`` is the midpoint of the box.  This is the subproblem
+    Crack/crack.c hands to LinA's reflective_newton.
+    """
+    h = 1.0 / (m - 1)
+    nc = m - 1
+    rr, cc = np.meshgrid(np.arange(nc), np.arange(nc), indexing="ij")
+    psi = []
+    for tri in (_TRI_LOWER, _TRI_UPPER):
+        cx = (cc.ravel() + np.mean([dc for (dr, dc) in tri])) * h
+        cy = (rr.ravel() + np.mean([dr for (dr, dc) in tri])) * h
+        dist = np.sqrt((cx - 0.5) ** 2 + (cy - 0.5) ** 2)
+        psi.append(np.exp(-dist / 0.08))
+    psi = np.stack(psi)
+    kl = [(_TRI_LOWER, gc * ell * _laplace_element(_TRI_LOWER, h)),
+          (_TRI_UPPER, gc * ell * _laplace_element(_TRI_UPPER, h))]
+    ml = [(_TRI_LOWER, _mass_element(_TRI_LOWER, h)), (_TRI_UPPER, _mass_element(_TRI_UPPER, h))]
+    vk, valid = _assemble(m, 1, kl, None)
+    vm, _ = _assemble(m, 1, ml, gc / ell + 2.0 * psi)
+    vf, _ = _assemble(m, 1, ml, (2.0 + drive) * psi)
+    indptr, indices, data, _ = _to_csr(m, 1, vk + vm, valid, np.zeros(0, dtype=np.int64), 0.0)
+    b = -vf[0, :, 3].copy()
+    nn = m * m
+    r = np.arange(nn) // m
+    c = np.arange(nn) % m
+    x, y = c * h, r * h
+    dx = np.where(x > 0.5, x - 0.5, 0.0)
+    lower = lower_scale * np.exp(-np.sqrt(dx * dx + (y - 0.5) ** 2) / ell)
+    upper = np.ones(nn)
+    x0 = 0.5 * (lower + upper)
+    return CSRSystem(nn, indptr, indices, data, b, dof=1,
+                     meta={"kind": "damage_qp", "m": m, "gc": gc, "ell": ell, "drive": drive,
+                           "lower": lower, "upper": upper, "x0": x0})

@@ -75,6 +75,7 @@ def lib():
         "rs_pcg_stock_amg": (C.c_int, [vp, C.c_int, C.c_int, C.c_double, dp, dp, C.c_double, C.c_int, dp]),
         "rs_amg_solve_fresh": (C.c_int, [vp, dp, dp, C.c_double, C.c_int]),
         "rs_bicgstab_ilu": (C.c_int, [vp, dp, dp, C.c_double, C.c_int, C.c_int]),
+        "rs_reflective_newton_qp": (C.c_int, [vp, dp, dp, dp, dp, C.c_int, C.c_int, C.c_double, C.c_double]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -244,6 +245,21 @@ def bicgstab_ilu(sysm, eps=1e-8, max_iter=1000):
     lib().rs_silence(1)
     try:
         it = lib().rs_bicgstab_ilu(A.ptr, _dp(x), _dp(b), eps, max_iter, 1)
+    finally:
+        lib().rs_silence(0)
+    return x, it
+
+
+def reflective_newton_qp(qp, solver=5, max_iter=50, eps=1e-8, bi_eps=1e-8):
+    """reflective_newton on min x.H.x/2 + x.b, lower <= x <= upper; returns (x, iterations)."""
+    H = RefMatrix.from_csr(qp.n, qp.indptr, qp.indices, qp.data)
+    b = np.array(qp.b, dtype=np.float64)
+    lo = np.array(qp.meta["lower"], dtype=np.float64)
+    up = np.array(qp.meta["upper"], dtype=np.float64)
+    x = np.array(qp.meta["x0"], dtype=np.float64)
+    lib().rs_silence(1)
+    try:
+        it = lib().rs_reflective_newton_qp(H.ptr, _dp(b), _dp(lo), _dp(up), _dp(x), solver, max_iter, eps, bi_eps)
     finally:
         lib().rs_silence(0)
     return x, it

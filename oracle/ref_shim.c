@@ -368,3 +368,54 @@ int rs_bicgstab_ilu(sparse_matrix* A, double* x, double* b, double eps, int max_
     free_sparse(bi_U);
     return it;
 }
+
+/* ---------------------------------------------------------- reflective Newton (reference) */
+#include "reflective_newton.h"
+
+static int rs_rn_local_bicgstab_ilu(sparse_matrix* M, double* X, double* b) {
+    /* BiCGStab_solve with the ILU(0) of M (BI_eps, BI_max_iter as set by the caller) */
+    bi_A = M;
+    bi_L = sparse_zero(M->size);
+    bi_U = sparse_zero(M->size);
+    if (!incomplete_LU_factorization(M, bi_L, bi_U)) {
+        free_sparse(bi_L);
+        free_sparse(bi_U);
+        return INDEFINITE;
+    }
+    BI_set_mat_mult(bi_matvec);
+    BI_set_precon(bi_ilu);
+    BI_print_info(NO);
+    int it = BiCGStab_solve(X, b, M->size);
+    free_sparse(bi_L);
+    free_sparse(bi_U);
+    return it < BI_get_max_iter() ? POSITIVE_DEFINITE : INDEFINITE;
+}
+
+/* minimise x.H.x/2 + x.b subject to lower <= x <= upper with reflective_newton
+   (LinA/reflective_newton.c:660); solver 3 = RN_PCG (ILU-PCG), 5 = BiCGStab+ILU(0) through the
+   local-solver slot.  Returns the Newton iterations; x holds the start on entry. */
+int rs_reflective_newton_qp(sparse_matrix* H, double* b, double* lower, double* upper, double* x, int solver,
+                            int max_iter, double eps, double bi_eps) {
+    int n = H->size;
+    int* idx = get_all_indices(n);
+    RN_print_info(RN_NO);
+    RN_init_statistics();
+    RN_set_params(max_iter, eps, 0.1, 0.9, 0.1, 250., 1., 0.6, 1.1, 1e-3, 1000.);
+    set_RN_Hesse(H);
+    set_RN_linear(b);
+    set_RN_functional(NULL);
+    RN_set_gradient(NULL);
+    set_RN_constraints(idx, lower, upper, n);
+    BI_set_eps(bi_eps);
+    BI_set_max_iter(1000);
+    BI_set_stat("", "");
+    if (solver == RN_UMF)
+        RN_set_local_solver(rs_rn_local_bicgstab_ilu);
+    else {
+        RN_set_local_solver(NULL);
+        RN_set_solver(solver);
+    }
+    int it = reflective_newton(x);
+    free(idx);
+    return it;
+}

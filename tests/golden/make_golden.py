@@ -3,7 +3,7 @@
 Run in a checkout where the reference tree is available (``make -C oracle ref``
 builds oracle/_ref/libLinA_ref.so from it):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]
 
 For each small seeded system it records what the reference computes:
 the AMG hierarchy of AMG_setup (LinA/Multigrid.c:1613) level by level (C/F
@@ -11,7 +11,9 @@ labels, A, P, R), the greedy colouring of each level, one preconditioner
 application (a V-cycle from the zero guess) for a seeded residual, and full
 pcg solves (LinA/PCGS.c:163) with the smoothers the GPU library implements
 (installed into the reference through AMG_set_smoother) and with the
-reference's own lexicographic SOR.  Tests compare the GPU library against
+reference's own lexicographic SOR.  For bound-constrained damage quadratics
+it records the minimiser and iteration count of reflective_newton with two
+of the reference's local solvers.  Tests compare the GPU library against
 these files on machines where the reference is absent.
 """
 from __future__ import annotations
@@ -50,6 +52,13 @@ SMOOTHERS = {
 }
 TOL = 1e-8
 MAX_IT = 500
+# bound-constrained damage quadratics solved by reflective_newton (LinA/reflective_newton.c:660)
+RN_CASES = {
+    "damage65_rn": lambda: problems.damage_qp(65),
+    "damage129_rn": lambda: problems.damage_qp(129),
+}
+# reference local solvers: name -> RN solver code (5 = RN_UMF slot running BiCGStab + ILU(0), 3 = RN_PCG)
+RN_SOLVERS = {"umf_bicgstab_ilu": 5, "pcg_ilu": 3}
 
 
 def system_digest(s) -> str:
@@ -128,16 +137,40 @@ def make_solve_case(name):
     return out
 
 
+def make_rn_case(name):
+    q = RN_CASES[name]()
+    out = {"n": np.int64(q.n), "indptr": q.indptr, "indices": q.indices, "data": q.data, "b": q.b,
+           "lower": q.meta["lower"], "upper": q.meta["upper"], "x0": q.meta["x0"]}
+    for sname, code in RN_SOLVERS.items():
+        x, it = ref.reflective_newton_qp(q, solver=code, max_iter=50, eps=1e-8, bi_eps=1e-8)
+        out[f"rn_{sname}_x"] = x
+        out[f"rn_{sname}_it"] = np.int64(it)
+    return out
+
+
 def main():
+    only = sys.argv[1:]
     if not ref.available():
         sys.exit("oracle/_ref/libLinA_ref.so is missing: run `make -C oracle ref` where the reference tree exists")
+    for name in RN_CASES:
+        if only and name not in only:
+            continue
+        data = make_rn_case(name)
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **data)
+        print(f"{path}: reflective Newton iterations "
+              + ", ".join(f"{k}={int(data[f'rn_{k}_it'])}" for k in RN_SOLVERS))
     for name in CASES:
+        if only and name not in only:
+            continue
         data = make_case(name)
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **data)
         print(f"{path}: sizes {list(data['sizes'])}, pcg iterations "
               + ", ".join(f"{k}={int(data[f'pcg_{k}_it'])}" for k in SMOOTHERS))
     for name in SOLVE_CASES:
+        if only and name not in only:
+            continue
         data = make_solve_case(name)
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **data)
