@@ -319,6 +319,49 @@ __global__ void fix_isolated_kernel(int n, const double* __restrict__ b, const d
         if (isoinv[i] != 0.0) x[i] = b[i] * isoinv[i];
 }
 
+// new finest-level values on the setup's pattern: scatter into the level's layout(s) and
+// refresh the Jacobi diagonal and the isolated-row inverses
+__global__ void update_values_kernel(long nnz, const double* __restrict__ val, const int* __restrict__ posA,
+                                     const int* __restrict__ posAcol, double* __restrict__ a64,
+                                     float* __restrict__ a32, double* __restrict__ c64, float* __restrict__ c32) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (long)gridDim.x * blockDim.x) {
+        const double v = val[k];
+        const int p = posA[k];
+        if (p >= 0) {
+            a64[p] = v;
+            a32[p] = float(v);
+        }
+        if (posAcol) {
+            const int q = posAcol[k];
+            if (q >= 0) {
+                c64[q] = v;
+                c32[q] = float(v);
+            }
+        }
+    }
+}
+
+__global__ void update_diag_kernel(int n, const double* __restrict__ val, const int* __restrict__ ptr,
+                                   const int* __restrict__ diagpos, const unsigned char* __restrict__ isolated,
+                                   double* __restrict__ dinv64, float* __restrict__ dinv32,
+                                   double* __restrict__ isoinv) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int dp = diagpos[i];
+        const double d = dp >= 0 ? val[dp] : 0.0;
+        const double inv = d != 0.0 ? 1.0 / d : 0.0;
+        dinv64[i] = inv;
+        dinv32[i] = float(inv);
+        double iso = 0.0;
+        if (isolated[i])
+            for (int q = ptr[i]; q < ptr[i + 1]; q++)
+                if (val[q] != 0.0) {
+                    iso = 1.0 / val[q];
+                    break;
+                }
+        isoinv[i] = iso;
+    }
+}
+
 template <typename TZ>
 __global__ void add_kernel(int n, double* __restrict__ x, const TZ* __restrict__ z) {
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
@@ -434,12 +477,14 @@ struct SellHost {
     std::vector<int> sptr{0}, col, rowmap;
     std::vector<double> val;
     std::vector<int> group_slice{0};
+    std::vector<int> pos;  // SELL position of each CSR entry (-1: not stored)
 };
 
 // Padding entries repeat a column the row already uses (or column 0 for an
 // empty row), so every gathered index lies inside the input vector.
 SellHost make_sell(const lina::Csr& A, int ncols, const std::vector<std::vector<int>>* groups) {
     SellHost S;
+    S.pos.assign(A.nnz(), -1);
     auto add_group = [&](const int* rows, int nr) {
         for (int base = 0; base < nr; base += 32) {
             int len = 0;
@@ -465,6 +510,7 @@ SellHost make_sell(const lina::Csr& A, int ncols, const std::vector<std::vector<
                     if (k < rl && A.col[A.ptr[r] + k] < ncols) {
                         S.col[q] = A.col[A.ptr[r] + k];
                         S.val[q] = A.val[A.ptr[r] + k];
+                        S.pos[A.ptr[r] + k] = (int)q;
                     } else {
                         // padding, or an explicit zero whose column lies outside the
                         // operand (the reference's (i, 0.0) placeholder of an empty row)
@@ -540,6 +586,12 @@ struct lina_gpu_amg {
     DCsr Aorig;                // unflipped finest matrix when signs exist (Krylov SpMV)
     bool has_signs = false;
     bool host_only = false;
+    // maps for lina_gpu_amg_update_values (built on first use, finest level)
+    bool upd_built = false;
+    long upd_nnz = 0;
+    int *upd_posA = nullptr, *upd_posAcol = nullptr, *upd_diagpos = nullptr, *upd_ptr = nullptr;
+    unsigned char* upd_isolated = nullptr;
+    double* upd_val = nullptr;  // staging for host values
     // Krylov work
     double *kr = nullptr, *kz = nullptr, *kp = nullptr, *kq = nullptr, *kx = nullptr, *kb = nullptr,
            *kt = nullptr;
@@ -1225,11 +1277,88 @@ int lina_gpu_amg_recompute(lina_gpu_amg* h, int n, const int* rowptr, const int*
     for (void* p : h->allocations) cudaFree(p);
     h->allocations.clear();
     h->dev_bytes = 0;
+    h->upd_built = false;
     h->Aorig = DCsr();
     int rc = upload_hierarchy(h);
     if (rc) return rc;
     if (h->has_signs) rc = h->upload_csr(h->Aorig, csr_from(n, rowptr, col, val));
     return rc;
+}
+
+namespace {
+
+// CSR entry -> layout position for a matrix uploaded by upload_csr (same layout choice)
+std::vector<int> layout_positions(const lina::Csr& c, const std::vector<std::vector<int>>* groups) {
+    if (csrv_lanes_for(c) > 0) {
+        std::vector<int> pos(c.nnz());
+        for (long k = 0; k < c.nnz(); k++) pos[k] = (int)k;
+        return pos;
+    }
+    return make_sell(c, c.ncols > 0 ? c.ncols : c.n, groups).pos;
+}
+
+int build_update_maps(lina_gpu_amg* h) {
+    const int f = h->depth - 1;
+    const lina::HostLevel& F = h->host.lv[f];
+    const lina::Csr& A = F.A;
+    int rc;
+    std::vector<int> posA = layout_positions(A, nullptr);
+    if ((rc = h->upload(&h->upd_posA, posA.data(), posA.size()))) return rc;
+    {
+        std::vector<int> colour;
+        const int nc = lina::greedy_colouring(A, colour);
+        std::vector<std::vector<int>> groups(nc);
+        for (int i = 0; i < A.n; i++) groups[colour[i]].push_back(i);
+        std::vector<int> posC = layout_positions(A, &groups);
+        if ((rc = h->upload(&h->upd_posAcol, posC.data(), posC.size()))) return rc;
+    }
+    std::vector<int> diagpos(A.n, -1);
+    std::vector<unsigned char> iso(A.n, 0);
+    for (int i = 0; i < A.n; i++) {
+        const bool skip = !F.labels.empty() && F.labels[i] == lina::kUndecided;
+        for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++)
+            if (A.col[p] == i && !skip) diagpos[i] = p;
+        iso[i] = (!F.labels.empty() && F.labels[i] == lina::kIsolated) ? 1 : 0;
+    }
+    if ((rc = h->upload(&h->upd_diagpos, diagpos.data(), diagpos.size()))) return rc;
+    if ((rc = h->upload(&h->upd_isolated, iso.data(), iso.size()))) return rc;
+    if ((rc = h->upload(&h->upd_ptr, A.ptr.data(), A.ptr.size()))) return rc;
+    if ((rc = h->alloc(&h->upd_val, std::max<long>(A.nnz(), 1)))) return rc;
+    CK(cudaStreamSynchronize(h->stream));  // the host vectors above go out of scope
+    h->upd_nnz = A.nnz();
+    h->upd_built = true;
+    return 0;
+}
+
+}  // namespace
+
+int lina_gpu_amg_update_values(lina_gpu_amg* h, const double* val, int flags) {
+    if (!h || h->host_only || !val) {
+        set_err("lina_gpu_amg_update_values: invalid argument");
+        return LINA_GPU_EINVAL;
+    }
+    if (h->depth < 2 || h->has_signs) {
+        set_err("lina_gpu_amg_update_values: %s; use lina_gpu_amg_recompute",
+                h->depth < 2 ? "a one-level hierarchy factorises its only matrix"
+                             : "rows of the setup matrix were sign-flipped");
+        return LINA_GPU_EINVAL;
+    }
+    int rc;
+    if (!h->upd_built && (rc = build_update_maps(h))) return rc;
+    const int f = h->depth - 1;
+    DLevel& L = h->lv[f];
+    const double* v = val;
+    if (!(flags & LINA_PCG_DEVICE_PTRS)) {
+        CK(cudaMemcpyAsync(h->upd_val, val, h->upd_nnz * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        v = h->upd_val;
+    }
+    go(update_values_kernel, grid_for(h->upd_nnz, kThreads), h->stream, h->upd_nnz, v, (const int*)h->upd_posA,
+       (const int*)h->upd_posAcol, L.A.v64, L.A.v32, L.Acol.v64, L.Acol.v32);
+    go(update_diag_kernel, grid_for(L.n, kThreads), h->stream, L.n, v, (const int*)h->upd_ptr,
+       (const int*)h->upd_diagpos, (const unsigned char*)h->upd_isolated, L.dinv64, L.dinv32, h->isoinv);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
 }
 
 int lina_gpu_amg_destroy(lina_gpu_amg* h) {

@@ -23,6 +23,7 @@ STOP_REFERENCE, STOP_RELATIVE = 0, 1
 PCG_DEVICE_PTRS, PCG_USE_X0, PCG_FINAL_PRECON, PCG_TIME_KERNELS, PCG_NORMALIZE, PCG_HOST_LOOP = 1, 2, 4, 8, 16, 32
 UNDECIDED, COARSE, FINE, ISOLATED = 0, 1, 2, 3
 OK, EINVAL, ECUDA, ESETUP, EBREAKDOWN, ENOCONV = 0, -1, -2, -3, -4, -5
+ELASTIC_RECOMPUTE = 64
 
 
 class AmgOptions(C.Structure):
@@ -52,6 +53,12 @@ class SolveInfo(C.Structure):
         ("smoother_launches", C.c_int),
         ("smoother_bytes", C.c_double),
     ]
+
+
+class ElasticProblem(C.Structure):
+    _fields_ = [("n_nodes", C.c_int), ("n_elems", C.c_int), ("xy", C.c_void_p), ("tri", C.c_void_p),
+                ("nu", C.c_double), ("n_fixed", C.c_int), ("fixed_dof", C.c_void_p), ("fixed_val", C.c_void_p),
+                ("n_sensors", C.c_int), ("sensor_dof", C.c_void_p), ("target", C.c_void_p)]
 
 
 class LinaError(RuntimeError):
@@ -113,6 +120,15 @@ def lib():
         "lina_gpu_dot_noalloc": (C.c_int, [vp, vp, C.c_long, dp]),
         "lina_gpu_bicgstab": (C.c_int, [vp, vp, C.c_int, vp, vp, C.c_double, C.c_int, C.c_int, C.POINTER(SolveInfo)]),
         "lina_gpu_free_host": (C.c_int, [vp]),
+        "lina_gpu_amg_update_values": (C.c_int, [vp, vp, C.c_int]),
+        "lina_gpu_elastic_create": (C.c_int, [C.POINTER(ElasticProblem), dp, C.POINTER(AmgOptions), C.POINTER(vp)]),
+        "lina_gpu_elastic_forward": (C.c_int, [vp, vp, C.c_double, C.c_int, C.c_int, vp, dp, C.POINTER(SolveInfo)]),
+        "lina_gpu_elastic_backward": (C.c_int, [vp, C.c_double, C.c_int, C.c_int, vp, vp, C.POINTER(SolveInfo)]),
+        "lina_gpu_elastic_sizes": (C.c_int, [vp, ip, lp]),
+        "lina_gpu_elastic_system": (C.c_int, [vp, ip, ip, dp, dp]),
+        "lina_gpu_elastic_amg": (vp, [vp]),
+        "lina_gpu_elastic_destroy": (C.c_int, [vp]),
+        "lina_gpu_elastic_assemble_host": (C.c_int, [C.POINTER(ElasticProblem), dp, ip, ip, dp, dp, lp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -461,6 +477,95 @@ class AMG:
     def close(self):
         if getattr(self, "h", None):
             lib().lina_gpu_amg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _ProblemArrays:
+    """Keeps the arrays an ElasticProblem points to alive."""
+
+    def __init__(self, xy, tri, nu, fixed_dof, fixed_val, sensor_dof, target):
+        self.xy = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1)
+        self.tri = np.ascontiguousarray(tri, dtype=np.int32).reshape(-1)
+        self.fd = np.ascontiguousarray(fixed_dof, dtype=np.int32)
+        self.fv = np.ascontiguousarray(fixed_val, dtype=np.float64)
+        self.sd = np.ascontiguousarray(sensor_dof if sensor_dof is not None else np.zeros(0), dtype=np.int32)
+        self.tg = np.ascontiguousarray(target if target is not None else np.zeros(len(self.sd)), dtype=np.float64)
+        self.p = ElasticProblem(len(self.xy) // 2, len(self.tri) // 3, self.xy.ctypes.data, self.tri.ctypes.data, nu,
+                                len(self.fd), self.fd.ctypes.data, self.fv.ctypes.data, len(self.sd),
+                                self.sd.ctypes.data, self.tg.ctypes.data)
+
+
+def elastic_assemble_host(xy, tri, nu, fixed_dof, fixed_val, young):
+    """The library's host assembly of A(young) and b; returns (indptr, indices, data, b)."""
+    pa = _ProblemArrays(xy, tri, nu, fixed_dof, fixed_val, None, None)
+    E = np.ascontiguousarray(young, dtype=np.float64)
+    nnz = C.c_long()
+    _check(lib().lina_gpu_elastic_assemble_host(C.byref(pa.p), _dp(E), None, None, None, None, C.byref(nnz)),
+           "elastic assembly")
+    n = 2 * pa.p.n_nodes
+    ptr, col = np.zeros(n + 1, np.int32), np.zeros(nnz.value, np.int32)
+    val, b = np.zeros(nnz.value), np.zeros(n)
+    _check(lib().lina_gpu_elastic_assemble_host(C.byref(pa.p), _dp(E), _ip(ptr), _ip(col), _dp(val), _dp(b),
+                                                C.byref(nnz)), "elastic assembly")
+    return ptr, col, val, b
+
+
+class ElasticAdjoint:
+    """Forward/backward pair of the P1 plane-strain adjoint (lina_gpu_elastic_*)."""
+
+    def __init__(self, xy, tri, nu, fixed_dof, fixed_val, sensor_dof, target, young, **opts):
+        self._pa = _ProblemArrays(xy, tri, nu, fixed_dof, fixed_val, sensor_dof, target)
+        self.n_elems = self._pa.p.n_elems
+        self.n = 2 * self._pa.p.n_nodes
+        opts.setdefault("dof", 2)
+        self.opts = options(**opts)
+        E = np.ascontiguousarray(young, dtype=np.float64)
+        h = C.c_void_p()
+        _check(lib().lina_gpu_elastic_create(C.byref(self._pa.p), _dp(E), C.byref(self.opts), C.byref(h)),
+               "elastic create")
+        self.h = h
+
+    def forward(self, young, tol=1e-12, max_iter=2000, warm=False, recompute=False):
+        """Returns (u, loss, SolveInfo)."""
+        E = np.ascontiguousarray(young, dtype=np.float64)
+        u = np.zeros(self.n)
+        loss = C.c_double()
+        info = SolveInfo()
+        flags = (PCG_USE_X0 if warm else 0) | (ELASTIC_RECOMPUTE if recompute else 0)
+        rc = lib().lina_gpu_elastic_forward(self.h, E.ctypes.data, tol, max_iter, flags, u.ctypes.data,
+                                            C.byref(loss), C.byref(info))
+        if rc not in (0, ENOCONV):
+            raise LinaError(f"elastic forward failed ({rc}): {last_error()}")
+        return u, loss.value, info
+
+    def backward(self, tol=1e-12, max_iter=2000):
+        """Returns (grad, lambda, SolveInfo) at the last forward solution."""
+        g = np.zeros(self.n_elems)
+        lam = np.zeros(self.n)
+        info = SolveInfo()
+        rc = lib().lina_gpu_elastic_backward(self.h, tol, max_iter, 0, g.ctypes.data, lam.ctypes.data,
+                                             C.byref(info))
+        if rc not in (0, ENOCONV):
+            raise LinaError(f"elastic backward failed ({rc}): {last_error()}")
+        return g, lam, info
+
+    def system(self):
+        n, nnz = C.c_int(), C.c_long()
+        _check(lib().lina_gpu_elastic_sizes(self.h, C.byref(n), C.byref(nnz)), "elastic sizes")
+        ptr, col = np.zeros(n.value + 1, np.int32), np.zeros(nnz.value, np.int32)
+        val, b = np.zeros(nnz.value), np.zeros(n.value)
+        _check(lib().lina_gpu_elastic_system(self.h, _ip(ptr), _ip(col), _dp(val), _dp(b)), "elastic system")
+        return ptr, col, val, b
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().lina_gpu_elastic_destroy(self.h)
             self.h = None
 
     def __del__(self):

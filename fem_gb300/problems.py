@@ -281,3 +281,78 @@ def damage_qp(m: int, gc: float = 1.0, ell: float = 0.03, drive: float = 100.0,
     return CSRSystem(nn, indptr, indices, data, b, dof=1,
                      meta={"kind": "damage_qp", "m": m, "gc": gc, "ell": ell, "drive": drive,
                            "lower": lower, "upper": upper, "x0": x0})
+
+
+def elastic_mesh(m: int, top_uy: float = 1e-3):
+    """The m x m grid of ``elasticity_p1`` as an unstructured triangle mesh.
+
+    Returns ``(xy[n_nodes, 2], tri[n_elems, 3], fixed_dof, fixed_val)``.  Triangle
+    ``e = t*(m-1)^2 + r*(m-1) + c`` is the lower (t = 0) or upper (t = 1) triangle
+    of cell (r, c), the element order of ``notch_damage`` and of the ``young``
+    argument of ``elasticity_p1``; vertices counter-clockwise.  Dirichlet dofs as
+    in ``elasticity_p1``: bottom edge clamped, top edge u_y = ``top_uy``.
+    """
+    h = 1.0 / (m - 1)
+    nn = m * m
+    r = np.arange(nn) // m
+    c = np.arange(nn) % m
+    xy = np.stack([c * h, r * h], axis=1).astype(np.float64)
+    nc = m - 1
+    rr, cc = np.meshgrid(np.arange(nc), np.arange(nc), indexing="ij")
+    rr = rr.ravel()
+    cc = cc.ravel()
+    tris = []
+    for tri in (_TRI_LOWER, _TRI_UPPER):
+        tris.append(np.stack([(rr + dr) * m + (cc + dc) for (dr, dc) in tri], axis=1))
+    tri = np.concatenate(tris).astype(np.int32)
+    bottom = np.nonzero(r == 0)[0]
+    top = np.nonzero(r == m - 1)[0]
+    fixed = np.concatenate([bottom, nn + bottom, nn + top])
+    fixed_val = np.concatenate([np.zeros(2 * len(bottom)), np.full(len(top), top_uy)])
+    order = np.argsort(fixed)
+    return xy, tri, fixed[order].astype(np.int32), fixed_val[order]
+
+
+def adjoint_case(m: int, seed: int = 0, sigma: float = 0.5, n_sensors: int = 256, median: float = 210.0):
+    """Material identification on the ``elastic_mesh(m)``: moduli, target moduli and sensors.
+
+    ``young`` and ``young_target`` are per-element lognormal fields
+    ``median * exp(sigma * z)`` with z standard normal from
+    ``numpy.random.default_rng(seed)`` and ``(seed + 1)``; ``n_sensors`` sensor
+    nodes are drawn without replacement from ``default_rng(seed + 2)`` among the
+    nodes off the top and bottom edges (so neither component is a Dirichlet dof),
+    and observe both displacement components: ``sensor_dof = [nodes, n_nodes + nodes]``.
+    The targets are the forward solution for ``young_target`` at those dofs; they
+    are computed by the caller's solver.
+    """
+    ne = 2 * (m - 1) ** 2
+    young = median * np.exp(sigma * np.random.default_rng(seed).standard_normal(ne))
+    young_t = median * np.exp(sigma * np.random.default_rng(seed + 1).standard_normal(ne))
+    nn = m * m
+    r = np.arange(nn) // m
+    candidates = np.nonzero((r > 0) & (r < m - 1))[0]
+    nodes = np.sort(np.random.default_rng(seed + 2).choice(candidates, size=n_sensors, replace=False))
+    sensor_dof = np.concatenate([nodes, nn + nodes]).astype(np.int32)
+    return {"m": m, "young": young, "young_target": young_t, "sensor_dof": sensor_dof}
+
+
+def element_gradient(m: int, u: np.ndarray, lam: np.ndarray, nu: float = 0.3) -> np.ndarray:
+    """dL/dE_e = -lambda_e^T Khat_e u_e for the ``elastic_mesh(m)`` (numpy, FP64).
+
+    ``lam`` must vanish on Dirichlet dofs; ``u`` holds the known values there.
+    Khat_e is the unit-modulus plane-strain element stiffness of ``_elastic_element``.
+    """
+    h = 1.0 / (m - 1)
+    nn = m * m
+    nc = m - 1
+    rr, cc = np.meshgrid(np.arange(nc), np.arange(nc), indexing="ij")
+    rr = rr.ravel()
+    cc = cc.ravel()
+    out = []
+    for tri in (_TRI_LOWER, _TRI_UPPER):
+        ke = _elastic_element(tri, h, 1.0, nu)
+        nodes = [(rr + dr) * m + (cc + dc) for (dr, dc) in tri]
+        ue = np.stack([v for k in nodes for v in (u[k], u[nn + k])], axis=1)
+        le = np.stack([v for k in nodes for v in (lam[k], lam[nn + k])], axis=1)
+        out.append(-np.einsum("ea,ab,eb->e", le, ke, ue))
+    return np.concatenate(out)

@@ -92,6 +92,13 @@ int lina_gpu_amg_create_host_only(int n, const int* rowptr, const int* col, cons
                                   const lina_gpu_amg_options* opt, lina_gpu_amg** out);
 /* AMG_recompute_coarse_matrices (LinA/Multigrid.c:1756): new fine matrix, same P and R. */
 int lina_gpu_amg_recompute(lina_gpu_amg* h, int n, const int* rowptr, const int* col, const double* val);
+/* New values for the finest matrix on the pattern given at creation (val[nnz], host pointer, or
+   device pointer with LINA_PCG_DEVICE_PTRS).  The Krylov operator, the finest smoother and its
+   diagonal take the new values; coarse levels keep the setup's (a preconditioner built for a
+   nearby matrix), so no host work is done.  No reference counterpart: AMG_recompute_coarse_matrices
+   (lina_gpu_amg_recompute) is the exact re-setup.  EINVAL for one-level hierarchies and for
+   matrices whose rows were sign-flipped at setup. */
+int lina_gpu_amg_update_values(lina_gpu_amg* h, const double* val, int flags);
 int lina_gpu_amg_destroy(lina_gpu_amg* h);
 /* change smoother, relaxation or precision of an existing hierarchy */
 int lina_gpu_amg_set_smoother(lina_gpu_amg* h, int smoother, double omega, int precision);
@@ -143,6 +150,58 @@ int lina_gpu_ilu_apply(lina_gpu_ilu* h, int precision, const double* r_dev, doub
    flags: LINA_PCG_DEVICE_PTRS, LINA_PCG_USE_X0; ilu_precision selects the precision of the ILU solves. */
 int lina_gpu_bicgstab(lina_gpu_matrix* A, lina_gpu_ilu* ilu, int ilu_precision, const double* b, double* x,
                       double tol, int max_iter, int flags, lina_gpu_solve_info* info);
+
+/* ---------------------------------------------------------------------------------------------
+   Adjoint gradient of P1 plane-strain elasticity with a per-element Young's modulus (no reference
+   counterpart; the reference's solvers applied to get_transpose(A), LinA/linear_algebra.c:1290,
+   are its oracle).
+   forward : A(E) = sum_e E_e Khat_e assembled on the GPU (Khat_e: the element stiffness with unit
+             modulus), Dirichlet dofs eliminated symmetrically (identity rows, known values lifted
+             into b), A u = b solved by AMG-PCG, L = 1/2 sum_s (u[sensor_dof_s] - target_s)^2.
+   backward: A^T lambda = dL/du with the same hierarchy (A is symmetric by construction, so the
+             transposed solve is the same operator), then dL/dE_e = -lambda_e^T Khat_e u_e per
+             element (lambda_e: the element's six adjoint values, zero on Dirichlet dofs).
+   Dof numbering: node k -> k (x), n_nodes + k (y), the reference's block ordering. */
+typedef struct lina_gpu_elastic lina_gpu_elastic;
+typedef struct lina_gpu_elastic_problem {
+    int n_nodes;
+    int n_elems;
+    const double* xy;          /* [2*n_nodes] x0, y0, x1, y1, ...                         */
+    const int* tri;            /* [3*n_elems] node indices of each triangle               */
+    double nu;                 /* Poisson's ratio (plane strain)                          */
+    int n_fixed;
+    const int* fixed_dof;      /* [n_fixed] Dirichlet dofs, distinct                      */
+    const double* fixed_val;   /* [n_fixed] their values                                  */
+    int n_sensors;
+    const int* sensor_dof;     /* [n_sensors] observed dofs, distinct, not Dirichlet      */
+    const double* target;      /* [n_sensors] observed values                             */
+} lina_gpu_elastic_problem;
+
+#define LINA_ELASTIC_RECOMPUTE 64  /* forward: rebuild the coarse levels for the new matrix
+                                      (AMG_recompute_coarse_matrices) instead of keeping them */
+
+/* builds the pattern, the per-entry element contributions and the AMG hierarchy of A(young)
+   (young: host array of n_elems moduli); opt as for lina_gpu_amg_create */
+int lina_gpu_elastic_create(const lina_gpu_elastic_problem* p, const double* young,
+                            const lina_gpu_amg_options* opt, lina_gpu_elastic** out);
+/* forward pass for the moduli `young` (n_elems); u (2*n_nodes) and loss may be NULL.
+   flags: LINA_PCG_DEVICE_PTRS (young and u on the device), LINA_PCG_USE_X0 (start from the
+   previous forward solution), LINA_ELASTIC_RECOMPUTE.  Stops at ||b - A u|| / ||b|| <= tol. */
+int lina_gpu_elastic_forward(lina_gpu_elastic* h, const double* young, double tol, int max_iter, int flags,
+                             double* u, double* loss, lina_gpu_solve_info* info);
+/* backward pass at the last forward solution: grad (n_elems) = dL/dE, lambda (2*n_nodes) may be
+   NULL; flags: LINA_PCG_DEVICE_PTRS */
+int lina_gpu_elastic_backward(lina_gpu_elastic* h, double tol, int max_iter, int flags, double* grad,
+                              double* lambda, lina_gpu_solve_info* info);
+/* sizes of the assembled system, and the current system copied to the host (NULL skips) */
+int lina_gpu_elastic_sizes(const lina_gpu_elastic* h, int* n, long* nnz);
+int lina_gpu_elastic_system(lina_gpu_elastic* h, int* rowptr, int* col, double* val, double* b);
+lina_gpu_amg* lina_gpu_elastic_amg(lina_gpu_elastic* h);
+int lina_gpu_elastic_destroy(lina_gpu_elastic* h);
+/* the same assembly on the host with the same arithmetic (bit-identical values); *nnz receives
+   the entry count; with rowptr == NULL only *nnz is computed */
+int lina_gpu_elastic_assemble_host(const lina_gpu_elastic_problem* p, const double* young, int* rowptr,
+                                   int* col, double* val, double* b, long* nnz);
 
 /* CUDA-event timing on the hierarchy's stream: elapsed milliseconds between begin and end */
 int lina_gpu_timer_begin(lina_gpu_amg* h);

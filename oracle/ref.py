@@ -121,6 +121,10 @@ class RefMatrix:
         lib().rs_to_csr(self.ptr, _ip(indptr), _ip(indices), _dp(data))
         return indptr, indices[:nnz], data[:nnz]
 
+    def transpose(self):
+        """get_transpose (LinA/linear_algebra.c:1290)."""
+        return RefMatrix(lib().rs_transpose(self.ptr, self.size))
+
     def __del__(self):
         if self.owned and self.ptr and _lib is not None:
             _lib.rs_free(self.ptr)

@@ -13,7 +13,9 @@ pcg solves (LinA/PCGS.c:163) with the smoothers the GPU library implements
 (installed into the reference through AMG_set_smoother) and with the
 reference's own lexicographic SOR.  For bound-constrained damage quadratics
 it records the minimiser and iteration count of reflective_newton with two
-of the reference's local solvers.  Tests compare the GPU library against
+of the reference's local solvers; and for a material-identification case the
+forward solutions and the adjoint solved with the reference's transpose of A.
+Tests compare the GPU library against
 these files on machines where the reference is absent.
 """
 from __future__ import annotations
@@ -57,6 +59,8 @@ RN_CASES = {
     "damage65_rn": lambda: problems.damage_qp(65),
     "damage129_rn": lambda: problems.damage_qp(129),
 }
+# material identification (adjoint) cases: name -> (grid size m, AMG depth)
+ADJOINT_CASES = {"adjoint65": (65, 5)}
 # reference local solvers: name -> RN solver code (5 = RN_UMF slot running BiCGStab + ILU(0), 3 = RN_PCG)
 RN_SOLVERS = {"umf_bicgstab_ilu": 5, "pcg_ilu": 3}
 
@@ -148,10 +152,50 @@ def make_rn_case(name):
     return out
 
 
+def _ref_solve(s, depth, rhs):
+    amg = ref.RefAMG(s, depth, 2, 2, ref.STANDARD)
+    x, it, _ = amg.pcg(rhs, 1e-13, 2000, ref.SMOOTHER_MC_SOR, 1.0)
+    return x, it
+
+
+def make_adjoint_case(name):
+    """Forward solves for the target and actual moduli, then the adjoint solve on the reference's
+    own transpose of A (get_transpose, LinA/linear_algebra.c:1290), all with the reference's pcg."""
+    m, depth = ADJOINT_CASES[name]
+    case = problems.adjoint_case(m, seed=0)
+    _, _, fixed_dof, fixed_val = problems.elastic_mesh(m)
+    sd = case["sensor_dof"]
+    st = problems.elasticity_p1(m, young=case["young_target"].reshape(2, -1))
+    ut, it_t = _ref_solve(st, depth, st.b)
+    target = ut[sd]
+    s = problems.elasticity_p1(m, young=case["young"].reshape(2, -1))
+    u, it_u = _ref_solve(s, depth, s.b)
+    u[fixed_dof] = fixed_val
+    src = np.zeros(s.n)
+    src[sd] = u[sd] - target
+    loss = 0.5 * float(np.sum(src[sd] ** 2))
+    At = ref.RefMatrix.from_csr(s.n, s.indptr, s.indices, s.data).transpose()
+    ip_, ix_, dv_ = At.to_csr()
+    sT = problems.CSRSystem(s.n, ip_, ix_, dv_, src, dof=2)
+    lam, it_l = _ref_solve(sT, depth, src)
+    lam[fixed_dof] = 0.0
+    grad = problems.element_gradient(m, u, lam)
+    return {"m": np.int64(m), "depth": np.int64(depth), "young": case["young"], "young_target": case["young_target"],
+            "sensor_dof": sd, "target": target, "u": u, "lam": lam, "grad": grad, "loss": np.float64(loss),
+            "it": np.array([it_t, it_u, it_l], dtype=np.int64)}
+
+
 def main():
     only = sys.argv[1:]
     if not ref.available():
         sys.exit("oracle/_ref/libLinA_ref.so is missing: run `make -C oracle ref` where the reference tree exists")
+    for name in ADJOINT_CASES:
+        if only and name not in only:
+            continue
+        data = make_adjoint_case(name)
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **data)
+        print(f"{path}: loss {float(data['loss']):.6e}, pcg iterations (target, forward, adjoint) {list(data['it'])}")
     for name in RN_CASES:
         if only and name not in only:
             continue

@@ -1,0 +1,181 @@
+"""Adjoint gradient of P1 plane-strain elasticity (lina_gpu_elastic_*).
+
+Oracle: the reference's own pcg solves of A(E) u = b and of get_transpose(A) lambda = dL/du
+(tests/golden/adjoint65.npz, made by tests/golden/make_golden.py), and central finite
+differences of the loss along seeded random directions.
+"""
+import os
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+from fem_gb300 import lina, problems
+from tests.conftest import ROOT
+
+GOLDEN = os.path.join(ROOT, "tests", "golden", "adjoint65.npz")
+NU = 0.3
+SOL_TOL = 1e-7     # solution and adjoint against the reference FP64 solves
+FD_TOL = 1e-6      # directional derivative against central differences
+FD_STEP = 1e-2     # relative step of the moduli
+
+
+def central_difference(loss_at, h=FD_STEP):
+    """Sixth-order central difference of t -> loss_at(t) at 0: truncation error O(h^6) (about 1e-8
+    relative at h = 1e-2 on these problems), and an amplification of the solves' error by 1.8/h."""
+    f = {k: loss_at(k * h) for k in (-3, -2, -1, 1, 2, 3)}
+    return (45 * (f[1] - f[-1]) - 9 * (f[2] - f[-2]) + (f[3] - f[-3])) / (60 * h)
+
+
+def load():
+    with np.load(GOLDEN) as z:
+        return {k: z[k] for k in z.files}
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def mesh(m):
+    return problems.elastic_mesh(m)
+
+
+@pytest.mark.parametrize("m", [9, 33])
+def test_host_assembly_matches_element_assembly(m):
+    """The library's gather assembly gives the pattern of the stencil assembly exactly and its
+    values to rounding."""
+    xy, tri, fd, fv = mesh(m)
+    E = problems.adjoint_case(m, seed=3, n_sensors=4)["young"]
+    ptr, col, val, b = lina.elastic_assemble_host(xy, tri, NU, fd, fv, E)
+    s = problems.elasticity_p1(m, young=E.reshape(2, -1))
+    assert np.array_equal(ptr, s.indptr) and np.array_equal(col, s.indices)
+    assert np.abs(val - s.data).max() <= 1e-14 * np.abs(s.data).max()
+    assert np.abs(b - s.b).max() <= 1e-14 * np.abs(s.b).max()
+
+
+def test_problem_validation():
+    xy, tri, fd, fv = mesh(9)
+    E = np.full(len(tri), 210.0)
+    with pytest.raises(lina.LinaError):  # sensor on a Dirichlet dof
+        lina.ElasticAdjoint(xy, tri, NU, fd, fv, np.array([fd[0]]), np.array([0.0]), E)
+    with pytest.raises(lina.LinaError):  # node index out of range
+        bad = tri.copy()
+        bad[0, 0] = len(xy)
+        lina.elastic_assemble_host(xy, bad, NU, fd, fv, E)
+    with pytest.raises(lina.LinaError):  # repeated Dirichlet dof
+        lina.elastic_assemble_host(xy, tri, NU, np.concatenate([fd, fd[:1]]), np.concatenate([fv, fv[:1]]), E)
+
+
+def _spsolve_loss(m, E, sd, target):
+    s = problems.elasticity_p1(m, young=E.reshape(2, -1))
+    A = sp.csr_matrix((s.data, s.indices, s.indptr), shape=(s.n, s.n)).tocsc()
+    u = spla.spsolve(A, s.b)
+    return 0.5 * float(np.sum((u[sd] - target) ** 2)), u, A
+
+
+def test_golden_adjoint_is_a_gradient():
+    """Pins the oracle: the reference's adjoint solves the transposed system, and the element
+    gradient built from it matches central differences of a direct solve."""
+    g = load()
+    m = int(g["m"])
+    sd, target = g["sensor_dof"], g["target"]
+    loss, u, A = _spsolve_loss(m, g["young"], sd, target)
+    assert rel(u, g["u"]) < 1e-9
+    src = np.zeros(A.shape[0])
+    src[sd] = u[sd] - target
+    _, _, fd, _ = mesh(m)
+    r = A.T @ g["lam"] - src
+    r[fd] = 0.0
+    assert np.linalg.norm(r) <= 1e-9 * np.linalg.norm(src)
+    rng = np.random.default_rng(11)
+    for _ in range(3):
+        d = rng.standard_normal(len(g["young"]))
+        fd_val = central_difference(lambda t: _spsolve_loss(m, g["young"] * (1 + t * d), sd, target)[0])
+        ad_val = float(np.dot(g["grad"], g["young"] * d))
+        assert abs(fd_val - ad_val) <= FD_TOL * abs(ad_val), (fd_val, ad_val)
+
+
+def _adjoint_for(m, case, target, **opts):
+    xy, tri, fd, fv = mesh(m)
+    return lina.ElasticAdjoint(xy, tri, NU, fd, fv, case["sensor_dof"], target, case["young"], **opts)
+
+
+@pytest.mark.gpu
+def test_device_assembly_is_bit_identical_to_host():
+    m = 33
+    case = problems.adjoint_case(m, seed=5, n_sensors=16)
+    xy, tri, fd, fv = mesh(m)
+    adj = _adjoint_for(m, case, np.zeros(32))
+    for E in (case["young"], case["young_target"]):
+        if E is not case["young"]:
+            adj.forward(E)
+        ptr, col, val, b = adj.system()
+        hp, hc, hv, hb = lina.elastic_assemble_host(xy, tri, NU, fd, fv, E)
+        assert np.array_equal(ptr, hp) and np.array_equal(col, hc)
+        assert np.array_equal(val, hv) and np.array_equal(b, hb)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [lina.PREC_FP64, lina.PREC_MIXED])
+@pytest.mark.parametrize("recompute", [False, True])
+def test_forward_backward_match_reference(precision, recompute):
+    g = load()
+    m = int(g["m"])
+    case = {"young": g["young"], "sensor_dof": g["sensor_dof"]}
+    adj = _adjoint_for(m, case, g["target"], depth=int(g["depth"]), coarsening=lina.STANDARD,
+                       precision=precision)
+    # start from the target moduli so that the forward pass with the golden moduli updates the matrix
+    u, loss, info = adj.forward(g["young_target"])
+    u, loss, info = adj.forward(g["young"], recompute=recompute)
+    assert info.status == 0 and info.true_rel_residual <= 1e-12
+    assert rel(u, g["u"]) <= SOL_TOL
+    assert abs(loss - float(g["loss"])) <= 1e-6 * float(g["loss"])
+    grad, lam, binfo = adj.backward()
+    assert binfo.status == 0
+    assert rel(lam, g["lam"]) <= SOL_TOL
+    assert rel(grad, g["grad"]) <= SOL_TOL
+
+
+# The loss differences are of order 1e-3 of the loss; solves for them stop at a relative residual of
+# FD_SOLVE_TOL so that their error stays below the truncation error of the stencil.
+FD_SOLVE_TOL = 1e-14
+
+
+def _fd_check(m, n_dirs, seed=0, **opts):
+    case = problems.adjoint_case(m, seed=seed)
+    xy, tri, fd, fv = mesh(m)
+    probe = lina.ElasticAdjoint(xy, tri, NU, fd, fv, case["sensor_dof"], np.zeros(len(case["sensor_dof"])),
+                                case["young_target"], **opts)
+    ut, _, _ = probe.forward(case["young_target"])
+    probe.close()
+    target = ut[case["sensor_dof"]]
+    adj = _adjoint_for(m, case, target, **opts)
+    E = case["young"]
+    _, loss, _ = adj.forward(E, tol=FD_SOLVE_TOL, max_iter=400)
+    grad, _, _ = adj.backward(tol=FD_SOLVE_TOL, max_iter=400)
+    rng = np.random.default_rng(seed + 100)
+    errs = []
+    for _ in range(n_dirs):
+        d = rng.standard_normal(len(E))
+        fd_val = central_difference(lambda t: adj.forward(E * (1 + t * d), tol=FD_SOLVE_TOL, max_iter=400,
+                                                          warm=True)[1])
+        ad_val = float(np.dot(grad, E * d))
+        errs.append(abs(fd_val - ad_val) / abs(ad_val))
+    return loss, np.array(errs)
+
+
+@pytest.mark.gpu
+def test_gradient_matches_finite_differences_small():
+    loss, errs = _fd_check(65, 5, depth=5, precision=lina.PREC_MIXED)
+    print("finite-difference relative errors (65 x 65):", errs)
+    assert loss > 0 and errs.max() <= FD_TOL, errs
+
+
+@pytest.mark.gpu
+def test_gradient_matches_finite_differences_513():
+    """The material-identification workload at full size: 513 x 513 nodes (526,338 dofs,
+    524,288 elements, 256 sensor nodes), 20 random directions."""
+    loss, errs = _fd_check(513, 20, depth=8, precision=lina.PREC_MIXED)
+    print("finite-difference relative errors (513 x 513):", errs)
+    assert loss > 0 and errs.max() <= FD_TOL, errs
