@@ -1032,6 +1032,16 @@ MatMult pcg_mat_multi = nullptr;
 Precon pcg_precon = nullptr;
 double pcg_res = 0;
 
+}  // namespace
+
+bool lina::api::device_matmult(MatMultFn f, int n, const double* x, double* y) {
+    return apply_matmult(f, f == PCG_mult ? pcg_default_A : nullptr, n, x, y);
+}
+
+int lina::api::device_precon(PreconFn f, int n, const double* r, double* z) { return apply_precon(f, n, r, z, nullptr); }
+
+namespace {
+
 MatMult bi_mat_mult = nullptr;
 Precon bi_precon = nullptr;
 int bi_max_iter = 1000;  // BiCGStab.c:12

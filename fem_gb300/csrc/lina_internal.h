@@ -33,5 +33,13 @@ double bi_eps_value();
 // the matrix RN_default_mat_mult multiplies with (RN_set_default_matrix)
 sparse_matrix* rn_default_matrix();
 
+// callbacks of the reference's solver interfaces applied to device vectors: the library's own
+// products and preconditioners (PCG_mult, RN_default_mat_mult, PCG_preconlr, PCG_AMG_precon,
+// BI_AMG_precon) run on the GPU, any other function on host copies
+using MatMultFn = void (*)(int, double*, double*);
+using PreconFn = int (*)(int, double*, double*);
+bool device_matmult(MatMultFn f, int n, const double* x, double* y);
+int device_precon(PreconFn f, int n, const double* r, double* z);
+
 }  // namespace api
 }  // namespace lina

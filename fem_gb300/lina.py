@@ -24,6 +24,7 @@ PCG_DEVICE_PTRS, PCG_USE_X0, PCG_FINAL_PRECON, PCG_TIME_KERNELS, PCG_NORMALIZE, 
 UNDECIDED, COARSE, FINE, ISOLATED = 0, 1, 2, 3
 OK, EINVAL, ECUDA, ESETUP, EBREAKDOWN, ENOCONV = 0, -1, -2, -3, -4, -5
 ELASTIC_RECOMPUTE = 64
+GMRES_APPLY_PRECON = 128
 
 
 class AmgOptions(C.Structure):
@@ -121,6 +122,8 @@ def lib():
         "lina_gpu_bicgstab": (C.c_int, [vp, vp, C.c_int, vp, vp, C.c_double, C.c_int, C.c_int, C.POINTER(SolveInfo)]),
         "lina_gpu_free_host": (C.c_int, [vp]),
         "lina_gpu_amg_update_values": (C.c_int, [vp, vp, C.c_int]),
+        "lina_gpu_gmres": (C.c_int, [vp, vp, vp, C.c_int, vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
+                                     C.POINTER(SolveInfo)]),
         "lina_gpu_elastic_create": (C.c_int, [C.POINTER(ElasticProblem), dp, C.POINTER(AmgOptions), C.POINTER(vp)]),
         "lina_gpu_elastic_forward": (C.c_int, [vp, vp, C.c_double, C.c_int, C.c_int, vp, dp, C.POINTER(SolveInfo)]),
         "lina_gpu_elastic_backward": (C.c_int, [vp, C.c_double, C.c_int, C.c_int, vp, vp, C.POINTER(SolveInfo)]),
@@ -351,6 +354,21 @@ def bicgstab(M: "Matrix", b, ilu: "ILU | None" = None, ilu_precision=PREC_FP64, 
     if rc not in (0, ENOCONV):
         raise LinaError(f"bicgstab failed ({rc}): {last_error()}")
     return x, info
+
+
+def gmres(M: "Matrix", b, ilu: "ILU | None" = None, amg: "AMG | None" = None, precon_precision=PREC_FP64, tol=1e-8,
+          i_max=30, max_iter=1000, check_each=False, y0=None, apply_precon=False):
+    """Restarted GMRES on the GPU with a right preconditioner; returns (y, SolveInfo), y the
+    preconditioned iterate (or x = B_r y with apply_precon)."""
+    bb = np.ascontiguousarray(b, dtype=np.float64)
+    y = np.zeros(M.n) if y0 is None else np.array(y0, dtype=np.float64)
+    info = SolveInfo()
+    flags = GMRES_APPLY_PRECON if apply_precon else 0
+    rc = lib().lina_gpu_gmres(M.h, ilu.h if ilu else None, amg.h if amg else None, precon_precision, bb.ctypes.data,
+                              y.ctypes.data, tol, i_max, max_iter, int(check_each), flags, C.byref(info))
+    if rc not in (0, ENOCONV):
+        raise LinaError(f"gmres failed ({rc}): {last_error()}")
+    return y, info
 
 
 class AMG:

@@ -151,6 +151,19 @@ int lina_gpu_ilu_apply(lina_gpu_ilu* h, int precision, const double* r_dev, doub
 int lina_gpu_bicgstab(lina_gpu_matrix* A, lina_gpu_ilu* ilu, int ilu_precision, const double* b, double* x,
                       double tol, int max_iter, int flags, lina_gpu_solve_info* info);
 
+/* Restarted GMRES (the gmres entry point, LinA/gmres.c:308) on A with a right preconditioner: the
+   ILU(0) `ilu`, one V-cycle of `amg` from a zero guess, or none (both NULL); precon_precision
+   selects the ILU solves' precision.  Solves A B_r y = b from the given y; y is the preconditioned
+   iterate, unless flags hold LINA_GMRES_APPLY_PRECON, in which case y receives x = B_r y.
+   Stops when ||b - A B_r y|| / ||b - A B_r y_0|| <= tol, tested at every step (check_each_iter)
+   or at restarts every i_max steps; the step limit max_iter is tested at restarts.  info->iterations
+   = Arnoldi steps, info->rel_residual = the last residual quotient.  Returns 0, LINA_GPU_ENOCONV
+   (step limit) or LINA_GPU_EBREAKDOWN (singular Hessenberg system). */
+#define LINA_GMRES_APPLY_PRECON 128
+int lina_gpu_gmres(lina_gpu_matrix* A, lina_gpu_ilu* ilu, lina_gpu_amg* amg, int precon_precision, const double* b,
+                   double* y, double tol, int i_max, int max_iter, int check_each_iter, int flags,
+                   lina_gpu_solve_info* info);
+
 /* ---------------------------------------------------------------------------------------------
    Adjoint gradient of P1 plane-strain elasticity with a per-element Young's modulus (no reference
    counterpart; the reference's solvers applied to get_transpose(A), LinA/linear_algebra.c:1290,

@@ -93,6 +93,25 @@ double euklid_norm(double* x1, int n);
 void scalar_mult(double a, double* x, int n);
 void vector_add(double* x, double* y, double factor, int n);
 
+int* zero_int_list(int n);
+int* clone_list(int* x, int n);
+double* generate_vector(int size, double val);
+void copy_vector_content(double* x, double* y, int x_pos, int y_pos, int size);
+void vector_pseudo_mult(double* x, double* y, int n);
+void enlarge_matrix(sparse_matrix* A, int mesh_size, int new_size, int equ_index, int var_index);
+void simple_enlarge_matrix(sparse_matrix* A, int add_size);
+
+/* ---- complete factorisations (linear_algebra.c:2909, :3040, :3122) ---- */
+void LU_factorzation(double** A, double** L, double** U, int size);
+void sparse_LU_factorization(sparse_matrix* A, sparse_matrix* L, sparse_matrix* U);
+void complete_LU_factorization(sparse_matrix* A, sparse_matrix* L, sparse_matrix* U);
+
+/* ---- active-set solver (linear_algebra.c:4923-5042): KKT loop around the caller's Solver ---- */
+int active_set_solver(sparse_matrix* A, double* Sol, double* b, sparse_matrix* B, double* L, double* U,
+                      int (*Solver)(sparse_matrix* A, double* X, double* b), int max_iter, double definiteness,
+                      int mode, ass_info** solver_info);
+void free_ass_info(ass_info** info);
+
 /* ---- incomplete factorisation and triangular solves (linear_algebra.c:1952-2043) ---- */
 int incomplete_LU_factorization(sparse_matrix* A, sparse_matrix* L, sparse_matrix* U);
 void L_triang_invert(sparse_matrix* L, double* x);

@@ -75,6 +75,9 @@ def lib():
         "rs_pcg_stock_amg": (C.c_int, [vp, C.c_int, C.c_int, C.c_double, dp, dp, C.c_double, C.c_int, dp]),
         "rs_amg_solve_fresh": (C.c_int, [vp, dp, dp, C.c_double, C.c_int]),
         "rs_bicgstab_ilu": (C.c_int, [vp, dp, dp, C.c_double, C.c_int, C.c_int]),
+        "rs_gmres": (C.c_int, [vp, dp, dp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, ip, dp]),
+        "rs_newton": (C.c_int, [vp, C.c_double, dp, dp, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double]),
+        "rs_active_set": (C.c_int, [vp, dp, dp, dp, dp, C.c_int, ip]),
         "rs_reflective_newton_qp": (C.c_int, [vp, dp, dp, dp, dp, C.c_int, C.c_int, C.c_double, C.c_double]),
     }
     for name, (res, args) in sig.items():
@@ -267,6 +270,53 @@ def reflective_newton_qp(qp, solver=5, max_iter=50, eps=1e-8, bi_eps=1e-8):
     finally:
         lib().rs_silence(0)
     return x, it
+
+
+def gmres(s, y0=None, tol=1e-8, i_max=30, maxiter=1000, check_each=False, use_ilu=True):
+    """The reference gmres on s's matrix with its ILU(0) as right preconditioner; returns
+    (y, iterations, rcode, nomatvec, precision) with y the preconditioned iterate."""
+    A = RefMatrix.from_csr(s.n, s.indptr, s.indices, s.data)
+    y = np.zeros(s.n) if y0 is None else np.array(y0, dtype=np.float64)
+    b = np.array(s.b, dtype=np.float64)
+    out = np.zeros(3, dtype=np.int32)
+    prec = C.c_double()
+    lib().rs_silence(1)
+    try:
+        lib().rs_gmres(A.ptr, _dp(y), _dp(b), tol, i_max, maxiter, int(check_each), int(use_ilu), _ip(out),
+                       C.byref(prec))
+    finally:
+        lib().rs_silence(0)
+    return y, int(out[0]), int(out[1]), int(out[2]), prec.value
+
+
+def newton(s, c, B, X0, maxiter=50, eps=1e-10, mode=1, i_max=30, gmres_maxiter=1000, gmres_tol=1e-10):
+    """Newton_solver for A X + c X^3 = B (A = s's matrix); returns (X, Newton steps)."""
+    A = RefMatrix.from_csr(s.n, s.indptr, s.indices, s.data)
+    X = np.array(X0, dtype=np.float64)
+    BB = np.array(B, dtype=np.float64)
+    lib().rs_silence(1)
+    try:
+        it = lib().rs_newton(A.ptr, c, _dp(BB), _dp(X), maxiter, eps, mode, i_max, gmres_maxiter, gmres_tol)
+    finally:
+        lib().rs_silence(0)
+    return X, it
+
+
+def active_set(s, lower, upper, x0=None, max_iter=100):
+    """active_set_solver with identity constraints lower <= x <= upper and a dense-LU KKT solver;
+    returns (x, iterations, final active count)."""
+    A = RefMatrix.from_csr(s.n, s.indptr, s.indices, s.data)
+    x = np.zeros(s.n) if x0 is None else np.array(x0, dtype=np.float64)
+    b = np.array(s.b, dtype=np.float64)
+    lo = np.array(lower, dtype=np.float64)
+    up = np.array(upper, dtype=np.float64)
+    na = C.c_int()
+    lib().rs_silence(1)
+    try:
+        it = lib().rs_active_set(A.ptr, _dp(x), _dp(b), _dp(lo), _dp(up), max_iter, C.byref(na))
+    finally:
+        lib().rs_silence(0)
+    return x, it, na.value
 
 
 def greedy_colouring(n, indptr, indices, data):

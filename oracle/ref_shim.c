@@ -419,3 +419,105 @@ int rs_reflective_newton_qp(sparse_matrix* H, double* b, double* lower, double* 
     free(idx);
     return it;
 }
+
+/* ---------------------------------------------------------- gmres, Newton, active set (reference) */
+#include "GMRES_Newton.h"
+#include "itlin.h"
+extern void gmres(int n, double* y, MATVEC* matvec, PRECON* preconr, PRECON* preconl, double* b,
+                  struct ITLIN_OPT* opt, struct ITLIN_INFO* info);
+
+static sparse_matrix *gm_A = NULL, *gm_L = NULL, *gm_U = NULL;
+static void gm_matvec(int n, double* y, double* z) {
+    double* r = sparse_mult(gm_A, y);
+    memcpy(z, r, n * sizeof(double));
+    free(r);
+}
+static void gm_ilu(int n, double* z, double* w) {
+    memcpy(w, z, n * sizeof(double));
+    L_triang_invert(gm_L, w);
+    U_triang_invert(gm_U, w);
+}
+
+/* the reference gmres (LinA/gmres.c:308) on A y = b with the ILU(0) of A as right preconditioner
+   (or none); y holds the start on entry and the preconditioned iterate on exit.
+   out: iterations, rcode, nomatvec; precision */
+int rs_gmres(sparse_matrix* A, double* y, double* b, double tol, int i_max, int maxiter, int check_each,
+             int use_ilu, int* out, double* precision) {
+    gm_A = A;
+    gm_L = sparse_zero(A->size);
+    gm_U = sparse_zero(A->size);
+    if (use_ilu) incomplete_LU_factorization(A, gm_L, gm_U);
+    struct ITLIN_OPT opt;
+    struct ITLIN_INFO info;
+    memset(&opt, 0, sizeof opt);
+    memset(&info, 0, sizeof info);
+    opt.tol = tol;
+    opt.i_max = i_max;
+    opt.maxiter = maxiter;
+    opt.termcheck = check_each ? CheckEachIter : CheckOnRestart;
+    opt.errorlevel = None;
+    opt.monitorlevel = None;
+    opt.datalevel = None;
+    gmres(A->size, y, gm_matvec, use_ilu ? gm_ilu : NULL, NULL, b, &opt, &info);
+    free_sparse(gm_L);
+    free_sparse(gm_U);
+    out[0] = info.iter;
+    out[1] = info.rcode;
+    out[2] = info.nomatvec;
+    *precision = info.precision;
+    return info.iter;
+}
+
+/* F_i(X) = (A X)_i + c X_i^3 on the pattern of A: a discretised nonlinear reaction-diffusion
+   operator for the Newton solver tests */
+static sparse_matrix* nw_A = NULL;
+static double nw_c = 0.0;
+static double nw_F(double* X, int i, int size) {
+    double s = 0;
+    for (int j = 0; j < nw_A->Len[i]; j++) s += nw_A->Values[i][j] * X[nw_A->Indices[i][j]];
+    return s + nw_c * X[i] * X[i] * X[i];
+}
+
+/* Newton_solver (LinA/GMRES_Newton.c:212) for F(X) = B from X; mode LARGE_SYSTEM (ILU-GMRES with
+   i_max, gmres_maxiter, gmres_tol) or SMALL_SYSTEM (sparse LU); returns the Newton steps */
+int rs_newton(sparse_matrix* A, double c, double* B, double* X, int maxiter, double eps, int mode, int i_max,
+              int gmres_maxiter, double gmres_tol) {
+    nw_A = A;
+    nw_c = c;
+    Newton_set_function(nw_F);
+    Newton_set_inhomo(B, A->size);
+    Newton_GMRES_options(i_max, gmres_maxiter, gmres_tol);
+    double* lo = malloc(A->size * sizeof(double));
+    double* hi = malloc(A->size * sizeof(double));
+    for (int i = 0; i < A->size; i++) lo[i] = -1e300, hi[i] = 1e300;
+    Newton_set_range(A->size, lo, hi);
+    free(lo);
+    free(hi);
+    return Newton_solver(A, X, maxiter, eps, mode, -1.0);
+}
+
+/* the dense-LU solver callback of the active-set tests */
+static int as_dense_lu(sparse_matrix* M, double* X, double* b) {
+    sparse_matrix* L = sparse_zero(M->size);
+    sparse_matrix* U = sparse_zero(M->size);
+    complete_LU_factorization(M, L, U);
+    memcpy(X, b, M->size * sizeof(double));
+    L_triang_invert(L, X);
+    U_triang_invert(U, X);
+    free_sparse(L);
+    free_sparse(U);
+    return 1;
+}
+
+/* active_set_solver (LinA/linear_algebra.c:4933) with B = identity: lower <= x <= upper, KKT
+   systems solved by a dense LU; returns the active-set iterations, *active_size the final count */
+int rs_active_set(sparse_matrix* A, double* x, double* b, double* lower, double* upper, int max_iter,
+                  int* active_size) {
+    sparse_matrix* B = sparse_identity(A->size);
+    ass_info* info = NULL;
+    int it = active_set_solver(A, x, b, B, lower, upper, as_dense_lu, max_iter, POS_DEFINITE, ASS_DEFAULT, &info);
+    *active_size = info->active_size;
+    free_ass_info(&info);
+    free_sparse(B);
+    return it;
+}

@@ -61,6 +61,8 @@ RN_CASES = {
 }
 # material identification (adjoint) cases: name -> (grid size m, AMG depth)
 ADJOINT_CASES = {"adjoint65": (65, 5)}
+# gmres / Newton_solver / active_set_solver runs of the reference, one file
+SOLVERS_FILE = "solvers"
 # reference local solvers: name -> RN solver code (5 = RN_UMF slot running BiCGStab + ILU(0), 3 = RN_PCG)
 RN_SOLVERS = {"umf_bicgstab_ilu": 5, "pcg_ilu": 3}
 
@@ -185,10 +187,44 @@ def make_adjoint_case(name):
             "it": np.array([it_t, it_u, it_l], dtype=np.int64)}
 
 
+def make_solvers():
+    """gmres with ILU(0) right preconditioning (both termination checks), Newton_solver on a cubic
+    reaction-diffusion problem (ILU-GMRES and sparse-LU steps) and active_set_solver on a
+    box-constrained Poisson problem, all run by the reference."""
+    out = {}
+    systems = {"poisson33": problems.poisson_p1(33, seed=0), "elast17": problems.elasticity_p1(17)}
+    for name, s in systems.items():
+        for check in (0, 1):
+            tol = 1e-8 if name == "poisson33" else 1e-10
+            y, it, rc, nmv, prec = ref.gmres(s, tol=tol, i_max=20, maxiter=1000, check_each=bool(check))
+            key = f"gmres_{name}_{check}"
+            out[key + "_y"], out[key + "_it"], out[key + "_rc"] = y, np.int64(it), np.int64(rc)
+            out[key + "_nomatvec"], out[key + "_precision"] = np.int64(nmv), np.float64(prec)
+            out[key + "_tol"] = np.float64(tol)
+            out[key + "_x"] = ref.ilu_apply(s, y)  # x = B_r y with the reference's ILU(0)
+    s = problems.poisson_p1(17, seed=2)
+    B = 10.0 * s.b
+    for mode in (0, 1):
+        X, it = ref.newton(s, 50.0, B, np.zeros(s.n), maxiter=50, eps=1e-10, mode=mode, i_max=20)
+        out[f"newton_{mode}_x"], out[f"newton_{mode}_it"] = X, np.int64(it)
+    out["newton_B"] = B
+    s = problems.poisson_p1(17, seed=1)
+    lo, up = np.full(s.n, -0.002), np.full(s.n, 0.002)
+    x, it, na = ref.active_set(s, lo, up, max_iter=100)
+    out["active_x"], out["active_it"], out["active_size"] = x, np.int64(it), np.int64(na)
+    out["active_lower"], out["active_upper"] = lo, up
+    return out
+
+
 def main():
     only = sys.argv[1:]
     if not ref.available():
         sys.exit("oracle/_ref/libLinA_ref.so is missing: run `make -C oracle ref` where the reference tree exists")
+    if not only or SOLVERS_FILE in only:
+        data = make_solvers()
+        path = os.path.join(HERE, f"{SOLVERS_FILE}.npz")
+        np.savez_compressed(path, **data)
+        print(f"{path}: " + ", ".join(f"{k}={int(v)}" for k, v in data.items() if k.endswith("_it")))
     for name in ADJOINT_CASES:
         if only and name not in only:
             continue
