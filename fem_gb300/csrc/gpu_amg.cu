@@ -923,6 +923,48 @@ struct lina_gpu_amg {
         correct_and_postsmooth<TX>(l, L, nu, b, x, cx, time_it);
     }
 
+    // nu smoothing sweeps from the current x (not from zero); the result ends in x
+    template <typename TX>
+    void smooth_warm(DLevel& L, int nu, const TX* b, TX* x) {
+        if (opt.smoother == LINA_SMOOTHER_JACOBI) {
+            TX* t = lvx<TX>(L, 1);
+            TX* cur = x;
+            for (int k = 0; k < nu; k++) {
+                TX* nxt = (cur == x) ? t : x;
+                csr<TX, M_JACOBI>(L.A, cur, nxt, b, lvdinv<TX>(L), TX(opt.omega));
+                cur = nxt;
+            }
+            if (cur != x) cudaMemcpyAsync(x, cur, (size_t)L.n * sizeof(TX), cudaMemcpyDeviceToDevice, stream);
+        } else {
+            for (int k = 0; k < nu; k++) sor_sweep(L, b, x, false);
+        }
+    }
+
+    // Full multigrid (FMG_recursive / AMG_full_multigrid, LinA/Multigrid.c:1582-1611): the right-hand
+    // side restricted to every level, the coarsest level solved, then on each finer level the
+    // prolongated coarse solution improved by one V-cycle that starts from it.  F is the finest
+    // right-hand side (signs applied, FP64 on the device); the result goes to X (FP64).
+    template <typename TX>
+    void fmg(const double* F, double* X) {
+        const int f = depth - 1;
+        TX* bf = lvx<TX>(lv[f], 2);
+        const int gf = grid_for(lv[f].n, kThreads);
+        go(convert_kernel<double, TX>, gf, stream, lv[f].n, F, bf);
+        for (int l = f; l > 0; l--) csr<TX, M_SPMV>(lv[l].R, lvx<TX>(lv[l], 2), lvx<TX>(lv[l - 1], 2));
+        coarse_solve<TX>(lvx<TX>(lv[0], 2), lvx<TX>(lv[0], 0));
+        for (int l = 1; l <= f; l++) {
+            DLevel& L = lv[l];
+            TX* x = lvx<TX>(L, 0);
+            const TX* b = lvx<TX>(L, 2);
+            csr<TX, M_SPMV>(L.P, lvx<TX>(lv[l - 1], 0), x);
+            const int nu = (opt.coarsening == LINA_AGGRESSIVE && l == f) ? opt.aggr_smoothing_iterations
+                                                                          : opt.smoothing_iterations;
+            smooth_warm<TX>(L, nu, b, x);
+            run_rest<TX>(l, L, nu, b, x, false);
+        }
+        go(convert_kernel<TX, double>, gf, stream, lv[f].n, (const TX*)lvx<TX>(lv[f], 0), X);
+    }
+
     // z = M^-1 r on the finest level (r FP64 on the device); mixed precision
     // leaves the result in kz32 (FP32), FP64 in z.
     void precondition(const double* r, double* z, bool time_it, bool apply_signs = true) {
@@ -1436,6 +1478,40 @@ int lina_gpu_amg_solve(lina_gpu_amg* h, const double* F, double* X, double eps, 
     if (iterations) *iterations = it;
     if (rel_residual) *rel_residual = (r0 != 0.0) ? rr / r0 : 0.0;
     return std::isfinite(rr) ? 0 : LINA_GPU_EBREAKDOWN;
+}
+
+int lina_gpu_amg_fmg(lina_gpu_amg* h, const double* F, double* X, int flags, double* rel_residual) {
+    if (!h || h->host_only || !F || !X) {
+        set_err("lina_gpu_amg_fmg: invalid argument");
+        return LINA_GPU_EINVAL;
+    }
+    const int n = h->lv[h->depth - 1].n;
+    const bool dev = (flags & LINA_PCG_DEVICE_PTRS) != 0;
+    cudaStream_t st = h->stream;
+    const int gv = grid_for(n, kThreads), gr = grid_red(n);
+    double *b = h->kb, *x = h->kx, *r = h->kr;
+    CK(cudaMemcpyAsync(b, F, n * sizeof(double), dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(x, X, n * sizeof(double), dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+    if (h->has_signs) go(mul_kernel, gv, st, n, b, (const double*)h->signs);
+    const DCsr& A = h->lv[h->depth - 1].A;
+    auto residual = [&]() -> double {
+        h->csr<double, M_RESID>(A, x, r, b);
+        go(norm2_kernel<double>, gr, st, n, (const double*)r, h->partials, h->ticket, h->sc);
+        if (read_scalars(h)) return -1.0;
+        return std::sqrt(h->sc_host->norm2);
+    };
+    const double r0 = residual();
+    if (r0 < 0) return LINA_GPU_ECUDA;
+    if (h->opt.precision == LINA_PREC_MIXED)
+        h->fmg<float>(b, x);
+    else
+        h->fmg<double>(b, x);
+    const double r1 = residual();
+    if (r1 < 0) return LINA_GPU_ECUDA;
+    CK(cudaMemcpyAsync(X, x, n * sizeof(double), dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (rel_residual) *rel_residual = (r0 != 0.0) ? r1 / r0 : 0.0;
+    return std::isfinite(r1) ? 0 : LINA_GPU_EBREAKDOWN;
 }
 
 int lina_gpu_spmv(lina_gpu_amg* h, int level, const double* x_dev, double* y_dev) {

@@ -803,8 +803,8 @@ amg_system_info* AMG_setup(sparse_matrix* A, int deg_of_freedom, int depth, int 
                            void (*coarsest_solver)(sparse_matrix*, sparse_matrix*, double*, double*, int),
                            int* (*Get_iter)(int depth)) {
     (void)prolongation_method;
-    if (cycle_structure != STAND_ALONE)
-        fprintf(stderr, "LinA-GB300: only the STAND_ALONE cycle structure runs on the GPU; using it\n");
+    if (cycle_structure != STAND_ALONE && cycle_structure != FULL_AMG)
+        fprintf(stderr, "LinA-GB300: unknown cycle structure %d; AMG_solve will skip the solution\n", cycle_structure);
     if (coarsest_solver != nullptr)
         fprintf(stderr, "LinA-GB300: a custom coarsest-level solver is not used; the GPU solves the coarsest level\n");
     if (Get_iter != nullptr && Get_iter != AMG_default_iterations)
@@ -879,6 +879,26 @@ int AMG_solve(amg_system_info* Data, double* F, double* Fine_Sol, amg_statistics
     lina_gpu_amg_set_smoother(h, kind, omega, gpu_precision);
     int iters = 0;
     double rel = 0;
+    if (Data->AMG_cycle_structure == FULL_AMG) {
+        // one full-multigrid pass (Multigrid.c:1908-1911); the reference's statistics keep r/r0 = 1
+        // because it does not recompute r after the pass
+        double r = 0;
+        int rc = lina_gpu_amg_fmg(h, F, Fine_Sol, 0, &r);
+        if (rc != 0 && rc != LINA_GPU_EBREAKDOWN) {
+            fprintf(stderr, "LinA-GB300: AMG_solve failed: %s\n", lina_gpu_last_error());
+            return -1;
+        }
+        if (Stat) AMG_add_stat(Stat, 1, r == 0 ? 0.0 : 1.0);
+        if (amg_info == YES) {
+            printf("\niterations: %d\n", 1);
+            printf("total relative residuum: %e\n", 1.0);
+        }
+        return 1;
+    }
+    if (Data->AMG_cycle_structure != STAND_ALONE) {
+        printf("Warning AMG: no solution method choosen -> skip\n");
+        return 0;
+    }
     int rc = lina_gpu_amg_solve(h, F, Fine_Sol, amg_eps, amg_max_iter, 0, &iters, &rel);
     if (rc != 0 && rc != LINA_GPU_EBREAKDOWN) {
         fprintf(stderr, "LinA-GB300: AMG_solve failed: %s\n", lina_gpu_last_error());

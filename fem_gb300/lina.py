@@ -122,6 +122,7 @@ def lib():
         "lina_gpu_bicgstab": (C.c_int, [vp, vp, C.c_int, vp, vp, C.c_double, C.c_int, C.c_int, C.POINTER(SolveInfo)]),
         "lina_gpu_free_host": (C.c_int, [vp]),
         "lina_gpu_amg_update_values": (C.c_int, [vp, vp, C.c_int]),
+        "lina_gpu_amg_fmg": (C.c_int, [vp, vp, vp, C.c_int, dp]),
         "lina_gpu_gmres": (C.c_int, [vp, vp, vp, C.c_int, vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
                                      C.POINTER(SolveInfo)]),
         "lina_gpu_elastic_create": (C.c_int, [C.POINTER(ElasticProblem), dp, C.POINTER(AmgOptions), C.POINTER(vp)]),
@@ -461,6 +462,14 @@ class AMG:
         if rc not in (0, -5):
             raise LinaError(f"pcg failed ({rc}): {last_error()}")
         return info
+
+    def fmg(self, F):
+        """One full-multigrid pass (AMG_solve with FULL_AMG); returns (x, ||F - A x|| / ||F||)."""
+        f = np.ascontiguousarray(F, dtype=np.float64)
+        x = np.zeros(self.n)
+        rel = C.c_double()
+        _check(lib().lina_gpu_amg_fmg(self.h, f.ctypes.data, x.ctypes.data, 0, C.byref(rel)), "FMG")
+        return x, rel.value
 
     def vcycle(self, r):
         rd = DeviceArray.from_host(np.asarray(r, dtype=np.float64))

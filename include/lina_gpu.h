@@ -111,6 +111,11 @@ int lina_gpu_pcg(lina_gpu_amg* h, const double* b, double* x, double tol, int ma
    final relative residual. */
 int lina_gpu_amg_solve(lina_gpu_amg* h, const double* F, double* X, double eps, int max_iter, int flags,
                        int* iterations, double* rel_residual);
+/* AMG_solve with the FULL_AMG cycle structure (AMG_full_multigrid, LinA/Multigrid.c:1595): the
+   right-hand side restricted to all levels, the coarsest solved, then on each finer level the
+   prolongated solution improved by one V-cycle started from it.  X receives the result (its input
+   is not used); *rel_residual = ||F - A X|| / ||F - A X_in||.  flags: LINA_PCG_DEVICE_PTRS. */
+int lina_gpu_amg_fmg(lina_gpu_amg* h, const double* F, double* X, int flags, double* rel_residual);
 /* one preconditioner application z = M^-1 r (device pointers), zero initial guess */
 int lina_gpu_vcycle(lina_gpu_amg* h, const double* r_dev, double* z_dev);
 /* y = A_level x on the device (level = depth-1 is the finest) */

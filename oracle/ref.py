@@ -75,6 +75,7 @@ def lib():
         "rs_pcg_stock_amg": (C.c_int, [vp, C.c_int, C.c_int, C.c_double, dp, dp, C.c_double, C.c_int, dp]),
         "rs_amg_solve_fresh": (C.c_int, [vp, dp, dp, C.c_double, C.c_int]),
         "rs_bicgstab_ilu": (C.c_int, [vp, dp, dp, C.c_double, C.c_int, C.c_int]),
+        "rs_amg_fmg": (C.c_int, [vp, dp, dp]),
         "rs_gmres": (C.c_int, [vp, dp, dp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, ip, dp]),
         "rs_newton": (C.c_int, [vp, C.c_double, dp, dp, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double]),
         "rs_active_set": (C.c_int, [vp, dp, dp, dp, dp, C.c_int, ip]),
@@ -197,6 +198,19 @@ class RefAMG:
         finally:
             lib().rs_silence(0)
         return x, it
+
+    def fmg(self, F, x0=None, smoother=SMOOTHER_REF_SOR, omega=1.0):
+        """AMG_solve with the FULL_AMG cycle structure (one full-multigrid pass); returns x."""
+        x = np.zeros(self.n) if x0 is None else np.array(x0, dtype=np.float64)
+        f = np.array(F, dtype=np.float64)
+        lib().rs_set_smoother(smoother, omega)
+        lib().rs_forget_colouring()
+        lib().rs_silence(1)
+        try:
+            lib().rs_amg_fmg(self.ptr, _dp(f), _dp(x))
+        finally:
+            lib().rs_silence(0)
+        return x
 
     def vcycle(self, r, smoother=SMOOTHER_REF_SOR, omega=1.0):
         z = np.zeros(self.n)

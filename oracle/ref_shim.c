@@ -521,3 +521,14 @@ int rs_active_set(sparse_matrix* A, double* x, double* b, double* lower, double*
     free_sparse(B);
     return it;
 }
+
+/* ---------------------------------------------------------- full multigrid (reference) */
+/* AMG_solve with the full-multigrid cycle structure (LinA/Multigrid.c:1582-1611, :1908) from X */
+int rs_amg_fmg(amg_system_info* I, double* F, double* X) {
+    AMG_print_info(NO);
+    int old = I->AMG_cycle_structure;
+    I->AMG_cycle_structure = FULL_AMG;
+    int it = AMG_solve(I, F, X, NULL);
+    I->AMG_cycle_structure = old;
+    return it;
+}

@@ -187,6 +187,20 @@ def make_adjoint_case(name):
             "it": np.array([it_t, it_u, it_l], dtype=np.int64)}
 
 
+def make_fmg():
+    """One full-multigrid pass (AMG_solve with FULL_AMG) of the reference for every hierarchy case
+    and the GPU smoothers."""
+    out = {}
+    for name, (factory, depth, coarsening) in CASES.items():
+        s = factory()
+        amg = ref.RefAMG(s, depth, 2, 2, coarsening)
+        for sname, (kind, omega) in SMOOTHERS.items():
+            if sname == "refsor":
+                continue
+            out[f"{name}_{sname}"] = amg.fmg(s.b, smoother=kind, omega=omega)
+    return out
+
+
 def make_solvers():
     """gmres with ILU(0) right preconditioning (both termination checks), Newton_solver on a cubic
     reaction-diffusion problem (ILU-GMRES and sparse-LU steps) and active_set_solver on a
@@ -220,6 +234,11 @@ def main():
     only = sys.argv[1:]
     if not ref.available():
         sys.exit("oracle/_ref/libLinA_ref.so is missing: run `make -C oracle ref` where the reference tree exists")
+    if not only or "fmg" in only:
+        data = make_fmg()
+        path = os.path.join(HERE, "fmg.npz")
+        np.savez_compressed(path, **data)
+        print(f"{path}: {len(data)} full-multigrid results")
     if not only or SOLVERS_FILE in only:
         data = make_solvers()
         path = os.path.join(HERE, f"{SOLVERS_FILE}.npz")

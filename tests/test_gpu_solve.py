@@ -7,6 +7,8 @@ mixed-precision path (FP32 V-cycle, FP64 flexible CG) must reach the true
 relative residual 1e-8 and a solution error against the accurate reference
 solution of at most 1e-7 relative (in the 2-norm).
 """
+import os
+
 import numpy as np
 import pytest
 import scipy.sparse as sp
@@ -199,3 +201,28 @@ def test_device_dot(n):
     got = lina.dot(lina.DeviceArray.from_host(a), lina.DeviceArray.from_host(b))
     want = float(np.dot(a, b))
     assert abs(got - want) <= 1e-13 * max(1.0, np.abs(a) @ np.abs(b))
+
+
+# ------------------------------------------------------------ full multigrid (A12)
+FMG_GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "fmg.npz")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", golden_cases())
+@pytest.mark.parametrize("smoother,code,omega", [("jacobi", lina.SMOOTHER_JACOBI, 0.6),
+                                                   ("mcsor", lina.SMOOTHER_MC_SOR, 1.0)])
+def test_fmg_matches_reference(name, smoother, code, omega):
+    """AMG_solve with the FULL_AMG cycle (FMG_recursive) against the reference's pass: FP64 to
+    rounding, the FP32 preconditioner to single precision."""
+    g = load_golden(name)
+    s = system_for(name)
+    with np.load(FMG_GOLDEN) as z:
+        x_ref = z[f"{name}_{smoother}"]
+    amg = lina.AMG.from_system(s, depth=int(g["depth"]), coarsening=int(g["coarsening"]))
+    amg.set_smoother(code, omega, lina.PREC_FP64)
+    x, rel = amg.fmg(s.b)
+    assert np.linalg.norm(x - x_ref) <= 1e-10 * np.linalg.norm(x_ref)
+    assert 0 < rel < 1
+    amg.set_smoother(code, omega, lina.PREC_MIXED)
+    x32, _ = amg.fmg(s.b)
+    assert np.linalg.norm(x32 - x_ref) <= 1e-5 * np.linalg.norm(x_ref)
