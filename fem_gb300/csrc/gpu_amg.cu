@@ -29,7 +29,7 @@ namespace {
 
 std::string g_err;
 unsigned long long g_launches = 0;  // kernels launched by this library (all handles)
-int g_layout = 0;                   // 0 automatic, 1 SELL-32 everywhere, 2 CSR-vector everywhere
+int g_layout = 0;  // 0 automatic, 1 SELL-32, 2 lane groups (size chosen per matrix), 3..6 groups of 4..32 lanes
 
 void set_err(const char* fmt, ...) {
     char buf[512];
@@ -52,7 +52,7 @@ void set_err(const char* fmt, ...) {
 constexpr int kThreads = 256;
 constexpr int kMaxBlocks = 16384;     // partials per reduction value
 constexpr int kGridCap = 152 * 12;    // grid-stride cap: 152 SMs x 12 blocks of 256
-constexpr int kReduceGrid = 152 * 8;  // kernels that end in a grid reduction: one wave of blocks
+constexpr int kReduceGrid = 152 * 4;  // streaming reductions: half a wave, four strides per loop trip
 
 // ---------------------------------------------------------------- reductions
 __device__ __forceinline__ double warp_sum(double v) {
@@ -158,17 +158,25 @@ __global__ void __launch_bounds__(kThreads) sell_kernel(int npos, const int* __r
         const TV* vp = val + p0 + lane;
         TX sum = TX(0);
         int k = 0;
-        for (; k + 4 <= len; k += 4) {
-            const int c0 = cp[32 * k], c1 = cp[32 * (k + 1)], c2 = cp[32 * (k + 2)], c3 = cp[32 * (k + 3)];
-            const TX v0 = TX(vp[32 * k]), v1 = TX(vp[32 * (k + 1)]), v2 = TX(vp[32 * (k + 2)]),
-                     v3 = TX(vp[32 * (k + 3)]);
-            const TX x0 = x[c0], x1 = x[c1], x2 = x[c2], x3 = x[c3];
-            sum += v0 * x0;
-            sum += v1 * x1;
-            sum += v2 * x2;
-            sum += v3 * x3;
+        // eight independent index loads, then eight gathers of x, then the products in stored
+        // order: more loads in flight per thread for the long rows of coarse operators.  The
+        // matrix streams through once (evict-first loads); x is read through the read-only path
+        // (no thread reads an entry of y written by another thread of the same launch, also in
+        // the in-place SOR mode, where rows of one colour do not couple).
+        for (; k + 8 <= len; k += 8) {
+            int c[8];
+            TV v[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) c[u] = __ldcs(cp + 32 * (k + u));
+#pragma unroll
+            for (int u = 0; u < 8; u++) v[u] = __ldcs(vp + 32 * (k + u));
+            TX xv[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) xv[u] = __ldg(x + c[u]);
+#pragma unroll
+            for (int u = 0; u < 8; u++) sum += TX(v[u]) * xv[u];
         }
-        for (; k < len; k++) sum += TX(vp[32 * k]) * x[cp[32 * k]];
+        for (; k < len; k++) sum += TX(__ldcs(vp + 32 * k)) * __ldg(x + __ldcs(cp + 32 * k));
         if constexpr (MODE == M_SPMV) {
             y[i] = sum;
         } else if constexpr (MODE == M_RESID) {
@@ -214,7 +222,20 @@ __global__ void __launch_bounds__(kThreads) csrv_kernel(int nrows, const int* __
             e0 = ptr[i + 1];
         }
         TX sum = TX(0);
-        for (int k = s0 + sub; k < e0; k += S) sum += TX(val[k]) * x[col[k]];
+        int k = s0 + sub;
+        // four strides of the group at a time: independent loads in flight, products summed in order
+        for (; k + 3 * S < e0; k += 4 * S) {
+            const int c0 = __ldcs(col + k), c1 = __ldcs(col + k + S), c2 = __ldcs(col + k + 2 * S),
+                      c3 = __ldcs(col + k + 3 * S);
+            const TV v0 = __ldcs(val + k), v1 = __ldcs(val + k + S), v2 = __ldcs(val + k + 2 * S),
+                     v3 = __ldcs(val + k + 3 * S);
+            const TX x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
+            sum += TX(v0) * x0;
+            sum += TX(v1) * x1;
+            sum += TX(v2) * x2;
+            sum += TX(v3) * x3;
+        }
+        for (; k < e0; k += S) sum += TX(__ldcs(val + k)) * __ldg(x + __ldcs(col + k));
 #pragma unroll
         for (int o = S / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, S);
         if (valid && sub == 0) {
@@ -246,16 +267,27 @@ template <typename TB, typename TX>
 __global__ void jacobi_first_kernel(int n, const TB* __restrict__ b, const double* __restrict__ sign,
                                     const TX* __restrict__ dinv, const double* __restrict__ isoinv, TX w,
                                     TX* __restrict__ x, TX* __restrict__ bout) {
-    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        double bd = double(b[i]);
-        if (sign) bd *= sign[i];
-        TX bi = TX(bd);
-        if (bout) bout[i] = bi;
-        if (isoinv && isoinv[i] != 0.0)
-            x[i] = TX(bd * isoinv[i]);
-        else
-            x[i] = w * dinv[i] * bi;
+    const long S = (long)gridDim.x * blockDim.x;
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    auto one = [&](long k, double bd, TX di, double iso) {
+        if (sign) bd *= sign[k];
+        const TX bi = TX(bd);
+        if (bout) bout[k] = bi;
+        x[k] = (iso != 0.0) ? TX(bd * iso) : w * di * bi;
+    };
+    for (; i + 3 * S < n; i += 4 * S) {
+        double bb[4], iso[4];
+        TX di[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            bb[u] = double(b[i + u * S]);
+            di[u] = dinv[i + u * S];
+            iso[u] = isoinv ? isoinv[i + u * S] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) one(i + u * S, bb[u], di[u], iso[u]);
     }
+    for (; i < n; i += S) one(i, double(b[i]), dinv[i], isoinv ? isoinv[i] : 0.0);
 }
 
 // x = isolated-row fix (zero elsewhere), optional conversion of b
@@ -369,6 +401,10 @@ __global__ void add_kernel(int n, double* __restrict__ x, const TZ* __restrict__
 }
 
 // ------------------------------------------------------------ Krylov kernels
+// The streaming Krylov kernels below take four grid strides per loop trip: the loads of the four
+// elements are independent, so each thread keeps several in flight; partial sums are added in a
+// fixed order (deterministic).
+
 // s_old = s; s = r.z; t = z.q (flexible CG)
 template <typename TZ>
 __global__ void __launch_bounds__(kThreads) dot_rz_kernel(int n, const double* __restrict__ r,
@@ -376,9 +412,24 @@ __global__ void __launch_bounds__(kThreads) dot_rz_kernel(int n, const double* _
                                                           int flexible, double* partials, unsigned* ticket,
                                                           KScalars* sc) {
     double v[2] = {0.0, 0.0};
-#pragma unroll 4
-    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        double zi = double(z[i]);
+    const long S = (long)gridDim.x * blockDim.x;
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + 3 * S < n; i += 4 * S) {
+        double zz[4], rr[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) zz[u] = double(z[i + u * S]), rr[u] = r[i + u * S];
+        if (flexible) {
+            double qq[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) qq[u] = q[i + u * S];
+#pragma unroll
+            for (int u = 0; u < 4; u++) v[1] += zz[u] * qq[u];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) v[0] += rr[u] * zz[u];
+    }
+    for (; i < n; i += S) {
+        const double zi = double(z[i]);
         v[0] += r[i] * zi;
         if (flexible) v[1] += zi * q[i];
     }
@@ -397,8 +448,20 @@ __global__ void update_p_kernel(int n, const TZ* __restrict__ z, double* __restr
     double beta = 0.0;
     if (!first) beta = flexible ? (-sc->alpha * sc->t / sc->s_old) : (sc->s / sc->s_old);
     if (blockIdx.x == 0 && threadIdx.x == 0) sc->beta = beta;
-    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-        p[i] = first ? double(z[i]) : double(z[i]) + beta * p[i];
+    const long S = (long)gridDim.x * blockDim.x;
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (first) {
+        for (; i < n; i += S) p[i] = double(z[i]);
+        return;
+    }
+    for (; i + 3 * S < n; i += 4 * S) {
+        double zz[4], pp[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) zz[u] = double(z[i + u * S]), pp[u] = p[i + u * S];
+#pragma unroll
+        for (int u = 0; u < 4; u++) p[i + u * S] = zz[u] + beta * pp[u];
+    }
+    for (; i < n; i += S) p[i] = double(z[i]) + beta * p[i];
 }
 
 // alpha = s / (p.q); x += alpha p; r -= alpha q; rr = r.r
@@ -408,10 +471,28 @@ __global__ void __launch_bounds__(kThreads) update_xr_kernel(int n, double* __re
                                                              unsigned* ticket, KScalars* sc) {
     const double alpha = sc->s / sc->pq;
     double v[1] = {0.0};
-#pragma unroll 4
-    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const long S = (long)gridDim.x * blockDim.x;
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + 3 * S < n; i += 4 * S) {
+        double xx[4], pp[4], rr[4], qq[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            xx[u] = x[i + u * S];
+            pp[u] = p[i + u * S];
+            rr[u] = r[i + u * S];
+            qq[u] = q[i + u * S];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            x[i + u * S] = xx[u] + alpha * pp[u];
+            const double ri = rr[u] - alpha * qq[u];
+            r[i + u * S] = ri;
+            v[0] += ri * ri;
+        }
+    }
+    for (; i < n; i += S) {
         x[i] += alpha * p[i];
-        double ri = r[i] - alpha * q[i];
+        const double ri = r[i] - alpha * q[i];
         r[i] = ri;
         v[0] += ri * ri;
     }
@@ -426,9 +507,17 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads) norm2_kernel(int n, const T* __restrict__ v, double* partials,
                                                          unsigned* ticket, KScalars* sc) {
     double a[1] = {0.0};
-#pragma unroll 4
-    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        double x = double(v[i]);
+    const long S = (long)gridDim.x * blockDim.x;
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + 3 * S < n; i += 4 * S) {
+        double w[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) w[u] = double(v[i + u * S]);
+#pragma unroll
+        for (int u = 0; u < 4; u++) a[0] += w[u] * w[u];
+    }
+    for (; i < n; i += S) {
+        const double x = double(v[i]);
         a[0] += x * x;
     }
     grid_reduce<1>(a, partials, ticket, [sc](double* t) { sc->norm2 = t[0]; });
@@ -458,16 +547,18 @@ struct DCsr {
     std::vector<int> group_row;     // colour c: rows[group_row[c] .. group_row[c+1])
 };
 
-// Layout choice: one thread per row (SELL-32) when rows are short and there
-// are enough of them to keep every SM busy; otherwise a group of lanes per row.
+// Layout choice, from sweeps of every level of the 2.1M-dof elasticity hierarchy on GB300: one
+// thread per row (SELL-32) for levels of 300k rows or more with rows up to 64 entries; lane groups
+// otherwise, 4 lanes per row from 100k rows (enough rows to fill the GPU, each lane keeps several
+// loads in flight), 8 from 8k rows, and wider groups for the small, dense coarsest levels.
 int csrv_lanes_for(const lina::Csr& c) {
     const double avg = c.n > 0 ? double(c.nnz()) / c.n : 0.0;
     if (g_layout == 1) return 0;
+    if (g_layout >= 3) return 4 << (g_layout - 3);
     if (g_layout == 0 && c.n >= 300000 && avg <= 64.0) return 0;
-    if (avg >= 64.0) return 32;
-    if (avg >= 24.0) return 16;
-    if (avg >= 8.0) return 8;
-    return 4;
+    if (c.n >= 100000 || avg < 8.0) return 4;
+    if (c.n >= 8000) return 8;
+    return avg >= 24.0 ? 16 : 8;
 }
 
 // Host-side SELL-32 construction; `order` lists the rows per group (colour)
@@ -738,7 +829,7 @@ struct lina_gpu_amg {
         const int npos = (slice1 - slice0) * 32;
         if (npos <= 0) return;
         int grid = (npos + kThreads - 1) / kThreads;
-        if (MODE == M_DOT && grid > kReduceGrid) grid = kReduceGrid;
+        if (MODE == M_DOT && grid > kMaxBlocks) grid = kMaxBlocks;
         g_launches++;
         sell_kernel<TV, TX, MODE><<<grid, kThreads, 0, stream>>>(
             npos, m.rowmap ? m.rowmap + (size_t)slice0 * 32 : nullptr, m.sptr + slice0, m.col, val, x, y, b, dinv,
@@ -752,7 +843,7 @@ struct lina_gpu_amg {
         if (nrows <= 0) return;
         const int S = m.lanes;
         long grid = ((long)nrows * S + kThreads - 1) / kThreads;
-        if (MODE == M_DOT && grid > kReduceGrid) grid = kReduceGrid;
+        if (MODE == M_DOT && grid > kMaxBlocks) grid = kMaxBlocks;
         if (grid > (1L << 30)) grid = 1L << 30;
         const int* rl = m.rows ? m.rows + r0 : nullptr;
         g_launches++;
@@ -1219,8 +1310,8 @@ void lina_gpu_default_options(lina_gpu_amg_options* o) {
 const char* lina_gpu_last_error(void) { return g_err.c_str(); }
 
 int lina_gpu_set_layout(int layout) {
-    if (layout < 0 || layout > 2) {
-        set_err("lina_gpu_set_layout: layout must be 0, 1 or 2");
+    if (layout < 0 || layout > 6) {
+        set_err("lina_gpu_set_layout: layout must be 0 to 6");
         return LINA_GPU_EINVAL;
     }
     g_layout = layout;
@@ -1671,6 +1762,10 @@ finish:
     true_residual(h, b, x);
     if (read_scalars(h)) return LINA_GPU_ECUDA;
     inf->true_rel_residual = (bnorm > 0) ? std::sqrt(h->sc_host->norm2) / bnorm : 0.0;
+    // the relative rule is met only when the true residual meets it (after the restarts are used up
+    // the recurrence may claim more than the arithmetic can deliver)
+    if (stop_rule == LINA_STOP_RELATIVE && inf->status == 0 && r0 > 0.0 && std::sqrt(h->sc_host->norm2) / r0 > tol)
+        inf->status = LINA_GPU_ENOCONV;
     if (flags & LINA_PCG_NORMALIZE) {
         CK(cudaMemcpyAsync(h->hscal, &hscale, sizeof(double), cudaMemcpyHostToDevice, st));
         go(scale_kernel, gv, st, n, x, h->hscal, 0);

@@ -260,9 +260,9 @@ void* lina_gpu_malloc_host(size_t bytes);   /* pinned host memory */
 int lina_gpu_free_host(void* p);
 int lina_gpu_device_count(void);
 int lina_gpu_set_device(int device);   /* select the GPU for hierarchies created afterwards */
-/* storage layout of matrices uploaded afterwards: 0 automatic (SELL-32 thread-per-row for large
-   levels with short rows, CSR with a lane group per row otherwise), 1 SELL-32 always,
-   2 CSR lane groups always */
+/* storage layout of matrices uploaded afterwards: 0 automatic (SELL-32 thread-per-row for levels of
+   300k rows or more, CSR with a lane group per row otherwise), 1 SELL-32 always, 2 CSR lane groups
+   always (group size chosen from the mean row length), 3..6 CSR lane groups of 4, 8, 16 or 32 lanes */
 int lina_gpu_set_layout(int layout);
 
 const char* lina_gpu_last_error(void);

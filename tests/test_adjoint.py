@@ -17,7 +17,7 @@ from tests.conftest import ROOT
 GOLDEN = os.path.join(ROOT, "tests", "golden", "adjoint65.npz")
 NU = 0.3
 SOL_TOL = 1e-7     # solution and adjoint against the reference FP64 solves
-FD_TOL = 1e-6      # directional derivative against central differences
+FD_TOL = 1e-6      # directional derivative against central differences (relative)
 FD_STEP = 1e-2     # relative step of the moduli
 
 
@@ -155,27 +155,42 @@ def _fd_check(m, n_dirs, seed=0, **opts):
     _, loss, _ = adj.forward(E, tol=FD_SOLVE_TOL, max_iter=400)
     grad, _, _ = adj.backward(tol=FD_SOLVE_TOL, max_iter=400)
     rng = np.random.default_rng(seed + 100)
-    errs = []
+    fds, ads = [], []
     for _ in range(n_dirs):
         d = rng.standard_normal(len(E))
-        fd_val = central_difference(lambda t: adj.forward(E * (1 + t * d), tol=FD_SOLVE_TOL, max_iter=400,
-                                                          warm=True)[1])
-        ad_val = float(np.dot(grad, E * d))
-        errs.append(abs(fd_val - ad_val) / abs(ad_val))
-    return loss, np.array(errs)
+        fds.append(central_difference(lambda t: adj.forward(E * (1 + t * d), tol=FD_SOLVE_TOL, max_iter=400,
+                                                              warm=True)[1]))
+        ads.append(float(np.dot(grad, E * d)))
+    return loss, np.array(fds), np.array(ads)
+
+
+def check_fd(fds, ads):
+    """Relative agreement |fd - ad| / |ad| <= FD_TOL on every direction whose derivative is not a
+    cancellation (|ad| at least a tenth of the root mean square over the directions); on the others
+    the difference, which stays at the solves' accuracy, is held to FD_TOL times that mean."""
+    rms = np.sqrt(np.mean(ads ** 2))
+    err = np.abs(fds - ads)
+    well = np.abs(ads) >= 0.1 * rms
+    rel = err[well] / np.abs(ads[well])
+    assert well.sum() >= 0.8 * len(ads)
+    assert rel.max() <= FD_TOL, rel
+    assert err.max() <= FD_TOL * rms, err / rms
+    return rel, err / rms
 
 
 @pytest.mark.gpu
 def test_gradient_matches_finite_differences_small():
-    loss, errs = _fd_check(65, 5, depth=5, precision=lina.PREC_MIXED)
-    print("finite-difference relative errors (65 x 65):", errs)
-    assert loss > 0 and errs.max() <= FD_TOL, errs
+    loss, fds, ads = _fd_check(65, 5, depth=5, precision=lina.PREC_MIXED)
+    assert loss > 0
+    rel, scaled = check_fd(fds, ads)
+    print("finite-difference relative errors (65 x 65):", rel, "scaled:", scaled)
 
 
 @pytest.mark.gpu
 def test_gradient_matches_finite_differences_513():
     """The material-identification workload at full size: 513 x 513 nodes (526,338 dofs,
     524,288 elements, 256 sensor nodes), 20 random directions."""
-    loss, errs = _fd_check(513, 20, depth=8, precision=lina.PREC_MIXED)
-    print("finite-difference relative errors (513 x 513):", errs)
-    assert loss > 0 and errs.max() <= FD_TOL, errs
+    loss, fds, ads = _fd_check(513, 20, depth=8, precision=lina.PREC_MIXED)
+    assert loss > 0
+    rel, scaled = check_fd(fds, ads)
+    print("finite-difference relative errors (513 x 513):", rel, "scaled:", scaled)
