@@ -139,7 +139,7 @@ enum { M_SPMV = 0, M_RESID = 1, M_JACOBI = 2, M_SOR = 3, M_ADD = 4, M_DOT = 5 };
 //  M_SOR  : x = x + w dinv (b - A x) for the rows of one colour (in place)
 //  M_ADD  : y = z + A x                             (z may alias y)
 //  M_DOT  : y = A x, and sum_i x_i y_i -> sc->pq
-template <typename TV, typename TX, int MODE>
+template <typename TV, typename TX, int MODE, bool LONG>
 __global__ void __launch_bounds__(kThreads) sell_kernel(int npos, const int* __restrict__ rowmap,
                                                         const int* __restrict__ sptr, const int* __restrict__ col,
                                                         const TV* __restrict__ val, const TX* x, TX* y,
@@ -158,23 +158,70 @@ __global__ void __launch_bounds__(kThreads) sell_kernel(int npos, const int* __r
         const TV* vp = val + p0 + lane;
         TX sum = TX(0);
         int k = 0;
-        // eight independent index loads, then eight gathers of x, then the products in stored
-        // order: more loads in flight per thread for the long rows of coarse operators.  The
-        // matrix streams through once (evict-first loads); x is read through the read-only path
-        // (no thread reads an entry of y written by another thread of the same launch, also in
-        // the in-place SOR mode, where rows of one colour do not couple).
-        for (; k + 8 <= len; k += 8) {
-            int c[8];
-            TV v[8];
+        // Batches of eight entries: eight index loads, eight value loads, eight gathers of x, then
+        // the products in stored order, so every thread keeps several loads in flight.  LONG rows
+        // (dense coarse operators) are software-pipelined: the indices and values of the next
+        // batch are loaded before the gathers of the current one.  Short rows run predicated
+        // batches instead (fewer registers, so more threads per SM).  The matrix streams through
+        // once (evict-first loads); x is read through the read-only path (no thread reads an
+        // entry of y written by another thread of the same launch, also in the in-place SOR
+        // mode, where rows of one colour do not couple).
+        if constexpr (LONG) {
+            if (len >= 8) {
+                int c[8];
+                TV v[8];
 #pragma unroll
-            for (int u = 0; u < 8; u++) c[u] = __ldcs(cp + 32 * (k + u));
+                for (int u = 0; u < 8; u++) c[u] = __ldcs(cp + 32 * u);
 #pragma unroll
-            for (int u = 0; u < 8; u++) v[u] = __ldcs(vp + 32 * (k + u));
-            TX xv[8];
+                for (int u = 0; u < 8; u++) v[u] = __ldcs(vp + 32 * u);
+                for (k = 8;; k += 8) {
+                    TX xv[8];
 #pragma unroll
-            for (int u = 0; u < 8; u++) xv[u] = __ldg(x + c[u]);
+                    for (int u = 0; u < 8; u++) xv[u] = __ldg(x + c[u]);
+                    const bool more = (k + 8 <= len);
+                    int cn[8];
+                    TV vn[8];
+                    if (more) {
 #pragma unroll
-            for (int u = 0; u < 8; u++) sum += TX(v[u]) * xv[u];
+                        for (int u = 0; u < 8; u++) cn[u] = __ldcs(cp + 32 * (k + u));
+#pragma unroll
+                        for (int u = 0; u < 8; u++) vn[u] = __ldcs(vp + 32 * (k + u));
+                    }
+#pragma unroll
+                    for (int u = 0; u < 8; u++) sum += TX(v[u]) * xv[u];
+                    if (!more) break;
+#pragma unroll
+                    for (int u = 0; u < 8; u++) c[u] = cn[u], v[u] = vn[u];
+                }
+            }
+        } else {
+            for (; k + 8 <= len; k += 8) {
+                int c[8];
+                TV v[8];
+                TX xv[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) c[u] = __ldcs(cp + 32 * (k + u));
+#pragma unroll
+                for (int u = 0; u < 8; u++) v[u] = __ldcs(vp + 32 * (k + u));
+#pragma unroll
+                for (int u = 0; u < 8; u++) xv[u] = __ldg(x + c[u]);
+#pragma unroll
+                for (int u = 0; u < 8; u++) sum += TX(v[u]) * xv[u];
+            }
+        }
+        if (k + 4 <= len) {
+            int c[4];
+            TV v[4];
+            TX xv[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) c[u] = __ldcs(cp + 32 * (k + u));
+#pragma unroll
+            for (int u = 0; u < 4; u++) v[u] = __ldcs(vp + 32 * (k + u));
+#pragma unroll
+            for (int u = 0; u < 4; u++) xv[u] = __ldg(x + c[u]);
+#pragma unroll
+            for (int u = 0; u < 4; u++) sum += TX(v[u]) * xv[u];
+            k += 4;
         }
         for (; k < len; k++) sum += TX(__ldcs(vp + 32 * k)) * __ldg(x + __ldcs(cp + 32 * k));
         if constexpr (MODE == M_SPMV) {
@@ -534,6 +581,7 @@ struct DCsr {
     long nnz = 0;        // stored entries of the CSR source
     long padded = 0;     // entries including slice padding
     int npos = 0;        // slice positions (multiple of 32)
+    bool long_rows = false;  // mean row length >= 24: the software-pipelined SELL variant
     int* sptr = nullptr;
     int* col = nullptr;
     double* v64 = nullptr;
@@ -547,16 +595,16 @@ struct DCsr {
     std::vector<int> group_row;     // colour c: rows[group_row[c] .. group_row[c+1])
 };
 
-// Layout choice, from sweeps of every level of the 2.1M-dof elasticity hierarchy on GB300: one
-// thread per row (SELL-32) for levels of 300k rows or more with rows up to 64 entries; lane groups
-// otherwise, 4 lanes per row from 100k rows (enough rows to fill the GPU, each lane keeps several
-// loads in flight), 8 from 8k rows, and wider groups for the small, dense coarsest levels.
+// Layout choice, from sweeps of every level of the 2.1M-dof elasticity hierarchy on GB300 in every
+// layout (FP32 and FP64): one thread per row (SELL-32; long rows software-pipelined) for levels of
+// 100k rows or more; a group of lanes per row for the small coarse levels, 8 lanes from 8k rows
+// (enough rows to fill the GPU, several loads in flight per lane), wider groups below.
 int csrv_lanes_for(const lina::Csr& c) {
     const double avg = c.n > 0 ? double(c.nnz()) / c.n : 0.0;
     if (g_layout == 1) return 0;
     if (g_layout >= 3) return 4 << (g_layout - 3);
-    if (g_layout == 0 && c.n >= 300000 && avg <= 64.0) return 0;
-    if (c.n >= 100000 || avg < 8.0) return 4;
+    if (g_layout == 0 && c.n >= 100000 && avg <= 256.0) return 0;
+    if (avg < 8.0) return 4;
     if (c.n >= 8000) return 8;
     return avg >= 24.0 ? 16 : 8;
 }
@@ -784,6 +832,7 @@ struct lina_gpu_amg {
             return cudaStreamSynchronize(stream) == cudaSuccess ? 0 : LINA_GPU_ECUDA;
         }
         SellHost S = make_sell(c, ncols, groups);
+        d.long_rows = c.n > 0 && double(c.nnz()) / c.n >= 24.0;
         if (S.col.size() > (size_t)INT_MAX) {
             set_err("padded matrix too large for 32-bit SELL offsets");
             return LINA_GPU_EINVAL;
@@ -831,9 +880,13 @@ struct lina_gpu_amg {
         int grid = (npos + kThreads - 1) / kThreads;
         if (MODE == M_DOT && grid > kMaxBlocks) grid = kMaxBlocks;
         g_launches++;
-        sell_kernel<TV, TX, MODE><<<grid, kThreads, 0, stream>>>(
-            npos, m.rowmap ? m.rowmap + (size_t)slice0 * 32 : nullptr, m.sptr + slice0, m.col, val, x, y, b, dinv,
-            w, z, partials, ticket, sc);
+        const int* rm = m.rowmap ? m.rowmap + (size_t)slice0 * 32 : nullptr;
+        if (m.long_rows)
+            sell_kernel<TV, TX, MODE, true><<<grid, kThreads, 0, stream>>>(npos, rm, m.sptr + slice0, m.col, val, x, y,
+                                                                            b, dinv, w, z, partials, ticket, sc);
+        else
+            sell_kernel<TV, TX, MODE, false><<<grid, kThreads, 0, stream>>>(npos, rm, m.sptr + slice0, m.col, val, x,
+                                                                             y, b, dinv, w, z, partials, ticket, sc);
     }
 
     template <typename TV, typename TX, int MODE>
