@@ -108,12 +108,43 @@ __device__ void grid_reduce(double (&v)[NV], double* partials, unsigned* ticket,
     }
 }
 
+// The block's sum of v, stored to partials[blockIdx.x] (no ticket: the SpMV+dot launches use a full
+// grid, and thousands of blocks on one atomic counter cost more than a second small launch).
+__device__ void block_partial(double v, double* partials) {
+    __shared__ double sm[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    v = warp_sum(v);
+    if (lane == 0) sm[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        double x = (lane < nw) ? sm[lane] : 0.0;
+        x = warp_sum(x);
+        if (lane == 0) partials[blockIdx.x] = x;
+    }
+}
+
 // Krylov scalars kept on the device so that no host round trip sits between kernels.
 struct KScalars {
     double s, s_old, pq, t, rr, alpha, beta, r0, norm2, aux, tol;
     int iter;
     int maxit;
 };
+
+// p.q from the block partials of an SpMV+dot launch, summed in block order by one block
+__global__ void dot_finish_kernel(int nparts, const double* __restrict__ partials, KScalars* sc) {
+    __shared__ double sm[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    double x = 0.0;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) x += partials[i];
+    x = warp_sum(x);
+    if (lane == 0) sm[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        double y = (lane < nw) ? sm[lane] : 0.0;
+        y = warp_sum(y);
+        if (lane == 0) sc->pq = y;
+    }
+}
 
 // last node of the graph-captured iteration: continue the device-side loop
 // while the residual test fails and the iteration budget lasts
@@ -237,10 +268,7 @@ __global__ void __launch_bounds__(kThreads) sell_kernel(int npos, const int* __r
             dot += double(x[i]) * double(sum);
         }
     }
-    if constexpr (MODE == M_DOT) {
-        double v[1] = {dot};
-        grid_reduce<1>(v, partials, ticket, [sc](double* t) { sc->pq = t[0]; });
-    }
+    if constexpr (MODE == M_DOT) block_partial(dot, partials);
 }
 
 // CSR with a group of S lanes per row, for levels whose rows are long (dense
@@ -300,10 +328,7 @@ __global__ void __launch_bounds__(kThreads) csrv_kernel(int nrows, const int* __
             }
         }
     }
-    if constexpr (MODE == M_DOT) {
-        double v[1] = {dot};
-        grid_reduce<1>(v, partials, ticket, [sc](double* t) { sc->pq = t[0]; });
-    }
+    if constexpr (MODE == M_DOT) block_partial(dot, partials);
 }
 
 // first pre-smoothing sweep from the zero guess: x = w dinv b (no SpMV); rows
@@ -725,6 +750,7 @@ struct lina_gpu_amg {
     DCsr Aorig;                // unflipped finest matrix when signs exist (Krylov SpMV)
     bool has_signs = false;
     bool host_only = false;
+    int timed_level = 0;       // level whose smoother sweeps LINA_PCG_TIME_KERNELS times (most entries)
     // maps for lina_gpu_amg_update_values (built on first use, finest level)
     bool upd_built = false;
     long upd_nnz = 0;
@@ -887,6 +913,10 @@ struct lina_gpu_amg {
         else
             sell_kernel<TV, TX, MODE, false><<<grid, kThreads, 0, stream>>>(npos, rm, m.sptr + slice0, m.col, val, x,
                                                                              y, b, dinv, w, z, partials, ticket, sc);
+        if (MODE == M_DOT) {
+            g_launches++;
+            dot_finish_kernel<<<1, kThreads, 0, stream>>>(grid, partials, sc);
+        }
     }
 
     template <typename TV, typename TX, int MODE>
@@ -913,6 +943,10 @@ struct lina_gpu_amg {
                 LINA_CSRV_CASE(32)
         }
 #undef LINA_CSRV_CASE
+        if (MODE == M_DOT) {
+            g_launches++;
+            dot_finish_kernel<<<1, kThreads, 0, stream>>>((int)grid, partials, sc);
+        }
     }
 
     // all rows of m (natural order)
@@ -1051,7 +1085,7 @@ struct lina_gpu_amg {
         DLevel& L = lv[l];
         const int nu = (opt.coarsening == LINA_AGGRESSIVE && l == depth - 1) ? opt.aggr_smoothing_iterations
                                                                              : opt.smoothing_iterations;
-        presmooth<TX, TX>(L, nu, b, nullptr, nullptr, const_cast<TX*>(b), x, false);
+        presmooth<TX, TX>(L, nu, b, nullptr, nullptr, const_cast<TX*>(b), x, time_it && l == timed_level);
         run_rest<TX>(l, L, nu, b, x, time_it);
     }
 
@@ -1063,8 +1097,8 @@ struct lina_gpu_amg {
         TX* cx = lvx<TX>(C, 0);
         csr<TX, M_RESID>(L.A, x, r, b);
         csr<TX, M_SPMV>(L.R, r, cb);
-        vcycle_level<TX>(l - 1, cb, cx, false);
-        correct_and_postsmooth<TX>(l, L, nu, b, x, cx, time_it);
+        vcycle_level<TX>(l - 1, cb, cx, time_it);
+        correct_and_postsmooth<TX>(l, L, nu, b, x, cx, time_it && l == timed_level);
     }
 
     // nu smoothing sweeps from the current x (not from zero); the result ends in x
@@ -1126,12 +1160,12 @@ struct lina_gpu_amg {
         const int nu = (opt.coarsening == LINA_AGGRESSIVE) ? opt.aggr_smoothing_iterations : opt.smoothing_iterations;
         const double* sign = (has_signs && apply_signs) ? signs : nullptr;
         if (opt.precision == LINA_PREC_MIXED) {
-            presmooth<double, float>(L, nu, r, sign, isoinv, L.b32, kz32, time_it);
+            presmooth<double, float>(L, nu, r, sign, isoinv, L.b32, kz32, time_it && l == timed_level);
             run_rest<float>(l, L, nu, L.b32, kz32, time_it);
         } else {
             double* b = const_cast<double*>(r);
             if (sign) b = L.b64;
-            presmooth<double, double>(L, nu, r, sign, isoinv, b, z, time_it);
+            presmooth<double, double>(L, nu, r, sign, isoinv, b, z, time_it && l == timed_level);
             run_rest<double>(l, L, nu, b, z, time_it);
         }
     }
@@ -1294,6 +1328,9 @@ int upload_hierarchy(lina_gpu_amg* h) {
     CK(cudaMemsetAsync(h->sc, 0, sizeof(KScalars), h->stream));
     if (!h->sc_host) CK(cudaMallocHost((void**)&h->sc_host, sizeof(KScalars)));
     CK(cudaStreamSynchronize(h->stream));
+    h->timed_level = depth - 1;
+    for (int l = 1; l < depth; l++)
+        if (h->lv[l].A.nnz > h->lv[h->timed_level].A.nnz) h->timed_level = l;
     return 0;
 }
 
@@ -1837,8 +1874,11 @@ finish:
         }
         inf->smoother_ms = tot;
         inf->smoother_launches = h->ev_used / 2;
-        const DLevel& L = h->lv[h->depth - 1];
+        const DLevel& L = h->lv[h->timed_level];
         double nnz = (double)L.A.nnz, nn = (double)L.n;
+        inf->timed_level = h->timed_level;
+        inf->timed_rows = L.n;
+        inf->timed_entries = L.A.nnz;
         if (h->opt.smoother == LINA_SMOOTHER_JACOBI)
             inf->smoother_bytes = mixed ? (8 * nnz + 4 * (nn + 1) + 16 * nn) : (12 * nnz + 4 * (nn + 1) + 32 * nn);
         else  // one colour launch: average share of the sweep

@@ -397,6 +397,9 @@ extern "C" int lina_gpu_gmres(lina_gpu_matrix* A, lina_gpu_ilu* ilu, lina_gpu_am
         info->smoother_ms = 0;
         info->smoother_launches = 0;
         info->smoother_bytes = 0;
+        info->timed_level = 0;
+        info->timed_rows = 0;
+        info->timed_entries = 0;
     }
     cleanup();
     if (rc) return rc;

@@ -53,6 +53,9 @@ class SolveInfo(C.Structure):
         ("smoother_ms", C.c_double),
         ("smoother_launches", C.c_int),
         ("smoother_bytes", C.c_double),
+        ("timed_level", C.c_int),
+        ("timed_rows", C.c_int),
+        ("timed_entries", C.c_long),
     ]
 
 

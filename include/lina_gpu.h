@@ -50,7 +50,8 @@ extern "C" {
 #define LINA_PCG_USE_X0 2        /* start from the given x (default: x = 0)               */
 #define LINA_PCG_FINAL_PRECON 4  /* apply M^-1 once more after the loop for the reference's
                                     pcg residuum (LinA/PCGS.c:217-218)                    */
-#define LINA_PCG_TIME_KERNELS 8  /* time the finest-level smoother launches with CUDA events */
+#define LINA_PCG_TIME_KERNELS 8  /* time the smoother sweeps of the level with the most stored entries
+                                    (the dominant kernel) with CUDA events                 */
 #define LINA_PCG_NORMALIZE 16    /* scale b and x by 1/||b|| during the solve, as pcg does */
 #define LINA_PCG_HOST_LOOP 32    /* drive every iteration from the host instead of the captured
                                     CUDA graph with its device-side while loop              */
@@ -79,6 +80,9 @@ typedef struct lina_gpu_solve_info {
     double smoother_ms;            /* total time of the timed smoother launches           */
     int smoother_launches;         /* number of timed smoother launches                   */
     double smoother_bytes;         /* algorithmic bytes of one timed launch               */
+    int timed_level;               /* level of the timed sweeps: the one with most entries */
+    int timed_rows;                /* its rows                                            */
+    long timed_entries;            /* its stored entries                                  */
 } lina_gpu_solve_info;
 
 void lina_gpu_default_options(lina_gpu_amg_options* opt);
