@@ -780,6 +780,20 @@ bool coarse_factor(const Csr& A, CoarseSolver& cs, std::string& err) {
 
 }  // namespace
 
+namespace {
+// one Galerkin factor product: on the GPU when asked for (same bits), on the host otherwise or
+// when the GPU product fails
+Csr galerkin_product(const Csr& A, const Csr& B, bool gpu) {
+    if (gpu) {
+        Csr C;
+        std::string err;
+        if (spgemm_gpu(A, B, C, err)) return C;
+        fprintf(stderr, "LinA-GB300: Galerkin product on the host (%s)\n", err.c_str());
+    }
+    return spgemm_ref(A, B);
+}
+}  // namespace
+
 // sparse_product (linear_algebra.c:186-222): row i of the result starts as
 // (i, 0.0); a*b is accumulated per column in the order of A's row entries;
 // zero factors are skipped; delete_zeros runs at the end.
@@ -947,9 +961,9 @@ bool amg_setup_host(const Csr& Ain, const AmgParams& p, HostHierarchy& h) {
         if (broke) fprintf(stderr, "LinA-GB300 warning: AMG level %d has a fine row without coarse interpolation\n", i);
         auto t3 = now();
         L.R = amg_transpose(L.P, nc);
-        Csr AP = spgemm_ref(L.A, L.P);
+        Csr AP = galerkin_product(L.A, L.P, p.gpu_products);
         AP.ncols = nc;
-        C.A = spgemm_ref(L.R, AP);
+        C.A = galerkin_product(L.R, AP, p.gpu_products);
         C.A.ncols = nc;
         if (!square_clean(C.A)) {
             h.error = "erroneous coarse matrix";
@@ -976,9 +990,9 @@ bool amg_recompute_host(HostHierarchy& h, const Csr& A) {
     h.lv[depth - 1].A.ncols = A.n;
     for (int i = depth - 1; i > 0; i--) {
         HostLevel& L = h.lv[i];
-        Csr AP = spgemm_ref(L.A, L.P);
+        Csr AP = galerkin_product(L.A, L.P, h.params.gpu_products);
         AP.ncols = L.coarse_size;
-        h.lv[i - 1].A = spgemm_ref(L.R, AP);
+        h.lv[i - 1].A = galerkin_product(L.R, AP, h.params.gpu_products);
         h.lv[i - 1].A.ncols = L.coarse_size;
         if (!square_clean(h.lv[i - 1].A)) {
             h.error = "erroneous coarse matrix";

@@ -36,6 +36,7 @@ struct AmgParams {
     double eps_minus = 0.3;       // strength thresholds (Multigrid.c:35-36)
     double eps_plus = 0.5;
     double matrix_tol = 0.1;      // interpolation truncation (Multigrid.c:37)
+    bool gpu_products = false;    // Galerkin products on the GPU (same results; host if it fails)
 };
 
 struct HostLevel {
@@ -74,6 +75,10 @@ bool amg_recompute_host(HostHierarchy& h, const Csr& A);
 
 // Reference-semantics SpGEMM (sparse_product, LinA/linear_algebra.c:186-222).
 Csr spgemm_ref(const Csr& A, const Csr& B);
+
+// The same product on the GPU, bit-identical (gpu_spgemm.cu); false with err set if the device
+// fails or a row has more distinct columns than its per-warp table.
+bool spgemm_gpu(const Csr& A, const Csr& B, Csr& C, std::string& err);
 
 // Greedy first-fit colouring of the symmetric nonzero graph (smoother ordering).
 int greedy_colouring(const Csr& A, std::vector<int>& colour);

@@ -1444,6 +1444,7 @@ static int amg_create_impl(int n, const int* rowptr, const int* col, const doubl
     p.eps_minus = opt->eps_minus;
     p.eps_plus = opt->eps_plus;
     p.matrix_tol = opt->matrix_tol;
+    p.gpu_products = !host_only;  // the Galerkin products on the GPU (bit-identical to the host's)
     if (!lina::amg_setup_host(csr_from(n, rowptr, col, val), p, h->host)) {
         set_err("AMG setup: %s", h->host.error.c_str());
         delete h;

@@ -125,6 +125,7 @@ def lib():
         "lina_gpu_bicgstab": (C.c_int, [vp, vp, C.c_int, vp, vp, C.c_double, C.c_int, C.c_int, C.POINTER(SolveInfo)]),
         "lina_gpu_free_host": (C.c_int, [vp]),
         "lina_gpu_amg_update_values": (C.c_int, [vp, vp, C.c_int]),
+        "lina_gpu_spgemm": (C.c_int, [C.c_int, C.c_int, ip, ip, dp, C.c_int, ip, ip, dp, C.c_long, ip, ip, dp, lp]),
         "lina_gpu_amg_fmg": (C.c_int, [vp, vp, vp, C.c_int, dp]),
         "lina_gpu_gmres": (C.c_int, [vp, vp, vp, C.c_int, vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
                                      C.POINTER(SolveInfo)]),
@@ -358,6 +359,23 @@ def bicgstab(M: "Matrix", b, ilu: "ILU | None" = None, ilu_precision=PREC_FP64, 
     if rc not in (0, ENOCONV):
         raise LinaError(f"bicgstab failed ({rc}): {last_error()}")
     return x, info
+
+
+def spgemm(a, b, ncols_b):
+    """C = A B on the GPU with the reference's sparse_product semantics; a and b are
+    (indptr, indices, data) triples; returns C's triple."""
+    ap, ac, av = (np.ascontiguousarray(a[0], np.int32), np.ascontiguousarray(a[1], np.int32),
+                  np.ascontiguousarray(a[2], np.float64))
+    bp, bc, bv = (np.ascontiguousarray(b[0], np.int32), np.ascontiguousarray(b[1], np.int32),
+                  np.ascontiguousarray(b[2], np.float64))
+    n, nb = len(ap) - 1, len(bp) - 1
+    nnz = C.c_long()
+    _check(lib().lina_gpu_spgemm(n, ncols_b, _ip(ap), _ip(ac), _dp(av), nb, _ip(bp), _ip(bc), _dp(bv), 0, None, None,
+                                 None, C.byref(nnz)), "spgemm")
+    cp, cc, cv = np.zeros(n + 1, np.int32), np.zeros(max(nnz.value, 1), np.int32), np.zeros(max(nnz.value, 1))
+    _check(lib().lina_gpu_spgemm(n, ncols_b, _ip(ap), _ip(ac), _dp(av), nb, _ip(bp), _ip(bc), _dp(bv),
+                                 max(nnz.value, 1), _ip(cp), _ip(cc), _dp(cv), C.byref(nnz)), "spgemm")
+    return cp, cc[:nnz.value], cv[:nnz.value]
 
 
 def gmres(M: "Matrix", b, ilu: "ILU | None" = None, amg: "AMG | None" = None, precon_precision=PREC_FP64, tol=1e-8,

@@ -173,6 +173,17 @@ int lina_gpu_gmres(lina_gpu_matrix* A, lina_gpu_ilu* ilu, lina_gpu_amg* amg, int
                    double* y, double tol, int i_max, int max_iter, int check_each_iter, int flags,
                    lina_gpu_solve_info* info);
 
+/* C = A B (A: n rows, columns indexing the nb rows of B; CSR, FP64) on the GPU with the
+   reference's sparse_product semantics (LinA/linear_algebra.c:186-222): row i starts as (i, 0.0),
+   products of nonzero factors accumulate per column in A's and B's stored order, zeros are deleted
+   (an emptied row keeps (i, 0.0)) -- bit-identical to the reference.  The AMG setup and recompute
+   of device hierarchies form their Galerkin products R (A P) with it.  Host arrays; *nnz receives
+   the entry count; with capacity 0 only *nnz is computed (C pointers may be NULL), otherwise
+   capacity must hold nnz entries.  LINA_GPU_ECUDA also when a row has more than 512 distinct
+   columns (the device table's bound). */
+int lina_gpu_spgemm(int n, int ncols_b, const int* Ap, const int* Ac, const double* Av, int nb, const int* Bp,
+                    const int* Bc, const double* Bv, long capacity, int* Cp, int* Cc, double* Cv, long* nnz);
+
 /* ---------------------------------------------------------------------------------------------
    Adjoint gradient of P1 plane-strain elasticity with a per-element Young's modulus (no reference
    counterpart; the reference's solvers applied to get_transpose(A), LinA/linear_algebra.c:1290,

@@ -187,6 +187,52 @@ def make_adjoint_case(name):
             "it": np.array([it_t, it_u, it_l], dtype=np.int64)}
 
 
+def spgemm_inputs(seed=7):
+    """Seeded rectangular CSR factors with explicit zeros, empty rows and exactly cancelling
+    products, as (indptr, indices, data) triples: A is 300 x 200, B is 200 x 150."""
+    rng = np.random.default_rng(seed)
+
+    def rand_csr(n, m, density, zero_rows):
+        rows = []
+        for i in range(n):
+            if i in zero_rows:
+                rows.append(([], []))
+                continue
+            k = rng.binomial(m, density)
+            cols = np.sort(rng.choice(m, size=k, replace=False))
+            vals = rng.standard_normal(k)
+            vals[rng.random(k) < 0.1] = 0.0  # explicit zeros
+            rows.append((cols, vals))
+        return rows
+
+    A = rand_csr(300, 200, 0.04, {5, 17, 123})
+    B = rand_csr(200, 150, 0.05, {3, 44})
+    # rows 10 and 11 of B are equal; row 7 of A takes +1 x row 10 and -1 x row 11: exact cancellation
+    B[11] = (np.array(B[10][0]), np.array(B[10][1]))
+    A[7] = (np.array([10, 11]), np.array([1.0, -1.0]))
+
+    def pack(rows):
+        ptr = np.zeros(len(rows) + 1, np.int32)
+        for i, (c, _) in enumerate(rows):
+            ptr[i + 1] = ptr[i] + len(c)
+        col = np.concatenate([np.asarray(c, np.int32) for c, _ in rows]).astype(np.int32)
+        val = np.concatenate([np.asarray(v, np.float64) for _, v in rows])
+        return ptr, col, val
+
+    return pack(A), pack(B)
+
+
+def make_spgemm():
+    """sparse_product (LinA/linear_algebra.c:186) of the reference on spgemm_inputs()."""
+    (ap, ac, av), (bp, bc, bv) = spgemm_inputs()
+    A = ref.RefMatrix.from_csr(len(ap) - 1, ap, ac, av)
+    B = ref.RefMatrix.from_csr(len(bp) - 1, bp, bc, bv)
+    C = ref.RefMatrix(ref.lib().rs_product(A.ptr, B.ptr))
+    cp, cc, cv = C.to_csr()
+    return {"a_ptr": ap, "a_col": ac, "a_val": av, "b_ptr": bp, "b_col": bc, "b_val": bv,
+            "c_ptr": cp, "c_col": cc, "c_val": cv}
+
+
 def make_fmg():
     """One full-multigrid pass (AMG_solve with FULL_AMG) of the reference for every hierarchy case
     and the GPU smoothers."""
@@ -234,6 +280,11 @@ def main():
     only = sys.argv[1:]
     if not ref.available():
         sys.exit("oracle/_ref/libLinA_ref.so is missing: run `make -C oracle ref` where the reference tree exists")
+    if not only or "spgemm" in only:
+        data = make_spgemm()
+        path = os.path.join(HERE, "spgemm.npz")
+        np.savez_compressed(path, **data)
+        print(f"{path}: product with {len(data['c_col'])} entries")
     if not only or "fmg" in only:
         data = make_fmg()
         path = os.path.join(HERE, "fmg.npz")
