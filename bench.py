@@ -61,6 +61,9 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=20.0, help="bound of the CPU baseline sample")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--workload", default="elasticity", choices=["elasticity", "damage", "adjoint"],
+                   help="elasticity: the headline AMG-PCG solve (default); damage: the reflective-Newton "
+                        "damage step on the same mesh; adjoint: the material-identification gradient")
     return p.parse_args()
 
 
@@ -283,6 +286,97 @@ def run_gb300(args, rank, world, local):
         print(json.dumps(out))
 
 
+def common_line(metric, value, unit, world, steps, warmup, ms, dtype, data, config, e2e, launches, clocks,
+                higher=True):
+    return {"metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": steps, "warmup": warmup,
+            "ms_per_step": ms / steps, "higher_is_better": higher, "scaling": "weak", "vs_baseline": None,
+            "dtype": dtype, "data": data, "config": config, "e2e": e2e, "gpu_launches": int(launches),
+            "clocks": clocks.summary()}
+
+
+def run_damage(args, rank, world, local):
+    """Phase-field damage step (AT2 quadratic, 1025 x 1025 nodes, 1.05M unknowns, bounds
+    d_prev <= d <= 1) by reflective Newton with the device BiCGStab + mixed-precision ILU(0) local
+    solver, through the C-ABI with host arrays: a step is one full minimisation from the same start.
+    gpu_launches counts the library's SpMV-family launches only."""
+    from fem_gb300 import lina, problems
+    q = problems.at2_damage(args.m)
+    lo, up, x0 = q.meta["lower"], q.meta["upper"], q.meta["x0"]
+    for _ in range(args.warmup):
+        lina.reflective_newton(q, lo, up, x0)
+    barrier(world)
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = lina.launches()
+    t0 = time.perf_counter()
+    its = [lina.reflective_newton(q, lo, up, x0)[1] for _ in range(args.steps)]
+    ms = max_over_ranks((time.perf_counter() - t0) * 1e3, world)
+    launches = lina.launches() - launches0
+    clocks.stop()
+    value = world * args.steps / (ms / 1e3)
+    out = common_line("reflective-Newton damage minimisations/s at 1.05M dofs to rel. decrease 1e-8", value,
+                      "solves/s", world, args.steps, args.warmup, ms, "f64 Newton / f32 ILU in f64 BiCGStab",
+                      "synthetic (seeded AT2 history field, notch lower bound)",
+                      {"workload": f"AT2 damage {args.m}x{args.m} nodes, {q.n} dofs, bounds d_prev <= d <= 1, "
+                                   "reflective Newton with device BiCGStab + ILU(0)", "dofs": q.n,
+                       "nnz": int(q.nnz)},
+                      {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 8 * 3 * q.n,
+                       "d2h_bytes_per_step": 8 * q.n}, launches, clocks)
+    out["newton_steps"] = its
+    out["roofline"] = None
+    out["cpu_baseline"] = None
+    if rank == 0:
+        print(json.dumps(out))
+
+
+def run_adjoint(args, rank, world, local):
+    """Material identification on the 513 x 513 elasticity mesh (526,338 dofs, 524,288 elements,
+    256 sensor nodes): a step is one forward solve and one backward (adjoint) solve with the
+    per-element gradient, through the C-ABI with host arrays, tolerance 1e-10."""
+    from fem_gb300 import lina, problems
+    m = 513 if args.m == 1025 else args.m
+    case = problems.adjoint_case(m, seed=0)
+    xy, tri, fd, fv = problems.elastic_mesh(m)
+    opts = dict(depth=DEFAULT_DEPTH.get(m, 8) - 1, precision=lina.PREC_MIXED)
+    probe = lina.ElasticAdjoint(xy, tri, 0.3, fd, fv, case["sensor_dof"], np.zeros(len(case["sensor_dof"])),
+                                case["young_target"], **opts)
+    ut, _, _ = probe.forward(case["young_target"], tol=1e-10)
+    probe.close()
+    adj = lina.ElasticAdjoint(xy, tri, 0.3, fd, fv, case["sensor_dof"], ut[case["sensor_dof"]], case["young"],
+                              **opts)
+    E = case["young"]
+
+    def step():
+        adj.forward(E, tol=1e-10)
+        return adj.backward(tol=1e-10)
+
+    for _ in range(args.warmup):
+        step()
+    barrier(world)
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = lina.launches()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    ms = max_over_ranks((time.perf_counter() - t0) * 1e3, world)
+    launches = lina.launches() - launches0
+    clocks.stop()
+    value = world * args.steps / (ms / 1e3)
+    n = 2 * m * m
+    out = common_line("adjoint gradients/s (forward + adjoint solve + per-element dL/dE) at 526k dofs", value,
+                      "gradients/s", world, args.steps, args.warmup, ms, "f32 preconditioner / f64 Krylov",
+                      "synthetic (seeded lognormal moduli, seeded sensors)",
+                      {"workload": f"P1 plane-strain elasticity {m}x{m} nodes, {n} dofs, {len(E)} elements, "
+                                   f"{len(case['sensor_dof']) // 2} sensor nodes, tol 1e-10", "dofs": n},
+                      {"value": value, "unit": "gradients/s", "h2d_bytes_per_step": 8 * len(E),
+                       "d2h_bytes_per_step": 8 * (2 * n + len(E))}, launches, clocks)
+    out["roofline"] = None
+    out["cpu_baseline"] = None
+    if rank == 0:
+        print(json.dumps(out))
+
+
 def run_reference(args, rank, world):
     """CPU implementation of the reference solve on the same workload (rank 0 only)."""
     if rank != 0:
@@ -360,7 +454,12 @@ def main():
     if world > 1:
         from fem_gb300 import lina
         lina.set_device(local)
-    run_gb300(args, rank, world, local)
+    if args.workload == "damage":
+        run_damage(args, rank, world, local)
+    elif args.workload == "adjoint":
+        run_adjoint(args, rank, world, local)
+    else:
+        run_gb300(args, rank, world, local)
 
 
 if __name__ == "__main__":

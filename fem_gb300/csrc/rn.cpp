@@ -788,3 +788,38 @@ void subspace_minimum(sparse_matrix* A, double* b, double* V1, double* V2, doubl
 }
 
 }  // extern "C"
+
+// ============================================================ CSR convenience entry point
+extern "C" int lina_gpu_reflective_newton_csr(int n, const int* ptr, const int* col, const double* val,
+                                              const double* b, const double* lower, const double* upper, double* x,
+                                              int solver, int max_iter, double eps, double bi_eps) {
+    if (n <= 0 || !ptr || !col || !val || !b || !lower || !upper || !x || max_iter < 1) {
+        lina::dev::set_error("lina_gpu_reflective_newton_csr: invalid argument");
+        return LINA_GPU_EINVAL;
+    }
+    sparse_matrix* H = lina::api::from_csr(n, ptr, col, val);
+    std::vector<double> bb(b, b + n), lo(lower, lower + n), up(upper, upper + n);
+    int* idx = get_all_indices(n);
+    // the reference's defaults (reflective_newton.c:6-16) with the caller's limit and tolerance
+    const int old_info = rn_info;
+    RN_print_info(RN_NO);
+    RN_set_params(max_iter, eps, 0.1, 0.9, 0.1, 250., 1., 0.6, 1.1, 1e-3, 1000.);
+    set_RN_Hesse(H);
+    set_RN_linear(bb.data());
+    set_RN_functional(nullptr);
+    RN_set_gradient(nullptr);
+    set_RN_constraints(idx, lo.data(), up.data(), n);
+    BI_set_eps(bi_eps);
+    BI_set_max_iter(1000);
+    RN_set_local_solver(nullptr);
+    RN_set_solver(solver);
+    const int it = reflective_newton(x);
+    set_RN_Hesse(nullptr);
+    set_RN_linear(nullptr);
+    set_RN_constraints(nullptr, nullptr, nullptr, 0);
+    RN_print_info(old_info);
+    lina::api::forget_device_matrix(H);
+    free_sparse(H);
+    free(idx);
+    return it;
+}

@@ -125,6 +125,8 @@ def lib():
         "lina_gpu_bicgstab": (C.c_int, [vp, vp, C.c_int, vp, vp, C.c_double, C.c_int, C.c_int, C.POINTER(SolveInfo)]),
         "lina_gpu_free_host": (C.c_int, [vp]),
         "lina_gpu_amg_update_values": (C.c_int, [vp, vp, C.c_int]),
+        "lina_gpu_reflective_newton_csr": (C.c_int, [C.c_int, ip, ip, dp, dp, dp, dp, dp, C.c_int, C.c_int,
+                                                     C.c_double, C.c_double]),
         "lina_gpu_spgemm": (C.c_int, [C.c_int, C.c_int, ip, ip, dp, C.c_int, ip, ip, dp, C.c_long, ip, ip, dp, lp]),
         "lina_gpu_amg_fmg": (C.c_int, [vp, vp, vp, C.c_int, dp]),
         "lina_gpu_gmres": (C.c_int, [vp, vp, vp, C.c_int, vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
@@ -359,6 +361,25 @@ def bicgstab(M: "Matrix", b, ilu: "ILU | None" = None, ilu_precision=PREC_FP64, 
     if rc not in (0, ENOCONV):
         raise LinaError(f"bicgstab failed ({rc}): {last_error()}")
     return x, info
+
+
+RN_GPU_BICGSTAB_ILU, RN_PCG = 6, 3
+
+
+def reflective_newton(s, lower, upper, x0, solver=RN_GPU_BICGSTAB_ILU, max_iter=50, eps=1e-8, bi_eps=1e-8):
+    """min x.A.x/2 + x.b over lower <= x <= upper (A, b from the CSRSystem s); returns (x, steps)."""
+    x = np.array(x0, dtype=np.float64)
+    ip_ = np.ascontiguousarray(s.indptr, np.int32)
+    ix_ = np.ascontiguousarray(s.indices, np.int32)
+    dv_ = np.ascontiguousarray(s.data, np.float64)
+    b = np.ascontiguousarray(s.b, np.float64)
+    lo = np.ascontiguousarray(lower, np.float64)
+    up = np.ascontiguousarray(upper, np.float64)
+    it = lib().lina_gpu_reflective_newton_csr(s.n, _ip(ip_), _ip(ix_), _dp(dv_), _dp(b), _dp(lo), _dp(up), _dp(x),
+                                              solver, max_iter, eps, bi_eps)
+    if it < 0:
+        raise LinaError(f"reflective_newton failed ({it}): {last_error()}")
+    return x, it
 
 
 def spgemm(a, b, ncols_b):

@@ -356,3 +356,75 @@ def element_gradient(m: int, u: np.ndarray, lam: np.ndarray, nu: float = 0.3) ->
         le = np.stack([v for k in nodes for v in (lam[k], lam[nn + k])], axis=1)
         out.append(-np.einsum("ea,ab,eb->e", le, ke, ue))
     return np.concatenate(out)
+
+
+def _smooth_field(m, seed, modes=4):
+    """A seeded smooth displacement field on the m x m grid: sums of sine modes, [2, m*m]."""
+    rng = np.random.default_rng(seed)
+    h = 1.0 / (m - 1)
+    r = np.arange(m * m) // m
+    c = np.arange(m * m) % m
+    x, y = c * h, r * h
+    u = np.zeros((2, m * m))
+    for comp in range(2):
+        for _ in range(modes):
+            kx, ky = rng.integers(1, 4, size=2)
+            amp = 1e-3 * rng.standard_normal()
+            ph = rng.uniform(0, 2 * np.pi)
+            u[comp] += amp * np.sin(np.pi * kx * x + ph) * np.sin(np.pi * ky * y)
+    return u
+
+
+def at2_damage(m: int, seed: int = 0, gc: float = 2.7e-3, sigma: float = 1.0, E: float = 210.0,
+               nu: float = 0.3) -> CSRSystem:
+    """Phase-field damage step of AT2 type on the m x m grid (scalar P1, one unknown per node).
+
+    Minimise ``sum_e [ (1-d)^2 H_e + gc (d^2/(2 ell) + (ell/2)|grad d|^2) ]`` over the elements,
+    ``ell = 2h``, subject to ``d_prev <= d <= 1``: the quadratic ``d.A.d/2 + d.b`` with
+    ``A = gc*ell*K + (gc/ell)*M + 2*M_H`` and ``b = -2*M_H*1`` (K the P1 Laplacian with natural
+    boundary, M the lumped mass, M_H the lumped mass weighted by H_e).  The history field H_e is
+    lognormal(sigma) from ``default_rng(seed)`` per element times the plane-strain strain energy
+    density of a seeded smooth displacement field; ``d_prev`` is 0.9 times the nodal notch field
+    (exp(-dist/ell) to the notch (0, 0.5)-(0.5, 0.5), the field of ``notch_damage``; the factor
+    keeps the box open where the notch field reaches 1); the start is the midpoint of the box.
+    Returned with meta lower/upper/x0 like ``damage_qp``.
+    """
+    h = 1.0 / (m - 1)
+    ell = 2.0 * h
+    nc = m - 1
+    u = _smooth_field(m, seed + 1)
+    rr, cc = np.meshgrid(np.arange(nc), np.arange(nc), indexing="ij")
+    rr = rr.ravel()
+    cc = cc.ravel()
+    rng = np.random.default_rng(seed)
+    psi = []
+    f = E / ((1.0 + nu) * (1.0 - 2.0 * nu))
+    D = f * np.array([[1.0 - nu, nu, 0.0], [nu, 1.0 - nu, 0.0], [0.0, 0.0, (1.0 - 2.0 * nu) / 2.0]])
+    for tri in (_TRI_LOWER, _TRI_UPPER):
+        b, cvec, area = _tri_geometry(tri, h)
+        nodes = [(rr + dr) * m + (cc + dc) for (dr, dc) in tri]
+        exx = sum(b[k] * u[0][nodes[k]] for k in range(3)) / (2 * area)
+        eyy = sum(cvec[k] * u[1][nodes[k]] for k in range(3)) / (2 * area)
+        gxy = sum(cvec[k] * u[0][nodes[k]] + b[k] * u[1][nodes[k]] for k in range(3)) / (2 * area)
+        eps = np.stack([exx, eyy, gxy])
+        psi.append(0.5 * np.einsum("ie,ij,je->e", eps, D, eps))
+    H = np.stack(psi) * np.exp(sigma * rng.standard_normal((2, nc * nc)))
+    kl = [(_TRI_LOWER, gc * ell * _laplace_element(_TRI_LOWER, h)),
+          (_TRI_UPPER, gc * ell * _laplace_element(_TRI_UPPER, h))]
+    ml = [(_TRI_LOWER, _mass_element(_TRI_LOWER, h)), (_TRI_UPPER, _mass_element(_TRI_UPPER, h))]
+    vk, valid = _assemble(m, 1, kl, None)
+    vm, _ = _assemble(m, 1, ml, gc / ell + 2.0 * H)
+    vf, _ = _assemble(m, 1, ml, 2.0 * H)
+    indptr, indices, data, _ = _to_csr(m, 1, vk + vm, valid, np.zeros(0, dtype=np.int64), 0.0)
+    b = -vf[0, :, 3].copy()
+    nn = m * m
+    r = np.arange(nn) // m
+    c = np.arange(nn) % m
+    x, y = c * h, r * h
+    dx = np.where(x > 0.5, x - 0.5, 0.0)
+    lower = 0.9 * np.exp(-np.sqrt(dx * dx + (y - 0.5) ** 2) / ell)
+    upper = np.ones(nn)
+    x0 = 0.5 * (lower + upper)
+    return CSRSystem(nn, indptr, indices, data, b, dof=1,
+                     meta={"kind": "at2_damage", "m": m, "gc": gc, "ell": ell, "lower": lower, "upper": upper,
+                           "x0": x0})

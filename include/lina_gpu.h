@@ -184,6 +184,15 @@ int lina_gpu_gmres(lina_gpu_matrix* A, lina_gpu_ilu* ilu, lina_gpu_amg* amg, int
 int lina_gpu_spgemm(int n, int ncols_b, const int* Ap, const int* Ac, const double* Av, int nb, const int* Bp,
                     const int* Bc, const double* Bv, long capacity, int* Cp, int* Cc, double* Cv, long* nnz);
 
+/* reflective_newton (LinA/reflective_newton.c:660) on min x.A.x/2 + x.b, lower <= x <= upper, for a
+   CSR Hessian and host arrays: the drop-in set-up done for the caller (the reference's default
+   parameters, every unknown bounded, local solver `solver` -- RN_GPU_BICGSTAB_ILU keeps the Newton
+   solves on the device -- with BiCGStab tolerance bi_eps).  x holds the start and receives the
+   minimiser; returns the Newton steps or a negative LINA_GPU_E* code. */
+int lina_gpu_reflective_newton_csr(int n, const int* ptr, const int* col, const double* val, const double* b,
+                                   const double* lower, const double* upper, double* x, int solver, int max_iter,
+                                   double eps, double bi_eps);
+
 /* ---------------------------------------------------------------------------------------------
    Adjoint gradient of P1 plane-strain elasticity with a per-element Young's modulus (no reference
    counterpart; the reference's solvers applied to get_transpose(A), LinA/linear_algebra.c:1290,

@@ -58,6 +58,7 @@ MAX_IT = 500
 RN_CASES = {
     "damage65_rn": lambda: problems.damage_qp(65),
     "damage129_rn": lambda: problems.damage_qp(129),
+    "at2_65_rn": lambda: problems.at2_damage(65),
 }
 # material identification (adjoint) cases: name -> (grid size m, AMG depth)
 ADJOINT_CASES = {"adjoint65": (65, 5)}
