@@ -1,19 +1,37 @@
-// gpu_ilu.cu - ILU(0) preconditioner application on the GPU by level scheduling.
+// gpu_ilu.cu - ILU(0) factorisation and application on the GPU.
 //
 // The factors are the reference's (incomplete_LU_factorization,
-// LinA/linear_algebra.c:1952-1982: L lower triangular with its diagonal, U
-// upper triangular with a unit diagonal); applying the preconditioner is the
-// forward solve L y = r followed by the backward solve U z = y
-// (L_triang_invert / U_triang_invert, :2008-2043).  Rows are grouped into
-// levels: a row's level is one more than the highest level among the rows it
-// depends on, so all rows of a level can be solved at once.  On the structured
-// meshes of this path the levels are anti-diagonals with a few hundred rows
-// each, so one thread block walks all levels in order with a block barrier
-// between levels: no inter-block waiting, no per-level launch.
+// LinA/linear_algebra.c:1952-1982, with row_times_row :1795): on A's pattern,
+// row by row, L_ij = a_ij - sum_{k<j} L_ik U_kj for j <= i and
+// U_ij = (a_ij - sum_{k<i} L_ik U_kj) / L_ii for j > i (U has a unit
+// diagonal; the sums run over k in ascending order).  Applying the
+// preconditioner is the forward solve L y = r and the backward solve U z = y
+// (L_triang_invert / U_triang_invert, :2008-2043).
+//
+// Both the factorisation and the solves are row-by-row recurrences: a row
+// needs the finished rows it couples to (smaller indices for the factorisation
+// and the forward solve, larger ones for the backward solve).  Rows are ordered
+// by level (one more than the highest level among the rows they need) and a
+// fixed pool of warps takes them in that order, 32 rows (one per lane) per
+// ticket from a counter; a row waits only for the rows it needs.  A warp takes
+// a ticket only after all smaller tickets were taken by running warps, and it
+// finishes its rows before it takes the next, so every row waited for is being
+// worked on: the passes cannot deadlock, whatever the launch order of blocks.
+// In the solves a row waits on the solution entries themselves: the pass first
+// fills x with a NaN pattern that arithmetic never produces (a result with that
+// pattern is stored as the canonical NaN), and an entry is final once it no
+// longer holds the pattern (aligned 32- and 64-bit stores are single-copy
+// atomic).  The factorisation publishes a row's values and then a flag holding
+// the pass number.  The waits are bounded: a wait that runs out sets an error
+// code that the host reads, and the pass ends instead of spinning on.  Products
+// and sums of the factorisation are rounded one at a time in the reference's
+// order, so the factors are bit-identical to the reference's.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -22,23 +40,194 @@
 
 namespace {
 
-constexpr int kBlock = 1024;
+constexpr int kT = 256;      // threads of the elementwise kernels
+constexpr int kPool = 128;   // threads of a block of the worker pool
+// a wait gives up after kWaitNs of device time (or kWaitPolls polls, whichever comes first); the
+// longest legitimate wait is the time the pool needs for the rows taken before a row, far below it
+constexpr unsigned long long kWaitNs = 2000000000ull;
+constexpr long kWaitPolls = 1L << 26;
+constexpr unsigned kMaxSleepNs = 256;
 
-template <typename TV, typename TX>
-__global__ void __launch_bounds__(kBlock) tri_levels_kernel(int nlev, const int* __restrict__ lev_ptr,
-                                                          const int* __restrict__ rows, const int* __restrict__ ptr,
-                                                          const int* __restrict__ col, const TV* __restrict__ val,
-                                                          const TX* __restrict__ dinv, const TX* __restrict__ b,
-                                                          TX* x) {
-    for (int l = 0; l < nlev; l++) {
-        const int k1 = lev_ptr[l + 1];
-        for (int k = lev_ptr[l] + threadIdx.x; k < k1; k += blockDim.x) {
-            const int i = rows[k];
-            TX s = b[i];
-            for (int p = ptr[i]; p < ptr[i + 1]; p++) s -= TX(val[p]) * x[col[p]];
-            x[i] = s * dinv[i];
+cudaStream_t st() { return (cudaStream_t)lina::dev::stream(); }
+
+__device__ __forceinline__ unsigned long long device_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// the next 32 rows of the order for this warp (the same value in every lane)
+__device__ __forceinline__ int take_chunk(unsigned* ticket) {
+    unsigned c = 0;
+    if ((threadIdx.x & 31) == 0) c = atomicAdd(ticket, 1u);
+    return (int)__shfl_sync(0xffffffffu, c, 0);
+}
+
+// bounded wait with back-off; `ready` polls the awaited value.  False (and *err = 1) when the wait
+// runs out or a pass failed elsewhere
+template <typename Ready>
+__device__ __forceinline__ bool wait_for(Ready ready, int* err) {
+    if (ready()) return true;
+    const unsigned long long t0 = device_ns();
+    long polls = 0;
+    unsigned ns = 32;
+    while (!ready()) {
+        if (++polls > kWaitPolls || *(volatile int*)err || device_ns() - t0 > kWaitNs) {
+            atomicCAS(err, 0, 1);
+            return false;
         }
-        __syncthreads();
+        __nanosleep(ns);
+        ns = ns < kMaxSleepNs ? 2 * ns : kMaxSleepNs;
+    }
+    return true;
+}
+
+template <typename T>
+struct Word;
+template <>
+struct Word<float> {
+    using U = unsigned;
+    static constexpr U kPending = 0xffffffffu;   // a NaN arithmetic does not produce
+    static constexpr U kNaN = 0x7fc00000u;
+};
+template <>
+struct Word<double> {
+    using U = unsigned long long;
+    static constexpr U kPending = 0xffffffffffffffffull;
+    static constexpr U kNaN = 0x7ff8000000000000ull;
+};
+
+template <typename T>
+__device__ __forceinline__ typename Word<T>::U bits(T v) {
+    typename Word<T>::U u;
+    memcpy(&u, &v, sizeof(T));
+    return u;
+}
+template <typename T>
+__device__ __forceinline__ T from_bits(typename Word<T>::U u) {
+    T v;
+    memcpy(&v, &u, sizeof(T));
+    return v;
+}
+
+// x_i = (b_i - sum_{p in [beg_i, end_i)} val_p x_{col_p}) * dinv_i (dinv null: unit diagonal), rows in
+// `order`; x holds the pending pattern on entry
+template <typename TV, typename TX>
+__global__ void __launch_bounds__(kPool) sptrsv_kernel(int n, const int* __restrict__ order,
+                                                       const int* __restrict__ beg, const int* __restrict__ end,
+                                                       const int* __restrict__ col, const TV* __restrict__ val,
+                                                       const TX* __restrict__ dinv, const TX* __restrict__ b, TX* x,
+                                                       unsigned* ticket, int* err) {
+    using U = typename Word<TX>::U;
+    volatile U* xw = reinterpret_cast<volatile U*>(x);
+    const int nchunks = (n + 31) >> 5;
+    for (int c = take_chunk(ticket); c < nchunks; c = take_chunk(ticket)) {
+        const int t = c * 32 + (threadIdx.x & 31);
+        if (t < n) {
+            const int i = order[t];
+            const int p1 = end[i];
+            TX s = b[i];
+            bool ok = true;
+            for (int p = beg[i]; p < p1; p++) {
+                const int k = col[p];
+                U u = xw[k];
+                ok = ok && (u != Word<TX>::kPending || wait_for([&] { return (u = xw[k]) != Word<TX>::kPending; }, err));
+                s -= TX(val[p]) * from_bits<TX>(u);
+            }
+            TX r = dinv ? s * dinv[i] : s;
+            U ur = bits(r);
+            if (ur == Word<TX>::kPending || !ok) ur = Word<TX>::kNaN;
+            xw[i] = ur;
+        }
+        __syncwarp();
+    }
+}
+
+__device__ __forceinline__ void publish_row(int* flag, int i, int epoch) {
+    __threadfence();
+    *(volatile int*)(flag + i) = epoch;
+}
+
+// position of column j in [lo, e) of the sorted column array (row k's upper part: U_kj)
+__device__ __forceinline__ bool find_upper(const int* col, int lo, int e, int j, int* pos) {
+    int hi = e - 1;
+    while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        const int c = col[mid];
+        if (c == j) {
+            *pos = mid;
+            return true;
+        }
+        if (c < j)
+            lo = mid + 1;
+        else
+            hi = mid - 1;
+    }
+    return false;
+}
+
+// ILU(0) of A (CSR, sorted columns) into f on A's pattern, rows in forward level order; ustart_k is
+// the first entry of row k right of the diagonal; *err = 2 on a zero pivot (the reference's failure),
+// 1 if a wait ran out
+__device__ __forceinline__ void ilu0_row(int i, const int* __restrict__ ptr, const int* __restrict__ col,
+                                         const double* __restrict__ a, const int* __restrict__ diagpos,
+                                         const int* __restrict__ ustart, double* f, int* flag, int epoch, int* err) {
+    const int r0 = ptr[i], r1 = ptr[i + 1];
+    bool ok = true;
+    for (int q = r0; q < r1 && ok; q++) {
+        const int k = col[q];
+        if (k < i) ok = wait_for([&] { return *(volatile const int*)(flag + k) == epoch; }, err);
+    }
+    if (ok) {
+        __threadfence();
+        const int di = diagpos[i];
+        for (int p = r0; p < r1; p++) {
+            const int j = col[p];
+            const int jmax = (j <= i) ? j - 1 : i - 1;
+            double s = 0.0;
+            for (int q = r0; q < r1 && col[q] <= jmax; q++) {
+                const int k = col[q];
+                int pos;
+                if (find_upper(col, __ldg(ustart + k), ptr[k + 1], j, &pos))
+                    s = __dadd_rn(s, __dmul_rn(__ldcg(f + q), __ldcg(f + pos)));
+            }
+            const double v = __dsub_rn(a[p], s);
+            if (j <= i) {
+                f[p] = v;
+            } else {
+                const double d = di >= 0 ? __ldcg(f + di) : 0.0;
+                if (d == 0.0) {
+                    atomicExch(err, 2);
+                    break;
+                }
+                f[p] = __ddiv_rn(v, d);
+            }
+        }
+    }
+    publish_row(flag, i, epoch);
+}
+
+__global__ void __launch_bounds__(kPool) ilu0_kernel(int n, const int* __restrict__ order, const int* __restrict__ ptr,
+                                                     const int* __restrict__ col, const double* __restrict__ a,
+                                                     const int* __restrict__ diagpos, const int* __restrict__ ustart,
+                                                     double* f, int* flag, int epoch, unsigned* ticket, int* err) {
+    const int nchunks = (n + 31) >> 5;
+    for (int c = take_chunk(ticket); c < nchunks; c = take_chunk(ticket)) {
+        const int t = c * 32 + (threadIdx.x & 31);
+        if (t < n) ilu0_row(order[t], ptr, col, a, diagpos, ustart, f, flag, epoch, err);
+        __syncwarp();
+    }
+}
+
+// 1/L_ii from the factor array (0 where the pattern has no diagonal: a division by zero follows,
+// as in the reference's triangular solve)
+__global__ void diag_inverse_kernel(int n, const int* __restrict__ diagpos, const double* __restrict__ f,
+                                    double* dinv64, float* dinv32) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double d = diagpos[i] >= 0 ? f[diagpos[i]] : 0.0;
+        const double v = 1.0 / d;
+        dinv64[i] = v;
+        dinv32[i] = float(v);
     }
 }
 
@@ -47,31 +236,120 @@ __global__ void cvt_kernel(long n, const TA* __restrict__ a, TB* __restrict__ b)
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) b[i] = TB(a[i]);
 }
 
+// one triangular factor as row segments [beg_i, end_i) of shared column and value arrays
 struct Factor {
     int nlev = 0;
-    std::vector<int> lev_ptr_h;
-    int *lev_ptr = nullptr, *rows = nullptr, *ptr = nullptr, *col = nullptr;
+    int *order = nullptr, *beg = nullptr, *end = nullptr, *col = nullptr;
     double *val64 = nullptr, *dinv64 = nullptr;
-    float *val32 = nullptr, *dinv32 = nullptr;
+    float *val32 = nullptr, *dinv32 = nullptr;  // dinv null: unit diagonal
 };
 
-template <typename T>
-bool upload(T** d, const std::vector<T>& h) {
-    size_t bytes = std::max<size_t>(1, h.size()) * sizeof(T);
-    if (cudaMalloc((void**)d, bytes) != cudaSuccess) return false;
-    return h.empty() || cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice) == cudaSuccess;
+struct Mem {
+    std::vector<void*> p;
+    template <typename T>
+    T* get(size_t count) {
+        void* q = nullptr;
+        if (cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T)) != cudaSuccess) return nullptr;
+        p.push_back(q);
+        return (T*)q;
+    }
+    template <typename T>
+    T* up(const std::vector<T>& h) {
+        T* d = get<T>(h.size());
+        if (d && !h.empty() && cudaMemcpy(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
+            return nullptr;
+        return d;
+    }
+    ~Mem() {
+        for (void* q : p) cudaFree(q);
+    }
+};
+
+// level order of rows: lower = rows need smaller indices (entries [beg_i, end_i) columns), else larger
+int level_order(int n, const std::vector<int>& beg, const std::vector<int>& end, const int* col, bool lower,
+                std::vector<int>& order) {
+    std::vector<int> lev(n, 0);
+    int nlev = 0;
+    for (int t = 0; t < n; t++) {
+        const int i = lower ? t : n - 1 - t;
+        int l = 0;
+        for (int k = beg[i]; k < end[i]; k++) l = std::max(l, lev[col[k]] + 1);
+        lev[i] = l;
+        nlev = std::max(nlev, l + 1);
+    }
+    std::vector<int> lp(nlev + 1, 0);
+    for (int i = 0; i < n; i++) lp[lev[i] + 1]++;
+    for (int l = 0; l < nlev; l++) lp[l + 1] += lp[l];
+    order.assign(n, 0);
+    for (int i = 0; i < n; i++) order[lp[lev[i]]++] = i;
+    return nlev;
 }
 
-// off-diagonal CSR of a triangular factor plus its inverse diagonal and level schedule;
-// lower = true: rows depend on smaller indices (forward), else on larger ones (backward)
-bool build_factor(Factor& f, int n, const int* p, const int* c, const double* v, bool lower, std::string& err) {
+std::string g_ilu_err;
+
+// blocks of the worker pool: enough warps to keep the widest levels busy, few enough that the
+// waiting warps do not crowd the memory system (LINA_ILU_POOL_BLOCKS_PER_SM, default 4 per SM)
+int pool_blocks(int n) {
+    static int per_grid = 0;
+    if (per_grid == 0) {
+        int dev = 0, sms = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+            sms = 1;
+        int per_sm = 4;
+        if (const char* e = getenv("LINA_ILU_POOL_BLOCKS_PER_SM")) per_sm = std::max(1, std::min(16, atoi(e)));
+        per_grid = sms * per_sm;
+    }
+    return std::max(1, std::min(per_grid, (n + kPool - 1) / kPool));
+}
+
+}  // namespace
+
+struct lina_gpu_ilu {
+    int n = 0;
+    Factor L, U;
+    Mem mem;
+    double* t64 = nullptr;
+    float *r32 = nullptr, *t32 = nullptr, *z32 = nullptr;
+    int* err = nullptr;
+    unsigned* ticket = nullptr;  // the pool's row counter, reset before every pass
+    int* flag = nullptr;         // rows finished by the factorisation
+    double* fval = nullptr;      // factor values on A's pattern (factorised on the device), else null
+    long fnnz = 0;
+};
+
+namespace {
+
+bool alloc_work(lina_gpu_ilu* h) {
+    const int n = h->n;
+    h->t64 = h->mem.get<double>(n);
+    h->r32 = h->mem.get<float>(n);
+    h->t32 = h->mem.get<float>(n);
+    h->z32 = h->mem.get<float>(n);
+    h->err = h->mem.get<int>(1);
+    h->ticket = h->mem.get<unsigned>(1);
+    return h->t64 && h->r32 && h->t32 && h->z32 && h->err && h->ticket &&
+           cudaMemset(h->err, 0, sizeof(int)) == cudaSuccess;
+}
+
+// a factor given as CSR with its diagonal (lower: L with diagonal; upper: U, diagonal 1 skipped)
+bool build_factor(lina_gpu_ilu* h, Factor& f, int n, const int* p, const int* c, const double* v, bool lower,
+                  std::string& err) {
     std::vector<int> ptr(n + 1, 0), col;
     std::vector<double> val, dinv(n, 0.0);
     col.reserve(p[n]);
     val.reserve(p[n]);
     for (int i = 0; i < n; i++) {
         double d = 0.0;
+        if (p[i + 1] < p[i]) {
+            err = "row pointers of a factor decrease";
+            return false;
+        }
         for (int k = p[i]; k < p[i + 1]; k++) {
+            if (c[k] < 0 || c[k] >= n) {
+                err = "column index of a factor outside the matrix";
+                return false;
+            }
             if (c[k] == i) {
                 d = v[k];
             } else {
@@ -90,47 +368,48 @@ bool build_factor(Factor& f, int n, const int* p, const int* c, const double* v,
         dinv[i] = 1.0 / d;
         ptr[i + 1] = (int)col.size();
     }
-    std::vector<int> lev(n, 0);
-    int nlev = 0;
-    for (int t = 0; t < n; t++) {
-        const int i = lower ? t : n - 1 - t;
-        int l = 0;
-        for (int k = ptr[i]; k < ptr[i + 1]; k++) l = std::max(l, lev[col[k]] + 1);
-        lev[i] = l;
-        nlev = std::max(nlev, l + 1);
-    }
-    std::vector<int> lp(nlev + 1, 0), rows(n);
-    for (int i = 0; i < n; i++) lp[lev[i] + 1]++;
-    for (int l = 0; l < nlev; l++) lp[l + 1] += lp[l];
-    std::vector<int> fill(lp.begin(), lp.end() - 1);
-    for (int i = 0; i < n; i++) rows[fill[lev[i]]++] = i;
+    std::vector<int> beg(ptr.begin(), ptr.end() - 1), end(ptr.begin() + 1, ptr.end()), order;
+    f.nlev = level_order(n, beg, end, col.data(), lower, order);
     std::vector<float> val32(val.begin(), val.end()), dinv32(dinv.begin(), dinv.end());
-    f.nlev = nlev;
-    f.lev_ptr_h = lp;
-    bool ok = upload(&f.lev_ptr, lp) && upload(&f.rows, rows) && upload(&f.ptr, ptr) && upload(&f.col, col) &&
-              upload(&f.val64, val) && upload(&f.dinv64, dinv) && upload(&f.val32, val32) &&
-              upload(&f.dinv32, dinv32);
-    if (!ok) err = "device allocation for the ILU factors failed";
-    return ok;
+    int* dptr = h->mem.up(ptr);
+    f.order = h->mem.up(order);
+    f.col = h->mem.up(col);
+    f.val64 = h->mem.up(val);
+    f.val32 = h->mem.up(val32);
+    // an upper factor with the reference's unit diagonal needs no scaling
+    bool unit = !lower;
+    for (int i = 0; unit && i < n; i++) unit = (dinv[i] == 1.0);
+    if (!unit) {
+        f.dinv64 = h->mem.up(dinv);
+        f.dinv32 = h->mem.up(dinv32);
+    }
+    if (!dptr || !f.order || !f.col || !f.val64 || !f.val32 || (!unit && (!f.dinv64 || !f.dinv32))) {
+        err = "device allocation for the ILU factors failed";
+        return false;
+    }
+    f.beg = dptr;
+    f.end = dptr + 1;
+    return true;
 }
 
-void free_factor(Factor& f) {
-    for (void* p : {(void*)f.lev_ptr, (void*)f.rows, (void*)f.ptr, (void*)f.col, (void*)f.val64, (void*)f.dinv64,
-                    (void*)f.val32, (void*)f.dinv32})
-        if (p) cudaFree(p);
-    f = Factor();
+int read_err(lina_gpu_ilu* h) {
+    int e = 0;
+    if (cudaMemcpyAsync(&e, h->err, sizeof(int), cudaMemcpyDeviceToHost, st()) != cudaSuccess ||
+        cudaStreamSynchronize(st()) != cudaSuccess)
+        return -1;
+    return e;
 }
 
-std::string g_ilu_err;
+template <typename TV, typename TX>
+void solve(lina_gpu_ilu* h, const Factor& f, const TV* val, const TX* dinv, const TX* b, TX* x) {
+    const int n = h->n;
+    cudaMemsetAsync(x, 0xff, (size_t)n * sizeof(TX), st());  // every entry pending
+    cudaMemsetAsync(h->ticket, 0, sizeof(unsigned), st());
+    sptrsv_kernel<TV, TX><<<pool_blocks(n), kPool, 0, st()>>>(n, f.order, f.beg, f.end, f.col, val, dinv, b, x,
+                                                              h->ticket, h->err);
+}
 
 }  // namespace
-
-struct lina_gpu_ilu {
-    int n = 0;
-    Factor L, U;
-    double* t64 = nullptr;
-    float *r32 = nullptr, *t32 = nullptr, *z32 = nullptr;
-};
 
 extern "C" {
 
@@ -141,23 +420,103 @@ int lina_gpu_ilu_create(int n, const int* Lptr, const int* Lcol, const double* L
     lina_gpu_ilu* h = new lina_gpu_ilu();
     h->n = n;
     std::string err;
-    if (!build_factor(h->L, n, Lptr, Lcol, Lval, true, err) || !build_factor(h->U, n, Uptr, Ucol, Uval, false, err) ||
-        cudaMalloc(&h->t64, n * sizeof(double)) != cudaSuccess || cudaMalloc(&h->r32, n * sizeof(float)) != cudaSuccess ||
-        cudaMalloc(&h->t32, n * sizeof(float)) != cudaSuccess || cudaMalloc(&h->z32, n * sizeof(float)) != cudaSuccess) {
+    if (!lina::dev::ready() || !build_factor(h, h->L, n, Lptr, Lcol, Lval, true, err) ||
+        !build_factor(h, h->U, n, Uptr, Ucol, Uval, false, err) || !alloc_work(h)) {
         g_ilu_err = err.empty() ? "device allocation failed" : err;
-        lina_gpu_ilu_destroy(h);
+        lina::dev::set_error(("ILU: " + g_ilu_err).c_str());
+        delete h;
         return LINA_GPU_EINVAL;
     }
     *out = h;
     return 0;
 }
 
+// ILU(0) of A factorised on the device (bit-identical to the reference's incomplete_LU_factorization)
+int lina_gpu_ilu_create_from_matrix(int n, const int* rowptr, const int* col, const double* val,
+                                    lina_gpu_ilu** out) {
+    if (!out || n <= 0 || !rowptr || !col || !val || rowptr[0] != 0) return LINA_GPU_EINVAL;
+    *out = nullptr;
+    const long nnz = rowptr[n];
+    std::vector<int> diag(n, -1), lbeg(n), lend(n), ubeg(n), uend(n);
+    for (int i = 0; i < n; i++) {
+        if (rowptr[i + 1] < rowptr[i]) return LINA_GPU_EINVAL;
+        int split = rowptr[i + 1];
+        for (int p = rowptr[i]; p < rowptr[i + 1]; p++) {
+            if (col[p] < 0 || col[p] >= n || (p > rowptr[i] && col[p] <= col[p - 1])) {
+                lina::dev::set_error("ILU: columns must be sorted, distinct and inside the matrix");
+                return LINA_GPU_EINVAL;
+            }
+            if (col[p] == i) diag[i] = p;
+            if (col[p] > i && split == rowptr[i + 1]) split = p;
+        }
+        lbeg[i] = rowptr[i];
+        lend[i] = diag[i] >= 0 ? diag[i] : split;  // strictly lower entries
+        ubeg[i] = split;
+        uend[i] = rowptr[i + 1];
+    }
+    lina_gpu_ilu* h = new lina_gpu_ilu();
+    h->n = n;
+    h->fnnz = nnz;
+    std::vector<int> lorder, uorder;
+    h->L.nlev = level_order(n, lbeg, lend, col, true, lorder);
+    h->U.nlev = level_order(n, ubeg, uend, col, false, uorder);
+    std::vector<int> ptr(rowptr, rowptr + n + 1), cols(col, col + nnz);
+    std::vector<double> vals(val, val + nnz);
+    Mem& m = h->mem;
+    int *dptr = nullptr, *dcol = nullptr, *ddiag = nullptr;
+    double* dval = nullptr;
+    bool ok = lina::dev::ready() && alloc_work(h);
+    if (ok) {
+        dptr = m.up(ptr);
+        dcol = m.up(cols);
+        ddiag = m.up(diag);
+        dval = m.up(vals);
+        h->fval = m.get<double>(nnz);
+        h->L.order = m.up(lorder);
+        h->U.order = m.up(uorder);
+        h->L.beg = m.up(lbeg);
+        h->L.end = m.up(lend);
+        h->U.beg = m.up(ubeg);
+        h->U.end = m.up(uend);
+        h->L.dinv64 = m.get<double>(n);
+        h->L.dinv32 = m.get<float>(n);
+        h->L.val32 = m.get<float>(nnz);
+        ok = dptr && dcol && ddiag && dval && h->fval && h->L.order && h->U.order && h->L.beg && h->L.end &&
+             h->U.beg && h->U.end && h->L.dinv64 && h->L.dinv32 && h->L.val32;
+    }
+    if (!ok) {
+        lina::dev::set_error("ILU: device allocation failed");
+        delete h;
+        return LINA_GPU_ECUDA;
+    }
+    h->L.col = h->U.col = dcol;
+    h->L.val64 = h->U.val64 = h->fval;
+    h->U.val32 = h->L.val32;
+    h->flag = m.get<int>(n);
+    if (!h->flag || cudaMemsetAsync(h->flag, 0, (size_t)n * sizeof(int), st()) != cudaSuccess ||
+        cudaMemsetAsync(h->ticket, 0, sizeof(unsigned), st()) != cudaSuccess) {
+        lina::dev::set_error("ILU: device allocation failed");
+        delete h;
+        return LINA_GPU_ECUDA;
+    }
+    ilu0_kernel<<<pool_blocks(n), kPool, 0, st()>>>(n, h->L.order, dptr, dcol, dval, ddiag, h->U.beg, h->fval,
+                                                    h->flag, 1, h->ticket, h->err);
+    diag_inverse_kernel<<<std::min(4096, (n + kT - 1) / kT), kT, 0, st()>>>(n, ddiag, h->fval, h->L.dinv64,
+                                                                             h->L.dinv32);
+    cvt_kernel<double, float><<<std::min<long>(4096, (nnz + kT - 1) / kT), kT, 0, st()>>>(nnz, h->fval, h->L.val32);
+    const int e = (cudaGetLastError() == cudaSuccess) ? read_err(h) : -1;
+    if (e != 0) {
+        lina::dev::set_error(e == 2 ? "ILU: zero pivot (incomplete_LU_factorization fails)"
+                                    : "ILU: device factorisation failed or a wait ran out");
+        delete h;
+        return e == 2 ? LINA_GPU_ESETUP : LINA_GPU_ECUDA;
+    }
+    *out = h;
+    return 0;
+}
+
 int lina_gpu_ilu_destroy(lina_gpu_ilu* h) {
-    if (!h) return 0;
-    free_factor(h->L);
-    free_factor(h->U);
-    for (void* p : {(void*)h->t64, (void*)h->r32, (void*)h->t32, (void*)h->z32})
-        if (p) cudaFree(p);
+    if (h) cudaStreamSynchronize(st());
     delete h;
     return 0;
 }
@@ -169,28 +528,39 @@ int lina_gpu_ilu_levels(const lina_gpu_ilu* h, int* nlev_L, int* nlev_U) {
     return 0;
 }
 
+int lina_gpu_ilu_factor_values(const lina_gpu_ilu* h, double* val) {
+    if (!h || !val || !h->fval) {
+        lina::dev::set_error("lina_gpu_ilu_factor_values: not a handle factorised on the device");
+        return LINA_GPU_EINVAL;
+    }
+    if (h->fnnz && cudaMemcpy(val, h->fval, h->fnnz * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return LINA_GPU_ECUDA;
+    return 0;
+}
+
 // z = U^-1 L^-1 r on device vectors (FP64); precision LINA_PREC_MIXED runs both solves in FP32.
 // The work is issued on the stream of the device vector toolkit and completes before return.
 int lina_gpu_ilu_apply(lina_gpu_ilu* h, int precision, const double* r_dev, double* z_dev) {
     if (!h || !r_dev || !z_dev) return LINA_GPU_EINVAL;
-    cudaStream_t st = (cudaStream_t)lina::dev::stream();
     const int n = h->n;
-    const int g = (int)std::min<long>(2048, (n + 255) / 256);
+    const int g = (int)std::min<long>(2048, (n + kT - 1) / kT);
     if (precision == LINA_PREC_MIXED) {
-        cvt_kernel<double, float><<<g, 256, 0, st>>>(n, r_dev, h->r32);
-        tri_levels_kernel<float, float><<<1, kBlock, 0, st>>>(h->L.nlev, h->L.lev_ptr, h->L.rows, h->L.ptr, h->L.col,
-                                                              h->L.val32, h->L.dinv32, h->r32, h->t32);
-        tri_levels_kernel<float, float><<<1, kBlock, 0, st>>>(h->U.nlev, h->U.lev_ptr, h->U.rows, h->U.ptr, h->U.col,
-                                                              h->U.val32, h->U.dinv32, h->t32, h->z32);
-        cvt_kernel<float, double><<<g, 256, 0, st>>>(n, h->z32, z_dev);
+        cvt_kernel<double, float><<<g, kT, 0, st()>>>(n, r_dev, h->r32);
+        solve<float, float>(h, h->L, h->L.val32, h->L.dinv32, h->r32, h->t32);
+        solve<float, float>(h, h->U, h->U.val32, h->U.dinv32, h->t32, h->z32);
+        cvt_kernel<float, double><<<g, kT, 0, st()>>>(n, h->z32, z_dev);
     } else {
-        tri_levels_kernel<double, double><<<1, kBlock, 0, st>>>(h->L.nlev, h->L.lev_ptr, h->L.rows, h->L.ptr,
-                                                                h->L.col, h->L.val64, h->L.dinv64, r_dev, h->t64);
-        tri_levels_kernel<double, double><<<1, kBlock, 0, st>>>(h->U.nlev, h->U.lev_ptr, h->U.rows, h->U.ptr,
-                                                                h->U.col, h->U.val64, h->U.dinv64, h->t64, z_dev);
+        solve<double, double>(h, h->L, h->L.val64, h->L.dinv64, r_dev, h->t64);
+        solve<double, double>(h, h->U, h->U.val64, h->U.dinv64, h->t64, z_dev);
     }
     if (cudaGetLastError() != cudaSuccess) return LINA_GPU_ECUDA;
-    return cudaStreamSynchronize(st) == cudaSuccess ? 0 : LINA_GPU_ECUDA;
+    const int e = read_err(h);
+    if (e != 0) {
+        lina::dev::set_error("ILU apply: a wait of the triangular solve ran out");
+        if (e > 0) cudaMemset(h->err, 0, sizeof(int));
+        return LINA_GPU_ECUDA;
+    }
+    return 0;
 }
 
 }  // extern "C"

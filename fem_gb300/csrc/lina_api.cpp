@@ -1336,25 +1336,6 @@ int BiCGStab_solve(double* X, double* b, int n) {
 // ============================================================ device BiCGStab and ILU(0) (C-ABI)
 extern "C" {
 
-int lina_gpu_ilu_create_from_matrix(int n, const int* rowptr, const int* col, const double* val,
-                                    lina_gpu_ilu** out) {
-    if (!out || n <= 0 || !rowptr || !col || !val) return LINA_GPU_EINVAL;
-    sparse_matrix* A = from_csr(n, rowptr, col, val);
-    sparse_matrix* L = sparse_zero(n);
-    sparse_matrix* U = sparse_zero(n);
-    int ok = incomplete_LU_factorization(A, L, U);
-    int rc = LINA_GPU_ESETUP;
-    if (ok) {
-        CsrCopy l = to_csr(L), u = to_csr(U);
-        rc = lina_gpu_ilu_create(n, l.ptr.data(), l.col.data(), l.val.data(), u.ptr.data(), u.col.data(),
-                                 u.val.data(), out);
-    }
-    free_sparse(A);
-    free_sparse(L);
-    free_sparse(U);
-    return rc;
-}
-
 int lina_gpu_bicgstab(lina_gpu_matrix* Am, lina_gpu_ilu* ilu, int ilu_precision, const double* b_in, double* x_out,
                       double tol, int max_iter, int flags, lina_gpu_solve_info* info) {
     if (!Am || !b_in || !x_out || max_iter < 0) return LINA_GPU_EINVAL;

@@ -10,6 +10,7 @@
 // the caller's functional, gradient and Hessian callbacks receive host copies
 // of the iterate, as they are host functions.  The default quadratic
 // functional q(x) = x.H.x/2 + x.b and its gradient run on the GPU.
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -342,6 +343,22 @@ struct Ctx {
 
 Ctx* g_ctx = nullptr;  // the call in progress (the reference's state is file-scope too)
 
+// LINA_RN_TIMING set: seconds per phase of each Newton step on stderr (diagnostics)
+struct PhaseClock {
+    bool on = std::getenv("LINA_RN_TIMING") != nullptr;
+    std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+    double lap() {
+        if (!on) return 0.0;
+        lina::dev::sync();
+        auto now = std::chrono::steady_clock::now();
+        double s = std::chrono::duration<double>(now - t).count();
+        t = now;
+        return s;
+    }
+};
+double g_t_ilu = 0.0, g_t_krylov = 0.0;
+int g_krylov_iters = 0;
+
 // u . (A v) on the device
 double bilinear(lina_gpu_matrix* A, const double* u, const double* v, double* tmp, int n) {
     lina::dev::sync();
@@ -527,13 +544,17 @@ bool get_subspace(Ctx& c) {
     switch (rn_solver_type) {
         case RN_GPU_BICGSTAB_ILU: {
             lina_gpu_ilu* ilu = nullptr;
+            PhaseClock pc;
             if (lina_gpu_ilu_create_from_matrix(n, c.Mc.ptr.data(), c.Mc.col.data(), c.Mc.val.data(), &ilu) != 0) {
                 rn_status = INDEFINITE;
                 break;
             }
             lina_gpu_solve_info info;
+            g_t_ilu = pc.lap();
             lina_gpu_bicgstab(c.Mdev, ilu, LINA_PREC_MIXED, c.rhs, c.V2, lina::api::bi_eps_value(),
                               BI_get_max_iter(), LINA_PCG_DEVICE_PTRS | LINA_PCG_USE_X0, &info);
+            g_t_krylov = pc.lap();
+            g_krylov_iters = info.iterations;
             lina_gpu_ilu_destroy(ilu);
             iter = info.iterations;
             rn_status = (info.status == 0 && iter < BI_get_max_iter()) ? POSITIVE_DEFINITE : INDEFINITE;
@@ -750,9 +771,17 @@ int reflective_newton(double* Xh) {
         lina::dev::d2h(c.hJ.data(), c.J, c.n);
         lina::dev::d2h(c.hG.data(), c.G, c.n);
         c.drop_M();
+        PhaseClock pc;
         assemble_M(c, lina::api::to_csr(rn_hesse));
+        const double t_asm = pc.lap();
         if (lina_gpu_matrix_create(c.n, c.n, c.Mc.ptr.data(), c.Mc.col.data(), c.Mc.val.data(), &c.Mdev) != 0) return -1;
+        const double t_up = pc.lap();
         if (!iterate(c)) return -1;
+        const double t_it = pc.lap();
+        if (pc.on)
+            fprintf(stderr, "RN step %d: assemble M %.3fs, upload %.3fs, step %.3fs (ILU set-up %.3fs, BiCGStab %.3fs "
+                            "in %d iterations)\n",
+                    iter, t_asm, t_up, t_it, g_t_ilu, g_t_krylov, g_krylov_iters);
         q = functional(c, c.X);
         dq = fabs((q - q0) / q0);
         if (iter < (int)Q.size()) Q[iter] = dq;

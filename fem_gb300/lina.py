@@ -119,6 +119,7 @@ def lib():
         "lina_gpu_ilu_create_from_matrix": (C.c_int, [C.c_int, ip, ip, dp, C.POINTER(vp)]),
         "lina_gpu_ilu_destroy": (C.c_int, [vp]),
         "lina_gpu_ilu_levels": (C.c_int, [vp, ip, ip]),
+        "lina_gpu_ilu_factor_values": (C.c_int, [vp, dp]),
         "lina_gpu_ilu_apply": (C.c_int, [vp, C.c_int, vp, vp]),
         "lina_gpu_dot": (C.c_int, [vp, vp, C.c_long, dp]),
         "lina_gpu_dot_noalloc": (C.c_int, [vp, vp, C.c_long, dp]),
@@ -324,8 +325,16 @@ class ILU:
         ix_ = np.ascontiguousarray(indices, dtype=np.int32)
         dv_ = np.ascontiguousarray(data, dtype=np.float64)
         h = C.c_void_p()
+        self.h = None
+        self.nnz = len(ix_)
         _check(lib().lina_gpu_ilu_create_from_matrix(self.n, _ip(ip_), _ip(ix_), _dp(dv_), C.byref(h)), "ILU")
         self.h = h
+
+    def factor_values(self):
+        """The factors on A's pattern: L_ij where j <= i, U_ij where j > i."""
+        f = np.zeros(max(self.nnz, 1))
+        _check(lib().lina_gpu_ilu_factor_values(self.h, _dp(f)), "ILU factor values")
+        return f[:self.nnz]
 
     def levels(self):
         a, b = C.c_int(), C.c_int()

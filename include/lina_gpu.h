@@ -143,12 +143,18 @@ long lina_gpu_matrix_padded_entries(const lina_gpu_matrix* m);
 
 /* ILU(0) preconditioner on the GPU: factors as incomplete_LU_factorization produces them
    (LinA/linear_algebra.c:1952: L lower with diagonal, U upper with unit diagonal), applied by
-   level-scheduled forward and backward solves. */
+   forward and backward solves with one thread per row in level order, each row waiting only for
+   the rows it needs. */
 typedef struct lina_gpu_ilu lina_gpu_ilu;
 int lina_gpu_ilu_create(int n, const int* Lptr, const int* Lcol, const double* Lval, const int* Uptr,
                         const int* Ucol, const double* Uval, lina_gpu_ilu** out);
-/* factorise A (CSR) with the reference's ILU(0) on the host, then upload; returns LINA_GPU_ESETUP on a zero pivot */
+/* ILU(0) of A (CSR, sorted distinct columns) factorised on the GPU, bit-identical to the reference's
+   incomplete_LU_factorization (row recurrences run in level order, each row waiting only for the rows
+   it needs); LINA_GPU_ESETUP on a zero pivot */
 int lina_gpu_ilu_create_from_matrix(int n, const int* rowptr, const int* col, const double* val, lina_gpu_ilu** out);
+/* the factors of a handle from lina_gpu_ilu_create_from_matrix on A's pattern (val[nnz]): L_ij where
+   j <= i, U_ij where j > i (U's unit diagonal is not stored) */
+int lina_gpu_ilu_factor_values(const lina_gpu_ilu* h, double* val);
 int lina_gpu_ilu_destroy(lina_gpu_ilu* h);
 int lina_gpu_ilu_levels(const lina_gpu_ilu* h, int* nlev_L, int* nlev_U);
 /* z = U^-1 L^-1 r (device vectors, FP64); LINA_PREC_MIXED solves in FP32 */

@@ -423,3 +423,61 @@ int port_pcg(port_amg* h, const double* B, double* X, double tol, int max_iter, 
     free(Q);
     return it;
 }
+
+/* ILU(0) of A (CSR, sorted distinct columns) on A's pattern: incomplete_LU_factorization
+   (LinA/linear_algebra.c:1952-1982) with row_times_row (:1795-1818).  f_p = L_ij for j <= i,
+   U_ij for j > i; the sums run over ascending k where (i, k) and (k, j) are in the pattern and
+   start at 0.  Returns 1, or 0 on a zero (or absent) pivot L_ii of a row with entries right of
+   the diagonal, as the reference does. */
+static int find_col(const int* col, int lo, int hi, int j) {
+    hi--;
+    while (lo <= hi) {
+        int mid = (lo + hi) >> 1;
+        if (col[mid] == j) return mid;
+        if (col[mid] < j)
+            lo = mid + 1;
+        else
+            hi = mid - 1;
+    }
+    return -1;
+}
+
+int port_ilu0(int n, const int* ptr, const int* col, const double* a, double* f) {
+    int* ustart = (int*)malloc((size_t)(n > 0 ? n : 1) * sizeof(int));
+    if (!ustart) return -1;
+    int ok = 1;
+    for (int i = 0; i < n && ok; i++) {
+        int r0 = ptr[i], r1 = ptr[i + 1];
+        int split = r1;
+        for (int p = r0; p < r1; p++)
+            if (col[p] > i) {
+                split = p;
+                break;
+            }
+        ustart[i] = split;
+        double d = 0.0;
+        for (int p = r0; p < r1; p++) {
+            int j = col[p];
+            int jmax = j <= i ? j - 1 : i - 1;
+            double s = 0.0;
+            for (int q = r0; q < r1 && col[q] <= jmax; q++) {
+                int k = col[q];
+                int pos = find_col(col, ustart[k], ptr[k + 1], j);
+                if (pos >= 0) s += f[q] * f[pos];
+            }
+            double v = a[p] - s;
+            if (j <= i) {
+                f[p] = v;
+                if (j == i) d = v;
+            } else {
+                if (d == 0.0) {
+                    ok = 0;
+                    break;
+                }
+                f[p] = v / d;
+            }
+        }
+    }
+    free(ustart);
+    return ok;
+}

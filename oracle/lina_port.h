@@ -13,6 +13,8 @@
  *                damped Jacobi and multicolour SOR (the GPU library's smoothers,
  *                same per-row update as AMG_SOR_smoother)
  *   - pcg                                (LinA/PCGS.c:163-233)
+ *   - ILU(0) factors                     (incomplete_LU_factorization,
+ *                                          LinA/linear_algebra.c:1952-1982)
  * The hierarchy (level matrices, P, R, labels) is an input.  Parity of this
  * restatement is pinned against the reference's own outputs stored under
  * tests/golden/ (generated by tests/golden/make_golden.py).
@@ -46,6 +48,8 @@ void port_vcycle(port_amg* h, const double* r, double* z);
 int port_pcg(port_amg* h, const double* b, double* x, double tol, int max_iter, int stop_rule,
              double max_seconds, double* pcg_res);
 void port_spmv(const port_amg* h, int l, const double* x, double* y);
+/* ILU(0) factors on A's pattern (L_ij where j <= i, U_ij where j > i); 1, or 0 on a zero pivot */
+int port_ilu0(int n, const int* ptr, const int* col, const double* a, double* f);
 
 #ifdef __cplusplus
 }

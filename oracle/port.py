@@ -36,6 +36,7 @@ def lib():
         "port_vcycle": (None, [vp, dp, dp]),
         "port_pcg": (C.c_int, [vp, dp, dp, C.c_double, C.c_int, C.c_int, C.c_double, dp]),
         "port_spmv": (None, [vp, C.c_int, dp, dp]),
+        "port_ilu0": (C.c_int, [C.c_int, ip, ip, dp, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -51,6 +52,18 @@ def _ip(a):
 
 def _dp(a):
     return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def ilu0(indptr, indices, data):
+    """ILU(0) factors on A's pattern (the C restatement); raises ArithmeticError on a zero pivot."""
+    ptr = np.ascontiguousarray(indptr, dtype=np.int32)
+    col = np.ascontiguousarray(indices, dtype=np.int32)
+    val = np.ascontiguousarray(data, dtype=np.float64)
+    f = np.zeros(max(len(col), 1))
+    rc = lib().port_ilu0(len(ptr) - 1, _ip(ptr), _ip(col), _dp(val), _dp(f))
+    if rc != 1:
+        raise ArithmeticError("ILU(0): zero pivot" if rc == 0 else "ILU(0): out of memory")
+    return f[:len(col)]
 
 
 class PortAMG:

@@ -258,6 +258,32 @@ def ilu_apply(sysm, r):
     return z
 
 
+def ilu_factors(n, indptr, indices, data):
+    """incomplete_LU_factorization of the reference; returns (ok, f) with f the factors on A's
+    pattern (L_ij where j <= i, U_ij where j > i), or (False, None) when it fails."""
+    A = RefMatrix.from_csr(n, indptr, indices, data)
+    Lp, Up = C.c_void_p(), C.c_void_p()
+    ok = lib().rs_ilu(A.ptr, C.byref(Lp), C.byref(Up)) == 1
+    Lm, Um = RefMatrix(Lp.value), RefMatrix(Up.value)
+    if not ok:
+        return False, None
+    ptr = np.asarray(indptr, dtype=np.int64)
+    col = np.asarray(indices, dtype=np.int64)
+    f = np.full(len(col), np.nan)
+    where = {}
+    for i in range(n):
+        for p in range(ptr[i], ptr[i + 1]):
+            where[(i, int(col[p]))] = p
+    for M, lower in ((Lm, True), (Um, False)):
+        mp, mc, mv = M.to_csr()
+        for i in range(n):
+            for q in range(mp[i], mp[i + 1]):
+                j = int(mc[q])
+                if (lower and j <= i) or (not lower and j > i):
+                    f[where[(i, j)]] = mv[q]
+    return True, f
+
+
 def bicgstab_ilu(sysm, eps=1e-8, max_iter=1000):
     """BiCGStab_solve with the ILU(0) preconditioner; returns (x, iterations)."""
     A = RefMatrix.from_csr(sysm.n, sysm.indptr, sysm.indices, sysm.data)

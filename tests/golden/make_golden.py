@@ -223,6 +223,49 @@ def spgemm_inputs(seed=7):
     return pack(A), pack(B)
 
 
+ILU_FILE = "ilu"
+
+
+def ilu_inputs():
+    """Matrices for the ILU(0) factors: name -> (indptr, indices, data).  Besides the model
+    problems, a seeded nonsymmetric matrix with ragged rows (rows holding only the diagonal, rows
+    with up to 12 entries) and a 3 x 3 matrix whose second pivot is exactly zero."""
+    out = {}
+    for name, s in (("poisson33", problems.poisson_p1(33, seed=0)), ("elast17", problems.elasticity_p1(17)),
+                    ("damage65", problems.damage_qp(65))):
+        out[name] = (s.indptr, s.indices, s.data)
+    rng = np.random.default_rng(21)
+    n = 400
+    rows = []
+    for i in range(n):
+        k = int(rng.integers(0, 12)) if i % 7 else 0
+        cols = set(int(c) for c in rng.integers(max(0, i - 40), min(n, i + 40), size=k)) | {i}
+        rows.append(sorted(cols))
+    ptr = np.cumsum([0] + [len(r) for r in rows]).astype(np.int32)
+    col = np.array([c for r in rows for c in r], dtype=np.int32)
+    val = rng.standard_normal(len(col))
+    for i in range(n):
+        d = ptr[i] + rows[i].index(i)
+        val[d] = 4.0 + 4.0 * rng.random()
+    out["nonsym400"] = (ptr, col, val)
+    out["zeropivot3"] = (np.array([0, 2, 5, 7], dtype=np.int32), np.array([0, 1, 0, 1, 2, 1, 2], dtype=np.int32),
+                         np.array([1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0]))
+    return out
+
+
+def make_ilu():
+    """incomplete_LU_factorization (LinA/linear_algebra.c:1952) of the reference on ilu_inputs()."""
+    out = {}
+    for name, (ptr, col, val) in ilu_inputs().items():
+        n = len(ptr) - 1
+        ok, f = ref.ilu_factors(n, ptr, col, val)
+        out[f"{name}_ptr"], out[f"{name}_col"], out[f"{name}_val"] = ptr, col, val
+        out[f"{name}_ok"] = np.int64(ok)
+        if ok:
+            out[f"{name}_f"] = f
+    return out
+
+
 def make_spgemm():
     """sparse_product (LinA/linear_algebra.c:186) of the reference on spgemm_inputs()."""
     (ap, ac, av), (bp, bc, bv) = spgemm_inputs()
@@ -286,6 +329,11 @@ def main():
         path = os.path.join(HERE, "spgemm.npz")
         np.savez_compressed(path, **data)
         print(f"{path}: product with {len(data['c_col'])} entries")
+    if not only or ILU_FILE in only:
+        data = make_ilu()
+        path = os.path.join(HERE, f"{ILU_FILE}.npz")
+        np.savez_compressed(path, **data)
+        print(f"{path}: " + ", ".join(f"{k}={int(v)}" for k, v in data.items() if k.endswith("_ok")))
     if not only or "fmg" in only:
         data = make_fmg()
         path = os.path.join(HERE, "fmg.npz")
