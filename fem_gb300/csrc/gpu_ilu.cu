@@ -47,6 +47,7 @@ constexpr int kPool = 128;   // threads of a block of the worker pool
 constexpr unsigned long long kWaitNs = 2000000000ull;
 constexpr long kWaitPolls = 1L << 26;
 constexpr unsigned kMaxSleepNs = 256;
+constexpr int kGroup = 4;  // solution entries a row of a triangular solve loads at once
 
 cudaStream_t st() { return (cudaStream_t)lina::dev::stream(); }
 
@@ -128,11 +129,22 @@ __global__ void __launch_bounds__(kPool) sptrsv_kernel(int n, const int* __restr
             const int p1 = end[i];
             TX s = b[i];
             bool ok = true;
-            for (int p = beg[i]; p < p1; p++) {
-                const int k = col[p];
-                U u = xw[k];
-                ok = ok && (u != Word<TX>::kPending || wait_for([&] { return (u = xw[k]) != Word<TX>::kPending; }, err));
-                s -= TX(val[p]) * from_bits<TX>(u);
+            // the entries of a group are loaded together (one round trip when they are final), then
+            // waited for and subtracted in column order
+            for (int p = beg[i]; p < p1; p += kGroup) {
+                int k[kGroup];
+                U u[kGroup];
+#pragma unroll
+                for (int q = 0; q < kGroup; q++) k[q] = p + q < p1 ? col[p + q] : -1;
+#pragma unroll
+                for (int q = 0; q < kGroup; q++) u[q] = k[q] >= 0 ? xw[k[q]] : U(0);
+#pragma unroll
+                for (int q = 0; q < kGroup; q++) {
+                    if (k[q] < 0) break;
+                    if (u[q] == Word<TX>::kPending)
+                        ok = ok && wait_for([&] { return (u[q] = xw[k[q]]) != Word<TX>::kPending; }, err);
+                    s -= TX(val[p + q]) * from_bits<TX>(u[q]);
+                }
             }
             TX r = dinv ? s * dinv[i] : s;
             U ur = bits(r);
@@ -288,7 +300,8 @@ int level_order(int n, const std::vector<int>& beg, const std::vector<int>& end,
 std::string g_ilu_err;
 
 // blocks of the worker pool: enough warps to keep the widest levels busy, few enough that the
-// waiting warps do not crowd the memory system (LINA_ILU_POOL_BLOCKS_PER_SM, default 4 per SM)
+// waiting warps do not crowd the memory system (LINA_ILU_POOL_BLOCKS_PER_SM, default 2 per SM: on
+// 1M- and 2M-row mesh matrices 1 and 2 blocks per SM were fastest, 4 about 10 % and 8 about 70 % slower)
 int pool_blocks(int n) {
     static int per_grid = 0;
     if (per_grid == 0) {
@@ -296,7 +309,7 @@ int pool_blocks(int n) {
         if (cudaGetDevice(&dev) != cudaSuccess ||
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
             sms = 1;
-        int per_sm = 4;
+        int per_sm = 2;
         if (const char* e = getenv("LINA_ILU_POOL_BLOCKS_PER_SM")) per_sm = std::max(1, std::min(16, atoi(e)));
         per_grid = sms * per_sm;
     }
