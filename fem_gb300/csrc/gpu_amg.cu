@@ -2108,3 +2108,277 @@ int lina_gpu_synchronize(void) {
 }
 
 }  // extern "C"
+
+// =================================================================== batched solves
+// Many independent systems in one CUDA graph: for every system a branch of
+//   start (x = 0, r = b, ||b||, and ||M^-1 b|| for the reference's rule)
+//   -> a one-thread kernel that sets the loop's limits and whether it runs at all
+//   -> a while-loop node whose body is the PCG iteration of lina_gpu_pcg
+//   -> the true residual ||b - A x||.
+// The branches share nothing (each system has its own vectors, reductions and scalars), so one
+// launch runs them all concurrently: the small systems, which are bound by launch and memory
+// latency, overlap one another and the large ones.
+namespace {
+
+struct BatchLimits {
+    double tol;
+    int maxit;
+    int pad;
+};
+
+__global__ void save_norm_kernel(KScalars* sc) { sc->aux = sc->norm2; }
+
+// sc->norm2 holds r0^2 (||b||^2 or ||M^-1 b||^2); the loop runs when r0 is a positive number
+__global__ void batch_start_kernel(cudaGraphConditionalHandle hd, KScalars* sc, const BatchLimits* lim) {
+    const double r0 = sqrt(sc->norm2);
+    sc->r0 = r0;
+    sc->tol = lim->tol;
+    sc->maxit = lim->maxit;
+    sc->iter = 0;
+    cudaGraphSetConditional(hd, (r0 > 0.0 && isfinite(r0) && lim->maxit > 0) ? 1u : 0u);
+}
+
+}  // namespace
+
+struct lina_gpu_batch {
+    std::vector<lina_gpu_amg*> sys;
+    int stop_rule = LINA_STOP_RELATIVE;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    BatchLimits* lim = nullptr;       // device
+    BatchLimits* lim_host = nullptr;  // pinned
+    KScalars* sc_host = nullptr;      // pinned, one per system
+    std::vector<long> k_start, k_iter, k_finish;  // kernels per branch part
+    ~lina_gpu_batch() {
+        if (stream) cudaStreamSynchronize(stream);
+        if (exec) cudaGraphExecDestroy(exec);
+        if (lim) cudaFree(lim);
+        if (lim_host) cudaFreeHost(lim_host);
+        if (sc_host) cudaFreeHost(sc_host);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+// capture the work `f` issues on h's stream as a graph (counting its kernels)
+template <typename F>
+int capture_on(lina_gpu_amg* h, cudaGraph_t* g, long* kernels, F f) {
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeRelaxed));
+    const unsigned long long before = g_launches;
+    f();
+    *kernels = (long)(g_launches - before);
+    g_launches = before;
+    cudaError_t e = cudaStreamEndCapture(h->stream, g);
+    if (e != cudaSuccess) {
+        set_err("batch capture failed: %s", cudaGetErrorString(e));
+        return LINA_GPU_ECUDA;
+    }
+    return 0;
+}
+
+int build_batch_graph(lina_gpu_batch* B) {
+    cudaGraph_t G = nullptr;
+    CK(cudaGraphCreate(&G, 0));
+    int rc = 0;
+    for (size_t s = 0; s < B->sys.size() && !rc; s++) {
+        lina_gpu_amg* h = B->sys[s];
+        const int n = h->lv[h->depth - 1].n;
+        const bool mixed = (h->opt.precision == LINA_PREC_MIXED);
+        const int gr = grid_red(n);
+        cudaGraph_t gstart = nullptr, gfin = nullptr;
+        rc = capture_on(h, &gstart, &B->k_start[s], [&] {
+            cudaMemsetAsync(h->kx, 0, (size_t)n * sizeof(double), h->stream);
+            cudaMemsetAsync(h->sc, 0, sizeof(KScalars), h->stream);
+            cudaMemcpyAsync(h->kr, h->kb, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, h->stream);
+            go(norm2_kernel<double>, gr, h->stream, n, (const double*)h->kb, h->partials, h->ticket, h->sc);
+            g_launches++;
+            save_norm_kernel<<<1, 1, 0, h->stream>>>(h->sc);
+            if (B->stop_rule == LINA_STOP_REFERENCE) {
+                h->precondition(h->kr, h->kz, false);
+                if (mixed)
+                    go(norm2_kernel<float>, gr, h->stream, n, (const float*)h->kz32, h->partials, h->ticket, h->sc);
+                else
+                    go(norm2_kernel<double>, gr, h->stream, n, (const double*)h->kz, h->partials, h->ticket, h->sc);
+            }
+        });
+        if (!rc)
+            rc = capture_on(h, &gfin, &B->k_finish[s], [&] { true_residual(h, h->kb, h->kx); });
+        cudaGraphNode_t n_start = nullptr, n_cond = nullptr, n_loop = nullptr, n_fin = nullptr;
+        cudaGraphConditionalHandle hd = 0;
+        cudaError_t e = rc ? cudaErrorUnknown : cudaGraphAddChildGraphNode(&n_start, G, nullptr, 0, gstart);
+        if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hd, G, 0, cudaGraphCondAssignDefault);
+        if (e == cudaSuccess) {
+            void* args[] = {(void*)&hd, (void*)&h->sc, (void*)&B->lim};
+            cudaKernelNodeParams kp = {};
+            kp.func = (void*)batch_start_kernel;
+            kp.gridDim = dim3(1);
+            kp.blockDim = dim3(1);
+            kp.kernelParams = args;
+            e = cudaGraphAddKernelNode(&n_cond, G, &n_start, 1, &kp);
+        }
+        cudaGraphNodeParams cp = {};
+        if (e == cudaSuccess) {
+            cp.type = cudaGraphNodeTypeConditional;
+            cp.conditional.handle = hd;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            e = cudaGraphAddNode(&n_loop, G, &n_cond, nullptr, 1, &cp);
+        }
+        if (e == cudaSuccess)
+            e = cudaStreamBeginCaptureToGraph(h->stream, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeRelaxed);
+        if (e == cudaSuccess) {
+            const unsigned long long before = g_launches;
+            h->issue_iteration(n, true, false);
+            loop_cond_kernel<<<1, 1, 0, h->stream>>>(hd, h->sc);
+            B->k_iter[s] = (long)(g_launches - before) + 1;
+            g_launches = before;
+            cudaGraph_t body = nullptr;
+            e = cudaStreamEndCapture(h->stream, &body);
+        }
+        if (e == cudaSuccess) e = cudaGraphAddChildGraphNode(&n_fin, G, &n_loop, 1, gfin);
+        if (gstart) cudaGraphDestroy(gstart);
+        if (gfin) cudaGraphDestroy(gfin);
+        if (!rc && e != cudaSuccess) {
+            set_err("batch graph construction failed: %s", cudaGetErrorString(e));
+            rc = LINA_GPU_ECUDA;
+        }
+    }
+    if (!rc) {
+        cudaError_t e = cudaGraphInstantiate(&B->exec, G, 0);
+        if (e != cudaSuccess) {
+            B->exec = nullptr;
+            set_err("batch graph instantiation failed: %s", cudaGetErrorString(e));
+            rc = LINA_GPU_ECUDA;
+        }
+    }
+    cudaGraphDestroy(G);
+    return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lina_gpu_batch_create(int count, lina_gpu_amg* const* systems, int stop_rule, lina_gpu_batch** out) {
+    if (!out || count < 1 || !systems || (stop_rule != LINA_STOP_REFERENCE && stop_rule != LINA_STOP_RELATIVE)) {
+        set_err("lina_gpu_batch_create: invalid argument");
+        return LINA_GPU_EINVAL;
+    }
+    *out = nullptr;
+    for (int i = 0; i < count; i++) {
+        if (!systems[i] || systems[i]->host_only) {
+            set_err("lina_gpu_batch_create: system %d is not a device hierarchy", i);
+            return LINA_GPU_EINVAL;
+        }
+        for (int j = 0; j < i; j++)
+            if (systems[j] == systems[i]) {
+                set_err("lina_gpu_batch_create: system %d appears twice", i);
+                return LINA_GPU_EINVAL;
+            }
+    }
+    lina_gpu_batch* B = new lina_gpu_batch();
+    B->sys.assign(systems, systems + count);
+    B->stop_rule = stop_rule;
+    B->k_start.assign(count, 0);
+    B->k_iter.assign(count, 0);
+    B->k_finish.assign(count, 0);
+    if (cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&B->lim, sizeof(BatchLimits)) != cudaSuccess ||
+        cudaMallocHost(&B->lim_host, sizeof(BatchLimits)) != cudaSuccess ||
+        cudaMallocHost(&B->sc_host, (size_t)count * sizeof(KScalars)) != cudaSuccess) {
+        set_err("lina_gpu_batch_create: allocation failed");
+        delete B;
+        return LINA_GPU_ECUDA;
+    }
+    // every system's hierarchy and vectors are ready before the capture
+    for (lina_gpu_amg* h : B->sys)
+        if (cudaStreamSynchronize(h->stream) != cudaSuccess) {
+            set_err("lina_gpu_batch_create: a system's stream failed");
+            delete B;
+            return LINA_GPU_ECUDA;
+        }
+    int rc = build_batch_graph(B);
+    if (rc) {
+        delete B;
+        return rc;
+    }
+    *out = B;
+    return 0;
+}
+
+int lina_gpu_batch_solve(lina_gpu_batch* B, const double* const* b, double* const* x, double tol, int max_iter,
+                         int flags, lina_gpu_solve_info* infos) {
+    if (!B || !b || !x || max_iter < 1) {
+        set_err("lina_gpu_batch_solve: invalid argument");
+        return LINA_GPU_EINVAL;
+    }
+    const int count = (int)B->sys.size();
+    for (int i = 0; i < count; i++)
+        if (!b[i] || !x[i]) {
+            set_err("lina_gpu_batch_solve: missing vector of system %d", i);
+            return LINA_GPU_EINVAL;
+        }
+    const bool dev = (flags & LINA_PCG_DEVICE_PTRS) != 0;
+    cudaStream_t st = B->stream;
+    B->lim_host->tol = tol;
+    B->lim_host->maxit = max_iter;
+    CK(cudaMemcpyAsync(B->lim, B->lim_host, sizeof(BatchLimits), cudaMemcpyHostToDevice, st));
+    for (int i = 0; i < count; i++) {
+        lina_gpu_amg* h = B->sys[i];
+        const int n = h->lv[h->depth - 1].n;
+        CK(cudaMemcpyAsync(h->kb, b[i], (size_t)n * sizeof(double),
+                           dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+    }
+    CK(cudaGraphLaunch(B->exec, st));
+    for (int i = 0; i < count; i++) {
+        lina_gpu_amg* h = B->sys[i];
+        const int n = h->lv[h->depth - 1].n;
+        CK(cudaMemcpyAsync(B->sc_host + i, h->sc, sizeof(KScalars), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(x[i], h->kx, (size_t)n * sizeof(double),
+                           dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+    }
+    CK(cudaStreamSynchronize(st));
+    int rc = 0;
+    for (int i = 0; i < count; i++) {
+        const KScalars& k = B->sc_host[i];
+        g_launches += (unsigned long long)(B->k_start[i] + 1 + B->k_finish[i] + (long)k.iter * B->k_iter[i]);
+        lina_gpu_solve_info inf{};
+        const double bnorm = std::sqrt(k.aux);
+        inf.iterations = k.iter;
+        inf.rel_residual = k.r0 > 0.0 ? std::sqrt(k.rr) / k.r0 : 0.0;
+        inf.true_rel_residual = bnorm > 0.0 ? std::sqrt(k.norm2) / bnorm : 0.0;
+        if (k.r0 > 0.0 && !std::isfinite(inf.rel_residual))
+            inf.status = LINA_GPU_EBREAKDOWN;
+        else if (inf.rel_residual > tol)
+            inf.status = LINA_GPU_ENOCONV;
+        // the relative rule is met only when the true residual meets it: otherwise the solve goes on
+        // from the batch's x with the single-system path (which restarts on the true residual)
+        if (B->stop_rule == LINA_STOP_RELATIVE && inf.status == 0 && inf.true_rel_residual > tol &&
+            inf.iterations < max_iter) {
+            lina_gpu_solve_info more{};
+            int r = lina_gpu_pcg(B->sys[i], b[i], x[i], tol, max_iter - inf.iterations, LINA_STOP_RELATIVE,
+                                 (flags & LINA_PCG_DEVICE_PTRS) | LINA_PCG_USE_X0, &more);
+            if (r && r != LINA_GPU_ENOCONV) return r;
+            inf.iterations += more.iterations;
+            inf.rel_residual = more.true_rel_residual;
+            inf.true_rel_residual = more.true_rel_residual;
+            inf.status = more.status;
+        } else if (B->stop_rule == LINA_STOP_RELATIVE && inf.status == 0 && inf.true_rel_residual > tol) {
+            inf.status = LINA_GPU_ENOCONV;
+        }
+        if (infos) infos[i] = inf;
+        if (inf.status && !rc) rc = inf.status == LINA_GPU_ENOCONV ? LINA_GPU_ENOCONV : inf.status;
+    }
+    return rc;
+}
+
+int lina_gpu_batch_size(const lina_gpu_batch* B) { return B ? (int)B->sys.size() : 0; }
+
+int lina_gpu_batch_destroy(lina_gpu_batch* B) {
+    delete B;
+    return 0;
+}
+
+}  // extern "C"

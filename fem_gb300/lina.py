@@ -89,6 +89,11 @@ def lib():
         "lina_gpu_amg_destroy": (C.c_int, [vp]),
         "lina_gpu_amg_set_smoother": (C.c_int, [vp, C.c_int, C.c_double, C.c_int]),
         "lina_gpu_pcg": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, C.POINTER(SolveInfo)]),
+        "lina_gpu_batch_create": (C.c_int, [C.c_int, C.POINTER(vp), C.c_int, C.POINTER(vp)]),
+        "lina_gpu_batch_solve": (C.c_int, [vp, C.POINTER(vp), C.POINTER(vp), C.c_double, C.c_int, C.c_int,
+                                           C.POINTER(SolveInfo)]),
+        "lina_gpu_batch_size": (C.c_int, [vp]),
+        "lina_gpu_batch_destroy": (C.c_int, [vp]),
         "lina_gpu_vcycle": (C.c_int, [vp, vp, vp]),
         "lina_gpu_spmv": (C.c_int, [vp, C.c_int, vp, vp]),
         "lina_gpu_amg_depth": (C.c_int, [vp]),
@@ -406,6 +411,49 @@ def spgemm(a, b, ncols_b):
     _check(lib().lina_gpu_spgemm(n, ncols_b, _ip(ap), _ip(ac), _dp(av), nb, _ip(bp), _ip(bc), _dp(bv),
                                  max(nnz.value, 1), _ip(cp), _ip(cc), _dp(cv), C.byref(nnz)), "spgemm")
     return cp, cc[:nnz.value], cv[:nnz.value]
+
+
+class Batch:
+    """Independent AMG-PCG solves in one CUDA graph launch (lina_gpu_batch_*)."""
+
+    def __init__(self, systems, stop=STOP_RELATIVE):
+        self.systems = list(systems)
+        self.sizes = [a.n for a in self.systems]
+        arr = (C.c_void_p * len(self.systems))(*[a.h.value if isinstance(a.h, C.c_void_p) else a.h
+                                                  for a in self.systems])
+        h = C.c_void_p()
+        self.h = None
+        _check(lib().lina_gpu_batch_create(len(self.systems), arr, stop, C.byref(h)), "batch create")
+        self.h = h
+
+    def solve(self, bs, tol=1e-8, max_iter=1000, device=False):
+        """bs: host arrays (or DeviceArray with device=True); returns (xs, [SolveInfo])."""
+        k = len(self.systems)
+        if device:
+            xs = [DeviceArray(n) for n in self.sizes]
+            bp = (C.c_void_p * k)(*[b.ptr for b in bs])
+            xp = (C.c_void_p * k)(*[x.ptr for x in xs])
+        else:
+            bb = [np.ascontiguousarray(b, dtype=np.float64) for b in bs]
+            xs = [np.zeros(n) for n in self.sizes]
+            bp = (C.c_void_p * k)(*[b.ctypes.data for b in bb])
+            xp = (C.c_void_p * k)(*[x.ctypes.data for x in xs])
+        infos = (SolveInfo * k)()
+        rc = lib().lina_gpu_batch_solve(self.h, bp, xp, tol, max_iter, PCG_DEVICE_PTRS if device else 0, infos)
+        if rc not in (0, ENOCONV):
+            raise LinaError(f"batch solve failed ({rc}): {last_error()}")
+        return xs, list(infos)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().lina_gpu_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def gmres(M: "Matrix", b, ilu: "ILU | None" = None, amg: "AMG | None" = None, precon_precision=PREC_FP64, tol=1e-8,

@@ -428,3 +428,138 @@ def at2_damage(m: int, seed: int = 0, gc: float = 2.7e-3, sigma: float = 1.0, E:
     return CSRSystem(nn, indptr, indices, data, b, dof=1,
                      meta={"kind": "at2_damage", "m": m, "gc": gc, "ell": ell, "lower": lower, "upper": upper,
                            "x0": x0})
+
+
+# ----------------------------------------------------------------------------- unstructured batches
+def delaunay_mesh(n_nodes: int, seed: int = 0, jitter: float = 0.35):
+    """Seeded unstructured triangle mesh of the unit square with about ``n_nodes`` nodes.
+
+    The nodes are a k x k lattice (k = round(sqrt(n_nodes))) whose interior points are moved by a
+    seeded uniform offset of up to ``jitter`` spacings in each direction; boundary nodes stay on
+    the edges.  The triangles are their Delaunay triangulation (scipy.spatial.Delaunay), ordered
+    counter-clockwise.  Returns ``(xy[n, 2], tri[n_elems, 3])``.
+    """
+    from scipy.spatial import Delaunay
+
+    k = max(3, int(round(np.sqrt(n_nodes))))
+    h = 1.0 / (k - 1)
+    r, c = np.divmod(np.arange(k * k), k)
+    xy = np.stack([c * h, r * h], axis=1)
+    rng = np.random.default_rng(seed)
+    inner = (r > 0) & (r < k - 1) & (c > 0) & (c < k - 1)
+    xy[inner] += rng.uniform(-jitter * h, jitter * h, size=(int(inner.sum()), 2))
+    tri = Delaunay(xy).simplices.astype(np.int64)
+    p = xy[tri]
+    area2 = (p[:, 1, 0] - p[:, 0, 0]) * (p[:, 2, 1] - p[:, 0, 1]) - (p[:, 2, 0] - p[:, 0, 0]) * (p[:, 1, 1] - p[:, 0, 1])
+    tri = tri[np.abs(area2) > 1e-9 * h * h]
+    flip = area2[np.abs(area2) > 1e-9 * h * h] < 0
+    tri[flip] = tri[flip][:, [0, 2, 1]]
+    return xy, tri.astype(np.int32)
+
+
+def _p1_gradients(xy, tri):
+    """b, c (shape [n_elems, 3]) and areas of P1 triangles: grad phi_a = (b_a, c_a) / (2 area)."""
+    x = xy[tri, 0]
+    y = xy[tri, 1]
+    b = np.stack([y[:, 1] - y[:, 2], y[:, 2] - y[:, 0], y[:, 0] - y[:, 1]], axis=1)
+    c = np.stack([x[:, 2] - x[:, 1], x[:, 0] - x[:, 2], x[:, 1] - x[:, 0]], axis=1)
+    area = 0.5 * np.abs(x[:, 0] * b[:, 0] + x[:, 1] * b[:, 1] + x[:, 2] * b[:, 2])
+    return b, c, area
+
+
+def _csr_eliminate(n, rows, cols, vals, fixed, fixed_val, b):
+    """Sum duplicates to a symmetric CSR matrix (sorted columns), then eliminate the fixed dofs
+    symmetrically."""
+    import scipy.sparse as sp
+
+    A = sp.coo_matrix((vals, (rows, cols)), shape=(n, n)).tocsr()
+    A.sum_duplicates()
+    A = ((A + A.T) * 0.5).tocsr()  # exactly symmetric: the sums of duplicates ran in different orders
+    A.sort_indices()
+    is_fixed = np.zeros(n, dtype=bool)
+    is_fixed[fixed] = True
+    u_d = np.zeros(n)
+    u_d[fixed] = fixed_val
+    b = b - A @ u_d
+    r = np.repeat(np.arange(n), np.diff(A.indptr))
+    keep = ~is_fixed[r] & ~is_fixed[A.indices]
+    diag = (r == A.indices) & is_fixed[r]
+    data = A.data.copy()
+    data[diag] = 1.0
+    keep |= diag
+    counts = np.bincount(r[keep], minlength=n)
+    indptr = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(counts, out=indptr[1:])
+    b[is_fixed] = u_d[is_fixed]
+    return indptr.astype(np.int32), A.indices[keep].astype(np.int32), data[keep], b
+
+
+def batch_system(kind: str, dofs: int, seed: int = 0, sigma: float = 1.5, nu: float = 0.3,
+                 top_uy: float = 1e-3) -> CSRSystem:
+    """One system of the batched workload on ``delaunay_mesh``: a per-element lognormal coefficient
+    (sigma 1.5, seeded) times the P1 stiffness.
+
+    ``kind`` "poisson": scalar Laplacian, homogeneous Dirichlet on the whole boundary, right-hand
+    side uniform in [-1, 1] on the free rows (``dofs`` nodes).  ``kind`` "elasticity": plane
+    strain, E_e = 210 * lognormal, nu 0.3, block dof ordering [u_x of all nodes, u_y of all nodes]
+    (dof 2), bottom edge clamped, top edge u_y = ``top_uy`` (``dofs / 2`` nodes).  Dirichlet
+    conditions by symmetric elimination, as in ``elasticity_p1``.
+    """
+    rng = np.random.default_rng(seed)
+    if kind == "poisson":
+        xy, tri = delaunay_mesh(dofs, seed)
+        nn = len(xy)
+        b_, c_, area = _p1_gradients(xy, tri)
+        kappa = np.exp(sigma * rng.standard_normal(len(tri)))
+        ke = (b_[:, :, None] * b_[:, None, :] + c_[:, :, None] * c_[:, None, :]) / (4.0 * area)[:, None, None]
+        ke *= kappa[:, None, None]
+        rows = np.repeat(tri, 3, axis=1).ravel()
+        cols = np.tile(tri, (1, 3)).ravel()
+        on_edge = (xy[:, 0] == 0.0) | (xy[:, 0] == 1.0) | (xy[:, 1] == 0.0) | (xy[:, 1] == 1.0)
+        fixed = np.nonzero(on_edge)[0]
+        rhs = rng.uniform(-1.0, 1.0, nn)
+        ptr, col, val, b = _csr_eliminate(nn, rows, cols, ke.ravel(), fixed, np.zeros(len(fixed)), rhs)
+        return CSRSystem(nn, ptr, col, val, b, dof=1, meta={"kind": kind, "seed": seed, "elements": len(tri)})
+    if kind == "elasticity":
+        xy, tri = delaunay_mesh(max(dofs // 2, 9), seed)
+        nn = len(xy)
+        b_, c_, area = _p1_gradients(xy, tri)
+        E = 210.0 * np.exp(sigma * rng.standard_normal(len(tri)))
+        ne = len(tri)
+        B = np.zeros((ne, 3, 6))
+        B[:, 0, 0::2] = b_
+        B[:, 1, 1::2] = c_
+        B[:, 2, 0::2] = c_
+        B[:, 2, 1::2] = b_
+        B /= (2.0 * area)[:, None, None]
+        D = np.array([[1.0 - nu, nu, 0.0], [nu, 1.0 - nu, 0.0], [0.0, 0.0, (1.0 - 2.0 * nu) / 2.0]])
+        D = D / ((1.0 + nu) * (1.0 - 2.0 * nu))
+        ke = np.einsum("eia,ij,ejb->eab", B, D, B) * (area * E)[:, None, None]
+        ke = 0.5 * (ke + ke.transpose(0, 2, 1))  # exactly symmetric
+        # element dof (a, p) -> global p * nn + node
+        gd = np.stack([tri, tri + nn], axis=2).reshape(ne, 6)
+        rows = np.repeat(gd, 6, axis=1).ravel()
+        cols = np.tile(gd, (1, 6)).ravel()
+        bottom = np.nonzero(xy[:, 1] == 0.0)[0]
+        top = np.nonzero(xy[:, 1] == 1.0)[0]
+        fixed = np.concatenate([bottom, nn + bottom, nn + top])
+        fval = np.concatenate([np.zeros(2 * len(bottom)), np.full(len(top), top_uy)])
+        order = np.argsort(fixed)
+        ptr, col, val, b = _csr_eliminate(2 * nn, rows, cols, ke.ravel(), fixed[order], fval[order],
+                                          np.zeros(2 * nn))
+        return CSRSystem(2 * nn, ptr, col, val, b, dof=2, meta={"kind": kind, "seed": seed, "elements": ne})
+    raise ValueError(f"unknown system kind {kind!r}")
+
+
+def batch_plan(count: int = 96, seed: int = 0, lo: int = 10_000, hi: int = 500_000):
+    """(kind, dofs, seed) of the batched workload: kinds alternate Poisson / elasticity, dof counts
+    log-uniform on [lo, hi] (seeded)."""
+    rng = np.random.default_rng(seed)
+    dofs = np.exp(rng.uniform(np.log(lo), np.log(hi), count)).astype(np.int64)
+    return [("poisson" if i % 2 == 0 else "elasticity", int(dofs[i]), seed * 1000 + i + 1) for i in range(count)]
+
+
+def batch_depth(n: int) -> int:
+    """AMG depth for a batched system: coarsest level of roughly a thousand rows (standard
+    coarsening shrinks a 2D P1 level by about 2.3x)."""
+    return int(min(10, max(2, 1 + np.ceil(np.log(max(n, 1000) / 1000.0) / np.log(2.3)))))

@@ -110,6 +110,22 @@ int lina_gpu_amg_set_smoother(lina_gpu_amg* h, int smoother, double omega, int p
 /* AMG-preconditioned CG on the hierarchy's finest matrix (pcg, LinA/PCGS.c:163). */
 int lina_gpu_pcg(lina_gpu_amg* h, const double* b, double* x, double tol, int max_iter,
                  int stop_rule, int flags, lina_gpu_solve_info* info);
+/* Batched AMG-PCG over independent systems (no reference counterpart: the reference solves them
+   one pcg call at a time).  One CUDA graph holds a branch per system: x = 0, the PCG loop of
+   lina_gpu_pcg on the device and the true residual.  One launch solves all systems concurrently.
+   The hierarchies stay owned by the caller.  They must outlive the batch, keep the smoother and
+   precision they had at creation, and be used by nothing else while a batch solve runs.  A system
+   may appear once.  stop_rule as for lina_gpu_pcg.  With LINA_STOP_RELATIVE, a system whose true
+   residual misses tol continues from the batch's x on its own (lina_gpu_pcg restarts from the
+   true residual); infos[i] then counts both parts. */
+typedef struct lina_gpu_batch lina_gpu_batch;
+int lina_gpu_batch_create(int count, lina_gpu_amg* const* systems, int stop_rule, lina_gpu_batch** out);
+/* b[i], x[i]: host arrays (device arrays with LINA_PCG_DEVICE_PTRS) of system i's size; infos may
+   be NULL.  Returns 0, LINA_GPU_ENOCONV when a system did not converge, or another error. */
+int lina_gpu_batch_solve(lina_gpu_batch* batch, const double* const* b, double* const* x, double tol,
+                         int max_iter, int flags, lina_gpu_solve_info* infos);
+int lina_gpu_batch_size(const lina_gpu_batch* batch);
+int lina_gpu_batch_destroy(lina_gpu_batch* batch);
 /* AMG_solve (LinA/Multigrid.c:1863): V-cycles from the initial guess X until ||F - A X|| / ||F - A X0||
    <= eps or max_iter cycles; flags may hold LINA_PCG_DEVICE_PTRS.  Returns the cycles done and the
    final relative residual. */

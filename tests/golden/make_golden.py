@@ -224,6 +224,26 @@ def spgemm_inputs(seed=7):
 
 
 ILU_FILE = "ilu"
+BATCH_FILE = "batch_small"
+# small systems of the batched workload: name -> (kind, dofs, seed)
+BATCH_CASES = {"bpoisson3k": ("poisson", 3000, 11), "belast4k": ("elasticity", 4000, 12),
+               "bpoisson12k": ("poisson", 12000, 13)}
+
+
+def make_batch():
+    """pcg of the reference (damped-Jacobi V-cycle, tolerance 1e-8 in its own rule) and an accurate
+    solution (1e-13) for small systems of the batched unstructured workload; the systems are stored."""
+    out = {}
+    for name, (kind, dofs, seed) in BATCH_CASES.items():
+        s = problems.batch_system(kind, dofs, seed)
+        depth = problems.batch_depth(s.n)
+        amg = ref.RefAMG(s, depth, 2, 2, ref.STANDARD)
+        x, it, res = amg.pcg(s.b, TOL, MAX_IT, ref.SMOOTHER_DAMPED_JACOBI, 0.6)
+        xt, _, _ = amg.pcg(s.b, 1e-13, 2000, ref.SMOOTHER_MC_SOR, 1.0)
+        out.update({f"{name}_ptr": s.indptr, f"{name}_col": s.indices, f"{name}_val": s.data, f"{name}_b": s.b,
+                    f"{name}_dof": np.int64(s.dof), f"{name}_depth": np.int64(depth), f"{name}_x": x,
+                    f"{name}_it": np.int64(it), f"{name}_x_tight": xt})
+    return out
 
 
 def ilu_inputs():
@@ -329,6 +349,11 @@ def main():
         path = os.path.join(HERE, "spgemm.npz")
         np.savez_compressed(path, **data)
         print(f"{path}: product with {len(data['c_col'])} entries")
+    if not only or BATCH_FILE in only:
+        data = make_batch()
+        path = os.path.join(HERE, f"{BATCH_FILE}.npz")
+        np.savez_compressed(path, **data)
+        print(f"{path}: " + ", ".join(f"{k}={int(v)}" for k, v in data.items() if k.endswith("_it")))
     if not only or ILU_FILE in only:
         data = make_ilu()
         path = os.path.join(HERE, f"{ILU_FILE}.npz")
