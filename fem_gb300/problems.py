@@ -444,7 +444,7 @@ def delaunay_mesh(n_nodes: int, seed: int = 0, jitter: float = 0.35):
     k = max(3, int(round(np.sqrt(n_nodes))))
     h = 1.0 / (k - 1)
     r, c = np.divmod(np.arange(k * k), k)
-    xy = np.stack([c * h, r * h], axis=1)
+    xy = np.stack([c / (k - 1), r / (k - 1)], axis=1)  # edges exactly at 0 and 1
     rng = np.random.default_rng(seed)
     inner = (r > 0) & (r < k - 1) & (c > 0) & (c < k - 1)
     xy[inner] += rng.uniform(-jitter * h, jitter * h, size=(int(inner.sum()), 2))

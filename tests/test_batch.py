@@ -67,6 +67,20 @@ def test_batch_plan():
     assert 8e6 <= d.sum() <= 20e6  # log-uniform on [10k, 500k]: mean about 125k
 
 
+@pytest.mark.parametrize("nodes", [162 ** 2, 55 ** 2, 100 ** 2])
+def test_batch_system_boundary_conditions(nodes):
+    """Every edge node is found (k x k lattices whose spacing does not divide 1 exactly included):
+    elasticity fixes both components on the bottom edge and u_y on the top edge, Poisson the whole
+    boundary; the right-hand sides are not zero."""
+    k = int(round(np.sqrt(nodes)))
+    e = problems.batch_system("elasticity", 2 * nodes, seed=4)
+    ident = np.diff(e.indptr) == 1
+    assert ident.sum() == 3 * k and np.linalg.norm(e.b) > 0
+    assert np.allclose(e.b[k * k:][ident[k * k:]], np.r_[np.zeros(k), np.full(k, 1e-3)])
+    p = problems.batch_system("poisson", nodes, seed=4)
+    assert (np.diff(p.indptr) == 1).sum() == 4 * (k - 1) and np.linalg.norm(p.b) > 0
+
+
 def test_batch_create_rejects_empty():
     h = C.c_void_p()
     assert lina.lib().lina_gpu_batch_create(0, None, lina.STOP_RELATIVE, C.byref(h)) == lina.EINVAL
