@@ -10,6 +10,7 @@
 // FP64/FP32.  Reductions are single-pass: each block writes one partial and the
 // last block to finish (atomic ticket, no waiting) sums the partials in a fixed
 // order, so results are bitwise reproducible from run to run.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -17,6 +18,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -30,6 +32,9 @@ namespace {
 std::string g_err;
 unsigned long long g_launches = 0;  // kernels launched by this library (all handles)
 int g_layout = 0;  // 0 automatic, 1 SELL-32, 2 lane groups (size chosen per matrix), 3..6 groups of 4..32 lanes
+// levels of at most this many rows run a multicolour-SOR V-cycle step as one thread-block-cluster launch
+// (0: one launch per colour and step)
+int g_fused_rows = 32768;
 
 void set_err(const char* fmt, ...) {
     char buf[512];
@@ -601,6 +606,280 @@ __global__ void __launch_bounds__(kThreads) norm2_kernel(int n, const T* __restr
 namespace {
 
 // a matrix on the device in SELL-32 layout (see sell_kernel)
+// ------------------------------------------------------------ cluster-fused V-cycle steps
+// On small levels a multicolour-SOR sweep is a chain of tiny launches (one per colour: 10-25 on the
+// coarse levels of elasticity hierarchies), each bound by launch and memory latency.  A level step
+// instead runs as one launch of a thread-block cluster:
+//   pre : x = 0 | sweep colour 0 | ... | colour c-1 (nu times) | r = b - A x | b_coarse = R r
+//   post: x += P e | sweep colour 0 | ... (nu times)
+// with a cluster barrier where the separate launches had a kernel boundary.  Every block keeps a
+// full copy of the level's x in its shared memory for the whole step: a row reads its neighbours
+// from its own SM, and a new entry is stored into every block's copy (the lanes of the row's group
+// share those stores) before the colour's barrier.  x is read from and written back to global
+// memory once per step.  Every row is computed exactly as csrv_kernel computes it (the same lane
+// groups, the same order of products and of the shuffle reduction), so the results are
+// bit-identical to the per-colour launches.
+namespace cg = cooperative_groups;
+
+constexpr int kFuseThreads = 512;
+constexpr int kFusedRowsMax = 24576;                     // a copy of x per block: 192 KB in FP64
+constexpr int kFusedSmemMax = kFusedRowsMax * 8;
+
+struct FusedStep {
+    int n, nc, ncolours, nu;
+    int sS, aS, rS, pS;  // lanes per row: colour-grouped A, natural A, R, P
+    const int *sptr, *scol, *srows, *sgroup;
+    const int4* shead;  // (row, first entry, end of entries) per position of the colour order
+    const int *aptr, *acol;
+    const int *rptr, *rcol;
+    const int *pptr, *pcol;
+    const void *sval, *aval, *rval, *pval, *dinv, *b, *e;
+    void *x, *r, *cb;
+    double w;
+};
+
+template <typename TX>
+struct LocalRead {
+    const TX* p;
+    __device__ __forceinline__ TX get(int j) const { return p[j]; }
+};
+template <typename TX>
+struct GlobalRead {
+    const TX* p;
+    __device__ __forceinline__ TX get(int j) const { return __ldcg(p + j); }
+};
+
+// entry i of every block's copy of x := v, the group's S lanes sharing the stores
+template <typename TX>
+__device__ __forceinline__ void broadcast_x(TX* xs, int i, TX v, int sub, int S) {
+    const cg::cluster_group cl = cg::this_cluster();
+    const int K = (int)cl.num_blocks();
+    for (int r = sub; r < K; r += S) cl.map_shared_rank(xs, (unsigned)r)[i] = v;
+}
+
+// sum_k val_k v_col_k over one row by a group of S lanes (the order of csrv_kernel); the butterfly
+// leaves the sum in every lane of the group
+template <typename TX, typename V>
+__device__ __forceinline__ TX fused_row_sum(bool valid, int s0, int e0, int sub, int S, const int* __restrict__ col,
+                                            const TX* __restrict__ val, const V& v) {
+    TX sum = TX(0);
+    if (valid) {
+        int k = s0 + sub;
+        for (; k + 3 * S < e0; k += 4 * S) {
+            const int c0 = __ldg(col + k), c1 = __ldg(col + k + S), c2 = __ldg(col + k + 2 * S),
+                      c3 = __ldg(col + k + 3 * S);
+            const TX v0 = __ldg(val + k), v1 = __ldg(val + k + S), v2 = __ldg(val + k + 2 * S),
+                     v3 = __ldg(val + k + 3 * S);
+            const TX x0 = v.get(c0), x1 = v.get(c1), x2 = v.get(c2), x3 = v.get(c3);
+            sum += TX(v0) * x0;
+            sum += TX(v1) * x1;
+            sum += TX(v2) * x2;
+            sum += TX(v3) * x3;
+        }
+        for (; k < e0; k += S) sum += TX(__ldg(val + k)) * v.get(__ldg(col + k));
+    }
+    for (int o = S / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, S);
+    return sum;
+}
+
+// rows [r0, r1) of the natural order in lane groups of S spread over the cluster; f(i, sum, sub)
+// is called by every lane of row i's group
+template <typename TX, typename V, typename F>
+__device__ __forceinline__ void fused_rows(int r0, int r1, int S, const int* __restrict__ ptr,
+                                           const int* __restrict__ col, const TX* __restrict__ val, const V& v,
+                                           F f) {
+    const int lane = threadIdx.x & 31, sub = lane & (S - 1);
+    const cg::cluster_group cl = cg::this_cluster();
+    const int warp = (int)(cl.thread_rank() >> 5), nwarps = (int)(cl.num_threads() >> 5);
+    const int per_warp = 32 / S;
+    for (int gb = r0 + warp * per_warp; gb < r1; gb += nwarps * per_warp) {
+        const int g = gb + lane / S;
+        const bool valid = g < r1;
+        int s0 = 0, e0 = 0;
+        if (valid) {
+            s0 = __ldg(ptr + g);
+            e0 = __ldg(ptr + g + 1);
+        }
+        const TX sum = fused_row_sum<TX>(valid, s0, e0, sub, S, col, val, v);
+        if (valid) f(g, sum, sub);
+    }
+}
+
+// The first row a lane group sweeps in a colour, fetched before the colour starts: everything
+// but the entries of x, which the previous colour may have changed.
+template <typename TX>
+struct SweepRow {
+    int i = 0, s0 = 0, e0 = 0;
+    int c[4];
+    TX v[4];
+    TX bi = TX(0), di = TX(0);
+};
+
+// the row at position g of the colour order: its head (row and entry range) is loaded one step
+// before the rest, so that no load of a step depends on another load of the same step
+template <typename TX>
+__device__ __forceinline__ int4 load_head(const FusedStep& st, int g, bool valid) {
+    return valid ? __ldg(st.shead + g) : make_int4(0, 0, 0, 0);
+}
+
+template <typename TX>
+__device__ __forceinline__ void build_sweep_row(SweepRow<TX>& p, int4 h, bool valid, int sub, int S,
+                                                const FusedStep& st, const TX* __restrict__ sval,
+                                                const TX* __restrict__ b, const TX* __restrict__ dinv) {
+    p.i = h.x;
+    p.s0 = h.y;
+    p.e0 = h.z;
+    if (valid) {
+        p.bi = __ldg(b + p.i);
+        p.di = __ldg(dinv + p.i);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const int k = p.s0 + sub + j * S;
+        const bool in = valid && k < p.e0;
+        p.c[j] = in ? __ldg(st.scol + k) : -1;
+        p.v[j] = in ? __ldg(sval + k) : TX(0);
+    }
+}
+
+template <typename TX>
+__device__ __forceinline__ void fetch_sweep_row(SweepRow<TX>& p, bool valid, int g, int sub, int S,
+                                                const FusedStep& st, const TX* __restrict__ sval,
+                                                const TX* __restrict__ b, const TX* __restrict__ dinv) {
+    build_sweep_row<TX>(p, load_head<TX>(st, g, valid), valid, sub, S, st, sval, b, dinv);
+}
+
+// the SOR update of a fetched row (the order of products of fused_row_sum: the first four strides
+// from the fetched entries, the rest as csrv_kernel walks them), stored into every copy of x
+template <typename TX>
+__device__ __forceinline__ void sweep_fetched_row(const SweepRow<TX>& p, bool valid, int sub, int S, TX w,
+                                                  const FusedStep& st, const TX* __restrict__ sval, TX* xs) {
+    TX sum = TX(0);
+    if (valid) {
+        TX xv[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) xv[j] = p.c[j] >= 0 ? xs[p.c[j]] : TX(0);
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            if (p.c[j] >= 0) sum += TX(p.v[j]) * xv[j];
+        int k = p.s0 + sub + 4 * S;
+        for (; k + 3 * S < p.e0; k += 4 * S) {
+            const int c0 = __ldg(st.scol + k), c1 = __ldg(st.scol + k + S), c2 = __ldg(st.scol + k + 2 * S),
+                      c3 = __ldg(st.scol + k + 3 * S);
+            const TX v0 = __ldg(sval + k), v1 = __ldg(sval + k + S), v2 = __ldg(sval + k + 2 * S),
+                     v3 = __ldg(sval + k + 3 * S);
+            const TX x0 = xs[c0], x1 = xs[c1], x2 = xs[c2], x3 = xs[c3];
+            sum += TX(v0) * x0;
+            sum += TX(v1) * x1;
+            sum += TX(v2) * x2;
+            sum += TX(v3) * x3;
+        }
+        for (; k < p.e0; k += S) sum += TX(__ldg(sval + k)) * xs[__ldg(st.scol + k)];
+    }
+    for (int o = S / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, S);
+    if (valid) broadcast_x(xs, p.i, xs[p.i] + w * p.di * (p.bi - sum), sub, S);
+}
+
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+
+// nu sweeps over the colours, a cluster barrier after each colour.  The first row a lane group
+// sweeps in a colour is loaded as a two-stage pipeline across the barriers: its head two colours
+// ahead, its entries, b and 1/a_ii one colour ahead, so after a barrier only shared-memory reads of
+// x are on the critical path.  Colours with more rows than the cluster has lane groups sweep the
+// remaining rows directly.
+template <typename TX>
+__device__ __forceinline__ void fused_sweeps(const FusedStep& st, TX* xs, const TX* __restrict__ b,
+                                             const TX* __restrict__ dinv) {
+    const TX w = TX(st.w);
+    const TX* sval = (const TX*)st.sval;
+    const int S = st.sS;
+    const int lane = threadIdx.x & 31, sub = lane & (S - 1);
+    const cg::cluster_group cl = cg::this_cluster();
+    const int warp = (int)(cl.thread_rank() >> 5), nwarps = (int)(cl.num_threads() >> 5);
+    const int per_warp = 32 / S;
+    const int first = warp * per_warp + lane / S;  // the group's row offset in a colour's first pass
+    const int steps = st.nu * st.ncolours;
+    if (steps == 0) return;
+    // colour of a step and its position range
+    auto range = [&](int step, int& r0, int& r1) {
+        const int c = step % st.ncolours;
+        r0 = __ldg(st.sgroup + c);
+        r1 = __ldg(st.sgroup + c + 1);
+    };
+    int r0, r1, n0, n1, m0, m1;
+    range(0, r0, r1);
+    SweepRow<TX> cur, nxt;
+    fetch_sweep_row<TX>(cur, r0 + first < r1, r0 + first, sub, S, st, sval, b, dinv);
+    int4 h1 = make_int4(0, 0, 0, 0);
+    n0 = n1 = 0;
+    if (steps > 1) {
+        range(1, n0, n1);
+        h1 = load_head<TX>(st, n0 + first, n0 + first < n1);
+    }
+    for (int step = 0; step < steps; step++) {
+        int4 h2 = make_int4(0, 0, 0, 0);
+        m0 = m1 = 0;
+        if (step + 2 < steps) {
+            range(step + 2, m0, m1);
+            h2 = load_head<TX>(st, m0 + first, m0 + first < m1);
+        }
+        if (step + 1 < steps) build_sweep_row<TX>(nxt, h1, n0 + first < n1, sub, S, st, sval, b, dinv);
+        sweep_fetched_row<TX>(cur, r0 + first < r1, sub, S, w, st, sval, xs);
+        for (int gb = r0 + warp * per_warp + nwarps * per_warp; gb < r1; gb += nwarps * per_warp) {
+            const int g = gb + lane / S;
+            SweepRow<TX> q;
+            fetch_sweep_row<TX>(q, g < r1, g, sub, S, st, sval, b, dinv);
+            sweep_fetched_row<TX>(q, g < r1, sub, S, w, st, sval, xs);
+        }
+        cluster_arrive();
+        cluster_wait();
+        cur = nxt;
+        r0 = n0;
+        r1 = n1;
+        h1 = h2;
+        n0 = m0;
+        n1 = m1;
+    }
+}
+
+// dynamic shared memory of a block: a copy of x (n entries)
+template <typename TX, bool PRE>
+__global__ void __launch_bounds__(kFuseThreads, 1) fused_step_kernel(const FusedStep st) {
+    extern __shared__ __align__(16) unsigned char fused_smem[];
+    const cg::cluster_group cl = cg::this_cluster();
+    TX* xs = reinterpret_cast<TX*>(fused_smem);
+    TX* xg = (TX*)st.x;
+    const TX* b = (const TX*)st.b;
+    const TX* dinv = (const TX*)st.dinv;
+    for (int j = (int)threadIdx.x; j < st.n; j += blockDim.x) xs[j] = PRE ? TX(0) : __ldcg(xg + j);
+    cl.sync();
+    if (PRE) {
+        fused_sweeps<TX>(st, xs, b, dinv);
+        TX* r = (TX*)st.r;
+        fused_rows<TX>(0, st.n, st.aS, st.aptr, st.acol, (const TX*)st.aval, LocalRead<TX>{xs},
+                       [&](int i, TX sum, int sub) {
+                           if (sub == 0) r[i] = b[i] - sum;
+                       });
+        cl.sync();
+        TX* cb = (TX*)st.cb;
+        fused_rows<TX>(0, st.nc, st.rS, st.rptr, st.rcol, (const TX*)st.rval, GlobalRead<TX>{r},
+                       [&](int i, TX sum, int sub) {
+                           if (sub == 0) cb[i] = sum;
+                       });
+    } else {
+        fused_rows<TX>(0, st.n, st.pS, st.pptr, st.pcol, (const TX*)st.pval, GlobalRead<TX>{(const TX*)st.e},
+                       [&](int i, TX sum, int sub) { broadcast_x(xs, i, xs[i] + sum, sub, st.pS); });
+        cl.sync();
+        fused_sweeps<TX>(st, xs, b, dinv);
+    }
+    // the sweeps ended with a cluster barrier: every copy is final; each block writes its share
+    const int chunk = (st.n + (int)cl.num_blocks() - 1) / (int)cl.num_blocks();
+    const int lo = (int)cl.block_rank() * chunk, hi = min(st.n, lo + chunk);
+    for (int j = lo + (int)threadIdx.x; j < hi; j += blockDim.x) xg[j] = xs[j];
+    cl.sync();  // no block leaves while another may still store into its shared memory
+}
+
 struct DCsr {
     int n = 0, ncols = 0;
     long nnz = 0;        // stored entries of the CSR source
@@ -618,6 +897,9 @@ struct DCsr {
     int* ptr = nullptr;
     int* rows = nullptr;
     std::vector<int> group_row;     // colour c: rows[group_row[c] .. group_row[c+1])
+    int* d_group_row = nullptr;     // the same offsets on the device
+    int* d_head = nullptr;          // per position of rows: (row, ptr[row], ptr[row + 1], 0)
+    int max_group_rows = 0;         // rows of the largest colour
 };
 
 // Layout choice, from sweeps of every level of the 2.1M-dof elasticity hierarchy on GB300 in every
@@ -851,6 +1133,16 @@ struct lina_gpu_amg {
                     d.group_row.push_back((int)all.size());
                 }
                 if ((rc = upload(&d.rows, all.data(), all.size()))) return rc;
+                if ((rc = upload(&d.d_group_row, d.group_row.data(), d.group_row.size()))) return rc;
+                std::vector<int> head(4 * all.size(), 0);
+                for (size_t g = 0; g < all.size(); g++) {
+                    head[4 * g] = all[g];
+                    head[4 * g + 1] = c.ptr[all[g]];
+                    head[4 * g + 2] = c.ptr[all[g] + 1];
+                }
+                if ((rc = upload(&d.d_head, head.data(), head.size()))) return rc;
+                for (size_t k = 0; k + 1 < d.group_row.size(); k++)
+                    d.max_group_rows = std::max(d.max_group_rows, d.group_row[k + 1] - d.group_row[k]);
             } else {
                 d.group_row.push_back(c.n);
             }
@@ -1085,8 +1377,117 @@ struct lina_gpu_amg {
         DLevel& L = lv[l];
         const int nu = (opt.coarsening == LINA_AGGRESSIVE && l == depth - 1) ? opt.aggr_smoothing_iterations
                                                                              : opt.smoothing_iterations;
+        if (fusable(L, time_it && l == timed_level)) {
+            DLevel& C = lv[l - 1];
+            launch_fused<TX, true>(L, C, nu, b, x, nullptr);
+            vcycle_level<TX>(l - 1, lvx<TX>(C, 2), lvx<TX>(C, 0), time_it);
+            launch_fused<TX, false>(L, C, nu, b, x, lvx<TX>(C, 0));
+            return;
+        }
         presmooth<TX, TX>(L, nu, b, nullptr, nullptr, const_cast<TX*>(b), x, time_it && l == timed_level);
         run_rest<TX>(l, L, nu, b, x, time_it);
+    }
+
+    // an interior level whose multicolour-SOR step runs as one cluster launch (a copy of its x fits a
+    // block's shared memory)
+    bool fusable(const DLevel& L, bool timed) const {
+        return g_fused_rows > 0 && opt.smoother == LINA_SMOOTHER_MC_SOR && !timed && L.n <= g_fused_rows &&
+               L.n <= kFusedRowsMax &&
+               L.ncolours > 0 && L.Acol.lanes > 0 && L.Acol.d_group_row && L.Acol.d_head && L.A.lanes > 0 &&
+               L.R.lanes > 0 && L.P.lanes > 0;
+    }
+
+    template <typename TX, bool PRE>
+    void launch_fused(DLevel& L, DLevel& C, int nu, const TX* b, TX* x, const TX* e) {
+        FusedStep st;
+        st.n = L.n;
+        st.nc = C.n;
+        st.ncolours = L.ncolours;
+        st.nu = nu;
+        st.sS = L.Acol.lanes;
+        st.aS = L.A.lanes;
+        st.rS = L.R.lanes;
+        st.pS = L.P.lanes;
+        st.sptr = L.Acol.ptr;
+        st.scol = L.Acol.col;
+        st.srows = L.Acol.rows;
+        st.sgroup = L.Acol.d_group_row;
+        st.shead = reinterpret_cast<const int4*>(L.Acol.d_head);
+        st.aptr = L.A.ptr;
+        st.acol = L.A.col;
+        st.rptr = L.R.ptr;
+        st.rcol = L.R.col;
+        st.pptr = L.P.ptr;
+        st.pcol = L.P.col;
+        if constexpr (sizeof(TX) == 8) {
+            st.sval = L.Acol.v64;
+            st.aval = L.A.v64;
+            st.rval = L.R.v64;
+            st.pval = L.P.v64;
+        } else {
+            st.sval = L.Acol.v32;
+            st.aval = L.A.v32;
+            st.rval = L.R.v32;
+            st.pval = L.P.v32;
+        }
+        st.dinv = lvdinv<TX>(L);
+        st.b = b;
+        st.e = e;
+        st.x = x;
+        st.r = lvx<TX>(L, 3);
+        st.cb = lvx<TX>(C, 2);
+        st.w = opt.omega;
+        const int K = fused_cluster_size<TX, PRE>();
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(K);
+        cfg.blockDim = dim3(kFuseThreads);
+        cfg.dynamicSmemBytes = (size_t)L.n * sizeof(TX);
+        cfg.stream = stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = K;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        g_launches++;
+        cudaLaunchKernelEx(&cfg, fused_step_kernel<TX, PRE>, st);
+    }
+
+    // 16 blocks per cluster where the GPU schedules such clusters, else (or with LINA_FUSED_CLUSTER=8)
+    // the portable 8.  Measured on the batch workload's 24-system sample: 16 blocks 3 % faster in total
+    // (the large elasticity systems gain, the 10k-row ones lose 2 %).
+    template <typename TX, bool PRE>
+    static int fused_cluster_size() {
+        static int k = 0;
+        if (k == 0) {
+            k = 8;
+            const char* env = getenv("LINA_FUSED_CLUSTER");
+            const bool want16 = !(env && atoi(env) == 8);
+            cudaFuncSetAttribute(fused_step_kernel<TX, PRE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 kFusedSmemMax);
+            if (want16 &&
+                cudaFuncSetAttribute(fused_step_kernel<TX, PRE>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+                    cudaSuccess) {
+                cudaLaunchConfig_t cfg = {};
+                cfg.gridDim = dim3(16);
+                cfg.blockDim = dim3(kFuseThreads);
+                cfg.dynamicSmemBytes = kFusedSmemMax;
+                cudaLaunchAttribute attr[1];
+                attr[0].id = cudaLaunchAttributeClusterDimension;
+                attr[0].val.clusterDim.x = 16;
+                attr[0].val.clusterDim.y = 1;
+                attr[0].val.clusterDim.z = 1;
+                cfg.attrs = attr;
+                cfg.numAttrs = 1;
+                int nclusters = 0;
+                if (cudaOccupancyMaxActiveClusters(&nclusters, fused_step_kernel<TX, PRE>, &cfg) == cudaSuccess &&
+                    nclusters > 0)
+                    k = 16;
+            }
+            cudaGetLastError();  // a refused attribute or query leaves no error behind
+        }
+        return k;
     }
 
     template <typename TX>
@@ -1398,6 +1799,15 @@ void lina_gpu_default_options(lina_gpu_amg_options* o) {
 }
 
 const char* lina_gpu_last_error(void) { return g_err.c_str(); }
+
+int lina_gpu_set_fused_rows(int max_rows) {
+    if (max_rows < 0) {
+        set_err("lina_gpu_set_fused_rows: max_rows must be >= 0");
+        return LINA_GPU_EINVAL;
+    }
+    g_fused_rows = max_rows;
+    return 0;
+}
 
 int lina_gpu_set_layout(int layout) {
     if (layout < 0 || layout > 6) {

@@ -110,6 +110,7 @@ def lib():
         "lina_gpu_device_count": (C.c_int, []),
         "lina_gpu_set_device": (C.c_int, [C.c_int]),
         "lina_gpu_set_layout": (C.c_int, [C.c_int]),
+        "lina_gpu_set_fused_rows": (C.c_int, [C.c_int]),
         "lina_gpu_last_error": (C.c_char_p, []),
         "lina_gpu_timer_begin": (C.c_int, [vp]),
         "lina_gpu_timer_end": (C.c_int, [vp, dp]),
@@ -254,6 +255,15 @@ LAYOUT_AUTO, LAYOUT_SELL, LAYOUT_CSRV = 0, 1, 2
 
 def set_layout(layout: int):
     _check(lib().lina_gpu_set_layout(int(layout)), "set layout")
+
+
+FUSED_ROWS_DEFAULT = 32768
+
+
+def set_fused_rows(max_rows: int):
+    """Levels of at most max_rows rows run a multicolour-SOR V-cycle step as one cluster launch
+    (0: one launch per colour)."""
+    _check(lib().lina_gpu_set_fused_rows(int(max_rows)), "set fused rows")
 
 
 def dot(a: "DeviceArray", b: "DeviceArray") -> float:

@@ -307,9 +307,15 @@ int lina_gpu_free_host(void* p);
 int lina_gpu_device_count(void);
 int lina_gpu_set_device(int device);   /* select the GPU for hierarchies created afterwards */
 /* storage layout of matrices uploaded afterwards: 0 automatic (SELL-32 thread-per-row for levels of
-   300k rows or more, CSR with a lane group per row otherwise), 1 SELL-32 always, 2 CSR lane groups
+   100k rows or more, CSR with a lane group per row otherwise), 1 SELL-32 always, 2 CSR lane groups
    always (group size chosen from the mean row length), 3..6 CSR lane groups of 4, 8, 16 or 32 lanes */
 int lina_gpu_set_layout(int layout);
+/* interior levels of at most max_rows rows (default 32768) run each multicolour-SOR V-cycle step
+   (pre: x = 0, the sweeps, the residual and the restriction; post: the prolongation and the sweeps)
+   as one launch of a thread-block cluster, with cluster barriers between the colours, instead of one
+   launch per colour and step; the results are bit-identical.  0 turns this off.  Takes effect for
+   solves issued afterwards (a hierarchy's captured solve graph keeps the choice it was captured with). */
+int lina_gpu_set_fused_rows(int max_rows);
 
 const char* lina_gpu_last_error(void);
 

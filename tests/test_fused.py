@@ -1,0 +1,83 @@
+"""Cluster-fused multicolour-SOR V-cycle steps (lina_gpu_set_fused_rows).
+
+The fused launch computes every row as the per-colour launches do, so V-cycles, FMG passes and
+whole PCG solves must agree bit for bit with the fusion on and off; the reference parity of the
+multicolour-SOR V-cycle itself is checked in test_gpu_solve.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from fem_gb300 import lina, problems
+from tests.conftest import ROOT, golden_cases, gpu_available, load_golden, system_for
+
+pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not gpu_available(), reason="no CUDA device")]
+
+BATCH = os.path.join(ROOT, "tests", "golden", "batch_small.npz")
+
+
+def systems():
+    out = []
+    for name in golden_cases("hierarchy"):
+        g = load_golden(name)
+        out.append((name, system_for(name), int(g["depth"]), int(g["coarsening"])))
+    with np.load(BATCH) as z:
+        for name in ("belast4k", "bpoisson12k"):
+            s = problems.CSRSystem(len(z[f"{name}_ptr"]) - 1, z[f"{name}_ptr"], z[f"{name}_col"], z[f"{name}_val"],
+                                   z[f"{name}_b"], dof=int(z[f"{name}_dof"]))
+            out.append((name, s, int(z[f"{name}_depth"]), lina.STANDARD))
+    return out
+
+
+CASES = systems()
+
+
+def build(s, depth, coarsening, precision, fused_rows):
+    lina.set_fused_rows(fused_rows)
+    try:
+        return lina.AMG.from_system(s, depth=depth, coarsening=coarsening, smoother=lina.SMOOTHER_MC_SOR, omega=1.0,
+                                    precision=precision)
+    finally:
+        lina.set_fused_rows(lina.FUSED_ROWS_DEFAULT)
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_vcycle_and_fmg_identical(case):
+    name, s, depth, coarsening = case
+    on = build(s, depth, coarsening, lina.PREC_FP64, lina.FUSED_ROWS_DEFAULT)
+    off = build(s, depth, coarsening, lina.PREC_FP64, 0)
+    r = np.random.default_rng(1).uniform(-1, 1, s.n)
+    lina.set_fused_rows(lina.FUSED_ROWS_DEFAULT)
+    z_on = on.vcycle(r)
+    x_on, _ = on.fmg(s.b)
+    lina.set_fused_rows(0)
+    try:
+        z_off = off.vcycle(r)
+        x_off, _ = off.fmg(s.b)
+    finally:
+        lina.set_fused_rows(lina.FUSED_ROWS_DEFAULT)
+    assert np.array_equal(z_on, z_off)
+    assert np.array_equal(x_on, x_off)
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+@pytest.mark.parametrize("precision", [lina.PREC_FP64, lina.PREC_MIXED])
+def test_pcg_identical(case, precision):
+    name, s, depth, coarsening = case
+    res = []
+    for rows in (lina.FUSED_ROWS_DEFAULT, 0):
+        amg = build(s, depth, coarsening, precision, rows)
+        lina.set_fused_rows(rows)
+        try:
+            res.append(amg.pcg(s.b, tol=1e-8, max_iter=500, stop=lina.STOP_RELATIVE))
+        finally:
+            lina.set_fused_rows(lina.FUSED_ROWS_DEFAULT)
+    (x1, i1), (x2, i2) = res
+    assert i1.status == 0 and i1.iterations == i2.iterations
+    assert np.array_equal(x1, x2)
+
+
+def test_fused_rows_validation():
+    with pytest.raises(lina.LinaError):
+        lina.set_fused_rows(-1)
