@@ -1097,7 +1097,10 @@ struct lina_gpu_amg {
         if (count) CK(cudaMemcpyAsync(*p, src, count * sizeof(T), cudaMemcpyHostToDevice, stream));
         return 0;
     }
-    int upload_csr(DCsr& d, const lina::Csr& c, const std::vector<std::vector<int>>* groups = nullptr) {
+    // pos_out (optional): the stored position of every CSR entry (-1: not stored), empty for the
+    // lane-group layout, whose positions are the CSR order
+    int upload_csr(DCsr& d, const lina::Csr& c, const std::vector<std::vector<int>>* groups = nullptr,
+                   std::vector<int>* pos_out = nullptr) {
         d = DCsr();
         d.n = c.n;
         d.ncols = c.ncols;
@@ -1150,6 +1153,7 @@ struct lina_gpu_amg {
             return cudaStreamSynchronize(stream) == cudaSuccess ? 0 : LINA_GPU_ECUDA;
         }
         SellHost S = make_sell(c, ncols, groups);
+        if (pos_out) pos_out->swap(S.pos);
         d.long_rows = c.n > 0 && double(c.nnz()) / c.n >= 24.0;
         if (S.col.size() > (size_t)INT_MAX) {
             set_err("padded matrix too large for 32-bit SELL offsets");
@@ -2344,7 +2348,40 @@ struct lina_gpu_matrix {
     DCsr A;
     double* dinv64 = nullptr;
     float* dinv32 = nullptr;
+    // for lina_gpu_matrix_update_values: stored position of each CSR entry (host until first use),
+    // the last diagonal entry of each row, staging for new values
+    long nnz = 0;
+    std::vector<int> pos_host, diag_host;
+    int *pos = nullptr, *diagpos = nullptr;
+    double* stage = nullptr;
 };
+
+namespace {
+
+// new values on the stored pattern: SELL (or CSR) values in both precisions and the inverse diagonal
+// (the last diagonal entry of a row, 0 where it is absent or zero, as at creation)
+__global__ void matrix_values_kernel(long nnz, const double* __restrict__ val, const int* __restrict__ pos,
+                                     double* __restrict__ v64, float* __restrict__ v32) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (long)gridDim.x * blockDim.x) {
+        const int p = pos ? pos[k] : (int)k;
+        if (p >= 0) {
+            v64[p] = val[k];
+            v32[p] = float(val[k]);
+        }
+    }
+}
+
+__global__ void matrix_dinv_kernel(int n, const double* __restrict__ val, const int* __restrict__ diagpos,
+                                   double* __restrict__ d64, float* __restrict__ d32) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int p = diagpos[i];
+        const double d = (p >= 0 && val[p] != 0.0) ? 1.0 / val[p] : 0.0;
+        d64[i] = d;
+        d32[i] = float(d);
+    }
+}
+
+}  // namespace
 
 int lina_gpu_matrix_create(int n, int ncols, const int* rowptr, const int* col, const double* val,
                            lina_gpu_matrix** out) {
@@ -2378,7 +2415,12 @@ int lina_gpu_matrix_create(int n, int ncols, const int* rowptr, const int* col, 
         for (int p = c.ptr[i]; p < c.ptr[i + 1]; p++)
             if (c.col[p] == i && c.val[p] != 0.0) dinv[i] = 1.0 / c.val[p];
     std::vector<float> dinv32(dinv.begin(), dinv.end());
-    int rc = h->upload_csr(m->A, c);
+    m->nnz = rowptr[n];
+    m->diag_host.assign(n, -1);
+    for (int i = 0; i < n; i++)
+        for (int p = c.ptr[i]; p < c.ptr[i + 1]; p++)
+            if (c.col[p] == i) m->diag_host[i] = p;
+    int rc = h->upload_csr(m->A, c, nullptr, &m->pos_host);
     if (!rc) rc = h->upload(&m->dinv64, dinv.data(), dinv.size());
     if (!rc) rc = h->upload(&m->dinv32, dinv32.data(), dinv32.size());
     if (!rc) rc = h->alloc(&h->partials, 2 * kMaxBlocks);
@@ -2392,6 +2434,36 @@ int lina_gpu_matrix_create(int n, int ncols, const int* rowptr, const int* col, 
         return rc;
     }
     *out = m;
+    return 0;
+}
+
+int lina_gpu_matrix_update_values(lina_gpu_matrix* m, const double* val, int flags) {
+    if (!m || !val) {
+        set_err("lina_gpu_matrix_update_values: invalid argument");
+        return LINA_GPU_EINVAL;
+    }
+    lina_gpu_amg* h = m->h;
+    int rc = 0;
+    if (!m->diagpos) {
+        if (!m->pos_host.empty()) rc = h->upload(&m->pos, m->pos_host.data(), m->pos_host.size());
+        if (!rc) rc = h->upload(&m->diagpos, m->diag_host.data(), m->diag_host.size());
+        if (!rc && !(flags & LINA_PCG_DEVICE_PTRS)) rc = h->alloc(&m->stage, (size_t)m->nnz);
+        if (!rc && cudaStreamSynchronize(h->stream) != cudaSuccess) rc = LINA_GPU_ECUDA;
+        if (rc) return rc;
+        m->pos_host = std::vector<int>();
+    }
+    const double* v = val;
+    if (!(flags & LINA_PCG_DEVICE_PTRS)) {
+        if (!m->stage && (rc = h->alloc(&m->stage, (size_t)m->nnz))) return rc;
+        CK(cudaMemcpyAsync(m->stage, val, (size_t)m->nnz * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        v = m->stage;
+    }
+    go(matrix_values_kernel, grid_for(m->nnz, kThreads), h->stream, m->nnz, v, (const int*)m->pos, m->A.v64,
+       m->A.v32);
+    go(matrix_dinv_kernel, grid_for(m->A.n, kThreads), h->stream, m->A.n, v, (const int*)m->diagpos, m->dinv64,
+       m->dinv32);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->stream));
     return 0;
 }
 

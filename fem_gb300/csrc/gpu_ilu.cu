@@ -47,7 +47,7 @@ constexpr int kPool = 128;   // threads of a block of the worker pool
 constexpr unsigned long long kWaitNs = 2000000000ull;
 constexpr long kWaitPolls = 1L << 26;
 constexpr unsigned kMaxSleepNs = 256;
-constexpr int kGroup = 4;  // solution entries a row of a triangular solve loads at once
+constexpr int kGroup = 8;  // solution entries a row of a triangular solve loads at once
 
 cudaStream_t st() { return (cudaStream_t)lina::dev::stream(); }
 
@@ -129,8 +129,9 @@ __global__ void __launch_bounds__(kPool) sptrsv_kernel(int n, const int* __restr
             const int p1 = end[i];
             TX s = b[i];
             bool ok = true;
-            // the entries of a group are loaded together (one round trip when they are final), then
-            // waited for and subtracted in column order
+            // the entries of a group are loaded together, and while some are pending all of those are
+            // read again together, so a row whose needed rows finish at about the same time waits one
+            // round trip, not one per entry; then the products are subtracted in column order
             for (int p = beg[i]; p < p1; p += kGroup) {
                 int k[kGroup];
                 U u[kGroup];
@@ -138,13 +139,21 @@ __global__ void __launch_bounds__(kPool) sptrsv_kernel(int n, const int* __restr
                 for (int q = 0; q < kGroup; q++) k[q] = p + q < p1 ? col[p + q] : -1;
 #pragma unroll
                 for (int q = 0; q < kGroup; q++) u[q] = k[q] >= 0 ? xw[k[q]] : U(0);
+                ok = ok && wait_for(
+                               [&] {
+                                   bool all = true;
 #pragma unroll
-                for (int q = 0; q < kGroup; q++) {
-                    if (k[q] < 0) break;
-                    if (u[q] == Word<TX>::kPending)
-                        ok = ok && wait_for([&] { return (u[q] = xw[k[q]]) != Word<TX>::kPending; }, err);
-                    s -= TX(val[p + q]) * from_bits<TX>(u[q]);
-                }
+                                   for (int q = 0; q < kGroup; q++)
+                                       if (k[q] >= 0 && u[q] == Word<TX>::kPending) {
+                                           u[q] = xw[k[q]];
+                                           all = all && u[q] != Word<TX>::kPending;
+                                       }
+                                   return all;
+                               },
+                               err);
+#pragma unroll
+                for (int q = 0; q < kGroup; q++)
+                    if (k[q] >= 0) s -= TX(val[p + q]) * from_bits<TX>(u[q]);
             }
             TX r = dinv ? s * dinv[i] : s;
             U ur = bits(r);
@@ -178,6 +187,105 @@ __device__ __forceinline__ bool find_upper(const int* col, int lo, int e, int j,
     return false;
 }
 
+// wait until the rows col[q] (q in [q0, q1), the entries left of the diagonal) show this pass,
+// polling up to eight flags together
+__device__ __forceinline__ bool wait_rows(const int* __restrict__ col, int q0, int q1, const int* flag, int epoch,
+                                          int* err) {
+    for (int q = q0; q < q1; q += 8) {
+        int k[8];
+        bool done[8];
+#pragma unroll
+        for (int t = 0; t < 8; t++) {
+            k[t] = q + t < q1 ? __ldg(col + q + t) : -1;
+            done[t] = k[t] < 0;
+        }
+        const bool ok = wait_for(
+            [&] {
+                bool all = true;
+#pragma unroll
+                for (int t = 0; t < 8; t++)
+                    if (!done[t]) {
+                        done[t] = *(volatile const int*)(flag + k[t]) == epoch;
+                        all = all && done[t];
+                    }
+                return all;
+            },
+            err);
+        if (!ok) return false;
+    }
+    return true;
+}
+
+// One row of the factorisation with the row and the upper parts of the rows it needs staged in
+// local arrays (rows of up to kRowMax entries, up to kLowMax of them left of the diagonal, needed
+// rows with up to kUMax entries right of theirs; false, with nothing waited for or written,
+// otherwise).  Everything that does not depend on other rows' factors (the pattern, A's values)
+// is loaded before the wait, the needed rows' factors in one batch after it.  The needed rows
+// k < i are taken in ascending order: L_ik is final when k is reached (its sum has every term from
+// rows before k), and the products L_ik U_kj are added to the sums of the entries j > k that row
+// k's upper part shares with row i.  Every sum thus gets its terms in ascending k, as in
+// row_times_row, rounded one at a time.
+constexpr int kRowMax = 32, kLowMax = 8, kUMax = 16;
+
+__device__ __forceinline__ int ilu0_row_staged(int i, int r0, int r1, const int* __restrict__ ptr,
+                                               const int* __restrict__ col, const double* __restrict__ a,
+                                               const int* __restrict__ ustart, double* f, const int* flag,
+                                               int epoch, int* err) {
+    const int len = r1 - r0;
+    if (len > kRowMax) return 0;
+    int cj[kRowMax];
+    int nlow = 0;
+    for (int p = 0; p < len; p++) {
+        cj[p] = __ldg(col + r0 + p);
+        if (cj[p] < i) nlow = p + 1;
+    }
+    if (nlow > kLowMax) return 0;
+    int u0[kLowMax], nu[kLowMax];
+    for (int q = 0; q < nlow; q++) {
+        u0[q] = __ldg(ustart + cj[q]);
+        nu[q] = __ldg(ptr + cj[q] + 1) - u0[q];
+        if (nu[q] > kUMax) return 0;
+    }
+    double av[kRowMax], sum[kRowMax];
+    for (int p = 0; p < len; p++) {
+        av[p] = __ldg(a + r0 + p);
+        sum[p] = 0.0;
+    }
+    int uc[kLowMax][kUMax];
+    for (int q = 0; q < nlow; q++)
+        for (int t = 0; t < nu[q]; t++) uc[q][t] = __ldg(col + u0[q] + t);
+    if (!wait_rows(col, r0, r0 + nlow, flag, epoch, err)) return -1;
+    __threadfence();
+    double uv[kLowMax][kUMax];
+    for (int q = 0; q < nlow; q++)
+        for (int t = 0; t < nu[q]; t++) uv[q][t] = __ldcg(f + u0[q] + t);
+    for (int q = 0; q < nlow; q++) {
+        const double L = __dsub_rn(av[q], sum[q]);
+        f[r0 + q] = L;
+        int pp = q + 1;
+        for (int t = 0; t < nu[q] && pp < len; t++) {
+            const int j = uc[q][t];
+            while (pp < len && cj[pp] < j) pp++;
+            if (pp < len && cj[pp] == j) sum[pp] = __dadd_rn(sum[pp], __dmul_rn(L, uv[q][t]));
+        }
+    }
+    double d = 0.0;  // L_ii (0 where the pattern has no diagonal)
+    for (int p = nlow; p < len; p++) {
+        const double v = __dsub_rn(av[p], sum[p]);
+        if (cj[p] == i) {
+            f[r0 + p] = v;
+            d = v;
+        } else {
+            if (d == 0.0) {
+                atomicExch(err, 2);
+                break;
+            }
+            f[r0 + p] = __ddiv_rn(v, d);
+        }
+    }
+    return 1;
+}
+
 // ILU(0) of A (CSR, sorted columns) into f on A's pattern, rows in forward level order; ustart_k is
 // the first entry of row k right of the diagonal; *err = 2 on a zero pivot (the reference's failure),
 // 1 if a wait ran out
@@ -185,34 +293,34 @@ __device__ __forceinline__ void ilu0_row(int i, const int* __restrict__ ptr, con
                                          const double* __restrict__ a, const int* __restrict__ diagpos,
                                          const int* __restrict__ ustart, double* f, int* flag, int epoch, int* err) {
     const int r0 = ptr[i], r1 = ptr[i + 1];
-    bool ok = true;
-    for (int q = r0; q < r1 && ok; q++) {
-        const int k = col[q];
-        if (k < i) ok = wait_for([&] { return *(volatile const int*)(flag + k) == epoch; }, err);
-    }
-    if (ok) {
-        __threadfence();
-        const int di = diagpos[i];
-        for (int p = r0; p < r1; p++) {
-            const int j = col[p];
-            const int jmax = (j <= i) ? j - 1 : i - 1;
-            double s = 0.0;
-            for (int q = r0; q < r1 && col[q] <= jmax; q++) {
-                const int k = col[q];
-                int pos;
-                if (find_upper(col, __ldg(ustart + k), ptr[k + 1], j, &pos))
-                    s = __dadd_rn(s, __dmul_rn(__ldcg(f + q), __ldcg(f + pos)));
-            }
-            const double v = __dsub_rn(a[p], s);
-            if (j <= i) {
-                f[p] = v;
-            } else {
-                const double d = di >= 0 ? __ldcg(f + di) : 0.0;
-                if (d == 0.0) {
-                    atomicExch(err, 2);
-                    break;
+    const int staged = ilu0_row_staged(i, r0, r1, ptr, col, a, ustart, f, flag, epoch, err);
+    if (staged == 0) {
+        int nlow = 0;
+        while (r0 + nlow < r1 && col[r0 + nlow] < i) nlow++;
+        if (wait_rows(col, r0, r0 + nlow, flag, epoch, err)) {
+            __threadfence();
+            const int di = diagpos[i];
+            for (int p = r0; p < r1; p++) {
+                const int j = col[p];
+                const int jmax = (j <= i) ? j - 1 : i - 1;
+                double s = 0.0;
+                for (int q = r0; q < r1 && col[q] <= jmax; q++) {
+                    const int k = col[q];
+                    int pos;
+                    if (find_upper(col, __ldg(ustart + k), ptr[k + 1], j, &pos))
+                        s = __dadd_rn(s, __dmul_rn(__ldcg(f + q), __ldcg(f + pos)));
                 }
-                f[p] = __ddiv_rn(v, d);
+                const double v = __dsub_rn(a[p], s);
+                if (j <= i) {
+                    f[p] = v;
+                } else {
+                    const double d = di >= 0 ? __ldcg(f + di) : 0.0;
+                    if (d == 0.0) {
+                        atomicExch(err, 2);
+                        break;
+                    }
+                    f[p] = __ddiv_rn(v, d);
+                }
             }
         }
     }
@@ -328,6 +436,9 @@ struct lina_gpu_ilu {
     unsigned* ticket = nullptr;  // the pool's row counter, reset before every pass
     int* flag = nullptr;         // rows finished by the factorisation
     double* fval = nullptr;      // factor values on A's pattern (factorised on the device), else null
+    int epoch = 0;               // factorisation passes (row flags hold the current one)
+    int *aptr = nullptr, *acol = nullptr, *adiag = nullptr;  // A's pattern (device factorisation)
+    double* aval = nullptr;                                  // A's values
     long fnnz = 0;
 };
 
@@ -411,6 +522,28 @@ int read_err(lina_gpu_ilu* h) {
         cudaStreamSynchronize(st()) != cudaSuccess)
         return -1;
     return e;
+}
+
+// ILU(0) of the handle's A (pattern and values on the device) into fval, the inverse diagonal and
+// the FP32 copy of the factors; each factorisation is a new pass of the row flags
+int factorise(lina_gpu_ilu* h) {
+    const int n = h->n;
+    const long nnz = h->fnnz;
+    h->epoch++;
+    cudaMemsetAsync(h->ticket, 0, sizeof(unsigned), st());
+    ilu0_kernel<<<pool_blocks(n), kPool, 0, st()>>>(n, h->L.order, h->aptr, h->acol, h->aval, h->adiag, h->U.beg,
+                                                    h->fval, h->flag, h->epoch, h->ticket, h->err);
+    diag_inverse_kernel<<<std::min(4096, (n + kT - 1) / kT), kT, 0, st()>>>(n, h->adiag, h->fval, h->L.dinv64,
+                                                                             h->L.dinv32);
+    cvt_kernel<double, float><<<std::min<long>(4096, (nnz + kT - 1) / kT), kT, 0, st()>>>(nnz, h->fval, h->L.val32);
+    const int e = (cudaGetLastError() == cudaSuccess) ? read_err(h) : -1;
+    if (e != 0) {
+        lina::dev::set_error(e == 2 ? "ILU: zero pivot (incomplete_LU_factorization fails)"
+                                    : "ILU: device factorisation failed or a wait ran out");
+        if (e > 0) cudaMemset(h->err, 0, sizeof(int));
+        return e == 2 ? LINA_GPU_ESETUP : LINA_GPU_ECUDA;
+    }
+    return 0;
 }
 
 template <typename TV, typename TX>
@@ -506,26 +639,38 @@ int lina_gpu_ilu_create_from_matrix(int n, const int* rowptr, const int* col, co
     h->L.val64 = h->U.val64 = h->fval;
     h->U.val32 = h->L.val32;
     h->flag = m.get<int>(n);
-    if (!h->flag || cudaMemsetAsync(h->flag, 0, (size_t)n * sizeof(int), st()) != cudaSuccess ||
-        cudaMemsetAsync(h->ticket, 0, sizeof(unsigned), st()) != cudaSuccess) {
+    h->aptr = dptr;
+    h->acol = dcol;
+    h->adiag = ddiag;
+    h->aval = dval;
+    if (!h->flag || cudaMemsetAsync(h->flag, 0, (size_t)n * sizeof(int), st()) != cudaSuccess) {
         lina::dev::set_error("ILU: device allocation failed");
         delete h;
         return LINA_GPU_ECUDA;
     }
-    ilu0_kernel<<<pool_blocks(n), kPool, 0, st()>>>(n, h->L.order, dptr, dcol, dval, ddiag, h->U.beg, h->fval,
-                                                    h->flag, 1, h->ticket, h->err);
-    diag_inverse_kernel<<<std::min(4096, (n + kT - 1) / kT), kT, 0, st()>>>(n, ddiag, h->fval, h->L.dinv64,
-                                                                             h->L.dinv32);
-    cvt_kernel<double, float><<<std::min<long>(4096, (nnz + kT - 1) / kT), kT, 0, st()>>>(nnz, h->fval, h->L.val32);
-    const int e = (cudaGetLastError() == cudaSuccess) ? read_err(h) : -1;
-    if (e != 0) {
-        lina::dev::set_error(e == 2 ? "ILU: zero pivot (incomplete_LU_factorization fails)"
-                                    : "ILU: device factorisation failed or a wait ran out");
+    const int rc = factorise(h);
+    if (rc) {
         delete h;
-        return e == 2 ? LINA_GPU_ESETUP : LINA_GPU_ECUDA;
+        return rc;
     }
     *out = h;
     return 0;
+}
+
+// new values of A on the pattern the handle was created with (val[nnz], host or, with
+// LINA_PCG_DEVICE_PTRS, device pointer): the factors are recomputed on the device, the level
+// schedules and the pattern are kept
+int lina_gpu_ilu_refactor(lina_gpu_ilu* h, const double* val, int flags) {
+    if (!h || !val || !h->fval) {
+        lina::dev::set_error("lina_gpu_ilu_refactor: not a handle factorised on the device");
+        return LINA_GPU_EINVAL;
+    }
+    const cudaMemcpyKind kind = (flags & LINA_PCG_DEVICE_PTRS) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    if (h->fnnz && cudaMemcpyAsync(h->aval, val, (size_t)h->fnnz * sizeof(double), kind, st()) != cudaSuccess) {
+        lina::dev::set_error("lina_gpu_ilu_refactor: copy of the values failed");
+        return LINA_GPU_ECUDA;
+    }
+    return factorise(h);
 }
 
 int lina_gpu_ilu_destroy(lina_gpu_ilu* h) {

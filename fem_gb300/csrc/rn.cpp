@@ -309,7 +309,12 @@ struct Ctx {
     lina_gpu_matrix* H = nullptr;     // device copy of the Hessian (cached by the API layer)
     lina_gpu_matrix* Mdev = nullptr;  // the scaled Newton matrix of this iteration
     CsrCopy Mc;                       // its CSR form
+    CsrCopy Hc;                       // the Hessian's CSR form
     sparse_matrix* Mrow = nullptr;    // its row-list form (built only when a solver needs it)
+    // the pattern Mdev and ilu were built for: a later step with the same pattern only sends new values
+    std::vector<int> pat_ptr, pat_col;
+    lina_gpu_ilu* ilu = nullptr;      // ILU(0) of M for RN_GPU_BICGSTAB_ILU
+    bool ilu_stale = false;           // M has new values the factors do not reflect yet
     double f_old = 0;                 // functional at the start of the step
 
     double* vec() {
@@ -326,11 +331,33 @@ struct Ctx {
         hX.resize(n), hG.resize(n), hD.resize(n), hJ.resize(n), hA.resize(n), hB.resize(n);
         return true;
     }
+    void drop_row_list() {
+        if (Mrow) free_sparse(Mrow);
+        Mrow = nullptr;
+    }
     void drop_M() {
         if (Mdev) lina_gpu_matrix_destroy(Mdev);
         Mdev = nullptr;
-        if (Mrow) { free_sparse(Mrow); }
-        Mrow = nullptr;
+        if (ilu) lina_gpu_ilu_destroy(ilu);
+        ilu = nullptr;
+        ilu_stale = false;
+        pat_ptr.clear();
+        pat_col.clear();
+        drop_row_list();
+    }
+    // M (host CSR in Mc) on the device: new values when the pattern is the last one, else a new matrix
+    bool upload_M() {
+        drop_row_list();
+        if (Mdev && Mc.ptr == pat_ptr && Mc.col == pat_col) {
+            if (lina_gpu_matrix_update_values(Mdev, Mc.val.data(), 0) != 0) return false;
+            ilu_stale = ilu != nullptr;
+            return true;
+        }
+        drop_M();
+        if (lina_gpu_matrix_create(n, n, Mc.ptr.data(), Mc.col.data(), Mc.val.data(), &Mdev) != 0) return false;
+        pat_ptr = Mc.ptr;
+        pat_col = Mc.col;
+        return true;
     }
     ~Ctx() {
         drop_M();
@@ -399,18 +426,16 @@ bool gradient(Ctx& c) {
 void assemble_M(Ctx& c, const CsrCopy& H) {
     const int n = c.n;
     CsrCopy& M = c.Mc;
-    M = CsrCopy();
     M.n = n;
     M.ptr.assign(n + 1, 0);
-    std::vector<int> rc;
-    std::vector<double> rv;
-    for (int i = 0; i < n; i++) {
-        rc.clear();
-        rv.clear();
+    // row i of D H D kept entries (both factors and both products nonzero), then |g_i| J_i on the
+    // diagonal; calls emit(k, v) in column order and returns the row's entry count
+    auto row = [&](int i, auto emit) {
+        int cnt = 0;
         const double di = c.hD[i];
+        const double add = c.hJ[i] != 0.0 ? fabs(c.hG[i]) * c.hJ[i] : 0.0;
+        bool diag_done = c.hJ[i] == 0.0;
         if (di != 0.0) {
-            // (H diag(D))_ik = H_ik D_k for nonzero factors, zero results deleted;
-            // then M_ik = D_i (H_ik D_k), zero results deleted again
             for (int p = H.ptr[i]; p < H.ptr[i + 1]; p++) {
                 const int k = H.col[p];
                 const double a = H.val[p], b = c.hD[k];
@@ -419,22 +444,48 @@ void assemble_M(Ctx& c, const CsrCopy& H) {
                 if (hd == 0.0) continue;
                 const double v = di * hd;
                 if (v == 0.0) continue;
-                rc.push_back(k), rv.push_back(v);
+                if (!diag_done && k >= i) {  // insert_sparse(M, |g_i| J_i, i, i)
+                    if (k == i) {
+                        emit(k, v + add);
+                        cnt++;
+                        diag_done = true;
+                        continue;
+                    }
+                    emit(i, add);
+                    cnt++;
+                    diag_done = true;
+                }
+                emit(k, v);
+                cnt++;
             }
         }
-        if (rc.empty()) rc.push_back(i), rv.push_back(0.0);  // the reference's (i, 0.0) of an empty row
-        if (c.hJ[i] != 0.0) {  // insert_sparse(M, |g_i| J_i, i, i)
-            const double add = fabs(c.hG[i]) * c.hJ[i];
-            size_t pos = 0;
-            while (pos < rc.size() && rc[pos] < i) pos++;
-            if (pos < rc.size() && rc[pos] == i)
-                rv[pos] += add;
-            else
-                rc.insert(rc.begin() + pos, i), rv.insert(rv.begin() + pos, add);
+        if (cnt == 0 && diag_done) {  // the reference's (i, 0.0) of an empty row
+            emit(i, 0.0);
+            return 1;
         }
-        M.col.insert(M.col.end(), rc.begin(), rc.end());
-        M.val.insert(M.val.end(), rv.begin(), rv.end());
-        M.ptr[i + 1] = (int)M.col.size();
+        if (!diag_done) {
+            if (cnt == 0) {  // (i, 0.0) of the empty row, then the diagonal added to it
+                emit(i, 0.0 + add);
+                return 1;
+            }
+            emit(i, add);
+            cnt++;
+        }
+        return cnt;
+    };
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; i++) M.ptr[i + 1] = row(i, [](int, double) {});
+    for (int i = 0; i < n; i++) M.ptr[i + 1] += M.ptr[i];
+    M.col.resize(M.ptr[n]);
+    M.val.resize(M.ptr[n]);
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; i++) {
+        int q = M.ptr[i];
+        row(i, [&](int k, double v) {
+            M.col[q] = k;
+            M.val[q] = v;
+            q++;
+        });
     }
 }
 
@@ -543,19 +594,26 @@ bool get_subspace(Ctx& c) {
     int iter = 0;
     switch (rn_solver_type) {
         case RN_GPU_BICGSTAB_ILU: {
-            lina_gpu_ilu* ilu = nullptr;
+            // the factors of the last step's pattern are recomputed in place; a new pattern starts afresh
             PhaseClock pc;
-            if (lina_gpu_ilu_create_from_matrix(n, c.Mc.ptr.data(), c.Mc.col.data(), c.Mc.val.data(), &ilu) != 0) {
+            int frc = 0;
+            if (!c.ilu)
+                frc = lina_gpu_ilu_create_from_matrix(n, c.Mc.ptr.data(), c.Mc.col.data(), c.Mc.val.data(), &c.ilu);
+            else if (c.ilu_stale)
+                frc = lina_gpu_ilu_refactor(c.ilu, c.Mc.val.data(), 0);
+            c.ilu_stale = false;
+            if (frc != 0) {
+                if (c.ilu) lina_gpu_ilu_destroy(c.ilu);
+                c.ilu = nullptr;
                 rn_status = INDEFINITE;
                 break;
             }
             lina_gpu_solve_info info;
             g_t_ilu = pc.lap();
-            lina_gpu_bicgstab(c.Mdev, ilu, LINA_PREC_MIXED, c.rhs, c.V2, lina::api::bi_eps_value(),
+            lina_gpu_bicgstab(c.Mdev, c.ilu, LINA_PREC_MIXED, c.rhs, c.V2, lina::api::bi_eps_value(),
                               BI_get_max_iter(), LINA_PCG_DEVICE_PTRS | LINA_PCG_USE_X0, &info);
             g_t_krylov = pc.lap();
             g_krylov_iters = info.iterations;
-            lina_gpu_ilu_destroy(ilu);
             iter = info.iterations;
             rn_status = (info.status == 0 && iter < BI_get_max_iter()) ? POSITIVE_DEFINITE : INDEFINITE;
             break;
@@ -770,11 +828,11 @@ int reflective_newton(double* Xh) {
         lina::dev::d2h(c.hD.data(), c.D, c.n);
         lina::dev::d2h(c.hJ.data(), c.J, c.n);
         lina::dev::d2h(c.hG.data(), c.G, c.n);
-        c.drop_M();
         PhaseClock pc;
-        assemble_M(c, lina::api::to_csr(rn_hesse));
+        if (own_hesse || iter == 0) c.Hc = lina::api::to_csr(rn_hesse);  // the Hessian changes only with a callback
+        assemble_M(c, c.Hc);
         const double t_asm = pc.lap();
-        if (lina_gpu_matrix_create(c.n, c.n, c.Mc.ptr.data(), c.Mc.col.data(), c.Mc.val.data(), &c.Mdev) != 0) return -1;
+        if (!c.upload_M()) return -1;
         const double t_up = pc.lap();
         if (!iterate(c)) return -1;
         const double t_it = pc.lap();

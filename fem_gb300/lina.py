@@ -126,6 +126,8 @@ def lib():
         "lina_gpu_ilu_destroy": (C.c_int, [vp]),
         "lina_gpu_ilu_levels": (C.c_int, [vp, ip, ip]),
         "lina_gpu_ilu_factor_values": (C.c_int, [vp, dp]),
+        "lina_gpu_ilu_refactor": (C.c_int, [vp, dp, C.c_int]),
+        "lina_gpu_matrix_update_values": (C.c_int, [vp, dp, C.c_int]),
         "lina_gpu_ilu_apply": (C.c_int, [vp, C.c_int, vp, vp]),
         "lina_gpu_dot": (C.c_int, [vp, vp, C.c_long, dp]),
         "lina_gpu_dot_noalloc": (C.c_int, [vp, vp, C.c_long, dp]),
@@ -298,6 +300,11 @@ class Matrix:
     def padded_entries(self):
         return lib().lina_gpu_matrix_padded_entries(self.h)
 
+    def update_values(self, data):
+        """New values on the pattern given at creation (CSR order)."""
+        dv_ = np.ascontiguousarray(data, dtype=np.float64)
+        _check(lib().lina_gpu_matrix_update_values(self.h, _dp(dv_), 0), "matrix update values")
+
     def spmv_device(self, x: DeviceArray, y: DeviceArray, precision=PREC_FP64):
         _check(lib().lina_gpu_matrix_spmv(self.h, precision, x.ptr, y.ptr), "matrix spmv")
 
@@ -344,6 +351,11 @@ class ILU:
         self.nnz = len(ix_)
         _check(lib().lina_gpu_ilu_create_from_matrix(self.n, _ip(ip_), _ip(ix_), _dp(dv_), C.byref(h)), "ILU")
         self.h = h
+
+    def refactor(self, data):
+        """New values of A on the same pattern; the factors are recomputed on the GPU."""
+        dv_ = np.ascontiguousarray(data, dtype=np.float64)
+        _check(lib().lina_gpu_ilu_refactor(self.h, _dp(dv_), 0), "ILU refactor")
 
     def factor_values(self):
         """The factors on A's pattern: L_ij where j <= i, U_ij where j > i."""

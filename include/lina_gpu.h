@@ -147,6 +147,10 @@ typedef struct lina_gpu_matrix lina_gpu_matrix;
 int lina_gpu_matrix_create(int n, int ncols, const int* rowptr, const int* col, const double* val,
                            lina_gpu_matrix** out);
 int lina_gpu_matrix_destroy(lina_gpu_matrix* m);
+/* new values on the pattern given at creation (val[nnz] in CSR order; host pointer, or device
+   pointer with LINA_PCG_DEVICE_PTRS): both value copies and the inverse diagonal are rewritten on
+   the device, the layout is kept */
+int lina_gpu_matrix_update_values(lina_gpu_matrix* m, const double* val, int flags);
 /* y = A x */
 int lina_gpu_matrix_spmv(lina_gpu_matrix* m, int precision, const void* x_dev, void* y_dev);
 /* `sweeps` damped Jacobi sweeps x <- x + w D^-1 (b - A x); tmp is a work vector; after an odd
@@ -171,6 +175,11 @@ int lina_gpu_ilu_create_from_matrix(int n, const int* rowptr, const int* col, co
 /* the factors of a handle from lina_gpu_ilu_create_from_matrix on A's pattern (val[nnz]): L_ij where
    j <= i, U_ij where j > i (U's unit diagonal is not stored) */
 int lina_gpu_ilu_factor_values(const lina_gpu_ilu* h, double* val);
+/* new values of A on the pattern of a handle from lina_gpu_ilu_create_from_matrix (val[nnz]; host
+   pointer, or device pointer with LINA_PCG_DEVICE_PTRS): the factors are recomputed on the device
+   (bit-identical to a new handle), the level schedules and the pattern are kept;
+   LINA_GPU_ESETUP on a zero pivot */
+int lina_gpu_ilu_refactor(lina_gpu_ilu* h, const double* val, int flags);
 int lina_gpu_ilu_destroy(lina_gpu_ilu* h);
 int lina_gpu_ilu_levels(const lina_gpu_ilu* h, int* nlev_L, int* nlev_U);
 /* z = U^-1 L^-1 r (device vectors, FP64); LINA_PREC_MIXED solves in FP32 */

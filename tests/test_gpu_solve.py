@@ -226,3 +226,30 @@ def test_fmg_matches_reference(name, smoother, code, omega):
     amg.set_smoother(code, omega, lina.PREC_MIXED)
     x32, _ = amg.fmg(s.b)
     assert np.linalg.norm(x32 - x_ref) <= 1e-5 * np.linalg.norm(x_ref)
+
+
+@pytest.mark.parametrize("name", golden_cases("hierarchy"))
+def test_matrix_update_values_equals_new_matrix(name):
+    """lina_gpu_matrix_update_values on a fixed pattern: SpMV and Jacobi sweeps equal those of a
+    matrix created from the new values, in both layouts."""
+    s = system_for(name)
+    rng = np.random.default_rng(3)
+    data2 = s.data * (1.0 + 0.2 * rng.random(len(s.data)))
+    x = rng.uniform(-1, 1, s.n)
+    for layout in (lina.LAYOUT_SELL, lina.LAYOUT_CSRV):
+        lina.set_layout(layout)
+        try:
+            M = lina.Matrix(s.n, s.indptr, s.indices, s.data)
+            M.update_values(data2)
+            F = lina.Matrix(s.n, s.indptr, s.indices, data2)
+        finally:
+            lina.set_layout(lina.LAYOUT_AUTO)
+        for prec in (lina.PREC_FP64, lina.PREC_MIXED):
+            assert np.array_equal(M.spmv(x, prec), F.spmv(x, prec))
+        b = lina.DeviceArray.from_host(rng.uniform(-1, 1, s.n))
+        outs = []
+        for mat in (M, F):
+            xd, td = lina.DeviceArray.from_host(np.zeros(s.n)), lina.DeviceArray(s.n)
+            mat.jacobi_device(b, xd, td, 0.6, 3)
+            outs.append(xd.to_host())
+        assert np.array_equal(outs[0], outs[1])

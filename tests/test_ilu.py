@@ -163,3 +163,43 @@ def test_gpu_apply_inverts_a_tridiagonal_matrix():
     assert np.linalg.norm(A @ z - r) / np.linalg.norm(r) <= 1e-13
     z32 = ilu.apply(r, lina.PREC_MIXED)
     assert np.linalg.norm(A @ z32 - r) / np.linalg.norm(r) <= 1e-5
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not gpu_available(), reason="no CUDA device")
+@pytest.mark.parametrize("name", ["nonsym400", "damage65"])
+def test_gpu_refactor_equals_new_factorisation(name):
+    """New values on the same pattern: the refactorised handle gives the factors and the
+    application of a handle created from the new values, bit for bit."""
+    g = load()
+    ptr, col, val = matrix(g, name)
+    n = len(ptr) - 1
+    rng = np.random.default_rng(12)
+    val2 = val * (1.0 + 0.1 * rng.standard_normal(len(val)))
+    ilu = lina.ILU(n, ptr, col, val)
+    ilu.refactor(val2)
+    fresh = lina.ILU(n, ptr, col, val2)
+    assert np.array_equal(ilu.factor_values(), fresh.factor_values())
+    assert np.array_equal(ilu.factor_values(), port.ilu0(ptr, col, val2))
+    r = rng.standard_normal(n)
+    for prec in (lina.PREC_FP64, lina.PREC_MIXED):
+        assert np.array_equal(ilu.apply(r, prec), fresh.apply(r, prec))
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not gpu_available(), reason="no CUDA device")
+def test_gpu_refactor_zero_pivot_keeps_handle_usable():
+    g = load()
+    ptr, col, val = matrix(g, "nonsym400")
+    ilu = lina.ILU(400, ptr, col, val)
+    # a row with no entries left of the diagonal and some right of it: a zero diagonal there is a
+    # zero pivot L_rr = a_rr = 0
+    rows = [r for r in range(400) if not (col[ptr[r]:ptr[r + 1]] < r).any() and (col[ptr[r]:ptr[r + 1]] > r).any()]
+    assert rows
+    r = rows[0]
+    bad = val.copy()
+    bad[ptr[r] + int(np.nonzero(col[ptr[r]:ptr[r + 1]] == r)[0][0])] = 0.0
+    with pytest.raises(lina.LinaError, match=f"\\({lina.ESETUP}\\)"):
+        ilu.refactor(bad)
+    ilu.refactor(val)
+    assert np.array_equal(ilu.factor_values(), g["nonsym400_f"])
