@@ -972,9 +972,50 @@ SellHost make_sell(const lina::Csr& A, int ncols, const std::vector<std::vector<
     };
     if (groups) {
         for (const auto& g : *groups) add_group(g.data(), (int)g.size());
-    } else {
-        add_group(nullptr, A.n);
+        return S;
     }
+    // natural order: the slices are independent, built in parallel (the same layout as add_group)
+    const int ns = (A.n + 31) / 32;
+    std::vector<int> slen(ns, 0);
+#pragma omp parallel for schedule(static)
+    for (int sl = 0; sl < ns; sl++) {
+        int len = 0;
+        for (int r = 32 * sl; r < std::min(A.n, 32 * sl + 32); r++) len = std::max(len, A.ptr[r + 1] - A.ptr[r]);
+        slen[sl] = len;
+    }
+    S.sptr.assign(ns + 1, 0);
+    for (int sl = 0; sl < ns; sl++) S.sptr[sl + 1] = S.sptr[sl] + 32 * slen[sl];
+    S.col.assign(S.sptr[ns], 0);
+    S.val.assign(S.sptr[ns], 0.0);
+    S.rowmap.assign(32 * (size_t)ns, -1);
+#pragma omp parallel for schedule(static)
+    for (int sl = 0; sl < ns; sl++) {
+        const size_t off = S.sptr[sl];
+        for (int l = 0; l < 32; l++) {
+            const int r = 32 * sl + l;
+            const bool valid = r < A.n;
+            const int rl = valid ? A.ptr[r + 1] - A.ptr[r] : 0;
+            int pad_col = 0;
+            for (int k = 0; k < rl; k++)
+                if (A.col[A.ptr[r] + k] < ncols) {
+                    pad_col = A.col[A.ptr[r] + k];
+                    break;
+                }
+            for (int k = 0; k < slen[sl]; k++) {
+                const size_t q = off + 32 * (size_t)k + l;
+                if (k < rl && A.col[A.ptr[r] + k] < ncols) {
+                    S.col[q] = A.col[A.ptr[r] + k];
+                    S.val[q] = A.val[A.ptr[r] + k];
+                    S.pos[A.ptr[r] + k] = (int)q;
+                } else {
+                    S.col[q] = pad_col;
+                    S.val[q] = 0.0;
+                }
+            }
+            S.rowmap[32 * (size_t)sl + l] = valid ? r : -1;
+        }
+    }
+    S.group_slice.push_back(ns);
     return S;
 }
 
@@ -1162,7 +1203,9 @@ struct lina_gpu_amg {
         d.padded = (long)S.col.size();
         d.npos = (int)S.rowmap.size();
         d.group_slice = S.group_slice;
-        std::vector<float> v32(S.val.begin(), S.val.end());
+        std::vector<float> v32(S.val.size());
+#pragma omp parallel for schedule(static)
+        for (long k = 0; k < (long)S.val.size(); k++) v32[k] = (float)S.val[k];
         int rc;
         if ((rc = upload(&d.sptr, S.sptr.data(), S.sptr.size()))) return rc;
         if ((rc = upload(&d.col, S.col.data(), S.col.size()))) return rc;
@@ -2411,15 +2454,18 @@ int lina_gpu_matrix_create(int n, int ncols, const int* rowptr, const int* col, 
     c.col.assign(col, col + rowptr[n]);
     c.val.assign(val, val + rowptr[n]);
     std::vector<double> dinv(n, 0.0);
-    for (int i = 0; i < n; i++)
-        for (int p = c.ptr[i]; p < c.ptr[i + 1]; p++)
-            if (c.col[p] == i && c.val[p] != 0.0) dinv[i] = 1.0 / c.val[p];
-    std::vector<float> dinv32(dinv.begin(), dinv.end());
+    std::vector<float> dinv32(n);
     m->nnz = rowptr[n];
     m->diag_host.assign(n, -1);
-    for (int i = 0; i < n; i++)
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; i++) {
         for (int p = c.ptr[i]; p < c.ptr[i + 1]; p++)
-            if (c.col[p] == i) m->diag_host[i] = p;
+            if (c.col[p] == i) {
+                m->diag_host[i] = p;
+                if (c.val[p] != 0.0) dinv[i] = 1.0 / c.val[p];
+            }
+        dinv32[i] = (float)dinv[i];
+    }
     int rc = h->upload_csr(m->A, c, nullptr, &m->pos_host);
     if (!rc) rc = h->upload(&m->dinv64, dinv.data(), dinv.size());
     if (!rc) rc = h->upload(&m->dinv32, dinv32.data(), dinv32.size());

@@ -374,11 +374,14 @@ struct Mem {
         return (T*)q;
     }
     template <typename T>
-    T* up(const std::vector<T>& h) {
-        T* d = get<T>(h.size());
-        if (d && !h.empty() && cudaMemcpy(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
-            return nullptr;
+    T* up(const T* h, size_t count) {
+        T* d = get<T>(count);
+        if (d && count && cudaMemcpy(d, h, count * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess) return nullptr;
         return d;
+    }
+    template <typename T>
+    T* up(const std::vector<T>& h) {
+        return up(h.data(), h.size());
     }
     ~Mem() {
         for (void* q : p) cudaFree(q);
@@ -584,14 +587,14 @@ int lina_gpu_ilu_create_from_matrix(int n, const int* rowptr, const int* col, co
     *out = nullptr;
     const long nnz = rowptr[n];
     std::vector<int> diag(n, -1), lbeg(n), lend(n), ubeg(n), uend(n);
-    for (int i = 0; i < n; i++) {
+    for (int i = 0; i < n; i++)
         if (rowptr[i + 1] < rowptr[i]) return LINA_GPU_EINVAL;
+    int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
+    for (int i = 0; i < n; i++) {
         int split = rowptr[i + 1];
         for (int p = rowptr[i]; p < rowptr[i + 1]; p++) {
-            if (col[p] < 0 || col[p] >= n || (p > rowptr[i] && col[p] <= col[p - 1])) {
-                lina::dev::set_error("ILU: columns must be sorted, distinct and inside the matrix");
-                return LINA_GPU_EINVAL;
-            }
+            if (col[p] < 0 || col[p] >= n || (p > rowptr[i] && col[p] <= col[p - 1])) bad = 1;
             if (col[p] == i) diag[i] = p;
             if (col[p] > i && split == rowptr[i + 1]) split = p;
         }
@@ -600,23 +603,25 @@ int lina_gpu_ilu_create_from_matrix(int n, const int* rowptr, const int* col, co
         ubeg[i] = split;
         uend[i] = rowptr[i + 1];
     }
+    if (bad) {
+        lina::dev::set_error("ILU: columns must be sorted, distinct and inside the matrix");
+        return LINA_GPU_EINVAL;
+    }
     lina_gpu_ilu* h = new lina_gpu_ilu();
     h->n = n;
     h->fnnz = nnz;
     std::vector<int> lorder, uorder;
     h->L.nlev = level_order(n, lbeg, lend, col, true, lorder);
     h->U.nlev = level_order(n, ubeg, uend, col, false, uorder);
-    std::vector<int> ptr(rowptr, rowptr + n + 1), cols(col, col + nnz);
-    std::vector<double> vals(val, val + nnz);
     Mem& m = h->mem;
     int *dptr = nullptr, *dcol = nullptr, *ddiag = nullptr;
     double* dval = nullptr;
     bool ok = lina::dev::ready() && alloc_work(h);
     if (ok) {
-        dptr = m.up(ptr);
-        dcol = m.up(cols);
+        dptr = m.up(rowptr, (size_t)n + 1);
+        dcol = m.up(col, (size_t)nnz);
         ddiag = m.up(diag);
-        dval = m.up(vals);
+        dval = m.up(val, (size_t)nnz);
         h->fval = m.get<double>(nnz);
         h->L.order = m.up(lorder);
         h->U.order = m.up(uorder);
