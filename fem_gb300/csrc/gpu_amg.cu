@@ -33,8 +33,10 @@ std::string g_err;
 unsigned long long g_launches = 0;  // kernels launched by this library (all handles)
 int g_layout = 0;  // 0 automatic, 1 SELL-32, 2 lane groups (size chosen per matrix), 3..6 groups of 4..32 lanes
 // levels of at most this many rows run a multicolour-SOR V-cycle step as one thread-block-cluster launch
-// (0: one launch per colour and step)
-int g_fused_rows = 32768;
+// (0: one launch per colour and step).  Measured on the batch workload: up to 24,576 rows the fused
+// steps win; at 49,152 the levels whose colours need several passes of the cluster's lane groups
+// made whole solves up to 30 % slower.
+int g_fused_rows = 24576;
 
 void set_err(const char* fmt, ...) {
     char buf[512];
@@ -622,8 +624,7 @@ namespace {
 namespace cg = cooperative_groups;
 
 constexpr int kFuseThreads = 512;
-constexpr int kFusedRowsMax = 24576;                     // a copy of x per block: 192 KB in FP64
-constexpr int kFusedSmemMax = kFusedRowsMax * 8;
+constexpr int kFusedSmemMax = 192 * 1024;  // a block's copy of x: 49,152 FP32 or 24,576 FP64 rows
 
 struct FusedStep {
     int n, nc, ncolours, nu;
@@ -1438,8 +1439,9 @@ struct lina_gpu_amg {
     // an interior level whose multicolour-SOR step runs as one cluster launch (a copy of its x fits a
     // block's shared memory)
     bool fusable(const DLevel& L, bool timed) const {
+        const long copy_bytes = (long)L.n * (opt.precision == LINA_PREC_MIXED ? 4 : 8);
         return g_fused_rows > 0 && opt.smoother == LINA_SMOOTHER_MC_SOR && !timed && L.n <= g_fused_rows &&
-               L.n <= kFusedRowsMax &&
+               copy_bytes <= kFusedSmemMax &&
                L.ncolours > 0 && L.Acol.lanes > 0 && L.Acol.d_group_row && L.Acol.d_head && L.A.lanes > 0 &&
                L.R.lanes > 0 && L.P.lanes > 0;
     }

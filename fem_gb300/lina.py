@@ -259,7 +259,7 @@ def set_layout(layout: int):
     _check(lib().lina_gpu_set_layout(int(layout)), "set layout")
 
 
-FUSED_ROWS_DEFAULT = 32768
+FUSED_ROWS_DEFAULT = 24576
 
 
 def set_fused_rows(max_rows: int):

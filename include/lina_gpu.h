@@ -319,7 +319,8 @@ int lina_gpu_set_device(int device);   /* select the GPU for hierarchies created
    100k rows or more, CSR with a lane group per row otherwise), 1 SELL-32 always, 2 CSR lane groups
    always (group size chosen from the mean row length), 3..6 CSR lane groups of 4, 8, 16 or 32 lanes */
 int lina_gpu_set_layout(int layout);
-/* interior levels of at most max_rows rows (default 32768) run each multicolour-SOR V-cycle step
+/* interior levels of at most max_rows rows (default 24576; a block's copy of x allows up to 49152
+   rows in FP32 and 24576 in FP64) run each multicolour-SOR V-cycle step
    (pre: x = 0, the sweeps, the residual and the restriction; post: the prolongation and the sweeps)
    as one launch of a thread-block cluster, with cluster barriers between the colours, instead of one
    launch per colour and step; the results are bit-identical.  0 turns this off.  Takes effect for
