@@ -192,28 +192,46 @@ class ImportanceQueue {
     uint64_t seq_ = 0;
 };
 
-// AMG_get_lambda (Multigrid.c:364-375)
-inline double lambda_of(const std::vector<int>& label, const Lists& T, int i, int size) {
-    int undec = 0, fine = 0;
-    for (int p = T.ptr[i]; p < T.ptr[i + 1]; p++) {
-        int J = T.idx[p];
-        if (label[J] == kUndecided) undec++;
-        if (label[J] == kFine) fine++;
-    }
-    return (double)i / size + undec + 2 * fine;
-}
-
 // AMG_coarsener (Multigrid.c:377-473).  `lev` is indexed by the graph's own
 // node numbers, exactly as the reference indexes its Levels argument (which,
 // in the aggressive second pass, is the fine-level array; the reference's
 // behaviour in that case is reproduced, not corrected).
+//
+// Two pieces of bookkeeping make it fast without changing a label or the
+// order of any queue operation:
+//  * The importance (AMG_get_lambda, Multigrid.c:364-375) counts, for node J,
+//    the undecided and fine nodes of T_J.  Those
+//    counts are kept up to date as labels change (a node X changing label
+//    touches the J with X in T_J, i.e. J in S_X), so the importance is formed
+//    from the same integers without walking T_J.
+//  * A node's row is scanned for undecided, not yet queued neighbours.  After
+//    one scan every neighbour is queued or decided.  A queued node leaves the
+//    queue only when it is decided: a changed key is removed and re-inserted at
+//    once.  So a later scan of the same row inserts nothing and is skipped.
 void coarsener(const Graph& A, std::vector<int>& label, std::vector<double>& imp, const Lists& S, const Lists& T,
                ImportanceQueue& q, const int* lev, int lev_size, int size, int seed, std::vector<int>& cursor) {
     auto level_of = [&](int i) { return (i < lev_size) ? lev[i] : -1; };
+    std::vector<int> undec(size, 0), fine(size, 0);
+    for (int j = 0; j < size; j++)
+        for (int p = T.ptr[j]; p < T.ptr[j + 1]; p++) {
+            const int l = label[T.idx[p]];
+            if (l == kUndecided) undec[j]++;
+            if (l == kFine) fine[j]++;
+        }
+    // AMG_get_lambda (Multigrid.c:364-375) from the counts
+    auto lambda = [&](int i) { return (double)i / size + undec[i] + 2 * fine[i]; };
+    auto decide = [&](int x, int to) {  // label[x]: undecided -> to
+        label[x] = to;
+        for (int p = S.ptr[x]; p < S.ptr[x + 1]; p++) {
+            undec[S.idx[p]]--;
+            if (to == kFine) fine[S.idx[p]]++;
+        }
+    };
+    std::vector<char> scanned(size, 0);
     int level = level_of(seed);
     int next = seed;
     do {
-        label[next] = kCoarse;
+        decide(next, kCoarse);
         const int b = A.ptr[next], e = A.ptr[next + 1];
         for (int p = b; p < e; p++) {
             int I = A.col[p];
@@ -222,14 +240,14 @@ void coarsener(const Graph& A, std::vector<int>& label, std::vector<double>& imp
         for (int p = T.ptr[next]; p < T.ptr[next + 1]; p++) {
             int I = T.idx[p];
             if (q.contains(I)) {
-                label[I] = kFine;
+                decide(I, kFine);
                 q.remove(I);
             }
         }
         for (int p = b; p < e; p++) {
             int I = A.col[p];
             if (A.nz[p] && q.contains(I)) {
-                double lam = lambda_of(label, T, I, size);
+                double lam = lambda(I);
                 if (lam != imp[I]) {
                     q.remove(I);
                     imp[I] = lam;
@@ -240,14 +258,17 @@ void coarsener(const Graph& A, std::vector<int>& label, std::vector<double>& imp
         for (int p = b; p < e; p++) {
             int I = A.col[p];
             if (I == next) continue;
-            for (int r = A.ptr[I]; r < A.ptr[I + 1]; r++) {
-                int J = A.col[r];
-                if (label[J] == kUndecided && A.nz[r] && !q.contains(J)) q.insert(J, imp[J]);
+            if (!scanned[I]) {
+                for (int r = A.ptr[I]; r < A.ptr[I + 1]; r++) {
+                    int J = A.col[r];
+                    if (label[J] == kUndecided && A.nz[r] && !q.contains(J)) q.insert(J, imp[J]);
+                }
+                scanned[I] = 1;
             }
             for (int r = S.ptr[I]; r < S.ptr[I + 1]; r++) {
                 int J = S.idx[r];
                 if (label[J] == kUndecided) {
-                    double lam = lambda_of(label, T, J, size);
+                    double lam = lambda(J);
                     if (lam != imp[J]) {
                         q.remove(J);
                         imp[J] = lam;

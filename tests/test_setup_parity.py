@@ -40,6 +40,10 @@ LIVE = [
     ("elast33_aggr", lambda: problems.elasticity_p1(33), 4, lina.AGGRESSIVE),
     ("elast33_young", lambda: problems.elasticity_p1(
         33, young=210.0 * np.exp(0.5 * np.random.default_rng(3).standard_normal((2, 32 * 32)))), 4, lina.STANDARD),
+    # larger cases: many ties in the coarsening queue, and an unstructured high-contrast system
+    ("elast129_std", lambda: problems.elasticity_p1(129), 6, lina.STANDARD),
+    ("elast129_aggr", lambda: problems.elasticity_p1(129), 6, lina.AGGRESSIVE),
+    ("batch_elast20k", lambda: problems.batch_system("elasticity", 20000, 7), 5, lina.STANDARD),
 ]
 
 
