@@ -10,6 +10,7 @@
 #include "amg_host.h"
 
 #include <algorithm>
+#include <climits>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -1019,6 +1020,158 @@ bool amg_recompute_host(HostHierarchy& h, const Csr& A) {
             h.error = "erroneous coarse matrix";
             return false;
         }
+    }
+    return coarse_factor(h.lv[0].A, h.coarse, h.error);
+}
+
+// ---------------------------------------------------------------- hierarchy files
+// A matrix file is the reference's write_sparse format (LinA/linear_algebra.c:832-845): int n,
+// int Len[n], then every row's column indices, then every row's values (native byte order).
+
+bool write_csr_file(const std::string& path, const Csr& A) {
+    FILE* f = fopen(path.c_str(), "wb");
+    if (!f) return false;
+    bool ok = fwrite(&A.n, sizeof(int), 1, f) == 1;
+    std::vector<int> len(A.n);
+    for (int i = 0; i < A.n; i++) len[i] = A.ptr[i + 1] - A.ptr[i];
+    ok = ok && (A.n == 0 || fwrite(len.data(), sizeof(int), A.n, f) == (size_t)A.n);
+    ok = ok && (A.col.empty() || fwrite(A.col.data(), sizeof(int), A.col.size(), f) == A.col.size());
+    ok = ok && (A.val.empty() || fwrite(A.val.data(), sizeof(double), A.val.size(), f) == A.val.size());
+    return fclose(f) == 0 && ok;
+}
+
+bool read_csr_file(const std::string& path, Csr& A, int ncols) {
+    FILE* f = fopen(path.c_str(), "rb");
+    if (!f) return false;
+    int n = 0;
+    bool ok = fread(&n, sizeof(int), 1, f) == 1 && n >= 0;
+    std::vector<int> len(ok ? n : 0);
+    ok = ok && (n == 0 || fread(len.data(), sizeof(int), n, f) == (size_t)n);
+    A = Csr();
+    A.n = n;
+    A.ncols = ncols;
+    A.ptr.assign(n + 1, 0);
+    for (int i = 0; ok && i < n; i++) {
+        ok = len[i] >= 0 && (long)A.ptr[i] + len[i] <= INT32_MAX;
+        if (ok) A.ptr[i + 1] = A.ptr[i] + len[i];
+    }
+    if (ok) {
+        A.col.resize(A.ptr[n]);
+        A.val.resize(A.ptr[n]);
+        ok = (A.col.empty() || fread(A.col.data(), sizeof(int), A.col.size(), f) == A.col.size()) &&
+             (A.val.empty() || fread(A.val.data(), sizeof(double), A.val.size(), f) == A.val.size());
+    }
+    // columns inside the operand, or the (i, 0.0) placeholder of an empty row
+    for (size_t k = 0; ok && k < A.col.size(); k++) ok = A.col[k] >= 0 && A.col[k] < std::max(ncols, n);
+    fclose(f);
+    return ok;
+}
+
+namespace {
+
+bool write_ints(const std::string& path, const std::vector<int>& v) {
+    FILE* f = fopen(path.c_str(), "wb");
+    if (!f) return false;
+    const int n = (int)v.size();
+    bool ok = fwrite(&n, sizeof(int), 1, f) == 1 && (n == 0 || fwrite(v.data(), sizeof(int), n, f) == (size_t)n);
+    return fclose(f) == 0 && ok;
+}
+
+bool read_ints(const std::string& path, std::vector<int>& v, int expect) {
+    FILE* f = fopen(path.c_str(), "rb");
+    if (!f) return false;
+    int n = 0;
+    bool ok = fread(&n, sizeof(int), 1, f) == 1 && n == expect;
+    v.assign(ok ? n : 0, 0);
+    ok = ok && (n == 0 || fread(v.data(), sizeof(int), n, f) == (size_t)n);
+    fclose(f);
+    return ok;
+}
+
+std::string level_file(const std::string& dir, int l, const char* what) {
+    char buf[64];
+    snprintf(buf, sizeof buf, "/L%d_%s", l, what);
+    return dir + buf;
+}
+
+}  // namespace
+
+bool amg_save_host(const HostHierarchy& h, const std::string& dir, std::string& err) {
+    const AmgParams& p = h.params;
+    FILE* f = fopen((dir + "/hierarchy.txt").c_str(), "w");
+    if (!f) {
+        err = "cannot write " + dir + "/hierarchy.txt";
+        return false;
+    }
+    // doubles in hexadecimal so that they read back exactly
+    fprintf(f, "lina-gb300-amg 1\ndepth %d\ndof %d\ncoarsening %d\nsmoothing %d %d\neps %a %a\nmatrix_tol %a\n"
+               "signs %d\n",
+            p.depth, p.dof, p.coarsening, p.smoothing_iterations, p.aggr_smoothing_iterations, p.eps_minus,
+            p.eps_plus, p.matrix_tol, h.signs.empty() ? 0 : 1);
+    for (int l = 0; l < p.depth; l++) fprintf(f, "level %d %d %d\n", l, h.lv[l].A.n, h.lv[l].coarse_size);
+    bool ok = fclose(f) == 0;
+    for (int l = 0; ok && l < p.depth; l++) {
+        const HostLevel& L = h.lv[l];
+        ok = write_csr_file(level_file(dir, l, "A"), L.A) && write_ints(level_file(dir, l, "dof_level"), L.dof_level);
+        if (ok && l > 0)
+            ok = write_csr_file(level_file(dir, l, "P"), L.P) && write_csr_file(level_file(dir, l, "R"), L.R) &&
+                 write_ints(level_file(dir, l, "labels"), L.labels);
+    }
+    if (ok && !h.signs.empty()) {
+        FILE* g = fopen((dir + "/signs").c_str(), "wb");
+        ok = g && fwrite(h.signs.data(), sizeof(double), h.signs.size(), g) == h.signs.size();
+        if (g) ok = (fclose(g) == 0) && ok;
+    }
+    if (!ok) err = "writing the hierarchy files in " + dir + " failed";
+    return ok;
+}
+
+bool amg_load_host(const std::string& dir, HostHierarchy& h) {
+    h = HostHierarchy();
+    FILE* f = fopen((dir + "/hierarchy.txt").c_str(), "r");
+    if (!f) {
+        h.error = "cannot read " + dir + "/hierarchy.txt";
+        return false;
+    }
+    AmgParams& p = h.params;
+    int version = 0, has_signs = 0;
+    bool ok = fscanf(f, " lina-gb300-amg %d depth %d dof %d coarsening %d smoothing %d %d eps %la %la matrix_tol %la "
+                        "signs %d",
+                     &version, &p.depth, &p.dof, &p.coarsening, &p.smoothing_iterations, &p.aggr_smoothing_iterations,
+                     &p.eps_minus, &p.eps_plus, &p.matrix_tol, &has_signs) == 10 &&
+              version == 1 && p.depth >= 1 && p.depth <= 64 && p.dof >= 1;
+    std::vector<int> sizes, coarse;
+    for (int l = 0; ok && l < p.depth; l++) {
+        int ll = -1, n = -1, c = -1;
+        ok = fscanf(f, " level %d %d %d", &ll, &n, &c) == 3 && ll == l && n >= 0 && c >= 0;
+        sizes.push_back(n);
+        coarse.push_back(c);
+    }
+    fclose(f);
+    if (ok) h.lv.assign(p.depth, HostLevel());
+    for (int l = 0; ok && l < p.depth; l++) {
+        HostLevel& L = h.lv[l];
+        const int n = sizes[l];
+        L.coarse_size = coarse[l];
+        ok = read_csr_file(level_file(dir, l, "A"), L.A, n) && L.A.n == n &&
+             read_ints(level_file(dir, l, "dof_level"), L.dof_level, n);
+        if (ok && l > 0) {
+            const int nc = sizes[l - 1];
+            ok = read_csr_file(level_file(dir, l, "P"), L.P, nc) && L.P.n == n &&
+                 read_csr_file(level_file(dir, l, "R"), L.R, n) && L.R.n == nc &&
+                 read_ints(level_file(dir, l, "labels"), L.labels, n);
+        }
+    }
+    if (ok && has_signs) {
+        const int n = sizes[p.depth - 1];
+        h.signs.assign(n, 0.0);
+        FILE* g = fopen((dir + "/signs").c_str(), "rb");
+        ok = g && fread(h.signs.data(), sizeof(double), n, g) == (size_t)n;
+        if (g) fclose(g);
+    }
+    if (!ok) {
+        h.error = "the hierarchy files in " + dir + " are missing or inconsistent";
+        return false;
     }
     return coarse_factor(h.lv[0].A, h.coarse, h.error);
 }

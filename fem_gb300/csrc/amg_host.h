@@ -80,6 +80,14 @@ Csr spgemm_ref(const Csr& A, const Csr& B);
 // fails or a row has more distinct columns than its per-warp table.
 bool spgemm_gpu(const Csr& A, const Csr& B, Csr& C, std::string& err);
 
+// Hierarchy files: every level's A, P, R in the reference's write_sparse format
+// (LinA/linear_algebra.c:832), labels and unknown numbers as int arrays, the
+// parameters in a text header.  Loading recomputes the coarsest factorisation.
+bool write_csr_file(const std::string& path, const Csr& A);
+bool read_csr_file(const std::string& path, Csr& A, int ncols);
+bool amg_save_host(const HostHierarchy& h, const std::string& dir, std::string& err);
+bool amg_load_host(const std::string& dir, HostHierarchy& h);
+
 // Greedy first-fit colouring of the symmetric nonzero graph (smoother ordering).
 int greedy_colouring(const Csr& A, std::vector<int>& colour);
 

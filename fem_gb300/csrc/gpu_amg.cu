@@ -13,6 +13,8 @@
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
+#include <sys/stat.h>
+
 #include <algorithm>
 #include <climits>
 #include <cmath>
@@ -1943,6 +1945,75 @@ int lina_gpu_amg_create(int n, const int* rowptr, const int* col, const double* 
 int lina_gpu_amg_create_host_only(int n, const int* rowptr, const int* col, const double* val,
                                   const lina_gpu_amg_options* opt, lina_gpu_amg** out) {
     return amg_create_impl(n, rowptr, col, val, opt, out, true);
+}
+
+int lina_gpu_amg_save(const lina_gpu_amg* h, const char* dir) {
+    if (!h || !dir) {
+        set_err("lina_gpu_amg_save: invalid argument");
+        return LINA_GPU_EINVAL;
+    }
+    mkdir(dir, 0755);  // may exist already; a failure shows when the files are written
+    std::string err;
+    if (!lina::amg_save_host(h->host, dir, err)) {
+        set_err("%s", err.c_str());
+        return LINA_GPU_EINVAL;
+    }
+    return 0;
+}
+
+int lina_gpu_amg_load(const char* dir, const lina_gpu_amg_options* opt, int host_only, lina_gpu_amg** out) {
+    if (!dir || !opt || !out ||
+        (opt->smoother != LINA_SMOOTHER_JACOBI && opt->smoother != LINA_SMOOTHER_MC_SOR) ||
+        (opt->precision != LINA_PREC_FP64 && opt->precision != LINA_PREC_MIXED) || opt->smoothing_iterations < 0 ||
+        opt->aggr_smoothing_iterations < 0) {
+        set_err("lina_gpu_amg_load: invalid argument");
+        return LINA_GPU_EINVAL;
+    }
+    *out = nullptr;
+    lina_gpu_amg* h = new lina_gpu_amg();
+    if (!lina::amg_load_host(dir, h->host)) {
+        set_err("AMG load: %s", h->host.error.c_str());
+        delete h;
+        return LINA_GPU_EINVAL;
+    }
+    // the hierarchy's own structure; the caller's options for the solve phase
+    const lina::AmgParams& p = h->host.params;
+    h->opt = *opt;
+    h->opt.depth = p.depth;
+    h->opt.dof = p.dof;
+    h->opt.coarsening = p.coarsening == lina::kAggressive ? LINA_AGGRESSIVE : LINA_STANDARD;
+    h->opt.eps_minus = p.eps_minus;
+    h->opt.eps_plus = p.eps_plus;
+    h->opt.matrix_tol = p.matrix_tol;
+    h->host.params.smoothing_iterations = opt->smoothing_iterations;
+    h->host.params.aggr_smoothing_iterations = opt->aggr_smoothing_iterations;
+    h->host.params.gpu_products = !host_only;
+    h->depth = p.depth;
+    if (host_only) {
+        h->host_only = true;
+        *out = h;
+        return 0;
+    }
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        set_err("cudaStreamCreate failed");
+        delete h;
+        return LINA_GPU_ECUDA;
+    }
+    int rc = upload_hierarchy(h);
+    if (!rc && h->has_signs) {
+        // the caller's matrix: the finest rows flipped back (the flip is an exact negation)
+        lina::Csr A = h->host.lv[h->depth - 1].A;
+        for (int i = 0; i < A.n; i++)
+            if (h->host.signs[i] < 0)
+                for (int q = A.ptr[i]; q < A.ptr[i + 1]; q++) A.val[q] = -A.val[q];
+        rc = h->upload_csr(h->Aorig, A);
+    }
+    if (rc) {
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return 0;
 }
 
 int lina_gpu_amg_recompute(lina_gpu_amg* h, int n, const int* rowptr, const int* col, const double* val) {

@@ -19,10 +19,12 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <string>
 #include <unordered_map>
 #include <vector>
 
 #include "BiCGStab.h"
+#include "amg_host.h"
 #include "Multigrid.h"
 #include "PCGS.h"
 #include "reflective_newton.h"
@@ -235,6 +237,42 @@ double get_matrix_element(sparse_matrix* A, int i, int j) {
 }
 
 double get_diag(sparse_matrix* A, int i) { return get_matrix_element(A, i, i); }
+
+int write_sparse(sparse_matrix* A, char* path, char* name) {
+    if (!A || !path || !name) return 0;
+    std::string file = std::string(path) + "/" + name;
+    FILE* f = fopen(file.c_str(), "wb");
+    if (!f) return 0;
+    const int n = A->size;
+    bool ok = fwrite(&n, sizeof(int), 1, f) == 1 && (n == 0 || fwrite(A->Len, sizeof(int), n, f) == (size_t)n);
+    for (int i = 0; ok && i < n; i++)
+        ok = A->Len[i] == 0 || fwrite(A->Indices[i], sizeof(int), A->Len[i], f) == (size_t)A->Len[i];
+    for (int i = 0; ok && i < n; i++)
+        ok = A->Len[i] == 0 || fwrite(A->Values[i], sizeof(double), A->Len[i], f) == (size_t)A->Len[i];
+    return (fclose(f) == 0 && ok) ? 1 : 0;
+}
+
+sparse_matrix* read_sparse(char* path, char* name) {
+    if (!path || !name) return nullptr;
+    std::string file = std::string(path) + "/" + name;
+    lina::Csr c;
+    // the file does not say how many columns the matrix has: only negative indices are rejected
+    if (!lina::read_csr_file(file, c, INT32_MAX)) return nullptr;
+    sparse_matrix* A = (sparse_matrix*)malloc(sizeof(sparse_matrix));
+    A->size = c.n;
+    A->Len = (int*)malloc(std::max(c.n, 1) * sizeof(int));
+    A->Indices = (int**)malloc(std::max(c.n, 1) * sizeof(int*));
+    A->Values = (double**)malloc(std::max(c.n, 1) * sizeof(double*));
+    for (int i = 0; i < c.n; i++) {
+        const int len = c.ptr[i + 1] - c.ptr[i];
+        A->Len[i] = len;
+        A->Indices[i] = (int*)malloc(std::max(len, 1) * sizeof(int));
+        A->Values[i] = (double*)malloc(std::max(len, 1) * sizeof(double));
+        std::copy(c.col.begin() + c.ptr[i], c.col.begin() + c.ptr[i + 1], A->Indices[i]);
+        std::copy(c.val.begin() + c.ptr[i], c.val.begin() + c.ptr[i + 1], A->Values[i]);
+    }
+    return A;
+}
 
 sparse_matrix* get_transpose(sparse_matrix* A, int new_size) {
     sparse_matrix* R = sparse_zero(new_size);

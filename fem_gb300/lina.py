@@ -87,6 +87,8 @@ def lib():
         "lina_gpu_amg_create_host_only": (C.c_int, [C.c_int, ip, ip, dp, C.POINTER(AmgOptions), C.POINTER(vp)]),
         "lina_gpu_amg_recompute": (C.c_int, [vp, C.c_int, ip, ip, dp]),
         "lina_gpu_amg_destroy": (C.c_int, [vp]),
+        "lina_gpu_amg_save": (C.c_int, [vp, C.c_char_p]),
+        "lina_gpu_amg_load": (C.c_int, [C.c_char_p, C.POINTER(AmgOptions), C.c_int, C.POINTER(vp)]),
         "lina_gpu_amg_set_smoother": (C.c_int, [vp, C.c_int, C.c_double, C.c_int]),
         "lina_gpu_pcg": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, C.POINTER(SolveInfo)]),
         "lina_gpu_batch_create": (C.c_int, [C.c_int, C.POINTER(vp), C.c_int, C.POINTER(vp)]),
@@ -507,6 +509,24 @@ class AMG:
         _check(fn(self.n, _ip(self._ip), _ip(self._ix), _dp(self._dv), C.byref(self.opts), C.byref(h)), "AMG setup")
         self.h = h
         self.depth = lib().lina_gpu_amg_depth(self.h)
+
+    def save(self, directory):
+        """Write the hierarchy to a directory (lina_gpu_amg_save)."""
+        _check(lib().lina_gpu_amg_save(self.h, os.fsencode(directory)), "AMG save")
+
+    @classmethod
+    def load(cls, directory, host_only=False, **opts):
+        """A hierarchy saved by save(): its structure from the files, the solve options from opts."""
+        self = cls.__new__(cls)
+        self.opts = options(**opts)
+        h = C.c_void_p()
+        self.h = None
+        _check(lib().lina_gpu_amg_load(os.fsencode(directory), C.byref(self.opts), int(host_only), C.byref(h)),
+               "AMG load")
+        self.h = h
+        self.depth = lib().lina_gpu_amg_depth(self.h)
+        self.n = self.level_size(self.depth - 1)
+        return self
 
     @classmethod
     def from_system(cls, s, host_only=False, **opts):

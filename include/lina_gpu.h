@@ -104,6 +104,16 @@ int lina_gpu_amg_recompute(lina_gpu_amg* h, int n, const int* rowptr, const int*
    matrices whose rows were sign-flipped at setup. */
 int lina_gpu_amg_update_values(lina_gpu_amg* h, const double* val, int flags);
 int lina_gpu_amg_destroy(lina_gpu_amg* h);
+/* Save a hierarchy to the directory dir (created if missing): every level's A, P and R in the
+   reference's write_sparse format (LinA/linear_algebra.c:832), labels and unknown numbers as int
+   arrays, the setup parameters in hierarchy.txt.  No reference counterpart: it lets a later run skip
+   AMG_setup. */
+int lina_gpu_amg_save(const lina_gpu_amg* h, const char* dir);
+/* A hierarchy saved by lina_gpu_amg_save, uploaded (or host-only when host_only is nonzero).  The
+   structure (depth, dof, coarsening, thresholds) comes from the files, the solve options (smoother,
+   omega, precision, sweeps) from opt; the coarsest factorisation is recomputed.  The result solves
+   exactly as the saved hierarchy did. */
+int lina_gpu_amg_load(const char* dir, const lina_gpu_amg_options* opt, int host_only, lina_gpu_amg** out);
 /* change smoother, relaxation or precision of an existing hierarchy */
 int lina_gpu_amg_set_smoother(lina_gpu_amg* h, int smoother, double omega, int precision);
 

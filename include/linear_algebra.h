@@ -68,6 +68,11 @@ int get_position(int* list, int size, int val, int* Flag);
 double get_matrix_element(sparse_matrix* A, int i, int j);
 double get_diag(sparse_matrix* A, int i);
 sparse_matrix* get_transpose(sparse_matrix* A, int new_size);
+/* binary matrix files (write_sparse / read_sparse, LinA/linear_algebra.c:832-869): the file
+   path/name holds int n, int Len[n], every row's indices, every row's values; 1 / a new matrix on
+   success, 0 / NULL otherwise */
+int write_sparse(sparse_matrix* A, char* path, char* name);
+sparse_matrix* read_sparse(char* path, char* name);
 void sparse_add(sparse_matrix* A, sparse_matrix* B, double factor);
 sparse_matrix* sparse_product(sparse_matrix* A, sparse_matrix* B);
 double* sparse_row_sum(sparse_matrix* A);
