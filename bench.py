@@ -389,7 +389,8 @@ def run_batch(args, rank, world, local):
     of the batch graph.  Beside it, the same systems solved one after another by the single-system
     FP64 path (and the single-system mixed path), on the same hierarchies."""
     from fem_gb300 import lina, problems
-    plan = problems.batch_plan(args.batch_count, seed=0)
+    # with several ranks each solves its dof-balanced share of the systems (no exchange)
+    plan = problems.batch_shard(problems.batch_plan(args.batch_count, seed=0), rank, world)
     t0 = time.perf_counter()
     systems = [problems.batch_system(*p) for p in plan]
     t_mesh = time.perf_counter() - t0
@@ -436,9 +437,15 @@ def run_batch(args, rank, world, local):
     t0 = time.perf_counter()
     loop64 = [a.pcg(b, tol=args.tol, max_iter=1000)[1] for a, b in zip(amgs, bs)]
     t_loop64 = time.perf_counter() - t0
-    n_sys = len(systems)
-    value = world * n_sys * args.steps / (ms / 1e3)
-    e2e = world * n_sys * args.steps / (ms_e2e / 1e3)
+    # whole job: all ranks' systems; every rank loops over its own share at the same time
+    n_sys = args.batch_count
+    dofs = int(sum_over_ranks(dofs, world))
+    nnz = int(sum_over_ranks(nnz, world))
+    t_loop64 = max_over_ranks(t_loop64, world)
+    t_loop_mixed = max_over_ranks(t_loop_mixed, world)
+    worst = max_over_ranks(worst, world)
+    value = n_sys * args.steps / (ms / 1e3)
+    e2e = n_sys * args.steps / (ms_e2e / 1e3)
     out = common_line(f"batched AMG-PCG: systems/s over {n_sys} unstructured systems ({dofs} dofs) to rel. res. "
                       f"{args.tol:g}, one graph launch", value, "systems/s", world, args.steps, args.warmup, ms,
                       "f32 preconditioner / f64 Krylov", "synthetic (seeded Delaunay meshes, lognormal coefficients)",
@@ -519,6 +526,15 @@ def init_dist(world):
 def barrier(world):
     if world > 1:
         _pg.barrier()
+
+
+def sum_over_ranks(v, world):
+    if world <= 1:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    _pg.all_reduce(t, op=_pg.ReduceOp.SUM)
+    return float(t.item())
 
 
 def max_over_ranks(v, world):

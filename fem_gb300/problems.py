@@ -563,3 +563,16 @@ def batch_depth(n: int) -> int:
     """AMG depth for a batched system: coarsest level of roughly a thousand rows (standard
     coarsening shrinks a 2D P1 level by about 2.3x)."""
     return int(min(10, max(2, 1 + np.ceil(np.log(max(n, 1000) / 1000.0) / np.log(2.3)))))
+
+
+def batch_shard(plan, rank: int, world: int):
+    """The systems of ``plan`` that rank ``rank`` of ``world`` solves: a greedy dof-balanced split
+    (largest system first, to the least-loaded rank; ties to the lower rank), every system on exactly
+    one rank, in plan order within a rank.  Independent systems need no exchange between ranks."""
+    load = [0] * world
+    owner = [0] * len(plan)
+    for k in sorted(range(len(plan)), key=lambda k: (-plan[k][1], k)):
+        r = min(range(world), key=lambda q: (load[q], q))
+        owner[k] = r
+        load[r] += plan[k][1]
+    return [p for p, o in zip(plan, owner) if o == rank]
