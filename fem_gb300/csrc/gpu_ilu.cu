@@ -67,13 +67,13 @@ __device__ __forceinline__ int take_chunk(unsigned* ticket) {
 // bounded wait with back-off; `ready` polls the awaited value.  False (and *err = 1) when the wait
 // runs out or a pass failed elsewhere
 template <typename Ready>
-__device__ __forceinline__ bool wait_for(Ready ready, int* err) {
+__device__ __forceinline__ bool wait_for(Ready ready, int* err, unsigned long long limit_ns = kWaitNs) {
     if (ready()) return true;
     const unsigned long long t0 = device_ns();
     long polls = 0;
     unsigned ns = 32;
     while (!ready()) {
-        if (++polls > kWaitPolls || *(volatile int*)err || device_ns() - t0 > kWaitNs) {
+        if (++polls > kWaitPolls || *(volatile int*)err || device_ns() - t0 > limit_ns) {
             atomicCAS(err, 0, 1);
             return false;
         }
@@ -162,6 +162,15 @@ __global__ void __launch_bounds__(kPool) sptrsv_kernel(int n, const int* __restr
         }
         __syncwarp();
     }
+}
+
+// one thread waits, through wait_for, for a flag that nothing sets: the wait must run out after
+// limit_ns, record the failure in *err and return (the failure path of every bounded wait above)
+__global__ void wait_probe_kernel(const int* flag, unsigned long long limit_ns, int* err,
+                                  unsigned long long* waited_ns) {
+    const unsigned long long t0 = device_ns();
+    wait_for([&] { return *(volatile const int*)flag != 0; }, err, limit_ns);
+    *waited_ns = device_ns() - t0;
 }
 
 __device__ __forceinline__ void publish_row(int* flag, int i, int epoch) {
@@ -676,6 +685,35 @@ int lina_gpu_ilu_refactor(lina_gpu_ilu* h, const double* val, int flags) {
         return LINA_GPU_ECUDA;
     }
     return factorise(h);
+}
+
+// The failure path of the bounded device waits, made to happen: a kernel waits up to limit_us
+// microseconds (at most one second) for a flag nothing sets.  Returns LINA_GPU_ECUDA with the
+// error text set, as the solves do when a wait runs out, and the time the wait took in
+// *waited_us; the device stays usable.
+int lina_gpu_wait_probe(int limit_us, double* waited_us) {
+    if (limit_us <= 0 || limit_us > 1000000) return LINA_GPU_EINVAL;
+    Mem m;
+    int* flag = m.get<int>(1);
+    int* err = m.get<int>(1);
+    unsigned long long* waited = m.get<unsigned long long>(1);
+    if (!flag || !err || !waited || cudaMemsetAsync(flag, 0, sizeof(int), st()) != cudaSuccess ||
+        cudaMemsetAsync(err, 0, sizeof(int), st()) != cudaSuccess)
+        return LINA_GPU_ECUDA;
+    wait_probe_kernel<<<1, 1, 0, st()>>>(flag, 1000ull * (unsigned long long)limit_us, err, waited);
+    int e = 0;
+    unsigned long long ns = 0;
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpyAsync(&e, err, sizeof(int), cudaMemcpyDeviceToHost, st()) != cudaSuccess ||
+        cudaMemcpyAsync(&ns, waited, sizeof(ns), cudaMemcpyDeviceToHost, st()) != cudaSuccess ||
+        cudaStreamSynchronize(st()) != cudaSuccess)
+        return LINA_GPU_ECUDA;
+    if (waited_us) *waited_us = ns / 1000.0;
+    if (e != 0) {
+        lina::dev::set_error("a device wait ran out (no row ever published the awaited value)");
+        return LINA_GPU_ECUDA;
+    }
+    return 0;
 }
 
 int lina_gpu_ilu_destroy(lina_gpu_ilu* h) {

@@ -129,6 +129,7 @@ def lib():
         "lina_gpu_ilu_levels": (C.c_int, [vp, ip, ip]),
         "lina_gpu_ilu_factor_values": (C.c_int, [vp, dp]),
         "lina_gpu_ilu_refactor": (C.c_int, [vp, dp, C.c_int]),
+        "lina_gpu_wait_probe": (C.c_int, [C.c_int, dp]),
         "lina_gpu_matrix_update_values": (C.c_int, [vp, dp, C.c_int]),
         "lina_gpu_ilu_apply": (C.c_int, [vp, C.c_int, vp, vp]),
         "lina_gpu_dot": (C.c_int, [vp, vp, C.c_long, dp]),

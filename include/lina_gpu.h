@@ -191,6 +191,11 @@ int lina_gpu_ilu_factor_values(const lina_gpu_ilu* h, double* val);
    LINA_GPU_ESETUP on a zero pivot */
 int lina_gpu_ilu_refactor(lina_gpu_ilu* h, const double* val, int flags);
 int lina_gpu_ilu_destroy(lina_gpu_ilu* h);
+/* The failure path of the bounded waits in the ILU kernels, made to happen: one thread waits for a
+   device flag that nothing sets, up to limit_us microseconds (1 to 1,000,000).  Returns
+   LINA_GPU_ECUDA with the error text a timed-out solve gives, and the time waited in *waited_us;
+   the device stays usable.  For tests of the library's failure handling. */
+int lina_gpu_wait_probe(int limit_us, double* waited_us);
 int lina_gpu_ilu_levels(const lina_gpu_ilu* h, int* nlev_L, int* nlev_U);
 /* z = U^-1 L^-1 r (device vectors, FP64); LINA_PREC_MIXED solves in FP32 */
 int lina_gpu_ilu_apply(lina_gpu_ilu* h, int precision, const double* r_dev, double* z_dev);

@@ -5,6 +5,7 @@ zero-pivot matrices (tests/golden/ilu.npz, made by tests/golden/make_golden.py);
 restatements (oracle/ilu.py, oracle/lina_port.c) are pinned to it bit for bit and check the
 device factors at full size.  The bar for the factors is bit-identity.
 """
+import ctypes as C
 import os
 
 import numpy as np
@@ -203,3 +204,18 @@ def test_gpu_refactor_zero_pivot_keeps_handle_usable():
         ilu.refactor(bad)
     ilu.refactor(val)
     assert np.array_equal(ilu.factor_values(), g["nonsym400_f"])
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not gpu_available(), reason="no CUDA device")
+def test_gpu_wait_runs_out_and_device_stays_usable():
+    """A device wait on a flag nothing sets ends after its limit with the error a timed-out solve
+    reports; the next solve works."""
+    waited = C.c_double()
+    rc = lina.lib().lina_gpu_wait_probe(200000, C.byref(waited))
+    assert rc == lina.ECUDA and "ran out" in lina.last_error()
+    assert 200e3 <= waited.value < 5e6
+    g = load()
+    ptr, col, val = matrix(g, "nonsym400")
+    assert np.array_equal(lina.ILU(400, ptr, col, val).factor_values(), g["nonsym400_f"])
+    assert lina.lib().lina_gpu_wait_probe(0, None) == lina.EINVAL
