@@ -107,42 +107,82 @@ struct Plan {
     std::vector<double> fixval;
     std::vector<double> geo;  // 7 per element: beta[3], gamma[3], area
     Dmat D{};
+    int kind = LINA_P1_ELASTIC;  // LINA_P1_LAPLACE: one unknown per node
+    int ncomp = 2;
     std::string error;
 };
 
-bool check_problem(const lina_gpu_elastic_problem* p, std::string& err) {
-    if (!p || p->n_nodes <= 0 || p->n_elems <= 0 || !p->xy || !p->tri || p->n_fixed < 0 || p->n_sensors < 0 ||
-        (p->n_fixed > 0 && (!p->fixed_dof || !p->fixed_val)) || (p->n_sensors > 0 && (!p->sensor_dof || !p->target))) {
+// a P1 mesh with Dirichlet dofs (dof c * n_nodes + node for component c)
+struct Mesh {
+    int kind = LINA_P1_ELASTIC;
+    int nn = 0, ne = 0;
+    const double* xy = nullptr;
+    const int* tri = nullptr;
+    double nu = 0.0;
+    int n_fixed = 0;
+    const int* fixed_dof = nullptr;
+    const double* fixed_val = nullptr;
+};
+
+bool check_mesh(const Mesh& m, std::string& err) {
+    if ((m.kind != LINA_P1_LAPLACE && m.kind != LINA_P1_ELASTIC) || m.nn <= 0 || m.ne <= 0 || !m.xy || !m.tri ||
+        m.n_fixed < 0 || (m.n_fixed > 0 && (!m.fixed_dof || !m.fixed_val))) {
         err = "invalid problem description";
         return false;
     }
-    if (!(p->nu > -1.0 && p->nu < 0.5)) {
+    if (m.kind == LINA_P1_ELASTIC && !(m.nu > -1.0 && m.nu < 0.5)) {
         err = "Poisson's ratio outside (-1, 0.5)";
         return false;
     }
-    if ((long)p->n_nodes * 2 > (long)INT32_MAX / 8) {
+    const int nc = m.kind == LINA_P1_ELASTIC ? 2 : 1;
+    if ((long)m.nn * nc > (long)INT32_MAX / 8) {
         err = "too many nodes for 32-bit indices";
         return false;
     }
-    for (long k = 0; k < 3L * p->n_elems; k++)
-        if (p->tri[k] < 0 || p->tri[k] >= p->n_nodes) {
+    for (long k = 0; k < 3L * m.ne; k++)
+        if (m.tri[k] < 0 || m.tri[k] >= m.nn) {
             err = "triangle node index out of range";
             return false;
         }
-    const int n = 2 * p->n_nodes;
+    const int n = nc * m.nn;
     std::vector<unsigned char> seen(n, 0);
-    for (int k = 0; k < p->n_fixed; k++) {
-        const int d = p->fixed_dof[k];
+    for (int k = 0; k < m.n_fixed; k++) {
+        const int d = m.fixed_dof[k];
         if (d < 0 || d >= n || seen[d]) {
             err = "Dirichlet dofs out of range or repeated";
             return false;
         }
         seen[d] = 1;
     }
-    std::vector<unsigned char> sens(n, 0);
+    return true;
+}
+
+Mesh mesh_of(const lina_gpu_elastic_problem* p) {
+    Mesh m;
+    m.kind = LINA_P1_ELASTIC;
+    m.nn = p->n_nodes;
+    m.ne = p->n_elems;
+    m.xy = p->xy;
+    m.tri = p->tri;
+    m.nu = p->nu;
+    m.n_fixed = p->n_fixed;
+    m.fixed_dof = p->fixed_dof;
+    m.fixed_val = p->fixed_val;
+    return m;
+}
+
+bool check_problem(const lina_gpu_elastic_problem* p, std::string& err) {
+    if (!p || p->n_sensors < 0 || (p->n_sensors > 0 && (!p->sensor_dof || !p->target))) {
+        err = "invalid problem description";
+        return false;
+    }
+    if (!check_mesh(mesh_of(p), err)) return false;
+    const int n = 2 * p->n_nodes;
+    std::vector<unsigned char> fixed(n, 0), sens(n, 0);
+    for (int k = 0; k < p->n_fixed; k++) fixed[p->fixed_dof[k]] = 1;
     for (int k = 0; k < p->n_sensors; k++) {
         const int d = p->sensor_dof[k];
-        if (d < 0 || d >= n || seen[d] || sens[d]) {
+        if (d < 0 || d >= n || fixed[d] || sens[d]) {
             err = "sensor dofs out of range, repeated or on a Dirichlet dof";
             return false;
         }
@@ -151,11 +191,19 @@ bool check_problem(const lina_gpu_elastic_problem* p, std::string& err) {
     return true;
 }
 
-bool build_plan(const lina_gpu_elastic_problem* p, Plan& P) {
-    if (!check_problem(p, P.error)) return false;
-    const int nn = p->n_nodes, ne = p->n_elems, n = 2 * nn;
+// The CSR pattern of the assembled matrix and, for every stored entry, the (element,
+// unit-coefficient value) pairs adding into it in element order; the entry of an element matrix is
+// the P1 Laplacian's |T| (beta_a beta_b + gamma_a gamma_b), or the plane-strain stiffness of unit
+// modulus (khat).
+bool build_plan(const Mesh& mesh, Plan& P) {
+    if (!check_mesh(mesh, P.error)) return false;
+    const Mesh* p = &mesh;
+    const int nc = mesh.kind == LINA_P1_ELASTIC ? 2 : 1;
+    const int nn = mesh.nn, ne = mesh.ne, n = nc * nn;
+    P.kind = mesh.kind;
+    P.ncomp = nc;
     P.nn = nn, P.ne = ne, P.n = n;
-    P.D = plane_strain(p->nu);
+    if (mesh.kind == LINA_P1_ELASTIC) P.D = plane_strain(mesh.nu);
     P.fixed.assign(n, 0);
     P.fixval.assign(n, 0.0);
     for (int k = 0; k < p->n_fixed; k++) {
@@ -207,7 +255,7 @@ bool build_plan(const lina_gpu_elastic_problem* p, Plan& P) {
         if (P.fixed[i])
             cnt = 1;
         else
-            for (int q = 0; q < 2; q++)
+            for (int q = 0; q < nc; q++)
                 for (int t = aptr[k]; t < aptr[k + 1]; t++) cnt += P.fixed[q * nn + acol[t]] ? 0 : 1;
         P.ptr[i + 1] = P.ptr[i] + cnt;
     }
@@ -223,7 +271,7 @@ bool build_plan(const lina_gpu_elastic_problem* p, Plan& P) {
             P.col[w] = i;
             continue;
         }
-        for (int q = 0; q < 2; q++)
+        for (int q = 0; q < nc; q++)
             for (int t = aptr[k]; t < aptr[k + 1]; t++) {
                 const int j = q * nn + acol[t];
                 if (!P.fixed[j]) P.col[w++] = j;
@@ -243,11 +291,11 @@ bool build_plan(const lina_gpu_elastic_problem* p, Plan& P) {
     auto dof = [&](int e, int a, int c) { return c * nn + p->tri[3L * e + a]; };
     for (int e = 0; e < ne; e++)
         for (int a = 0; a < 3; a++)
-            for (int pc = 0; pc < 2; pc++) {
+            for (int pc = 0; pc < nc; pc++) {
                 const int i = dof(e, a, pc);
                 if (P.fixed[i]) continue;
                 for (int b = 0; b < 3; b++)
-                    for (int qc = 0; qc < 2; qc++) {
+                    for (int qc = 0; qc < nc; qc++) {
                         const int j = dof(e, b, qc);
                         if (P.fixed[j])
                             lcnt[i + 1]++;
@@ -279,13 +327,14 @@ bool build_plan(const lina_gpu_elastic_problem* p, Plan& P) {
         for (int k = 0; k < 3; k++) g.beta[k] = P.geo[7L * e + k], g.gamma[k] = P.geo[7L * e + 3 + k];
         g.area = P.geo[7L * e + 6];
         for (int a = 0; a < 3; a++)
-            for (int pc = 0; pc < 2; pc++) {
+            for (int pc = 0; pc < nc; pc++) {
                 const int i = dof(e, a, pc);
                 if (P.fixed[i]) continue;
                 for (int b = 0; b < 3; b++)
-                    for (int qc = 0; qc < 2; qc++) {
+                    for (int qc = 0; qc < nc; qc++) {
                         const int j = dof(e, b, qc);
-                        const double k = khat(g, P.D, a, pc, b, qc);
+                        const double k = nc == 2 ? khat(g, P.D, a, pc, b, qc)
+                                                 : g.area * (g.beta[a] * g.beta[b] + g.gamma[a] * g.gamma[b]);
                         if (P.fixed[j]) {
                             const int q = lf[i]++;
                             P.lelem[q] = e;
@@ -474,7 +523,7 @@ extern "C" {
 int lina_gpu_elastic_assemble_host(const lina_gpu_elastic_problem* p, const double* young, int* rowptr, int* col,
                                    double* val, double* b, long* nnz) {
     Plan P;
-    if (!build_plan(p, P)) {
+    if (!check_problem(p, P.error) || !build_plan(mesh_of(p), P)) {
         fail("lina_gpu_elastic_assemble_host: %s", P.error.c_str());
         return LINA_GPU_EINVAL;
     }
@@ -499,7 +548,7 @@ int lina_gpu_elastic_create(const lina_gpu_elastic_problem* p, const double* you
     *out = nullptr;
     lina_gpu_elastic* h = new lina_gpu_elastic();
     Plan& P = h->plan;
-    if (!build_plan(p, P)) {
+    if (!check_problem(p, P.error) || !build_plan(mesh_of(p), P)) {
         fail("lina_gpu_elastic_create: %s", P.error.c_str());
         delete h;
         return LINA_GPU_EINVAL;
@@ -642,6 +691,168 @@ lina_gpu_amg* lina_gpu_elastic_amg(lina_gpu_elastic* h) { return h ? h->amg : nu
 
 int lina_gpu_elastic_destroy(lina_gpu_elastic* h) {
     delete h;
+    return 0;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- general P1 assembly
+struct lina_gpu_p1 {
+    Plan plan;
+    cudaStream_t st = nullptr;
+    int *d_cptr = nullptr, *d_celem = nullptr, *d_lptr = nullptr, *d_lelem = nullptr;
+    double *d_ccoef = nullptr, *d_lcoef = nullptr, *d_fixval = nullptr, *d_coef = nullptr, *d_val = nullptr,
+           *d_b = nullptr;
+    unsigned char* d_fixed = nullptr;
+    std::vector<void*> mem;
+    bool assembled = false;
+
+    ~lina_gpu_p1() {
+        if (st) cudaStreamSynchronize(st);
+        for (void* p : mem) cudaFree(p);
+        if (st) cudaStreamDestroy(st);
+    }
+    template <typename T>
+    bool alloc(T** p, size_t count) {
+        if (count == 0) count = 1;
+        if (cudaMalloc((void**)p, count * sizeof(T)) != cudaSuccess) {
+            *p = nullptr;
+            return false;
+        }
+        mem.push_back((void*)*p);
+        return true;
+    }
+    template <typename T>
+    bool upload(T** p, const T* src, size_t count) {
+        if (!alloc(p, count)) return false;
+        return count == 0 || cudaMemcpyAsync(*p, src, count * sizeof(T), cudaMemcpyHostToDevice, st) == cudaSuccess;
+    }
+};
+
+namespace {
+
+Mesh mesh_of(const lina_gpu_p1_problem* p) {
+    Mesh m;
+    if (!p) {
+        m.kind = 0;
+        return m;
+    }
+    m.kind = p->kind;
+    m.nn = p->n_nodes;
+    m.ne = p->n_elems;
+    m.xy = p->xy;
+    m.tri = p->tri;
+    m.nu = p->nu;
+    m.n_fixed = p->n_fixed;
+    m.fixed_dof = p->fixed_dof;
+    m.fixed_val = p->fixed_val;
+    return m;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lina_gpu_p1_create(const lina_gpu_p1_problem* p, lina_gpu_p1** out) {
+    if (!out) return LINA_GPU_EINVAL;
+    *out = nullptr;
+    lina_gpu_p1* h = new lina_gpu_p1();
+    Plan& P = h->plan;
+    if (!build_plan(mesh_of(p), P)) {
+        fail("lina_gpu_p1_create: %s", P.error.c_str());
+        delete h;
+        return LINA_GPU_EINVAL;
+    }
+    const long nnz = P.ptr[P.n];
+    bool ok = cuda_ok(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking), "stream");
+    ok = ok && h->upload(&h->d_cptr, P.cptr.data(), P.cptr.size()) &&
+         h->upload(&h->d_celem, P.celem.data(), P.celem.size()) &&
+         h->upload(&h->d_ccoef, P.ccoef.data(), P.ccoef.size()) && h->upload(&h->d_lptr, P.lptr.data(), P.lptr.size()) &&
+         h->upload(&h->d_lelem, P.lelem.data(), P.lelem.size()) &&
+         h->upload(&h->d_lcoef, P.lcoef.data(), P.lcoef.size()) &&
+         h->upload(&h->d_fixed, P.fixed.data(), P.fixed.size()) &&
+         h->upload(&h->d_fixval, P.fixval.data(), P.fixval.size()) && h->alloc(&h->d_coef, (size_t)P.ne) &&
+         h->alloc(&h->d_val, (size_t)nnz) && h->alloc(&h->d_b, (size_t)P.n) &&
+         cuda_ok(cudaStreamSynchronize(h->st), "upload");
+    if (!ok) {
+        fail("lina_gpu_p1_create: device allocation or upload failed");
+        delete h;
+        return LINA_GPU_ECUDA;
+    }
+    *out = h;
+    return 0;
+}
+
+int lina_gpu_p1_assemble(lina_gpu_p1* h, const double* coef, int flags) {
+    if (!h || !coef) return LINA_GPU_EINVAL;
+    const Plan& P = h->plan;
+    const double* c = coef;
+    if (!(flags & LINA_PCG_DEVICE_PTRS)) {
+        if (!cuda_ok(cudaMemcpyAsync(h->d_coef, coef, P.ne * sizeof(double), cudaMemcpyHostToDevice, h->st), "copy"))
+            return LINA_GPU_ECUDA;
+        c = h->d_coef;
+    }
+    const long nnz = P.ptr[P.n];
+    assemble_values_kernel<<<grid(nnz), kT, 0, h->st>>>(nnz, h->d_cptr, h->d_celem, h->d_ccoef, c, h->d_val);
+    assemble_rhs_kernel<<<grid(P.n), kT, 0, h->st>>>(P.n, h->d_lptr, h->d_lelem, h->d_lcoef, h->d_fixed, h->d_fixval, c,
+                                                     h->d_b);
+    if (!cuda_ok(cudaGetLastError(), "assembly") || !cuda_ok(cudaStreamSynchronize(h->st), "assembly"))
+        return LINA_GPU_ECUDA;
+    h->assembled = true;
+    return 0;
+}
+
+int lina_gpu_p1_sizes(const lina_gpu_p1* h, int* n, long* nnz) {
+    if (!h) return LINA_GPU_EINVAL;
+    if (n) *n = h->plan.n;
+    if (nnz) *nnz = h->plan.ptr[h->plan.n];
+    return 0;
+}
+
+int lina_gpu_p1_download(lina_gpu_p1* h, int* rowptr, int* col, double* val, double* b) {
+    if (!h) return LINA_GPU_EINVAL;
+    const Plan& P = h->plan;
+    if (rowptr) std::copy(P.ptr.begin(), P.ptr.end(), rowptr);
+    if (col) std::copy(P.col.begin(), P.col.end(), col);
+    if ((val || b) && !h->assembled) {
+        fail("lina_gpu_p1_download: nothing assembled yet");
+        return LINA_GPU_EINVAL;
+    }
+    if (val && !cuda_ok(cudaMemcpyAsync(val, h->d_val, P.ptr[P.n] * sizeof(double), cudaMemcpyDeviceToHost, h->st), "copy"))
+        return LINA_GPU_ECUDA;
+    if (b && !cuda_ok(cudaMemcpyAsync(b, h->d_b, P.n * sizeof(double), cudaMemcpyDeviceToHost, h->st), "copy"))
+        return LINA_GPU_ECUDA;
+    return cuda_ok(cudaStreamSynchronize(h->st), "copy") ? 0 : LINA_GPU_ECUDA;
+}
+
+int lina_gpu_p1_device(lina_gpu_p1* h, const double** val_dev, const double** b_dev) {
+    if (!h || !h->assembled) return LINA_GPU_EINVAL;
+    if (val_dev) *val_dev = h->d_val;
+    if (b_dev) *b_dev = h->d_b;
+    return 0;
+}
+
+int lina_gpu_p1_destroy(lina_gpu_p1* h) {
+    delete h;
+    return 0;
+}
+
+int lina_gpu_p1_assemble_host(const lina_gpu_p1_problem* p, const double* coef, int* rowptr, int* col, double* val,
+                              double* b, long* nnz) {
+    Plan P;
+    if (!build_plan(mesh_of(p), P)) {
+        fail("lina_gpu_p1_assemble_host: %s", P.error.c_str());
+        return LINA_GPU_EINVAL;
+    }
+    if (nnz) *nnz = P.ptr[P.n];
+    if (!rowptr) return 0;
+    if (!coef || !col || !val || !b) {
+        fail("lina_gpu_p1_assemble_host: missing output");
+        return LINA_GPU_EINVAL;
+    }
+    std::copy(P.ptr.begin(), P.ptr.end(), rowptr);
+    std::copy(P.col.begin(), P.col.end(), col);
+    assemble_host(P, coef, val, b);
     return 0;
 }
 

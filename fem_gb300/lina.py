@@ -43,6 +43,14 @@ class AmgOptions(C.Structure):
     ]
 
 
+class P1Problem(C.Structure):
+    _fields_ = [("kind", C.c_int), ("n_nodes", C.c_int), ("n_elems", C.c_int), ("xy", C.c_void_p), ("tri", C.c_void_p),
+                ("nu", C.c_double), ("n_fixed", C.c_int), ("fixed_dof", C.c_void_p), ("fixed_val", C.c_void_p)]
+
+
+P1_LAPLACE, P1_ELASTIC = 1, 2
+
+
 class SolveInfo(C.Structure):
     _fields_ = [
         ("iterations", C.c_int),
@@ -87,6 +95,13 @@ def lib():
         "lina_gpu_amg_create_host_only": (C.c_int, [C.c_int, ip, ip, dp, C.POINTER(AmgOptions), C.POINTER(vp)]),
         "lina_gpu_amg_recompute": (C.c_int, [vp, C.c_int, ip, ip, dp]),
         "lina_gpu_amg_destroy": (C.c_int, [vp]),
+        "lina_gpu_p1_create": (C.c_int, [C.POINTER(P1Problem), C.POINTER(vp)]),
+        "lina_gpu_p1_assemble": (C.c_int, [vp, vp, C.c_int]),
+        "lina_gpu_p1_sizes": (C.c_int, [vp, ip, C.POINTER(C.c_long)]),
+        "lina_gpu_p1_download": (C.c_int, [vp, ip, ip, dp, dp]),
+        "lina_gpu_p1_device": (C.c_int, [vp, C.POINTER(vp), C.POINTER(vp)]),
+        "lina_gpu_p1_destroy": (C.c_int, [vp]),
+        "lina_gpu_p1_assemble_host": (C.c_int, [C.POINTER(P1Problem), dp, ip, ip, dp, dp, C.POINTER(C.c_long)]),
         "lina_gpu_amg_save": (C.c_int, [vp, C.c_char_p]),
         "lina_gpu_amg_load": (C.c_int, [C.c_char_p, C.POINTER(AmgOptions), C.c_int, C.POINTER(vp)]),
         "lina_gpu_amg_set_smoother": (C.c_int, [vp, C.c_int, C.c_double, C.c_int]),
@@ -438,6 +453,70 @@ def spgemm(a, b, ncols_b):
     return cp, cc[:nnz.value], cv[:nnz.value]
 
 
+def _p1_problem(kind, xy, tri, nu, fixed_dof, fixed_val):
+    keep = (np.ascontiguousarray(xy, dtype=np.float64).reshape(-1, 2), np.ascontiguousarray(tri, dtype=np.int32).reshape(-1, 3),
+            np.ascontiguousarray(fixed_dof, dtype=np.int32), np.ascontiguousarray(fixed_val, dtype=np.float64))
+    p = P1Problem(kind, len(keep[0]), len(keep[1]), keep[0].ctypes.data, keep[1].ctypes.data, float(nu), len(keep[2]),
+                  keep[2].ctypes.data if len(keep[2]) else None, keep[3].ctypes.data if len(keep[3]) else None)
+    return p, keep
+
+
+def p1_assemble_host(kind, xy, tri, coef, nu=0.3, fixed_dof=(), fixed_val=()):
+    """Host P1 assembly (lina_gpu_p1_assemble_host); returns (indptr, indices, data, b)."""
+    p, keep = _p1_problem(kind, xy, tri, nu, fixed_dof, fixed_val)
+    nnz = C.c_long()
+    _check(lib().lina_gpu_p1_assemble_host(C.byref(p), None, None, None, None, None, C.byref(nnz)), "P1 assembly")
+    n = p.n_nodes * (2 if kind == P1_ELASTIC else 1)
+    ptr, col = np.zeros(n + 1, np.int32), np.zeros(max(nnz.value, 1), np.int32)
+    val, b = np.zeros(max(nnz.value, 1)), np.zeros(n)
+    cf = np.ascontiguousarray(coef, dtype=np.float64)
+    _check(lib().lina_gpu_p1_assemble_host(C.byref(p), _dp(cf), _ip(ptr), _ip(col), _dp(val), _dp(b), None),
+           "P1 assembly")
+    return ptr, col[:nnz.value], val[:nnz.value], b
+
+
+class P1Assembly:
+    """P1 Laplacian or plane-strain elasticity assembled on the GPU into a fixed CSR pattern."""
+
+    def __init__(self, kind, xy, tri, nu=0.3, fixed_dof=(), fixed_val=()):
+        p, self._keep = _p1_problem(kind, xy, tri, nu, fixed_dof, fixed_val)
+        h = C.c_void_p()
+        self.h = None
+        _check(lib().lina_gpu_p1_create(C.byref(p), C.byref(h)), "P1 create")
+        self.h = h
+        n, nnz = C.c_int(), C.c_long()
+        _check(lib().lina_gpu_p1_sizes(self.h, C.byref(n), C.byref(nnz)), "P1 sizes")
+        self.n, self.nnz = n.value, nnz.value
+
+    def assemble(self, coef):
+        cf = np.ascontiguousarray(coef, dtype=np.float64)
+        _check(lib().lina_gpu_p1_assemble(self.h, cf.ctypes.data, 0), "P1 assemble")
+
+    def system(self):
+        """(indptr, indices, data, b) of the last assembly, copied to the host."""
+        ptr, col = np.zeros(self.n + 1, np.int32), np.zeros(max(self.nnz, 1), np.int32)
+        val, b = np.zeros(max(self.nnz, 1)), np.zeros(self.n)
+        _check(lib().lina_gpu_p1_download(self.h, _ip(ptr), _ip(col), _dp(val), _dp(b)), "P1 download")
+        return ptr, col[:self.nnz], val[:self.nnz], b
+
+    def device_values(self):
+        """Device pointers (values, b) of the last assembly."""
+        v, b = C.c_void_p(), C.c_void_p()
+        _check(lib().lina_gpu_p1_device(self.h, C.byref(v), C.byref(b)), "P1 device")
+        return v.value, b.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().lina_gpu_p1_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Batch:
     """Independent AMG-PCG solves in one CUDA graph launch (lina_gpu_batch_*)."""
 
@@ -577,6 +656,15 @@ class AMG:
 
     def set_smoother(self, smoother, omega, precision):
         _check(lib().lina_gpu_amg_set_smoother(self.h, smoother, omega, precision), "set smoother")
+
+    def update_values(self, data=None, device_ptr=None):
+        """New finest values on the creation pattern (lina_gpu_amg_update_values): a host array, or a
+        device pointer (e.g. P1Assembly.device_values())."""
+        if device_ptr is not None:
+            _check(lib().lina_gpu_amg_update_values(self.h, device_ptr, PCG_DEVICE_PTRS), "AMG update values")
+        else:
+            dv_ = np.ascontiguousarray(data, dtype=np.float64)
+            _check(lib().lina_gpu_amg_update_values(self.h, dv_.ctypes.data, 0), "AMG update values")
 
     def recompute(self, indptr, indices, data):
         ip_ = np.ascontiguousarray(indptr, dtype=np.int32)

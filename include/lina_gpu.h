@@ -250,6 +250,44 @@ int lina_gpu_reflective_newton_csr(int n, const int* ptr, const int* col, const 
              transposed solve is the same operator), then dL/dE_e = -lambda_e^T Khat_e u_e per
              element (lambda_e: the element's six adjoint values, zero on Dirichlet dofs).
    Dof numbering: node k -> k (x), n_nodes + k (y), the reference's block ordering. */
+/* P1 (linear triangle) assembly on the GPU, straight into CSR: the scalar Laplacian (one unknown
+   per node; FEM2D's set_matrix_Aij_11_2D with insert_A_bbV_a, FEM2D/FEM2D.c:5949, :4728) or
+   plane-strain elasticity (two per node, block ordering [x of all nodes, y of all nodes]), each
+   element's matrix scaled by a per-element coefficient (conductivity, Young's modulus).  The
+   pattern holds every pair of nodes sharing a triangle (both components for elasticity); Dirichlet
+   dofs are eliminated symmetrically (identity rows, known values lifted into b).  Every stored
+   entry sums its element contributions in element order with each product and sum rounded on its
+   own, so the device values equal the host ones bit for bit.  No reference counterpart for the
+   elimination: the reference resets rows only (Crack/crack.c:6445). */
+#define LINA_P1_LAPLACE 1
+#define LINA_P1_ELASTIC 2
+typedef struct lina_gpu_p1 lina_gpu_p1;
+typedef struct lina_gpu_p1_problem {
+    int kind;                 /* LINA_P1_LAPLACE or LINA_P1_ELASTIC                     */
+    int n_nodes, n_elems;
+    const double* xy;         /* 2 per node                                              */
+    const int* tri;           /* 3 node indices per element                              */
+    double nu;                /* Poisson's ratio (LINA_P1_ELASTIC)                       */
+    int n_fixed;
+    const int* fixed_dof;     /* Dirichlet dofs: component * n_nodes + node              */
+    const double* fixed_val;
+} lina_gpu_p1_problem;
+int lina_gpu_p1_create(const lina_gpu_p1_problem* p, lina_gpu_p1** out);
+/* assemble with the per-element coefficients coef[n_elems] (host; device with LINA_PCG_DEVICE_PTRS):
+   the matrix values and the right-hand side stay on the device */
+int lina_gpu_p1_assemble(lina_gpu_p1* h, const double* coef, int flags);
+int lina_gpu_p1_sizes(const lina_gpu_p1* h, int* n, long* nnz);
+/* host copies of the pattern, the values and b of the last assembly (any pointer may be NULL) */
+int lina_gpu_p1_download(lina_gpu_p1* h, int* rowptr, int* col, double* val, double* b);
+/* the device arrays of the last assembly (owned by the handle): values on the pattern of rowptr/col,
+   e.g. for lina_gpu_amg_update_values(..., LINA_PCG_DEVICE_PTRS) */
+int lina_gpu_p1_device(lina_gpu_p1* h, const double** val_dev, const double** b_dev);
+int lina_gpu_p1_destroy(lina_gpu_p1* h);
+/* the same assembly on the host (rowptr[n+1], col[nnz], val[nnz], b[n]; *nnz alone when rowptr is
+   NULL) */
+int lina_gpu_p1_assemble_host(const lina_gpu_p1_problem* p, const double* coef, int* rowptr, int* col, double* val,
+                              double* b, long* nnz);
+
 typedef struct lina_gpu_elastic lina_gpu_elastic;
 typedef struct lina_gpu_elastic_problem {
     int n_nodes;
