@@ -29,6 +29,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -161,6 +163,200 @@ __global__ void __launch_bounds__(kPool) sptrsv_kernel(int n, const int* __restr
             xw[i] = ur;
         }
         __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------- one-block level-synchronous solves
+// A triangular solve whose rows are listed level by level (positions), run by one block: the rows of
+// a level in parallel, a __syncthreads between levels.  The solution entries of the last
+// kWinLevels + 1 levels stay in a shared-memory ring (slot = position mod ring size), so a row reads
+// the rows it needs from shared memory; entries of older levels are read back from the
+// position-major solution in global memory, which the block itself wrote.  Each level's rows (first
+// entry, b, 1/L_ii) and entries (encoded source, value) lie contiguously in position-major arrays,
+// each level's slice 16-byte aligned, and one thread copies them into shared memory S - 1 levels
+// ahead with bulk (TMA) copies completing on a per-stage barrier: a level then costs
+// shared-memory reads, a few products and a block barrier.  The stages are kept small (a row's
+// entries end where the next row's begin) to fit many.  Products are subtracted in the factor's
+// entry order, so the results equal sptrsv_kernel's.
+constexpr int kWinLevels = 3;               // levels back whose entries the ring holds
+constexpr int kWinThreads = 1024;
+constexpr int kWinSmemMax = 220 * 1024;
+constexpr int kWinMaxStages = 6;
+
+__host__ __device__ constexpr int align16(int b) { return (b + 15) & ~15; }
+
+struct WinLayout {  // byte offsets inside one stage
+    int head, dinv, b, enc, val, bytes;
+};
+__host__ __device__ inline WinLayout win_layout(int max_rows, int max_ent, int tx, int tv, bool dinv) {
+    WinLayout L;
+    L.head = 0;
+    L.dinv = align16(L.head + 4 * max_rows);
+    L.b = align16(L.dinv + (dinv ? tx * max_rows : 0));
+    L.enc = align16(L.b + tx * max_rows);
+    L.val = align16(L.enc + 4 * max_ent);
+    L.bytes = align16(L.val + tv * max_ent);
+    return L;
+}
+
+template <typename TV, typename TX>
+struct WinArgs {
+    int nlev, ringmask, max_rows, max_ent;
+    const int4* bounds;  // level -> (first position, rows, first packed entry, entries); starts are
+                         // multiples of 4, so every level's slice of every array is 16-byte aligned
+    const int* head;     // position -> first packed entry
+    const int* enc;      // packed entry -> ring slot, or -(position + 1) of an older row
+    const TV* val;       // packed entry -> factor value
+    const TX* dinv;      // position -> 1 / L_ii (null: unit diagonal)
+    const TX* bpos;      // position -> right-hand side
+    TX* xpos;            // position -> solution
+    int* err;            // set when a wait for a copy runs out
+};
+
+// shared-memory barriers of the bulk copies (one per stage)
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// true once the phase of `parity` has completed; bounded like every wait of this file: after
+// kWaitNs (or kWaitPolls polls), or at once when a pass failed elsewhere, *err = 4 and false
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int* err) {
+    const unsigned addr = smem_addr(bar);
+    unsigned done = 0;
+    unsigned long long t0 = 0;
+    for (long polls = 0;; polls++) {
+        if (polls == 1) t0 = device_ns();
+        asm volatile(
+            "{\n .reg .pred P;\n mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n selp.b32 %0, 1, 0, P;\n}\n"
+            : "=r"(done)
+            : "r"(addr), "r"(parity)
+            : "memory");
+        if (done) return true;
+        // the error word and the clock are read every 64 polls: a read of global memory costs as much
+        // as the wait it would interrupt
+        if ((polls & 63) == 63 && (polls > kWaitPolls || *(volatile int*)err || device_ns() - t0 > kWaitNs)) {
+            atomicCAS(err, 0, 4);
+            return false;
+        }
+    }
+}
+
+// thread 0: bulk-copy level l's slices (16-byte aligned, sizes multiples of 16) into stage l % S;
+// the stage's barrier completes when all bytes have landed
+template <typename TV, typename TX, int S>
+__device__ __forceinline__ void win_issue(const WinArgs<TV, TX>& a, unsigned char* stages, uint64_t* bars,
+                                          const WinLayout& L, int l, int4 bd) {
+    unsigned char* st = stages + (l % S) * L.bytes;
+    uint64_t* bar = bars + (l % S);
+    const int pr = (bd.y + 3) & ~3, pe = (bd.w + 3) & ~3;  // padded rows and entries
+    const unsigned nb_head = 4u * pr, nb_dinv = a.dinv ? (unsigned)sizeof(TX) * pr : 0u,
+                   nb_b = (unsigned)sizeof(TX) * pr, nb_enc = 4u * pe, nb_val = (unsigned)sizeof(TV) * pe;
+    // the stage was last read through ordinary loads; order those before the copies' writes
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)),
+                 "r"(nb_head + nb_dinv + nb_b + nb_enc + nb_val)
+                 : "memory");
+    auto bulk = [&](unsigned char* dst, const void* src, unsigned bytes) {
+        if (bytes)
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                    smem_addr(dst)),
+                "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                : "memory");
+    };
+    bulk(st + L.head, a.head + bd.x, nb_head);
+    if (a.dinv) bulk(st + L.dinv, a.dinv + bd.x, nb_dinv);
+    bulk(st + L.b, a.bpos + bd.x, nb_b);
+    bulk(st + L.enc, a.enc + bd.z, nb_enc);
+    bulk(st + L.val, a.val + bd.z, nb_val);
+}
+
+template <typename TV, typename TX, int S, bool RING_ONLY>
+__global__ void __launch_bounds__(kWinThreads, 1) sptrsv_window_kernel(const WinArgs<TV, TX> a) {
+    extern __shared__ __align__(16) unsigned char win_smem[];
+    const int tid = threadIdx.x, T = blockDim.x;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(win_smem);
+    TX* ring = reinterpret_cast<TX*>(win_smem + align16(8 * S));
+    unsigned char* stages = win_smem + align16(8 * S) + align16((a.ringmask + 1) * (int)sizeof(TX));
+    const WinLayout L = win_layout(a.max_rows, a.max_ent, sizeof(TX), sizeof(TV), a.dinv != nullptr);
+    if (tid == 0) {
+        for (int k = 0; k < S; k++) mbar_init(bars + k);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        for (int l = 0; l < S - 1 && l < a.nlev; l++) win_issue<TV, TX, S>(a, stages, bars, L, l, __ldg(a.bounds + l));
+    }
+    __syncthreads();
+    // bounds of the level being solved and of the next one to copy, loaded one level ahead
+    int4 cur = __ldg(a.bounds);
+    int4 nb = S - 1 < a.nlev ? __ldg(a.bounds + S - 1) : make_int4(0, 0, 0, 0);
+    for (int l = 0; l < a.nlev; l++) {
+        // the stage of level l + S - 1 was read in level l - 1, which every thread has finished
+        if (tid == 0 && l + S - 1 < a.nlev) win_issue<TV, TX, S>(a, stages, bars, L, l + S - 1, nb);
+        const int4 nb2 = l + S < a.nlev ? __ldg(a.bounds + l + S) : make_int4(0, 0, 0, 0);
+        const int4 next = l + 1 < a.nlev ? __ldg(a.bounds + l + 1) : make_int4(0, 0, 0, 0);
+        mbar_wait(bars + (l % S), (unsigned)((l / S) & 1), a.err);
+        const unsigned char* st = stages + (l % S) * L.bytes;
+        const int* head = reinterpret_cast<const int*>(st + L.head);
+        const TX* dv = reinterpret_cast<const TX*>(st + L.dinv);
+        const TX* bv = reinterpret_cast<const TX*>(st + L.b);
+        const int* enc = reinterpret_cast<const int*>(st + L.enc);
+        const TV* val = reinterpret_cast<const TV*>(st + L.val);
+        const int t0 = cur.x, nr = cur.y, q0 = cur.z, qe = cur.z + cur.w;
+        for (int r = tid; r < nr; r += T) {
+            const int k0 = head[r] - q0, k1 = (r + 1 < nr ? head[r + 1] : qe) - q0;
+            TX s = bv[r];
+            for (int k = k0; k < k1; k++) {
+                const int e = enc[k];
+                const TX v = (RING_ONLY || e >= 0) ? ring[e] : __ldcg(a.xpos + (-e - 1));
+                s -= TX(val[k]) * v;
+            }
+            const TX res = a.dinv ? s * dv[r] : s;
+            ring[(t0 + r) & a.ringmask] = res;
+            a.xpos[t0 + r] = res;
+        }
+        __syncthreads();
+        cur = next;
+        nb = nb2;
+    }
+    // after a failed wait no copy of this block may still be landing when it exits: wait (bounded,
+    // not cut short by the error) for the last stages' copies
+    if (tid == 0 && *(volatile int*)a.err)
+        for (int l = a.nlev > S ? a.nlev - S : 0; l < a.nlev; l++) {
+            const unsigned addr = smem_addr(bars + (l % S));
+            const unsigned long long t0 = device_ns();
+            unsigned done = 0;
+            while (!done && device_ns() - t0 < kWaitNs)
+                asm volatile(
+                    "{\n .reg .pred P;\n mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n selp.b32 %0, 1, 0, P;\n}\n"
+                    : "=r"(done)
+                    : "r"(addr), "r"((unsigned)((l / S) & 1))
+                    : "memory");
+        }
+}
+
+// bpos[t] = b[row[t]] (0 on padding positions): the right-hand side in position order
+template <typename TX>
+__global__ void gather_pos_kernel(int n, const int* __restrict__ row, const TX* __restrict__ b, TX* __restrict__ bpos) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+        bpos[t] = row[t] >= 0 ? b[row[t]] : TX(0);
+}
+
+// x[row[t]] = xpos[t]: the solution from position order (padding positions skipped)
+template <typename TX>
+__global__ void scatter_pos_kernel(int n, const int* __restrict__ row, const TX* __restrict__ xpos, TX* __restrict__ x) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+        if (row[t] >= 0) x[row[t]] = xpos[t];
+}
+
+
+// packed copies of the factor values (entry order of the window) and of 1/L_ii (position order)
+__global__ void pack_values_kernel(long ne, const int* __restrict__ perm, const double* __restrict__ v64,
+                                   const float* __restrict__ v32, double* __restrict__ w64, float* __restrict__ w32) {
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < ne; q += (long)gridDim.x * blockDim.x) {
+        const int p = perm[q];  // -1: padding
+        w64[q] = p >= 0 ? v64[p] : 0.0;
+        w32[q] = p >= 0 ? v32[p] : 0.0f;
     }
 }
 
@@ -371,6 +567,18 @@ struct Factor {
     int *order = nullptr, *beg = nullptr, *end = nullptr, *col = nullptr;
     double *val64 = nullptr, *dinv64 = nullptr;
     float *val32 = nullptr, *dinv32 = nullptr;  // dinv null: unit diagonal
+    // the one-block level-synchronous solve (s32 / s64 = 0: the row pool in that precision)
+    struct Win {
+        int s32 = 0, s64 = 0;  // cp.async stages
+        int ringmask = 0, max_rows = 0, max_ent = 0;
+        long ne = 0;      // packed entries (padded)
+        bool ring_only = true;  // every needed row lies within the ring's levels
+        int npos = 0;     // positions (padded)
+        size_t smem32 = 0, smem64 = 0;
+        int *bounds = nullptr, *head = nullptr, *row = nullptr, *enc = nullptr, *vperm = nullptr;
+        double *val64 = nullptr, *dinv64 = nullptr;
+        float *val32 = nullptr, *dinv32 = nullptr;
+    } win;
 };
 
 struct Mem {
@@ -399,7 +607,7 @@ struct Mem {
 
 // level order of rows: lower = rows need smaller indices (entries [beg_i, end_i) columns), else larger
 int level_order(int n, const std::vector<int>& beg, const std::vector<int>& end, const int* col, bool lower,
-                std::vector<int>& order) {
+                std::vector<int>& order, std::vector<int>* lev_out = nullptr, std::vector<int>* lp_out = nullptr) {
     std::vector<int> lev(n, 0);
     int nlev = 0;
     for (int t = 0; t < n; t++) {
@@ -414,6 +622,11 @@ int level_order(int n, const std::vector<int>& beg, const std::vector<int>& end,
     for (int l = 0; l < nlev; l++) lp[l + 1] += lp[l];
     order.assign(n, 0);
     for (int i = 0; i < n; i++) order[lp[lev[i]]++] = i;
+    if (lp_out) {  // level starts (lp was advanced to the ends by the fill)
+        lp_out->assign(nlev + 1, 0);
+        for (int l = 0; l < nlev; l++) (*lp_out)[l + 1] = lp[l];
+    }
+    if (lev_out) lev_out->swap(lev);
     return nlev;
 }
 
@@ -446,6 +659,9 @@ struct lina_gpu_ilu {
     float *r32 = nullptr, *t32 = nullptr, *z32 = nullptr;
     int* err = nullptr;
     unsigned* ticket = nullptr;  // the pool's row counter, reset before every pass
+    double *bpos64 = nullptr, *xpos64 = nullptr;  // position-major work of the one-block solves
+    float *bpos32 = nullptr, *xpos32 = nullptr;
+    int npos = 0;                                  // their length
     int* flag = nullptr;         // rows finished by the factorisation
     double* fval = nullptr;      // factor values on A's pattern (factorised on the device), else null
     int epoch = 0;               // factorisation passes (row flags hold the current one)
@@ -466,6 +682,124 @@ bool alloc_work(lina_gpu_ilu* h) {
     h->ticket = h->mem.get<unsigned>(1);
     return h->t64 && h->r32 && h->t32 && h->z32 && h->err && h->ticket &&
            cudaMemset(h->err, 0, sizeof(int)) == cudaSuccess;
+}
+
+// The one-block solve's position-major arrays for a factor: levels from level_order (lev, lp), row
+// i's needed entries [beg_i, end_i) of the column array col (in the order they are subtracted).
+// Disabled (no stages) where its shared memory would not fit.
+template <typename TV, typename TX>
+size_t win_smem(int ring, int max_rows, int max_ent, bool dinv, int stages) {
+    return (size_t)align16(8 * stages) + align16(ring * (int)sizeof(TX)) +
+           (size_t)stages * win_layout(max_rows, max_ent, sizeof(TX), sizeof(TV), dinv).bytes;
+}
+
+bool build_window(lina_gpu_ilu* h, Factor& f, int n, const std::vector<int>& order, const std::vector<int>& lev,
+                  const std::vector<int>& lp, const std::vector<int>& beg, const std::vector<int>& end,
+                  const int* col, bool has_dinv) {
+    Factor::Win& w = f.win;
+    w = Factor::Win();
+    const int nlev = (int)lp.size() - 1;
+    if (nlev <= 0) return true;
+    // padded positions and entries: every level starts at a multiple of 4 in both
+    std::vector<int> P(nlev + 1, 0), Q(nlev + 1, 0), ecount(nlev, 0);
+    long ptot = 0, qtot = 0;
+    for (int l = 0; l < nlev; l++) {
+        long e = 0;
+        for (int t = lp[l]; t < lp[l + 1]; t++) e += end[order[t]] - beg[order[t]];
+        ecount[l] = (int)e;
+        P[l] = (int)ptot;
+        Q[l] = (int)qtot;
+        ptot += (lp[l + 1] - lp[l] + 3) & ~3;
+        qtot += (e + 3) & ~3;
+        if (ptot > INT32_MAX / 4 || qtot > INT32_MAX / 4) return true;  // too large: the row pool
+    }
+    P[nlev] = (int)ptot;
+    Q[nlev] = (int)qtot;
+    std::vector<int> ppos(n);
+    for (int l = 0; l < nlev; l++)
+        for (int t = lp[l]; t < lp[l + 1]; t++) ppos[order[t]] = P[l] + (t - lp[l]);
+    int maxwin = 0, max_rows = 0, max_ent = 0;
+    for (int l = 0; l < nlev; l++) {
+        maxwin = std::max(maxwin, P[l + 1] - P[std::max(0, l - kWinLevels)]);
+        max_rows = std::max(max_rows, P[l + 1] - P[l]);
+        max_ent = std::max(max_ent, Q[l + 1] - Q[l]);
+    }
+    int ring = 1;
+    while (ring < maxwin) ring *= 2;
+    for (int S = kWinMaxStages; S >= 2 && w.s32 == 0; S--)
+        if (win_smem<float, float>(ring, max_rows, max_ent, has_dinv, S) <= (size_t)kWinSmemMax) w.s32 = S;
+    for (int S = kWinMaxStages; S >= 2 && w.s64 == 0; S--)
+        if (win_smem<double, double>(ring, max_rows, max_ent, has_dinv, S) <= (size_t)kWinSmemMax) w.s64 = S;
+    if (w.s32 == 0 && w.s64 == 0) return true;
+    std::vector<int> head(ptot, 0), row(ptot, -1), enc(qtot, 0), vperm(qtot, -1), bounds(4 * (size_t)nlev);
+    int older = 0;
+#pragma omp parallel for schedule(dynamic, 16) reduction(| : older)
+    for (int l = 0; l < nlev; l++) {
+        int q = Q[l];
+        for (int t = lp[l]; t < lp[l + 1]; t++) {
+            const int i = order[t], pp = P[l] + (t - lp[l]);
+            row[pp] = i;
+            head[pp] = q;
+            for (int p = beg[i]; p < end[i]; p++, q++) {
+                const int j = col[p];
+                vperm[q] = p;
+                enc[q] = lev[i] - lev[j] <= kWinLevels ? (ppos[j] & (ring - 1)) : -(ppos[j] + 1);
+                if (enc[q] < 0) older = 1;
+            }
+        }
+        bounds[4 * (size_t)l] = P[l];
+        bounds[4 * (size_t)l + 1] = lp[l + 1] - lp[l];
+        bounds[4 * (size_t)l + 2] = Q[l];
+        bounds[4 * (size_t)l + 3] = ecount[l];
+    }
+    w.ring_only = older == 0;
+    w.ringmask = ring - 1;
+    w.max_rows = max_rows;
+    w.max_ent = max_ent;
+    w.ne = qtot;
+    w.npos = (int)ptot;
+    if (w.s32) w.smem32 = win_smem<float, float>(ring, max_rows, max_ent, has_dinv, w.s32);
+    if (w.s64) w.smem64 = win_smem<double, double>(ring, max_rows, max_ent, has_dinv, w.s64);
+    Mem& m = h->mem;
+    w.bounds = m.up(bounds);
+    w.head = m.up(head);
+    w.row = m.up(row);
+    w.enc = m.up(enc);
+    w.vperm = m.up(vperm);
+    w.val64 = m.get<double>(w.ne);
+    w.val32 = m.get<float>(w.ne);
+    bool ok = w.bounds && w.head && w.row && w.enc && w.vperm && w.val64 && w.val32;
+    if (has_dinv) {
+        w.dinv64 = m.get<double>(w.npos);
+        w.dinv32 = m.get<float>(w.npos);
+        ok = ok && w.dinv64 && w.dinv32;
+    }
+    if (ok && h->npos < w.npos) {  // position-major work vectors, shared by both factors
+        h->bpos64 = m.get<double>(w.npos);
+        h->xpos64 = m.get<double>(w.npos);
+        h->bpos32 = m.get<float>(w.npos);
+        h->xpos32 = m.get<float>(w.npos);
+        ok = h->bpos64 && h->xpos64 && h->bpos32 && h->xpos32;
+        h->npos = w.npos;
+    }
+    if (!ok) {
+        w = Factor::Win();
+        return false;
+    }
+    return true;
+}
+
+// the window's packed copies of a factor's values and inverse diagonal (after every factorisation)
+void pack_window(Factor& f, int n) {
+    Factor::Win& w = f.win;
+    if (!w.s32 && !w.s64) return;
+    pack_values_kernel<<<std::min<long>(4096, (w.ne + kT - 1) / kT), kT, 0, st()>>>(w.ne, w.vperm, f.val64, f.val32,
+                                                                                   w.val64, w.val32);
+    if (w.dinv64) {
+        const int g = std::min(4096, (w.npos + kT - 1) / kT);
+        gather_pos_kernel<double><<<g, kT, 0, st()>>>(w.npos, w.row, f.dinv64, w.dinv64);
+        gather_pos_kernel<float><<<g, kT, 0, st()>>>(w.npos, w.row, f.dinv32, w.dinv32);
+    }
 }
 
 // a factor given as CSR with its diagonal (lower: L with diagonal; upper: U, diagonal 1 skipped)
@@ -505,7 +839,8 @@ bool build_factor(lina_gpu_ilu* h, Factor& f, int n, const int* p, const int* c,
         ptr[i + 1] = (int)col.size();
     }
     std::vector<int> beg(ptr.begin(), ptr.end() - 1), end(ptr.begin() + 1, ptr.end()), order;
-    f.nlev = level_order(n, beg, end, col.data(), lower, order);
+    std::vector<int> lev, lp;
+    f.nlev = level_order(n, beg, end, col.data(), lower, order, &lev, &lp);
     std::vector<float> val32(val.begin(), val.end()), dinv32(dinv.begin(), dinv.end());
     int* dptr = h->mem.up(ptr);
     f.order = h->mem.up(order);
@@ -525,6 +860,11 @@ bool build_factor(lina_gpu_ilu* h, Factor& f, int n, const int* p, const int* c,
     }
     f.beg = dptr;
     f.end = dptr + 1;
+    if (!build_window(h, f, n, order, lev, lp, beg, end, col.data(), !unit)) {
+        err = "device allocation for the ILU factors failed";
+        return false;
+    }
+    pack_window(f, n);
     return true;
 }
 
@@ -548,6 +888,8 @@ int factorise(lina_gpu_ilu* h) {
     diag_inverse_kernel<<<std::min(4096, (n + kT - 1) / kT), kT, 0, st()>>>(n, h->adiag, h->fval, h->L.dinv64,
                                                                              h->L.dinv32);
     cvt_kernel<double, float><<<std::min<long>(4096, (nnz + kT - 1) / kT), kT, 0, st()>>>(nnz, h->fval, h->L.val32);
+    pack_window(h->L, n);
+    pack_window(h->U, n);
     const int e = (cudaGetLastError() == cudaSuccess) ? read_err(h) : -1;
     if (e != 0) {
         lina::dev::set_error(e == 2 ? "ILU: zero pivot (incomplete_LU_factorization fails)"
@@ -558,9 +900,67 @@ int factorise(lina_gpu_ilu* h) {
     return 0;
 }
 
+template <typename TV, typename TX, int S, bool RING_ONLY>
+void launch_window_t(const WinArgs<TV, TX>& a, size_t smem) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(sptrsv_window_kernel<TV, TX, S, RING_ONLY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kWinSmemMax);
+        attr = true;
+    }
+    sptrsv_window_kernel<TV, TX, S, RING_ONLY><<<1, kWinThreads, smem, st()>>>(a);
+}
+
+template <typename TV, typename TX, int S>
+void launch_window(lina_gpu_ilu* h, const Factor& f, const WinArgs<TV, TX>& a, size_t smem) {
+    (void)h;
+    if (f.win.ring_only)
+        launch_window_t<TV, TX, S, true>(a, smem);
+    else
+        launch_window_t<TV, TX, S, false>(a, smem);
+}
+
 template <typename TV, typename TX>
 void solve(lina_gpu_ilu* h, const Factor& f, const TV* val, const TX* dinv, const TX* b, TX* x) {
     const int n = h->n;
+    const Factor::Win& w = f.win;
+    const int stages = sizeof(TX) == 8 ? w.s64 : w.s32;
+    if (stages) {
+        WinArgs<TV, TX> a;
+        a.nlev = f.nlev;
+        a.ringmask = w.ringmask;
+        a.max_rows = w.max_rows;
+        a.max_ent = w.max_ent;
+        a.bounds = reinterpret_cast<const int4*>(w.bounds);
+        a.head = w.head;
+        a.enc = w.enc;
+        TX* bpos;
+        if constexpr (sizeof(TX) == 8) {
+            a.val = (const TV*)w.val64;
+            a.dinv = dinv ? (const TX*)w.dinv64 : nullptr;
+            bpos = (TX*)h->bpos64;
+            a.xpos = (TX*)h->xpos64;
+        } else {
+            a.val = (const TV*)w.val32;
+            a.dinv = dinv ? (const TX*)w.dinv32 : nullptr;
+            bpos = (TX*)h->bpos32;
+            a.xpos = (TX*)h->xpos32;
+        }
+        a.bpos = bpos;
+        a.err = h->err;
+        const int g = std::min(4096, (w.npos + kT - 1) / kT);
+        gather_pos_kernel<TX><<<g, kT, 0, st()>>>(w.npos, w.row, b, bpos);
+        const size_t smem = sizeof(TX) == 8 ? w.smem64 : w.smem32;
+        switch (stages) {
+            case 6: launch_window<TV, TX, 6>(h, f, a, smem); break;
+            case 5: launch_window<TV, TX, 5>(h, f, a, smem); break;
+            case 4: launch_window<TV, TX, 4>(h, f, a, smem); break;
+            case 3: launch_window<TV, TX, 3>(h, f, a, smem); break;
+            default: launch_window<TV, TX, 2>(h, f, a, smem); break;
+        }
+        scatter_pos_kernel<TX><<<g, kT, 0, st()>>>(w.npos, w.row, a.xpos, x);
+        return;
+    }
     cudaMemsetAsync(x, 0xff, (size_t)n * sizeof(TX), st());  // every entry pending
     cudaMemsetAsync(h->ticket, 0, sizeof(unsigned), st());
     sptrsv_kernel<TV, TX><<<pool_blocks(n), kPool, 0, st()>>>(n, f.order, f.beg, f.end, f.col, val, dinv, b, x,
@@ -619,9 +1019,9 @@ int lina_gpu_ilu_create_from_matrix(int n, const int* rowptr, const int* col, co
     lina_gpu_ilu* h = new lina_gpu_ilu();
     h->n = n;
     h->fnnz = nnz;
-    std::vector<int> lorder, uorder;
-    h->L.nlev = level_order(n, lbeg, lend, col, true, lorder);
-    h->U.nlev = level_order(n, ubeg, uend, col, false, uorder);
+    std::vector<int> lorder, uorder, llev, ulev, llp, ulp;
+    h->L.nlev = level_order(n, lbeg, lend, col, true, lorder, &llev, &llp);
+    h->U.nlev = level_order(n, ubeg, uend, col, false, uorder, &ulev, &ulp);
     Mem& m = h->mem;
     int *dptr = nullptr, *dcol = nullptr, *ddiag = nullptr;
     double* dval = nullptr;
@@ -652,6 +1052,12 @@ int lina_gpu_ilu_create_from_matrix(int n, const int* rowptr, const int* col, co
     h->L.col = h->U.col = dcol;
     h->L.val64 = h->U.val64 = h->fval;
     h->U.val32 = h->L.val32;
+    if (!build_window(h, h->L, n, lorder, llev, llp, lbeg, lend, col, true) ||
+        !build_window(h, h->U, n, uorder, ulev, ulp, ubeg, uend, col, false)) {
+        lina::dev::set_error("ILU: device allocation failed");
+        delete h;
+        return LINA_GPU_ECUDA;
+    }
     h->flag = m.get<int>(n);
     h->aptr = dptr;
     h->acol = dcol;
