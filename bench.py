@@ -65,6 +65,8 @@ def parse():
                    help="elasticity: the headline AMG-PCG solve (default); damage: the reflective-Newton "
                         "damage step on the same mesh; adjoint: the material-identification gradient; "
                         "batch: independent unstructured systems solved in one graph launch")
+    p.add_argument("--sell-bits", type=int, default=16, choices=[16, 32],
+                   help="column-index width of the SELL-32 matrices (16: offsets from two bases per slice)")
     p.add_argument("--batch-count", type=int, default=96, help="systems of the batch workload")
     p.add_argument("--batch-matrix-tol", type=float, default=0.3,
                    help="interpolation truncation of the batch workload's hierarchies (with 0.1 the "
@@ -268,7 +270,7 @@ def run_gb300(args, rank, world, local):
                                f"AMG-PCG mixed precision to true rel-res {args.tol:g}",
                    "dofs": n, "nnz": int(s.nnz), "amg_depth": depth, "level_sizes": sizes,
                    "coarsening": "standard", "matrix_tol": args.matrix_tol, "smoother": args.smoother,
-                   "omega": omega, "sweeps": "2+2",
+                   "omega": omega, "sweeps": "2+2", "sell_index_bits": args.sell_bits,
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs exceed L2 (finest matrix > 129 MB), no flush"},
         "iterations": it_mixed, "true_rel_residual": trr, "dofs_per_s": value * n, "setup_s": setup_s,
@@ -553,9 +555,10 @@ def main():
         run_reference(args, rank, world)
         return
     init_dist(world)
+    from fem_gb300 import lina
     if world > 1:
-        from fem_gb300 import lina
         lina.set_device(local)
+    lina.set_sell_index_bits(args.sell_bits)
     if args.workload == "damage":
         run_damage(args, rank, world, local)
     elif args.workload == "adjoint":

@@ -37,6 +37,7 @@
 #include <string>
 #include <vector>
 
+#include "bulk_copy.cuh"
 #include "gpu_ops.h"
 #include "lina_gpu.h"
 
@@ -213,34 +214,9 @@ struct WinArgs {
     int* err;            // set when a wait for a copy runs out
 };
 
-// shared-memory barriers of the bulk copies (one per stage)
-__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(bar)) : "memory");
-}
-
-// true once the phase of `parity` has completed; bounded like every wait of this file: after
-// kWaitNs (or kWaitPolls polls), or at once when a pass failed elsewhere, *err = 4 and false
+// the bulk copies' barriers (one per stage) wait with this file's error word, code 4
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int* err) {
-    const unsigned addr = smem_addr(bar);
-    unsigned done = 0;
-    unsigned long long t0 = 0;
-    for (long polls = 0;; polls++) {
-        if (polls == 1) t0 = device_ns();
-        asm volatile(
-            "{\n .reg .pred P;\n mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n selp.b32 %0, 1, 0, P;\n}\n"
-            : "=r"(done)
-            : "r"(addr), "r"(parity)
-            : "memory");
-        if (done) return true;
-        // the error word and the clock are read every 64 polls: a read of global memory costs as much
-        // as the wait it would interrupt
-        if ((polls & 63) == 63 && (polls > kWaitPolls || *(volatile int*)err || device_ns() - t0 > kWaitNs)) {
-            atomicCAS(err, 0, 4);
-            return false;
-        }
-    }
+    return bulk::mbar_wait(bar, parity, err, 4, kWaitNs);
 }
 
 // thread 0: bulk-copy level l's slices (16-byte aligned, sizes multiples of 16) into stage l % S;
@@ -254,23 +230,16 @@ __device__ __forceinline__ void win_issue(const WinArgs<TV, TX>& a, unsigned cha
     const unsigned nb_head = 4u * pr, nb_dinv = a.dinv ? (unsigned)sizeof(TX) * pr : 0u,
                    nb_b = (unsigned)sizeof(TX) * pr, nb_enc = 4u * pe, nb_val = (unsigned)sizeof(TV) * pe;
     // the stage was last read through ordinary loads; order those before the copies' writes
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)),
-                 "r"(nb_head + nb_dinv + nb_b + nb_enc + nb_val)
-                 : "memory");
-    auto bulk = [&](unsigned char* dst, const void* src, unsigned bytes) {
-        if (bytes)
-            asm volatile(
-                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
-                    smem_addr(dst)),
-                "l"(src), "r"(bytes), "r"(smem_addr(bar))
-                : "memory");
+    bulk::fence_proxy_async();
+    bulk::mbar_expect_tx(bar, nb_head + nb_dinv + nb_b + nb_enc + nb_val);
+    auto put = [&](unsigned char* dst, const void* src, unsigned bytes) {
+        if (bytes) bulk::copy(dst, src, bytes, bar);
     };
-    bulk(st + L.head, a.head + bd.x, nb_head);
-    if (a.dinv) bulk(st + L.dinv, a.dinv + bd.x, nb_dinv);
-    bulk(st + L.b, a.bpos + bd.x, nb_b);
-    bulk(st + L.enc, a.enc + bd.z, nb_enc);
-    bulk(st + L.val, a.val + bd.z, nb_val);
+    put(st + L.head, a.head + bd.x, nb_head);
+    if (a.dinv) put(st + L.dinv, a.dinv + bd.x, nb_dinv);
+    put(st + L.b, a.bpos + bd.x, nb_b);
+    put(st + L.enc, a.enc + bd.z, nb_enc);
+    put(st + L.val, a.val + bd.z, nb_val);
 }
 
 template <typename TV, typename TX, int S, bool RING_ONLY>
@@ -282,8 +251,8 @@ __global__ void __launch_bounds__(kWinThreads, 1) sptrsv_window_kernel(const Win
     unsigned char* stages = win_smem + align16(8 * S) + align16((a.ringmask + 1) * (int)sizeof(TX));
     const WinLayout L = win_layout(a.max_rows, a.max_ent, sizeof(TX), sizeof(TV), a.dinv != nullptr);
     if (tid == 0) {
-        for (int k = 0; k < S; k++) mbar_init(bars + k);
-        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        for (int k = 0; k < S; k++) bulk::mbar_init(bars + k);
+        bulk::fence_mbar_init();
         for (int l = 0; l < S - 1 && l < a.nlev; l++) win_issue<TV, TX, S>(a, stages, bars, L, l, __ldg(a.bounds + l));
     }
     __syncthreads();
@@ -322,17 +291,8 @@ __global__ void __launch_bounds__(kWinThreads, 1) sptrsv_window_kernel(const Win
     // after a failed wait no copy of this block may still be landing when it exits: wait (bounded,
     // not cut short by the error) for the last stages' copies
     if (tid == 0 && *(volatile int*)a.err)
-        for (int l = a.nlev > S ? a.nlev - S : 0; l < a.nlev; l++) {
-            const unsigned addr = smem_addr(bars + (l % S));
-            const unsigned long long t0 = device_ns();
-            unsigned done = 0;
-            while (!done && device_ns() - t0 < kWaitNs)
-                asm volatile(
-                    "{\n .reg .pred P;\n mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n selp.b32 %0, 1, 0, P;\n}\n"
-                    : "=r"(done)
-                    : "r"(addr), "r"((unsigned)((l / S) & 1))
-                    : "memory");
-        }
+        for (int l = a.nlev > S ? a.nlev - S : 0; l < a.nlev; l++)
+            bulk::mbar_drain(bars + (l % S), (unsigned)((l / S) & 1), kWaitNs);
 }
 
 // bpos[t] = b[row[t]] (0 on padding positions): the right-hand side in position order

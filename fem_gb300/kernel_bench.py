@@ -26,7 +26,9 @@ def main():
     ap.add_argument("--level", type=int, default=-1, help="AMG level (default: the finest matrix itself)")
     ap.add_argument("--depth", type=int, default=10)
     ap.add_argument("--matrix-tol", type=float, default=0.1)
+    ap.add_argument("--sell-bits", type=int, default=16, choices=[16, 32], help="SELL-32 column-index width")
     args = ap.parse_args()
+    lina.set_sell_index_bits(args.sell_bits)
     s = problems.elasticity_p1(args.m)
     if args.level >= 0:
         amg = lina.AMG.from_system(s, depth=args.depth, coarsening=lina.STANDARD, matrix_tol=args.matrix_tol,
@@ -49,7 +51,8 @@ def main():
         for _ in range(args.reps):
             M.spmv_device(b, t, prec)
         out[f"spmv_{dt.__name__}_ms"] = (time.perf_counter() - t0) * 1e3 / max(args.reps, 1)
-    out.update(level=args.level, n=n, nnz=int(ip[-1]), padded=int(M.padded_entries))
+    out.update(level=args.level, n=n, nnz=int(ip[-1]), padded=int(M.padded_entries),
+               index_bits=M.index_bits())
     print(out)
 
 

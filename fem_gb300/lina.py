@@ -128,6 +128,9 @@ def lib():
         "lina_gpu_set_device": (C.c_int, [C.c_int]),
         "lina_gpu_set_layout": (C.c_int, [C.c_int]),
         "lina_gpu_set_fused_rows": (C.c_int, [C.c_int]),
+        "lina_gpu_set_sell_index_bits": (C.c_int, [C.c_int]),
+        "lina_gpu_matrix_index_bits": (C.c_int, [vp]),
+        "lina_gpu_level_index_bits": (C.c_int, [vp, C.c_int, ip, ip, ip]),
         "lina_gpu_last_error": (C.c_char_p, []),
         "lina_gpu_timer_begin": (C.c_int, [vp]),
         "lina_gpu_timer_end": (C.c_int, [vp, dp]),
@@ -286,6 +289,12 @@ def set_fused_rows(max_rows: int):
     _check(lib().lina_gpu_set_fused_rows(int(max_rows)), "set fused rows")
 
 
+def set_sell_index_bits(bits: int):
+    """16 (the default): SELL-32 matrices with long rows uploaded afterwards also get 16-bit column
+    offsets (two bases per slice, where the columns fit), read by FP32 passes; 32: int columns only."""
+    _check(lib().lina_gpu_set_sell_index_bits(int(bits)), "set SELL index bits")
+
+
 def dot(a: "DeviceArray", b: "DeviceArray") -> float:
     r = C.c_double()
     _check(lib().lina_gpu_dot(a.ptr, b.ptr, a.n, C.byref(r)), "dot")
@@ -317,6 +326,10 @@ class Matrix:
     @property
     def padded_entries(self):
         return lib().lina_gpu_matrix_padded_entries(self.h)
+
+    def index_bits(self):
+        """Column-index width of the FP32 passes: 16 or 32 (SELL-32), 0 for the lane-group CSR layout."""
+        return lib().lina_gpu_matrix_index_bits(self.h)
 
     def update_values(self, data):
         """New values on the pattern given at creation (CSR order)."""
@@ -612,6 +625,13 @@ class AMG:
     def from_system(cls, s, host_only=False, **opts):
         opts.setdefault("dof", s.dof)
         return cls(s.n, s.indptr, s.indices, s.data, host_only=host_only, **opts)
+
+    def index_bits(self, lv):
+        """(A, P, R) column-index widths of the FP32 passes over level lv: 16 or 32 for SELL-32, 0 for
+        the lane-group CSR layout or a missing matrix."""
+        a, p, r = C.c_int(), C.c_int(), C.c_int()
+        _check(lib().lina_gpu_level_index_bits(self.h, lv, C.byref(a), C.byref(p), C.byref(r)), "index bits")
+        return a.value, p.value, r.value
 
     def level(self, lv) -> Level:
         L = lib()

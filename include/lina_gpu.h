@@ -170,6 +170,9 @@ int lina_gpu_matrix_jacobi(lina_gpu_matrix* m, int precision, double omega, int 
 int lina_gpu_matrix_rows(const lina_gpu_matrix* m);
 /* stored entries including the SELL-32 slice padding */
 long lina_gpu_matrix_padded_entries(const lina_gpu_matrix* m);
+/* column-index width the matrix's FP32 passes read: 16 or 32 (SELL-32), 0 for the lane-group CSR
+   layout */
+int lina_gpu_matrix_index_bits(const lina_gpu_matrix* m);
 
 /* ILU(0) preconditioner on the GPU: factors as incomplete_LU_factorization produces them
    (LinA/linear_algebra.c:1952: L lower with diagonal, U upper with unit diagonal), applied by
@@ -337,6 +340,9 @@ unsigned long long lina_gpu_launches(void);
 
 /* hierarchy inspection (host copies of what the GPU holds) */
 int lina_gpu_amg_depth(const lina_gpu_amg* h);
+/* column-index width the FP32 passes over a level's A, P and R read: 16 or 32 (SELL-32), 0 (lane-
+   group CSR layout, or no such matrix) */
+int lina_gpu_level_index_bits(const lina_gpu_amg* h, int level, int* A_bits, int* P_bits, int* R_bits);
 int lina_gpu_level_sizes(const lina_gpu_amg* h, int level, int* n, long* nnz_A, long* nnz_P, long* nnz_R,
                          int* n_colours);
 int lina_gpu_level_export(const lina_gpu_amg* h, int level, int* labels, int* A_ptr, int* A_col, double* A_val,
@@ -379,6 +385,12 @@ int lina_gpu_set_layout(int layout);
    launch per colour and step; the results are bit-identical.  0 turns this off.  Takes effect for
    solves issued afterwards (a hierarchy's captured solve graph keeps the choice it was captured with). */
 int lina_gpu_set_fused_rows(int max_rows);
+/* 16 (default): SELL-32 matrices with long rows (at least 24 stored entries per row on average)
+   uploaded afterwards also get 16-bit column indices, a 15-bit offset from one of two bases per
+   slice of 32 rows, where every slice's columns fit two such windows; FP32 passes read those (2
+   bytes less per stored entry), FP64 passes the int columns.  32: int columns only.  The results
+   are identical. */
+int lina_gpu_set_sell_index_bits(int bits);
 
 const char* lina_gpu_last_error(void);
 
