@@ -151,30 +151,55 @@ Graph graph_of(const Csr& A) {
 // Max-priority queue with the ordering of the reference's red-black tree
 // (red_black_tree.c:174-197, :513-523, :620-658): keys compare with '>';
 // a new node goes after every node whose key is <= its own, and the largest
-// is the rightmost node, so among equal keys the latest insertion wins.  A
-// binary heap on (key, insertion sequence) with lazy deletion yields the same
-// choice.
+// is the rightmost node, so among equal keys the latest insertion wins.  An
+// indexed binary heap on (key, insertion sequence) yields the same choice; it
+// holds one entry per queued node (a changed key moves the node's entry in
+// place), so it never grows past the level's size.
 class ImportanceQueue {
    public:
-    explicit ImportanceQueue(int n) : live_(n, 0) {}
-    bool contains(int i) const { return live_[i] != 0; }
+    explicit ImportanceQueue(int n) : pos_(n, -1) {}
+    bool contains(int i) const { return pos_[i] >= 0; }
     void insert(int i, double key) {
-        uint64_t s = ++seq_;
-        live_[i] = s;
-        heap_.push(Entry{key, s, i});
-    }
-    void remove(int i) { live_[i] = 0; }
-    int pop_largest() {
-        while (!heap_.empty()) {
-            Entry e = heap_.top();
-            if (live_[e.node] == e.seq) {
-                heap_.pop();
-                live_[e.node] = 0;
-                return e.node;
-            }
-            heap_.pop();
+        if (pos_[i] >= 0) {
+            update(i, key);
+            return;
         }
-        return -1;
+        heap_.push_back(Entry{key, ++seq_, i});
+        pos_[i] = (int)heap_.size() - 1;
+        up(pos_[i]);
+    }
+    // the node's key changes (and it counts as inserted now)
+    void update(int i, double key) {
+        const int p = pos_[i];
+        const Entry old = heap_[p];
+        heap_[p].key = key;
+        heap_[p].seq = ++seq_;
+        if (before(old, heap_[p]))
+            up(p);
+        else
+            down(p);
+    }
+    void remove(int i) {
+        const int p = pos_[i];
+        if (p < 0) return;
+        pos_[i] = -1;
+        const int last = (int)heap_.size() - 1;
+        if (p != last) {
+            const Entry moved = heap_[last];
+            heap_[p] = moved;
+            pos_[moved.node] = p;
+            heap_.pop_back();
+            up(p);
+            down(pos_[moved.node]);
+        } else {
+            heap_.pop_back();
+        }
+    }
+    int pop_largest() {
+        if (heap_.empty()) return -1;
+        const int top = heap_[0].node;
+        remove(top);
+        return top;
     }
 
    private:
@@ -182,14 +207,42 @@ class ImportanceQueue {
         double key;
         uint64_t seq;
         int node;
-        bool operator<(const Entry& o) const {
-            if (key > o.key) return false;
-            if (o.key > key) return true;
-            return seq < o.seq;
-        }
     };
-    std::priority_queue<Entry> heap_;
-    std::vector<uint64_t> live_;
+    // a below b: a smaller key, or an equal key inserted earlier
+    static bool before(const Entry& a, const Entry& b) {
+        if (a.key > b.key) return false;
+        if (b.key > a.key) return true;
+        return a.seq < b.seq;
+    }
+    void up(int p) {
+        Entry e = heap_[p];
+        while (p > 0) {
+            const int q = (p - 1) >> 1;
+            if (!before(heap_[q], e)) break;
+            heap_[p] = heap_[q];
+            pos_[heap_[p].node] = p;
+            p = q;
+        }
+        heap_[p] = e;
+        pos_[e.node] = p;
+    }
+    void down(int p) {
+        const int n = (int)heap_.size();
+        Entry e = heap_[p];
+        for (;;) {
+            int c = 2 * p + 1;
+            if (c >= n) break;
+            if (c + 1 < n && before(heap_[c], heap_[c + 1])) c++;
+            if (!before(e, heap_[c])) break;
+            heap_[p] = heap_[c];
+            pos_[heap_[p].node] = p;
+            p = c;
+        }
+        heap_[p] = e;
+        pos_[e.node] = p;
+    }
+    std::vector<Entry> heap_;
+    std::vector<int> pos_;
     uint64_t seq_ = 0;
 };
 
@@ -249,8 +302,7 @@ void coarsener(const Graph& A, std::vector<int>& label, std::vector<double>& imp
             int I = A.col[p];
             if (A.nz[p] && q.contains(I)) {
                 double lam = lambda(I);
-                if (lam != imp[I]) {
-                    q.remove(I);
+                if (lam != imp[I]) {  // removed and re-inserted: the node's entry moves
                     imp[I] = lam;
                     q.insert(I, lam);
                 }
@@ -270,8 +322,7 @@ void coarsener(const Graph& A, std::vector<int>& label, std::vector<double>& imp
                 int J = S.idx[r];
                 if (label[J] == kUndecided) {
                     double lam = lambda(J);
-                    if (lam != imp[J]) {
-                        q.remove(J);
+                    if (lam != imp[J]) {  // (re-)inserted with its new key
                         imp[J] = lam;
                         q.insert(J, lam);
                     }
