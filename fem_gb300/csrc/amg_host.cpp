@@ -152,7 +152,7 @@ Graph graph_of(const Csr& A) {
 // (red_black_tree.c:174-197, :513-523, :620-658): keys compare with '>';
 // a new node goes after every node whose key is <= its own, and the largest
 // is the rightmost node, so among equal keys the latest insertion wins.  An
-// indexed binary heap on (key, insertion sequence) yields the same choice; it
+// indexed 4-ary heap on (key, insertion sequence) yields the same choice; it
 // holds one entry per queued node (a changed key moves the node's entry in
 // place), so it never grows past the level's size.
 class ImportanceQueue {
@@ -217,7 +217,7 @@ class ImportanceQueue {
     void up(int p) {
         Entry e = heap_[p];
         while (p > 0) {
-            const int q = (p - 1) >> 1;
+            const int q = (p - 1) >> 2;
             if (!before(heap_[q], e)) break;
             heap_[p] = heap_[q];
             pos_[heap_[p].node] = p;
@@ -230,9 +230,12 @@ class ImportanceQueue {
         const int n = (int)heap_.size();
         Entry e = heap_[p];
         for (;;) {
-            int c = 2 * p + 1;
-            if (c >= n) break;
-            if (c + 1 < n && before(heap_[c], heap_[c + 1])) c++;
+            const int c0 = 4 * p + 1;
+            if (c0 >= n) break;
+            int c = c0;
+            const int ce = std::min(n, c0 + 4);
+            for (int k = c0 + 1; k < ce; k++)
+                if (before(heap_[c], heap_[k])) c = k;
             if (!before(e, heap_[c])) break;
             heap_[p] = heap_[c];
             pos_[heap_[p].node] = p;
