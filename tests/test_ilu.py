@@ -147,6 +147,26 @@ def test_gpu_factors_full_size_match_restatement():
 
 @pytest.mark.gpu
 @pytest.mark.skipif(not gpu_available(), reason="no CUDA device")
+def test_gpu_factors_wide_levels_match_restatement():
+    """Two levels of 1,000 and 99,000 rows (every row past the first thousand couples to three of
+    them, symmetrically): 99,000 rows factorised concurrently by the row pool, bit-identical to the
+    C restatement."""
+    n, k = 100_000, 1_000
+    rng = np.random.default_rng(12)
+    rows = np.repeat(np.arange(k, n), 3)
+    cols = rng.integers(0, k, len(rows))
+    v = rng.uniform(-1, 1, len(rows))
+    A = sp.coo_matrix((v, (rows, cols)), shape=(n, n))
+    A = (A + A.T + sp.diags(10.0 + rng.random(n))).tocsr()
+    A.sum_duplicates()
+    A.sort_indices()
+    ilu = lina.ILU(n, A.indptr, A.indices, A.data)
+    assert ilu.levels()[0] == 2
+    assert np.array_equal(ilu.factor_values(), port.ilu0(A.indptr, A.indices, A.data))
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not gpu_available(), reason="no CUDA device")
 def test_gpu_apply_inverts_a_tridiagonal_matrix():
     """On a tridiagonal matrix ILU(0) is the exact LU factorisation, so the application solves
     A z = r: 1,000,000 rows (more than the GPU holds threads at once), nonsymmetric, one level per
