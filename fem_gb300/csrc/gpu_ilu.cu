@@ -219,7 +219,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int* e
     return bulk::mbar_wait(bar, parity, err, 4, kWaitNs);
 }
 
-// thread 0: bulk-copy level l's slices (16-byte aligned, sizes multiples of 16) into stage l % S;
+// the issuing thread: bulk-copy level l's slices (16-byte aligned, sizes multiples of 16) into stage l % S;
 // the stage's barrier completes when all bytes have landed
 template <typename TV, typename TX, int S>
 __device__ __forceinline__ void win_issue(const WinArgs<TV, TX>& a, unsigned char* stages, uint64_t* bars,
@@ -250,7 +250,10 @@ __global__ void __launch_bounds__(kWinThreads, 1) sptrsv_window_kernel(const Win
     TX* ring = reinterpret_cast<TX*>(win_smem + align16(8 * S));
     unsigned char* stages = win_smem + align16(8 * S) + align16((a.ringmask + 1) * (int)sizeof(TX));
     const WinLayout L = win_layout(a.max_rows, a.max_ent, sizeof(TX), sizeof(TV), a.dinv != nullptr);
-    if (tid == 0) {
+    // the copies are issued by the block's last thread: rows go to the lowest threads first, so on
+    // levels narrower than the block its warp has no row and the issue costs the level nothing
+    const int issuer = T - 1;
+    if (tid == issuer) {
         for (int k = 0; k < S; k++) bulk::mbar_init(bars + k);
         bulk::fence_mbar_init();
         for (int l = 0; l < S - 1 && l < a.nlev; l++) win_issue<TV, TX, S>(a, stages, bars, L, l, __ldg(a.bounds + l));
@@ -261,7 +264,7 @@ __global__ void __launch_bounds__(kWinThreads, 1) sptrsv_window_kernel(const Win
     int4 nb = S - 1 < a.nlev ? __ldg(a.bounds + S - 1) : make_int4(0, 0, 0, 0);
     for (int l = 0; l < a.nlev; l++) {
         // the stage of level l + S - 1 was read in level l - 1, which every thread has finished
-        if (tid == 0 && l + S - 1 < a.nlev) win_issue<TV, TX, S>(a, stages, bars, L, l + S - 1, nb);
+        if (tid == issuer && l + S - 1 < a.nlev) win_issue<TV, TX, S>(a, stages, bars, L, l + S - 1, nb);
         const int4 nb2 = l + S < a.nlev ? __ldg(a.bounds + l + S) : make_int4(0, 0, 0, 0);
         const int4 next = l + 1 < a.nlev ? __ldg(a.bounds + l + 1) : make_int4(0, 0, 0, 0);
         mbar_wait(bars + (l % S), (unsigned)((l / S) & 1), a.err);
@@ -290,7 +293,7 @@ __global__ void __launch_bounds__(kWinThreads, 1) sptrsv_window_kernel(const Win
     }
     // after a failed wait no copy of this block may still be landing when it exits: wait (bounded,
     // not cut short by the error) for the last stages' copies
-    if (tid == 0 && *(volatile int*)a.err)
+    if (tid == issuer && *(volatile int*)a.err)
         for (int l = a.nlev > S ? a.nlev - S : 0; l < a.nlev; l++)
             bulk::mbar_drain(bars + (l % S), (unsigned)((l / S) & 1), kWaitNs);
 }
