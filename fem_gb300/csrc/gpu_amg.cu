@@ -1220,11 +1220,14 @@ struct lina_gpu_amg {
             return LINA_GPU_EINVAL;
         }
         const int ncols = c.ncols > 0 ? c.ncols : c.n;
-        for (size_t k = 0; k < c.col.size(); k++)
-            if (c.col[k] < 0 || (c.col[k] >= ncols && c.val[k] != 0.0)) {
-                set_err("matrix entry with column %d outside [0, %d)", c.col[k], ncols);
-                return LINA_GPU_EINVAL;
-            }
+        long bad = -1;
+#pragma omp parallel for schedule(static) reduction(max : bad)
+        for (long k = 0; k < (long)c.col.size(); k++)
+            if (c.col[k] < 0 || (c.col[k] >= ncols && c.val[k] != 0.0)) bad = std::max(bad, k);
+        if (bad >= 0) {
+            set_err("matrix entry with column %d outside [0, %d)", c.col[bad], ncols);
+            return LINA_GPU_EINVAL;
+        }
         d.lanes = csrv_lanes_for(c);
         if (d.lanes > 0) {
             // CSR-vector: sanitise placeholder columns outside the operand, keep the CSR arrays
@@ -2626,8 +2629,13 @@ int lina_gpu_matrix_create(int n, int ncols, const int* rowptr, const int* col, 
     c.n = n;
     c.ncols = ncols;
     c.ptr.assign(rowptr, rowptr + n + 1);
-    c.col.assign(col, col + rowptr[n]);
-    c.val.assign(val, val + rowptr[n]);
+    c.col.resize(rowptr[n]);
+    c.val.resize(rowptr[n]);
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; i++) {
+        std::copy(col + rowptr[i], col + rowptr[i + 1], c.col.begin() + rowptr[i]);
+        std::copy(val + rowptr[i], val + rowptr[i + 1], c.val.begin() + rowptr[i]);
+    }
     std::vector<double> dinv(n, 0.0);
     std::vector<float> dinv32(n);
     m->nnz = rowptr[n];

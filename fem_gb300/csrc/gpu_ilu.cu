@@ -29,12 +29,14 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <climits>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "bulk_copy.cuh"
@@ -656,13 +658,20 @@ size_t win_smem(int ring, int max_rows, int max_ent, bool dinv, int stages) {
            (size_t)stages * win_layout(max_rows, max_ent, sizeof(TX), sizeof(TV), dinv).bytes;
 }
 
-bool build_window(lina_gpu_ilu* h, Factor& f, int n, const std::vector<int>& order, const std::vector<int>& lev,
-                  const std::vector<int>& lp, const std::vector<int>& beg, const std::vector<int>& end,
-                  const int* col, bool has_dinv) {
-    Factor::Win& w = f.win;
+// host side of a factor's window layout (plan_window) and its upload (upload_window); the plan
+// needs no device, so the plans of L and U can be made at the same time
+struct WinPlan {
+    Factor::Win w;
+    std::vector<int> head, row, enc, vperm, bounds;
+};
+
+void plan_window(WinPlan& pl, int n, const std::vector<int>& order, const std::vector<int>& lev,
+                 const std::vector<int>& lp, const std::vector<int>& beg, const std::vector<int>& end, const int* col,
+                 bool has_dinv) {
+    Factor::Win& w = pl.w;
     w = Factor::Win();
     const int nlev = (int)lp.size() - 1;
-    if (nlev <= 0) return true;
+    if (nlev <= 0) return;
     // padded positions and entries: every level starts at a multiple of 4 in both
     std::vector<int> P(nlev + 1, 0), Q(nlev + 1, 0), ecount(nlev, 0);
     long ptot = 0, qtot = 0;
@@ -674,7 +683,7 @@ bool build_window(lina_gpu_ilu* h, Factor& f, int n, const std::vector<int>& ord
         Q[l] = (int)qtot;
         ptot += (lp[l + 1] - lp[l] + 3) & ~3;
         qtot += (e + 3) & ~3;
-        if (ptot > INT32_MAX / 4 || qtot > INT32_MAX / 4) return true;  // too large: the row pool
+        if (ptot > INT32_MAX / 4 || qtot > INT32_MAX / 4) return;  // too large: the row pool
     }
     P[nlev] = (int)ptot;
     Q[nlev] = (int)qtot;
@@ -693,8 +702,17 @@ bool build_window(lina_gpu_ilu* h, Factor& f, int n, const std::vector<int>& ord
         if (win_smem<float, float>(ring, max_rows, max_ent, has_dinv, S) <= (size_t)kWinSmemMax) w.s32 = S;
     for (int S = kWinMaxStages; S >= 2 && w.s64 == 0; S--)
         if (win_smem<double, double>(ring, max_rows, max_ent, has_dinv, S) <= (size_t)kWinSmemMax) w.s64 = S;
-    if (w.s32 == 0 && w.s64 == 0) return true;
-    std::vector<int> head(ptot, 0), row(ptot, -1), enc(qtot, 0), vperm(qtot, -1), bounds(4 * (size_t)nlev);
+    if (w.s32 == 0 && w.s64 == 0) return;
+    pl.head.assign(ptot, 0);
+    pl.row.assign(ptot, -1);
+    pl.enc.assign(qtot, 0);
+    pl.vperm.assign(qtot, -1);
+    pl.bounds.assign(4 * (size_t)nlev, 0);
+    int* head = pl.head.data();
+    int* row = pl.row.data();
+    int* enc = pl.enc.data();
+    int* vperm = pl.vperm.data();
+    int* bounds = pl.bounds.data();
     int older = 0;
 #pragma omp parallel for schedule(dynamic, 16) reduction(| : older)
     for (int l = 0; l < nlev; l++) {
@@ -723,12 +741,20 @@ bool build_window(lina_gpu_ilu* h, Factor& f, int n, const std::vector<int>& ord
     w.npos = (int)ptot;
     if (w.s32) w.smem32 = win_smem<float, float>(ring, max_rows, max_ent, has_dinv, w.s32);
     if (w.s64) w.smem64 = win_smem<double, double>(ring, max_rows, max_ent, has_dinv, w.s64);
+}
+
+// the plan's arrays on the device; a factor without a plan (levels too wide or too large) keeps
+// the row pool
+bool upload_window(lina_gpu_ilu* h, Factor& f, const WinPlan& pl, bool has_dinv) {
+    Factor::Win& w = f.win;
+    w = pl.w;
+    if (!w.s32 && !w.s64) return true;
     Mem& m = h->mem;
-    w.bounds = m.up(bounds);
-    w.head = m.up(head);
-    w.row = m.up(row);
-    w.enc = m.up(enc);
-    w.vperm = m.up(vperm);
+    w.bounds = m.up(pl.bounds);
+    w.head = m.up(pl.head);
+    w.row = m.up(pl.row);
+    w.enc = m.up(pl.enc);
+    w.vperm = m.up(pl.vperm);
     w.val64 = m.get<double>(w.ne);
     w.val32 = m.get<float>(w.ne);
     bool ok = w.bounds && w.head && w.row && w.enc && w.vperm && w.val64 && w.val32;
@@ -750,6 +776,14 @@ bool build_window(lina_gpu_ilu* h, Factor& f, int n, const std::vector<int>& ord
         return false;
     }
     return true;
+}
+
+bool build_window(lina_gpu_ilu* h, Factor& f, int n, const std::vector<int>& order, const std::vector<int>& lev,
+                  const std::vector<int>& lp, const std::vector<int>& beg, const std::vector<int>& end,
+                  const int* col, bool has_dinv) {
+    WinPlan pl;
+    plan_window(pl, n, order, lev, lp, beg, end, col, has_dinv);
+    return upload_window(h, f, pl, has_dinv);
 }
 
 // the window's packed copies of a factor's values and inverse diagonal (after every factorisation)
@@ -952,9 +986,19 @@ int lina_gpu_ilu_create(int n, const int* Lptr, const int* Lcol, const double* L
     return 0;
 }
 
-// ILU(0) of A factorised on the device (bit-identical to the reference's incomplete_LU_factorization)
+// ILU(0) of A factorised on the device (bit-identical to the reference's incomplete_LU_factorization).
+// LINA_ILU_TIMING set: seconds per set-up phase on stderr (diagnostics).
 int lina_gpu_ilu_create_from_matrix(int n, const int* rowptr, const int* col, const double* val,
                                     lina_gpu_ilu** out) {
+    const bool timing = getenv("LINA_ILU_TIMING") != nullptr;
+    auto t_prev = std::chrono::steady_clock::now();
+    auto lap = [&](const char* what) {
+        if (!timing) return;
+        cudaStreamSynchronize(st());
+        const auto now = std::chrono::steady_clock::now();
+        fprintf(stderr, "ILU set-up %s %.1f ms\n", what, std::chrono::duration<double>(now - t_prev).count() * 1e3);
+        t_prev = now;
+    };
     if (!out || n <= 0 || !rowptr || !col || !val || rowptr[0] != 0) return LINA_GPU_EINVAL;
     *out = nullptr;
     const long nnz = rowptr[n];
@@ -983,8 +1027,17 @@ int lina_gpu_ilu_create_from_matrix(int n, const int* rowptr, const int* col, co
     h->n = n;
     h->fnnz = nnz;
     std::vector<int> lorder, uorder, llev, ulev, llp, ulp;
+    lap("pattern checks and splits");
+    // the level schedules and window plans of L and U are independent: U's on a second thread
+    WinPlan lplan, uplan;
+    std::thread upper([&] {
+        h->U.nlev = level_order(n, ubeg, uend, col, false, uorder, &ulev, &ulp);
+        plan_window(uplan, n, uorder, ulev, ulp, ubeg, uend, col, false);
+    });
     h->L.nlev = level_order(n, lbeg, lend, col, true, lorder, &llev, &llp);
-    h->U.nlev = level_order(n, ubeg, uend, col, false, uorder, &ulev, &ulp);
+    plan_window(lplan, n, lorder, llev, llp, lbeg, lend, col, true);
+    upper.join();
+    lap("level schedules and window plans");
     Mem& m = h->mem;
     int *dptr = nullptr, *dcol = nullptr, *ddiag = nullptr;
     double* dval = nullptr;
@@ -1012,11 +1065,11 @@ int lina_gpu_ilu_create_from_matrix(int n, const int* rowptr, const int* col, co
         delete h;
         return LINA_GPU_ECUDA;
     }
+    lap("uploads");
     h->L.col = h->U.col = dcol;
     h->L.val64 = h->U.val64 = h->fval;
     h->U.val32 = h->L.val32;
-    if (!build_window(h, h->L, n, lorder, llev, llp, lbeg, lend, col, true) ||
-        !build_window(h, h->U, n, uorder, ulev, ulp, ubeg, uend, col, false)) {
+    if (!upload_window(h, h->L, lplan, true) || !upload_window(h, h->U, uplan, false)) {
         lina::dev::set_error("ILU: device allocation failed");
         delete h;
         return LINA_GPU_ECUDA;
@@ -1031,11 +1084,13 @@ int lina_gpu_ilu_create_from_matrix(int n, const int* rowptr, const int* col, co
         delete h;
         return LINA_GPU_ECUDA;
     }
+    lap("window uploads");
     const int rc = factorise(h);
     if (rc) {
         delete h;
         return rc;
     }
+    lap("factorisation");
     *out = h;
     return 0;
 }
