@@ -65,6 +65,9 @@ def parse():
                    help="elasticity: the headline AMG-PCG solve (default); damage: the reflective-Newton "
                         "damage step on the same mesh; adjoint: the material-identification gradient; "
                         "batch: independent unstructured systems solved in one graph launch")
+    p.add_argument("--coarsening", default="standard", choices=["standard", "pmis"],
+                   help="standard: the reference's sequential coarsening (default); pmis: labels computed on "
+                        "the GPU (opt-in, other hierarchies)")
     p.add_argument("--sell-bits", type=int, default=16, choices=[16, 32],
                    help="column-index width of the SELL-32 matrices (16: offsets from two bases per slice)")
     p.add_argument("--batch-count", type=int, default=96, help="systems of the batch workload")
@@ -184,7 +187,8 @@ def run_gb300(args, rank, world, local):
         raise SystemExit("no CUDA device")
     s = build_system(m)
     t0 = time.perf_counter()
-    amg = lina.AMG.from_system(s, depth=depth, coarsening=lina.STANDARD, smoother=smoother, omega=omega,
+    coarsening = lina.PMIS if args.coarsening == "pmis" else lina.STANDARD
+    amg = lina.AMG.from_system(s, depth=depth, coarsening=coarsening, smoother=smoother, omega=omega,
                                precision=lina.PREC_MIXED, matrix_tol=args.matrix_tol)
     setup_s = time.perf_counter() - t0
     n = s.n
@@ -269,7 +273,7 @@ def run_gb300(args, rank, world, local):
         "config": {"workload": f"degraded plane-strain P1 elasticity {m}x{m} nodes, {n} dofs, "
                                f"AMG-PCG mixed precision to true rel-res {args.tol:g}",
                    "dofs": n, "nnz": int(s.nnz), "amg_depth": depth, "level_sizes": sizes,
-                   "coarsening": "standard", "matrix_tol": args.matrix_tol, "smoother": args.smoother,
+                   "coarsening": args.coarsening, "matrix_tol": args.matrix_tol, "smoother": args.smoother,
                    "omega": omega, "sweeps": "2+2", "sell_index_bits": args.sell_bits,
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs exceed L2 (finest matrix > 129 MB), no flush"},

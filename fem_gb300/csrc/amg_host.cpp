@@ -383,6 +383,21 @@ int standard_coarsening(const Csr& A, const std::vector<int>& lev, int dof, cons
     return coarse;
 }
 
+// PMIS labels (gpu_pmis.cu) with the reference's handling of points without strong dependencies
+// (standard_coarsening, Multigrid.c:506-548: isolated, or coarse) and its count of the coarse
+// level (isolated points counted as coarse).  -1 with err set if the device fails.
+int pmis_coarsening(const Csr& A, const Lists& S, const Lists& T, std::vector<int>& label, std::string& err) {
+    const int n = A.n;
+    label.assign(n, kUndecided);
+    for (int i = 0; i < n; i++)
+        if (S.size(i) == 0) label[i] = is_isolated(A, i) ? kIsolated : kCoarse;
+    if (!pmis_gpu(n, S.ptr, S.idx, T.ptr, T.idx, label, err)) return -1;
+    int coarse = 0;
+    for (int i = 0; i < n; i++)
+        if (label[i] == kCoarse || label[i] == kIsolated) coarse++;
+    return coarse;
+}
+
 // aggressive_coarsening (Multigrid.c:550-607) with Get_2nd_strong_connected
 // (:187-217), get_2nd_max_coupled (:99-119) and the distance-two pattern of
 // get_2nd_strong_connection_sets (:260-292).
@@ -1016,10 +1031,14 @@ bool amg_setup_host(const Csr& Ain, const AmgParams& p, HostHierarchy& h) {
         Lists T = transpose_lists(S, L.A.n);
         auto t1 = now();
         bool aggressive = (p.coarsening == kAggressive && i == depth - 1);
-        if (aggressive)
+        if (aggressive) {
             L.coarse_size = aggressive_coarsening(L.A, lev, p.dof, S, T, p.eps_minus, p.eps_plus, L.labels);
-        else
+        } else if (p.coarsening == kPmis) {
+            L.coarse_size = pmis_coarsening(L.A, S, T, L.labels, h.error);
+            if (L.coarse_size < 0) return false;
+        } else {
             L.coarse_size = standard_coarsening(L.A, lev, p.dof, S, T, L.labels, true);
+        }
         auto t2 = now();
         std::vector<int> map;
         int nc = coarse_map(L.labels, map);

@@ -16,7 +16,8 @@ namespace lina {
 
 // labels of LinA/Multigrid.h:23-27
 enum { kUndecided = 0, kCoarse = 1, kFine = 2, kIsolated = 3 };
-enum { kAggressive = 1, kStandard = 2 };
+// coarsenings: the reference's (LinA/Multigrid.h:29-31) and PMIS on the GPU (this library's, opt-in)
+enum { kAggressive = 1, kStandard = 2, kPmis = 3 };
 
 struct Csr {
     int n = 0;      // rows
@@ -32,7 +33,8 @@ struct AmgParams {
     int depth = 2;
     int smoothing_iterations = 2;
     int aggr_smoothing_iterations = 2;
-    int coarsening = kStandard;   // kAggressive: finest level coarsened aggressively
+    int coarsening = kStandard;   // kAggressive: finest level coarsened aggressively; kPmis: PMIS
+                                  // labels on every level (gpu_pmis.cu)
     double eps_minus = 0.3;       // strength thresholds (Multigrid.c:35-36)
     double eps_plus = 0.5;
     double matrix_tol = 0.1;      // interpolation truncation (Multigrid.c:37)
@@ -87,6 +89,12 @@ bool write_csr_file(const std::string& path, const Csr& A);
 bool read_csr_file(const std::string& path, Csr& A, int ncols);
 bool amg_save_host(const HostHierarchy& h, const std::string& dir, std::string& err);
 bool amg_load_host(const std::string& dir, HostHierarchy& h);
+
+// PMIS labels on the GPU (gpu_pmis.cu) from the strong-connection sets S (sptr, sidx) and their
+// transpose T: label holds kIsolated / kCoarse for the points decided beforehand and kUndecided
+// for the rest, and returns with every point decided.  False with err set if the device fails.
+bool pmis_gpu(int n, const std::vector<int>& sptr, const std::vector<int>& sidx, const std::vector<int>& tptr,
+              const std::vector<int>& tidx, std::vector<int>& label, std::string& err);
 
 // Greedy first-fit colouring of the symmetric nonzero graph (smoother ordering).
 int greedy_colouring(const Csr& A, std::vector<int>& colour);

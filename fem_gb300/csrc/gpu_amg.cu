@@ -2002,7 +2002,9 @@ static int amg_create_impl(int n, const int* rowptr, const int* col, const doubl
     p.depth = opt->depth;
     p.smoothing_iterations = opt->smoothing_iterations;
     p.aggr_smoothing_iterations = opt->aggr_smoothing_iterations;
-    p.coarsening = opt->coarsening == LINA_AGGRESSIVE ? lina::kAggressive : lina::kStandard;
+    p.coarsening = opt->coarsening == LINA_AGGRESSIVE ? lina::kAggressive
+                   : opt->coarsening == LINA_PMIS     ? lina::kPmis
+                                                      : lina::kStandard;
     p.eps_minus = opt->eps_minus;
     p.eps_plus = opt->eps_plus;
     p.matrix_tol = opt->matrix_tol;
@@ -2082,7 +2084,9 @@ int lina_gpu_amg_load(const char* dir, const lina_gpu_amg_options* opt, int host
     h->opt = *opt;
     h->opt.depth = p.depth;
     h->opt.dof = p.dof;
-    h->opt.coarsening = p.coarsening == lina::kAggressive ? LINA_AGGRESSIVE : LINA_STANDARD;
+    h->opt.coarsening = p.coarsening == lina::kAggressive ? LINA_AGGRESSIVE
+                        : p.coarsening == lina::kPmis     ? LINA_PMIS
+                                                          : LINA_STANDARD;
     h->opt.eps_minus = p.eps_minus;
     h->opt.eps_plus = p.eps_plus;
     h->opt.matrix_tol = p.matrix_tol;

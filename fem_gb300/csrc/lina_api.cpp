@@ -855,7 +855,7 @@ amg_system_info* AMG_setup(sparse_matrix* A, int deg_of_freedom, int depth, int 
     o.depth = depth;
     o.smoothing_iterations = smoothing_iterations;
     o.aggr_smoothing_iterations = aggr_smoothing_iterations;
-    o.coarsening = (coarsening == AGGRESSIVE) ? LINA_AGGRESSIVE : LINA_STANDARD;
+    o.coarsening = (coarsening == AGGRESSIVE) ? LINA_AGGRESSIVE : (coarsening == LINA_PMIS) ? LINA_PMIS : LINA_STANDARD;
     o.eps_minus = amg_eps_minus;
     o.eps_plus = amg_eps_plus;
     o.matrix_tol = amg_tol;

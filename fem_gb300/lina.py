@@ -16,7 +16,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libLinA_gb300.so")
 
-AGGRESSIVE, STANDARD = 1, 2
+AGGRESSIVE, STANDARD, PMIS = 1, 2, 3  # PMIS: labels computed on the GPU (opt-in, not the reference's)
 SMOOTHER_JACOBI, SMOOTHER_MC_SOR = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 STOP_REFERENCE, STOP_RELATIVE = 0, 1

@@ -28,9 +28,12 @@ extern "C" {
 #define LINA_GPU_EBREAKDOWN -4  /* Krylov breakdown (zero or NaN inner product) */
 #define LINA_GPU_ENOCONV -5     /* iteration limit reached before the tolerance */
 
-/* coarsening strategies, values of LinA/Multigrid.h:29-31 */
+/* coarsening strategies, values of LinA/Multigrid.h:29-31, and PMIS: an opt-in extension that
+   computes the C/F labels on the GPU as a parallel independent set (fast set-up; labels, and so
+   hierarchies and iteration counts, differ from the reference's sequential coarsening) */
 #define LINA_AGGRESSIVE 1
 #define LINA_STANDARD 2
+#define LINA_PMIS 3
 
 /* smoothers of the GPU V-cycle */
 #define LINA_SMOOTHER_JACOBI 0   /* damped Jacobi, x += w D^-1 (b - A x)                 */
@@ -63,7 +66,7 @@ typedef struct lina_gpu_amg_options {
     int depth;                     /* number of levels                                    */
     int smoothing_iterations;      /* sweeps per pre/post smoothing                       */
     int aggr_smoothing_iterations; /* sweeps on the finest level when coarsening is aggressive */
-    int coarsening;                /* LINA_AGGRESSIVE or LINA_STANDARD                    */
+    int coarsening;                /* LINA_AGGRESSIVE, LINA_STANDARD or LINA_PMIS         */
     double eps_minus, eps_plus;    /* strength thresholds (set_connection_thresholds)     */
     double matrix_tol;             /* interpolation truncation (AMG_set_matrix_tolerance) */
     int smoother;                  /* LINA_SMOOTHER_*                                     */
