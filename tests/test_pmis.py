@@ -110,3 +110,17 @@ def test_pmis_hierarchy_solves(precision):
     assert info.status == 0
     A = sp.csr_matrix((s.data, s.indices, s.indptr), shape=(s.n, s.n))
     assert np.linalg.norm(s.b - A @ x) <= 1e-7 * np.linalg.norm(s.b)
+
+
+def test_pmis_hierarchy_files_round_trip(tmp_path):
+    """A PMIS hierarchy saved and loaded keeps its coarsening and solves exactly as before."""
+    s = problems.poisson_p1(65, seed=3)
+    opts = dict(smoother=lina.SMOOTHER_JACOBI, omega=0.6, precision=lina.PREC_MIXED)
+    a = lina.AMG.from_system(s, depth=4, coarsening=lina.PMIS, **opts)
+    a.save(tmp_path / "h")
+    b = lina.AMG.load(tmp_path / "h", **opts)
+    assert a.sizes() == b.sizes()
+    x1, i1 = a.pcg(s.b, tol=1e-8, max_iter=300)
+    x2, i2 = b.pcg(s.b, tol=1e-8, max_iter=300)
+    assert i1.status == 0 and i1.iterations == i2.iterations
+    assert np.array_equal(x1, x2)
