@@ -402,7 +402,8 @@ def run_batch(args, rank, world, local):
     t_mesh = time.perf_counter() - t0
     t0 = time.perf_counter()
     # multicolour SOR: with damped Jacobi the large high-contrast elasticity systems stall
-    amgs = [lina.AMG.from_system(s, depth=problems.batch_depth(s.n), coarsening=lina.STANDARD,
+    coarsening = lina.PMIS if args.coarsening == "pmis" else lina.STANDARD
+    amgs = [lina.AMG.from_system(s, depth=problems.batch_depth(s.n), coarsening=coarsening,
                                  smoother=lina.SMOOTHER_MC_SOR, omega=1.0, precision=lina.PREC_MIXED,
                                  matrix_tol=args.batch_matrix_tol) for s in systems]
     t_setup = time.perf_counter() - t0
@@ -456,7 +457,8 @@ def run_batch(args, rank, world, local):
                       f"{args.tol:g}, one graph launch", value, "systems/s", world, args.steps, args.warmup, ms,
                       "f32 preconditioner / f64 Krylov", "synthetic (seeded Delaunay meshes, lognormal coefficients)",
                       {"workload": f"{n_sys} systems, half P1 Poisson and half P1 plane-strain elasticity on seeded "
-                                   "Delaunay meshes, dofs log-uniform on [10k, 500k], sigma 1.5; standard coarsening, "
+                                   "Delaunay meshes, dofs log-uniform on [10k, 500k], sigma 1.5; "
+                                   f"{args.coarsening} coarsening, "
                                    f"matrix_tol {args.batch_matrix_tol:g}, multicolour SOR 2+2; inputs larger than "
                                    "L2 (no flush)", "systems": n_sys, "dofs": dofs, "nnz": nnz},
                       {"value": e2e, "unit": "systems/s", "h2d_bytes_per_step": 8 * dofs,
