@@ -524,11 +524,14 @@ struct RowAcc {
     std::vector<double> val;
     std::vector<int> mark;
     std::vector<int> touched;
-    int id = 0;
-    explicit RowAcc(int n) : val(n, 0.0), mark(n, -1) {}
+    std::vector<uint64_t> bits;  // touched columns of the row as a bitmap (collect)
+    int id = 0, lo = 0, hi = -1;
+    explicit RowAcc(int n) : val(n, 0.0), mark(n, -1), bits((size_t)n / 64 + 1, 0) {}
     void begin() {
         id++;
         touched.clear();
+        lo = INT_MAX;
+        hi = -1;
     }
     void add(int c, double a) {
         if (mark[c] == id) {
@@ -537,16 +540,38 @@ struct RowAcc {
             mark[c] = id;
             val[c] = a;
             touched.push_back(c);
+            lo = std::min(lo, c);
+            hi = std::max(hi, c);
         }
     }
     void remove(int c) {
         if (mark[c] == id) mark[c] = -1;
     }
-    // present columns in increasing order with their values
+    // present columns in increasing order with their values.  The touched columns are ordered by
+    // a bitmap over their span when that is narrow (the usual case: a row's couplings are local),
+    // else by sorting.
     void collect(std::vector<int>& cols, std::vector<double>& vals) {
-        std::sort(touched.begin(), touched.end());
         cols.clear();
         vals.clear();
+        if (touched.empty()) return;
+        const int w0 = lo >> 6, w1 = hi >> 6;
+        if ((long)(w1 - w0 + 1) <= 8L * (long)touched.size()) {
+            for (int c : touched) bits[(size_t)c >> 6] |= 1ull << (c & 63);
+            for (int w = w0; w <= w1; w++) {
+                uint64_t m = bits[(size_t)w];
+                bits[(size_t)w] = 0;
+                while (m) {
+                    const int c = (w << 6) + __builtin_ctzll(m);
+                    m &= m - 1;
+                    if (mark[c] == id) {
+                        cols.push_back(c);
+                        vals.push_back(val[c]);
+                    }
+                }
+            }
+            return;
+        }
+        std::sort(touched.begin(), touched.end());
         int prev = -1;
         for (int c : touched) {
             if (c == prev) continue;
