@@ -48,7 +48,8 @@ DEFAULT_DEPTH = {65: 5, 129: 6, 257: 8, 513: 9, 1025: 10}
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--steps", type=int, default=None,
+                   help="timed steps (default 20; 5 for --impl reference, whose steps are CPU solves)")
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--m", type=int, default=1025, help="grid nodes per side")
@@ -74,7 +75,10 @@ def parse():
     p.add_argument("--batch-matrix-tol", type=float, default=0.3,
                    help="interpolation truncation of the batch workload's hierarchies (with 0.1 the "
                         "high-contrast elasticity systems need far more iterations)")
-    return p.parse_args()
+    a = p.parse_args()
+    if a.steps is None:
+        a.steps = 5 if a.impl == "reference" else 20
+    return a
 
 
 def dist_info():
