@@ -352,7 +352,8 @@ def run_adjoint(args, rank, world, local):
     m = 513 if args.m == 1025 else args.m
     case = problems.adjoint_case(m, seed=0)
     xy, tri, fd, fv = problems.elastic_mesh(m)
-    opts = dict(depth=DEFAULT_DEPTH.get(m, 8) - 1, precision=lina.PREC_MIXED)
+    opts = dict(depth=DEFAULT_DEPTH.get(m, 8) - 1, precision=lina.PREC_MIXED,
+                coarsening=lina.PMIS if args.coarsening == "pmis" else lina.STANDARD)
     probe = lina.ElasticAdjoint(xy, tri, 0.3, fd, fv, case["sensor_dof"], np.zeros(len(case["sensor_dof"])),
                                 case["young_target"], **opts)
     ut, _, _ = probe.forward(case["young_target"], tol=1e-10)
