@@ -1163,7 +1163,7 @@ struct lina_gpu_amg {
     std::vector<void*> allocations;
     // CUDA graph of one PCG iteration inside a device-side while loop
     cudaGraphExec_t gexec = nullptr;
-    int g_prec = -1, g_smoother = -1;
+    int g_prec = -1, g_smoother = -1, g_flexible = -1;
     double g_omega = 0.0;
     long g_kernels = 0;  // kernels per captured iteration
     void drop_graph() {
@@ -1717,9 +1717,17 @@ struct lina_gpu_amg {
     const DCsr& krylov_matrix() const { return has_signs ? Aorig : lv[depth - 1].A; }
 
     // one PCG iteration: z = M^-1 r (unless reused), s = r.z, p = z + beta p, q = A p, x/r update
+    // flexible beta (Polak-Ribiere form) by default for the mixed-precision preconditioner, whose FP32
+    // rounding makes it vary slightly from one application to the next; the reference's beta = s/s_old
+    // (PCGS.c:200) for FP64; LINA_PCG_BETA_* flags choose either explicitly
+    int beta_mode = -1;
+    int flexible_beta() const {
+        if (beta_mode >= 0) return beta_mode;
+        return opt.precision == LINA_PREC_MIXED ? 1 : 0;
+    }
     void issue_iteration(int n, bool precon, bool time_it) {
         const bool mixed = (opt.precision == LINA_PREC_MIXED);
-        const int flexible = mixed ? 1 : 0;
+        const int flexible = flexible_beta();
         const int gr = grid_red(n), gv = grid_for(n, kThreads);
         if (precon) precondition(kr, kz, time_it);
         if (mixed)
@@ -1738,7 +1746,9 @@ struct lina_gpu_amg {
 
     // capture issue_iteration + the loop test into a while-loop graph (cached per configuration)
     int ensure_graph(int n) {
-        if (gexec && g_prec == opt.precision && g_smoother == opt.smoother && g_omega == opt.omega) return 0;
+        if (gexec && g_prec == opt.precision && g_smoother == opt.smoother && g_omega == opt.omega &&
+            g_flexible == flexible_beta())
+            return 0;
         drop_graph();
         cudaGraph_t g = nullptr;
         CK(cudaGraphCreate(&g, 0));
@@ -1777,6 +1787,7 @@ struct lina_gpu_amg {
         g_prec = opt.precision;
         g_smoother = opt.smoother;
         g_omega = opt.omega;
+        g_flexible = flexible_beta();
         return 0;
     }
 };
@@ -2357,6 +2368,7 @@ int lina_gpu_pcg(lina_gpu_amg* h, const double* b_in, double* x_out, double tol,
     const bool dev = (flags & LINA_PCG_DEVICE_PTRS) != 0;
     const bool mixed = (h->opt.precision == LINA_PREC_MIXED);
     const bool time_it = (flags & LINA_PCG_TIME_KERNELS) != 0;
+    h->beta_mode = (flags & LINA_PCG_BETA_FLEXIBLE) ? 1 : (flags & LINA_PCG_BETA_STANDARD) ? 0 : -1;
     h->ev_used = 0;
     cudaStream_t st = h->stream;
     double *b = h->kb, *x = h->kx, *r = h->kr, *z = h->kz;
@@ -2475,6 +2487,7 @@ int lina_gpu_pcg(lina_gpu_amg* h, const double* b_in, double* x_out, double tol,
             if (converged || it >= max_iter) break;
         }
         inf->iterations = it;
+        inf->restarts = restarts;
         inf->rel_residual = rel;
         if (inf->status == 0 && rel > tol) inf->status = LINA_GPU_ENOCONV;
     }
@@ -2961,6 +2974,7 @@ int build_batch_graph(lina_gpu_batch* B) {
                                               cudaStreamCaptureModeRelaxed);
         if (e == cudaSuccess) {
             const unsigned long long before = g_launches;
+            h->beta_mode = -1;  // the precision's default beta
             h->issue_iteration(n, true, false);
             loop_cond_kernel<<<1, 1, 0, h->stream>>>(hd, h->sc);
             B->k_iter[s] = (long)(g_launches - before) + 1;

@@ -172,15 +172,13 @@ extern "C" int lina_gpu_dot(const double* a_dev, const double* b_dev, long n, do
 }
 
 // ---------------------------------------------------------------- allocation-free dot product
-// Some callers cannot allocate device memory at the point where they need a
-// reduction: code that runs while its stream is being captured into a CUDA
-// graph (cudaMalloc is not permitted during capture), a host function
-// enqueued with cudaLaunchHostFunc (which may not make CUDA calls that
-// allocate), or an integration whose device memory is fixed up front by the
-// host application.  lina_gpu_dot computes the same product but obtains its
-// partial-sum buffer from the library's allocator on first use;
-// lina_gpu_dot_noalloc keeps that scratch in a fixed array that the module
-// itself defines in device memory, so the call allocates nothing.
+// Some callers cannot allocate device memory where they need a reduction: an
+// application that reserves the GPU's memory for its own pool when it starts
+// (so a cudaMalloc in the middle of its time step fails or is forbidden), or a
+// job that runs under a hard device-memory quota.  lina_gpu_dot computes the
+// same product but obtains its partial-sum buffer from cudaMalloc on first
+// use; lina_gpu_dot_noalloc keeps that scratch in a fixed array that the
+// module itself defines in device memory, so the call allocates nothing.
 //
 // The array holds one partial sum per block of 2048 elements plus the result
 // and an arrival counter: 16,384 partials, so at most 33,554,432 elements per
@@ -189,9 +187,21 @@ extern "C" int lina_gpu_dot(const double* a_dev, const double* b_dev, long n, do
 // keeps the last call's contents; the arrival counter is cleared before every
 // launch.  Calls whose kernels overlap on the GPU (different streams, other
 // threads) race on the shared array and give wrong results: issue them one at
-// a time.  The first call on each device looks up the array's device address
-// with cudaGetSymbolAddress (with that device current); make that first call
-// before any stream capture begins.
+// a time.
+//
+// The call is synchronous: it waits for the library's own stream (the drop-in
+// BLAS-1 helpers may still be writing a or b there), runs on the legacy
+// default stream, and copies the result to the host.  It therefore cannot be
+// captured into a CUDA graph, and it may not be called from a host function
+// enqueued on a stream (such functions may make no CUDA calls).  Vectors that
+// the caller produced on its own non-blocking streams must be complete before
+// the call: synchronize those streams first.
+//
+// The first call on each device looks up the array's device address with
+// cudaGetSymbolAddress (with that device current) and keeps it for the life of
+// the process.  Make that first call before any stream capture begins.  A
+// cudaDeviceReset unloads the module and invalidates the kept address: do not
+// use this entry point after the host application resets the device.
 namespace {
 
 constexpr int kNoAllocThreads = 256;
@@ -278,6 +288,12 @@ extern "C" int lina_gpu_dot_noalloc(const double* a_dev, const double* b_dev, lo
     if (n == 0) {
         *result = 0.0;
         return 0;
+    }
+    // the library's drop-in vector helpers run on its non-blocking stream, which the legacy default
+    // stream does not wait for
+    if (lina::dev::g_stream && cudaStreamSynchronize(lina::dev::g_stream) != cudaSuccess) {
+        lina::dev::set_error("lina_gpu_dot_noalloc: waiting for the library's stream failed");
+        return LINA_GPU_ECUDA;
     }
     if (cudaMemsetAsync(scratch + kNoAllocCounter, 0, sizeof(double), 0) != cudaSuccess) {
         lina::dev::set_error("lina_gpu_dot_noalloc: clearing the arrival counter failed");

@@ -21,6 +21,7 @@ SMOOTHER_JACOBI, SMOOTHER_MC_SOR = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 STOP_REFERENCE, STOP_RELATIVE = 0, 1
 PCG_DEVICE_PTRS, PCG_USE_X0, PCG_FINAL_PRECON, PCG_TIME_KERNELS, PCG_NORMALIZE, PCG_HOST_LOOP = 1, 2, 4, 8, 16, 32
+PCG_BETA_FLEXIBLE, PCG_BETA_STANDARD = 256, 512
 UNDECIDED, COARSE, FINE, ISOLATED = 0, 1, 2, 3
 OK, EINVAL, ECUDA, ESETUP, EBREAKDOWN, ENOCONV = 0, -1, -2, -3, -4, -5
 ELASTIC_RECOMPUTE = 64
@@ -64,6 +65,7 @@ class SolveInfo(C.Structure):
         ("timed_level", C.c_int),
         ("timed_rows", C.c_int),
         ("timed_entries", C.c_long),
+        ("restarts", C.c_int),
     ]
 
 

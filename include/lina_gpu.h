@@ -58,6 +58,10 @@ extern "C" {
 #define LINA_PCG_NORMALIZE 16    /* scale b and x by 1/||b|| during the solve, as pcg does */
 #define LINA_PCG_HOST_LOOP 32    /* drive every iteration from the host instead of the captured
                                     CUDA graph with its device-side while loop              */
+#define LINA_PCG_BETA_FLEXIBLE 256  /* beta = -alpha_prev (z.q_prev) / s_old (flexible CG), the default
+                                       for LINA_PREC_MIXED                                   */
+#define LINA_PCG_BETA_STANDARD 512  /* beta = s / s_old (the reference's, LinA/PCGS.c:200), the default
+                                       for LINA_PREC_FP64                                    */
 
 typedef struct lina_gpu_amg lina_gpu_amg;
 
@@ -86,6 +90,7 @@ typedef struct lina_gpu_solve_info {
     int timed_level;               /* level of the timed sweeps: the one with most entries */
     int timed_rows;                /* its rows                                            */
     long timed_entries;            /* its stored entries                                  */
+    int restarts;                  /* restarts of the recurrence from the true residual   */
 } lina_gpu_solve_info;
 
 void lina_gpu_default_options(lina_gpu_amg_options* opt);
@@ -358,13 +363,18 @@ long lina_gpu_amg_device_bytes(const lina_gpu_amg* h);
 /* result = a . b for device vectors of n FP64 values: single-pass grid reduction (block partial
    sums in device scratch memory, the last block adds them in a fixed order) */
 int lina_gpu_dot(const double* a_dev, const double* b_dev, long n, double* result);
-/* The same product for callers that cannot allocate device memory (code running during a stream
-   capture into a CUDA graph, host functions enqueued on a stream, hosts whose device memory is fixed
-   in advance).  No counterpart in the reference.  Its scratch is a 128 KB array defined in device
-   memory by the library and kept on every GPU that loads it; n is limited to 33,554,432 elements
-   (larger n returns LINA_GPU_EINVAL).  It runs on the legacy default stream and returns the result
-   on the host.  All calls share the scratch array: calls that overlap on the GPU race.  The first
-   call on a device looks up the array's address and should come before any stream capture. */
+/* The same product for callers that cannot allocate device memory at the point of the call: an
+   application that reserves the GPU's memory for its own pool when it starts, or a job under a hard
+   device-memory quota, where a cudaMalloc during the computation fails or is not allowed.  No
+   counterpart in the reference.  Its scratch is a 128 KB array defined in device memory by the
+   library and kept on every GPU that loads it; n is limited to 33,554,432 elements (larger n returns
+   LINA_GPU_EINVAL).  The call is synchronous: it waits for the library's own stream, runs on the
+   legacy default stream and returns the result on the host, so it cannot be captured into a CUDA
+   graph nor called from a host function enqueued on a stream.  Inputs the caller wrote on its own
+   non-blocking streams must be complete (those streams synchronized) before the call.  All calls
+   share the scratch array: calls that overlap on the GPU race.  The first call on a device looks up
+   the array's address and keeps it; make it before any stream capture, and do not use this entry
+   point after a cudaDeviceReset. */
 int lina_gpu_dot_noalloc(const double* a_dev, const double* b_dev, long n, double* result);
 
 /* device memory helpers so that callers need no CUDA runtime of their own */

@@ -1,9 +1,10 @@
 """lina_gpu_dot_noalloc: the dot product for callers that cannot allocate device memory.
 
-Such callers (code running while its stream is captured into a CUDA graph, host
-functions enqueued on a stream, hosts with a fixed device-memory budget) get the
-same result as lina_gpu_dot, whose partial sums live in memory the library
-allocates; this entry point keeps them in a fixed device array instead.  The
+Such callers (an application that reserves the GPU's memory for its own pool at
+start-up, a job under a hard device-memory quota) cannot have the library call
+cudaMalloc in the middle of their computation.  They get the same result as
+lina_gpu_dot, whose partial sums live in memory the library allocates; this
+entry point keeps them in a fixed device array instead.  The
 test allocates its own input vectors (the caller still provides inputs and
 outputs) and compares the two entry points through the C-ABI on two calls in a
 row, since every call reuses the shared array.
