@@ -61,6 +61,8 @@ def parse():
                    help="interpolation truncation (AMG_set_matrix_tolerance); 0.1 is the reference default")
     p.add_argument("--cpu-seconds", type=float, default=20.0, help="bound of the CPU baseline sample")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--ref-sor", type=int, default=1,
+                   help="reference arm: also time one solve with the reference's lexicographic SOR (1) or not (0)")
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--workload", default="elasticity", choices=["elasticity", "damage", "adjoint", "batch"],
                    help="elasticity: the headline AMG-PCG solve (default); damage: the reflective-Newton "
@@ -165,20 +167,35 @@ def build_system(m):
     return problems.elasticity_p1(m)
 
 
-def cpu_baseline(amg, s, smoother, omega, full_iterations, tol, seconds):
-    """CPU restatement (oracle) of the same solve on the same hierarchy, bounded sample."""
+def cpu_baseline(args, s, depth, omega):
+    """The CPU baseline: the reference's set-up and FP64 pcg restated in C (oracle/), OpenMP over the host
+    cores, on the same system and settings; whole solves, as many as fit the time bound (at least one).
+    Returns the cpu_baseline record and the last solution (the FP64 oracle solution of this system)."""
     from oracle import port
-    kind = port.JACOBI if smoother == "jacobi" else port.MC_SOR
-    P = port.PortAMG(port.levels_from_amg(amg), kind, omega, 2, 2)
+    kind = port.JACOBI if args.smoother == "jacobi" else port.MC_SOR
     t0 = time.perf_counter()
-    x, it, _ = P.pcg(s.b, tol, 100000, 1, seconds)
-    dt = time.perf_counter() - t0
-    per_it = dt / max(it, 1)
-    value = 1.0 / (per_it * full_iterations)
+    P = port.PortAMG.setup(s, depth, 2, args.matrix_tol, kind, omega, 2, 2)
+    setup_s = time.perf_counter() - t0
+    times, its, x = [], [], None
+    while not times or (sum(times) < args.cpu_seconds and len(times) < 20):
+        t0 = time.perf_counter()
+        x, it, _ = P.pcg(s.b, args.tol, 2000, 1)
+        times.append(time.perf_counter() - t0)
+        its.append(it)
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
-            "sample": f"{it} PCG iterations ({dt:.1f} s) of the same FP64 solve on the same hierarchy, "
-                      f"scaled to a full solve of {full_iterations} iterations"}
+    rec = {"value": len(times) / sum(times), "unit": "solves/s", "cores": cores, "kind": "port",
+           "sample": f"{len(times)} whole FP64 solves ({its[0]} PCG iterations each, {sum(times):.1f} s) on the "
+                     f"hierarchy of the restated AMG_setup ({setup_s:.1f} s, not timed)",
+           "iterations": its[0], "setup_s": setup_s}
+    return rec, x
+
+
+def reference_digest(m):
+    """The reference's own results for the benchmark system, if committed (tests/golden)."""
+    path = os.path.join(ROOT, "tests", "golden", f"elast{m}_digest.npz")
+    if not os.path.exists(path):
+        return None
+    return np.load(path)
 
 
 def run_gb300(args, rank, world, local):
@@ -221,6 +238,7 @@ def run_gb300(args, rank, world, local):
     # kernel timing: the same solves again, driven iteration by iteration from the host with
     # CUDA events (on the library's stream) around every smoother sweep of the level with the most
     # stored entries, whose sweeps are the largest share of an iteration
+    x_mixed = x_dev.to_host()
     kinfos = [solve_dev(lina.PCG_TIME_KERNELS) for _ in range(args.steps)]
     sm_ms = sum(i.smoother_ms for i in kinfos)
     sm_n = sum(i.smoother_launches for i in kinfos)
@@ -256,17 +274,43 @@ def run_gb300(args, rank, world, local):
         ms64 = max_over_ranks(amg.timer_end(), world)
         k64 = [solve_dev(lina.PCG_TIME_KERNELS) for _ in range(2)]
         sm64 = sum(i.smoother_ms for i in k64) / max(1, sum(i.smoother_launches for i in k64))
+        x64 = x_dev.to_host()
         fp64 = {"value": world * args.steps / (ms64 / 1e3), "unit": "solves/s",
                 "iterations": [i.iterations for i in i64],
                 "true_rel_residual": max(i.true_rel_residual for i in i64),
                 "smoother_gbs": k64[0].smoother_bytes / (sm64 / 1e3) / 1e9 if sm64 else None}
         amg.set_smoother(smoother, omega, lina.PREC_MIXED)
 
+    # parity at this size: the reference's own FP64 pcg (its stopping rule ||r|| / ||M^-1 r0||) on the same
+    # system, from the committed digest, against both GPU paths under the same rule; solution errors
+    # against the FP64 oracle solution (the restated reference solve, whole vector) and against the
+    # reference's tight solve (tolerance 1e-13, its committed subsample)
+    parity = {}
+    g = reference_digest(m) if (depth == 10 and args.matrix_tol == 0.1 and args.smoother == "jacobi"
+                                and args.coarsening == "standard" and omega == 0.6) else None
+    if g is not None:
+        idx = g["sample_index"]
+        xt = g["tight_xs"]
+        ref_rule = {}
+        for prec, name in ((lina.PREC_MIXED, "mixed"), (lina.PREC_FP64, "fp64")):
+            amg.set_smoother(smoother, omega, prec)
+            xr, ir = amg.pcg(s.b, tol=args.tol, max_iter=2000, stop=lina.STOP_REFERENCE,
+                             flags=lina.PCG_NORMALIZE | lina.PCG_FINAL_PRECON)
+            ref_rule[name] = {"iterations": ir.iterations,
+                              "err_vs_ref_tight": float(np.linalg.norm(xr[idx] - xt) / np.linalg.norm(xt))}
+        amg.set_smoother(smoother, omega, lina.PREC_MIXED)
+        it_ref = int(g["pcg_jacobi_it"])
+        parity = {"reference_iterations": it_ref, "reference_rule": ref_rule,
+                  "mixed_iterations_vs_reference": ref_rule["mixed"]["iterations"] / it_ref,
+                  "err_vs_ref_tight": float(np.linalg.norm(x_mixed[idx] - xt) / np.linalg.norm(xt)),
+                  "reference_sor_iterations": int(g["pcg_refsor_it"]) if "pcg_refsor_it" in g else None}
     cpu = None
     if rank == 0 and not args.no_cpu:
-        full_it = fp64["iterations"][0] if fp64 else it_mixed[0]
-        cpu = cpu_baseline(amg, s, args.smoother, omega, full_it, args.tol, args.cpu_seconds)
+        cpu, x_port = cpu_baseline(args, s, depth, omega)
+        parity["err_vs_fp64_oracle"] = float(np.linalg.norm(x_mixed - x_port) / np.linalg.norm(x_port))
 
+    if cpu is not None and fp64 is not None:
+        parity["fp64_err_vs_fp64_oracle"] = float(np.linalg.norm(x64 - x_port) / np.linalg.norm(x_port))
     traffic = profiled_traffic()
     sizes = amg.sizes()
     out = {
@@ -274,14 +318,10 @@ def run_gb300(args, rank, world, local):
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 preconditioner / f64 Krylov",
         "data": "synthetic (seeded structured P1 mesh, notch damage field)",
-        "config": {"workload": f"degraded plane-strain P1 elasticity {m}x{m} nodes, {n} dofs, "
-                               f"AMG-PCG mixed precision to true rel-res {args.tol:g}",
-                   "dofs": n, "nnz": int(s.nnz), "amg_depth": depth, "level_sizes": sizes,
-                   "coarsening": args.coarsening, "matrix_tol": args.matrix_tol, "smoother": args.smoother,
-                   "omega": omega, "sweeps": "2+2", "sell_index_bits": args.sell_bits,
-                   "parallelism": "replicas" if world > 1 else "single GPU",
-                   "l2": "inputs exceed L2 (finest matrix > 129 MB), no flush"},
-        "iterations": it_mixed, "true_rel_residual": trr, "dofs_per_s": value * n, "setup_s": setup_s,
+        "config": workload_config(args, s, depth, omega, sizes),
+        "parallelism": "replicas" if world > 1 else "single GPU", "sell_index_bits": args.sell_bits,
+        "iterations": it_mixed, "restarts": max(i.restarts for i in infos), "true_rel_residual": trr,
+        "dofs_per_s": value * n, "setup_s": setup_s, "parity": parity,
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},
         "gpu_launches": int(launches),
         "fp64_gpu": fp64,
@@ -484,45 +524,79 @@ def run_batch(args, rank, world, local):
 
 
 def run_reference(args, rank, world):
-    """CPU implementation of the reference solve on the same workload (rank 0 only)."""
+    """The reference's CPU solve path on the same workload (rank 0 only): its AMG_setup and pcg restated
+    in C under oracle/ (amg_setup_port.c, lina_port.c; hierarchies, V-cycles and whole pcg solves
+    bit-identical to the reference compiled from its sources, tests/test_oracle_port.py), OpenMP over all
+    host cores where the reference's loops allow it.  The GPU library is not loaded.  Every timed step is
+    one whole solve; a second leg times the reference's default lexicographic SOR smoother."""
     if rank != 0:
         return
-    from fem_gb300 import lina
+    from fem_gb300 import problems  # numpy only: the seeded system
     from oracle import port
     m = args.m
     depth = args.depth or DEFAULT_DEPTH.get(m, 8)
     omega = args.omega or (0.6 if args.smoother == "jacobi" else 1.0)
     s = build_system(m)
-    # hierarchy: the library's host setup, identical to the reference's AMG_setup (pinned by tests)
-    amg = lina.AMG.from_system(s, host_only=True, depth=depth, coarsening=lina.STANDARD, matrix_tol=args.matrix_tol)
     kind = port.JACOBI if args.smoother == "jacobi" else port.MC_SOR
-    P = port.PortAMG(port.levels_from_amg(amg), kind, omega, 2, 2)
-    # one full solve fixes the iteration count of the workload
     t0 = time.perf_counter()
-    _, it_full, _ = P.pcg(s.b, args.tol, 2000, 1, 600.0)
-    t_full = time.perf_counter() - t0
-    per_it = [t_full / max(it_full, 1)]
-    sample_it = 2
-    for k in range(args.warmup + args.steps):
+    P = port.PortAMG.setup(s, depth, 2, args.matrix_tol, kind, omega, 2, 2)
+    setup_s = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        P.pcg(s.b, args.tol, 2000, 1)
+    times, its = [], []
+    x = None
+    for _ in range(args.steps):
         t0 = time.perf_counter()
-        _, it, _ = P.pcg(s.b, 0.0, sample_it, 1)
-        if k >= args.warmup:
-            per_it.append((time.perf_counter() - t0) / max(it, 1))
-    value = 1.0 / (statistics.median(per_it) * it_full)
+        x, it, _ = P.pcg(s.b, args.tol, 2000, 1)
+        times.append(time.perf_counter() - t0)
+        its.append(it)
+    total = sum(times)
+    value = args.steps / total
+    A = _csr_matvec(s)
+    trr = float(np.linalg.norm(s.b - A(x)) / np.linalg.norm(s.b))
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    sample = (f"one full solve ({it_full} iterations, {t_full:.1f} s) plus {args.steps} samples of {sample_it} "
-              f"iterations, scaled to a full solve")
+    # the reference's default smoother: lexicographic SOR (AMG_SOR_smoother, LinA/Multigrid.c:1345), omega 1,
+    # serial as in the reference; one whole solve
+    sor = None
+    if args.ref_sor:
+        Q = port.PortAMG.setup(s, depth, 2, args.matrix_tol, port.REF_SOR, 1.0, 2, 2)
+        t0 = time.perf_counter()
+        xs, it_s, _ = Q.pcg(s.b, args.tol, 2000, 1)
+        dt = time.perf_counter() - t0
+        sor = {"value": 1.0 / dt, "unit": "solves/s", "iterations": it_s, "seconds": dt,
+               "true_rel_residual": float(np.linalg.norm(s.b - A(xs)) / np.linalg.norm(s.b))}
+    sample = (f"{args.steps} whole FP64 solves ({sum(its)} PCG iterations, {total:.1f} s) after {args.warmup} "
+              f"untimed ones; hierarchy built by the restated AMG_setup in {setup_s:.1f} s (not timed)")
     out = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded structured P1 mesh, notch damage field)",
-           "impl": "reference",
-           "config": {"workload": f"degraded plane-strain P1 elasticity {m}x{m} nodes, {s.n} dofs, "
-                                  f"AMG-PCG to true rel-res {args.tol:g}", "dofs": s.n, "amg_depth": depth,
-                      "matrix_tol": args.matrix_tol,
-                      "smoother": args.smoother, "omega": omega},
+           "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded structured P1 mesh, notch damage field)", "impl": "reference",
+           "config": workload_config(args, s, depth, omega, P.sizes()),
+           "iterations": its, "true_rel_residual": trr, "setup_s": setup_s, "dofs_per_s": value * s.n,
            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample},
-           "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+           "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "reference_sor": sor}
     print(json.dumps(out))
+
+
+def _csr_matvec(s):
+    """y = A x for a CSR system with numpy only (residual checks outside the timed regions)."""
+    rows = np.repeat(np.arange(s.n), np.diff(s.indptr))
+
+    def mv(x):
+        return np.bincount(rows, weights=s.data * x[s.indices], minlength=s.n)
+    return mv
+
+
+def workload_config(args, s, depth, omega, sizes):
+    """The workload both arms run, described identically by both."""
+    m = args.m
+    return {"workload": f"degraded plane-strain P1 elasticity {m}x{m} nodes, {s.n} dofs, AMG-PCG "
+                        f"(one V-cycle per iteration) to true rel-res {args.tol:g}",
+            "dofs": s.n, "nnz": int(s.nnz), "amg_depth": depth, "level_sizes": [int(v) for v in sizes],
+            "coarsening": args.coarsening, "matrix_tol": args.matrix_tol, "smoother": args.smoother,
+            "omega": omega, "sweeps": "2+2", "tol": args.tol,
+            "l2": "inputs exceed L2 (finest matrix > 129 MB), no flush"}
 
 
 _pg = None

@@ -42,6 +42,7 @@ int g_fused_rows = 24576;
 // 16: SELL-32 matrices with long rows uploaded afterwards also get 16-bit column offsets (two bases
 // per slice, where every slice's columns fit), read by FP32 passes; 32: int columns only
 int g_sell_bits = 16;
+int g_quads = 1;  // FP32 passes read the quad layout (sellq_kernel); 0 keeps the one-entry SELL layout
 
 void set_err(const char* fmt, ...) {
     char buf[512];
@@ -136,10 +137,13 @@ __device__ void block_partial(double v, double* partials) {
 }
 
 // Krylov scalars kept on the device so that no host round trip sits between kernels.
+constexpr int kFcgMax = 8;  // longest direction history of the truncated flexible CG
 struct KScalars {
     double s, s_old, pq, t, rr, alpha, beta, r0, norm2, aux, tol;
     int iter;
     int maxit;
+    double tj[kFcgMax];   // z . q_{k-j}, j = 1..m (truncated flexible CG)
+    double pqh[kFcgMax];  // p_i . q_i of the kept directions, by history slot i mod m
 };
 
 // p.q from the block partials of an SpMV+dot launch, summed in block order by one block
@@ -299,6 +303,97 @@ __global__ void __launch_bounds__(kThreads) sell_kernel(int npos, int nrows, con
     if constexpr (MODE == M_DOT) block_partial(dot, partials);
 }
 
+// SELL-32 in quads, for the FP32 passes over natural-order matrices: slice s holds its 32 rows' entries
+// in groups of four consecutive entries of a row, group g of the row in lane l at sptr[s] / 4 + 32 g + l
+// (rows padded to a multiple of four with the row's own first column and value 0), values as float4 and
+// the four 16-bit column offsets (bases per slice, as in sell_kernel) as one uint2.  A lane moves 24 bytes
+// of matrix data per load pair where the one-entry layout moves 6, so the same registers keep four times
+// as many bytes in flight: measured on the 2.1M-dof elasticity hierarchy (GB300), the FP32 sweeps of
+// its long-row levels 7 and 8 went from 64-69 us to 52-60 us, level 6 from 27 to 20 us and the finest
+// level (14 entries per row, padded to 16) from 44 to 37 us.  Batches of two groups (eight entries) are
+// software-pipelined; at most 51 registers (five blocks of 256 per SM).  Entries are summed in stored
+// order, so the results equal sell_kernel's bit for bit.
+__device__ __forceinline__ int quad_col(unsigned d, int2 base) {
+    return ((d & 0x8000u) ? base.y : base.x) + (int)(d & 0x7fffu);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kThreads, 5) sellq_kernel(int n, const int* __restrict__ sptr,
+                                                            const int2* __restrict__ sbase,
+                                                            const uint2* __restrict__ col4,
+                                                            const float4* __restrict__ val4, const float* x,
+                                                            float* y, const float* __restrict__ b,
+                                                            const float* __restrict__ dinv, float w,
+                                                            const float* z) {
+    const int npos = ((n + 31) >> 5) << 5;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < npos; t += gridDim.x * blockDim.x) {
+        const int i = t;
+        if (i >= n) continue;
+        const int sl = t >> 5, lane = t & 31;
+        const int g0 = sptr[sl] >> 2;
+        const int ng = (sptr[sl + 1] - sptr[sl]) >> 7;  // groups of four per row
+        const int2 cb = __ldg(sbase + sl);
+        const uint2* cp = col4 + g0 + lane;
+        const float4* vp = val4 + g0 + lane;
+        float sum = 0.f;
+        int k = 0;
+        if (ng >= 2) {
+            uint2 c[2];
+            float4 v[2];
+#pragma unroll
+            for (int u = 0; u < 2; u++) c[u] = __ldcs(cp + 32 * u);
+#pragma unroll
+            for (int u = 0; u < 2; u++) v[u] = __ldcs(vp + 32 * u);
+            for (k = 2;; k += 2) {
+                float xv[8];
+#pragma unroll
+                for (int u = 0; u < 2; u++) {
+                    xv[4 * u + 0] = __ldg(x + quad_col(c[u].x & 0xffffu, cb));
+                    xv[4 * u + 1] = __ldg(x + quad_col(c[u].x >> 16, cb));
+                    xv[4 * u + 2] = __ldg(x + quad_col(c[u].y & 0xffffu, cb));
+                    xv[4 * u + 3] = __ldg(x + quad_col(c[u].y >> 16, cb));
+                }
+                const bool more = (k + 2 <= ng);
+                uint2 cn[2];
+                float4 vn[2];
+                if (more) {
+#pragma unroll
+                    for (int u = 0; u < 2; u++) cn[u] = __ldcs(cp + 32 * (k + u));
+#pragma unroll
+                    for (int u = 0; u < 2; u++) vn[u] = __ldcs(vp + 32 * (k + u));
+                }
+#pragma unroll
+                for (int u = 0; u < 2; u++) {
+                    sum += v[u].x * xv[4 * u];
+                    sum += v[u].y * xv[4 * u + 1];
+                    sum += v[u].z * xv[4 * u + 2];
+                    sum += v[u].w * xv[4 * u + 3];
+                }
+                if (!more) break;
+#pragma unroll
+                for (int u = 0; u < 2; u++) c[u] = cn[u], v[u] = vn[u];
+            }
+        }
+        for (; k < ng; k++) {
+            const uint2 c = __ldcs(cp + 32 * k);
+            const float4 v = __ldcs(vp + 32 * k);
+            sum += v.x * __ldg(x + quad_col(c.x & 0xffffu, cb));
+            sum += v.y * __ldg(x + quad_col(c.x >> 16, cb));
+            sum += v.z * __ldg(x + quad_col(c.y & 0xffffu, cb));
+            sum += v.w * __ldg(x + quad_col(c.y >> 16, cb));
+        }
+        if constexpr (MODE == M_SPMV) {
+            y[i] = sum;
+        } else if constexpr (MODE == M_RESID) {
+            y[i] = b[i] - sum;
+        } else if constexpr (MODE == M_JACOBI) {
+            y[i] = x[i] + w * dinv[i] * (b[i] - sum);
+        } else if constexpr (MODE == M_ADD) {
+            y[i] = z[i] + sum;
+        }
+    }
+}
+
 // CSR with a group of S lanes per row, for levels whose rows are long (dense
 // coarse operators) or too few to fill the GPU one thread per row.  Lanes of a
 // group read consecutive entries of their row (coalesced); `rows` lists the
@@ -455,13 +550,18 @@ __global__ void fix_isolated_kernel(int n, const double* __restrict__ b, const d
 // refresh the Jacobi diagonal and the isolated-row inverses
 __global__ void update_values_kernel(long nnz, const double* __restrict__ val, const int* __restrict__ posA,
                                      const int* __restrict__ posAcol, double* __restrict__ a64,
-                                     float* __restrict__ a32, double* __restrict__ c64, float* __restrict__ c32) {
+                                     float* __restrict__ a32, double* __restrict__ c64, float* __restrict__ c32,
+                                     const int* __restrict__ posQ, float* __restrict__ q32) {
     for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (long)gridDim.x * blockDim.x) {
         const double v = val[k];
         const int p = posA[k];
         if (p >= 0) {
             a64[p] = v;
             a32[p] = float(v);
+        }
+        if (posQ) {
+            const int q = posQ[k];
+            if (q >= 0) q32[q] = float(v);
         }
         if (posAcol) {
             const int q = posAcol[k];
@@ -564,12 +664,118 @@ __global__ void update_p_kernel(int n, const TZ* __restrict__ z, double* __restr
     for (; i < n; i += S) p[i] = double(z[i]) + beta * p[i];
 }
 
-// alpha = s / (p.q); x += alpha p; r -= alpha q; rr = r.r
+// Truncated flexible CG (Notay's FCG(m)): the new direction is made A-orthogonal to the last m
+// directions, p_k = z - sum_{j=1..min(k,m)} (z.q_{k-j} / p_{k-j}.q_{k-j}) p_{k-j}.  With a preconditioner
+// that varies slightly between applications (the FP32 V-cycle's rounding) the longer orthogonalisation
+// keeps the convergence of CG with an exact preconditioner; m = 1 is the flexible CG above.  The
+// kept directions p_i and q_i = A p_i live in rings of m slots (slot i mod m), written by
+// update_xr_kernel; the slots are found from the device's iteration counter, so the captured graph
+// needs no pointer changes.
+
+// s_old = s; s = r.z; tj[j-1] = z.q_{k-j}, j = 1..min(k, M)
+template <typename TZ, int M>
+__global__ void __launch_bounds__(kThreads) fcg_dot_kernel(int n, const double* __restrict__ r,
+                                                           const TZ* __restrict__ z, const double* __restrict__ qh,
+                                                           double* partials, unsigned* ticket, KScalars* sc) {
+    const int k = sc->iter;
+    const int nprev = k < M ? k : M;
+    const double* qs[M];
+#pragma unroll
+    for (int j = 1; j <= M; j++) qs[j - 1] = qh + (size_t)((k - j + M * kFcgMax) % M) * n;
+    double v[M + 1];
+#pragma unroll
+    for (int j = 0; j <= M; j++) v[j] = 0.0;
+    // U grid strides per loop trip, all loads of a trip issued before the products (independent loads
+    // in flight); the sums are taken in a fixed order
+    constexpr int U = (M <= 3) ? 4 : 2;
+    const long S = (long)gridDim.x * blockDim.x;
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + (U - 1) * S < n; i += U * S) {
+        double zz[U], rr[U], qq[M][U];
+#pragma unroll
+        for (int u = 0; u < U; u++) zz[u] = double(z[i + u * S]), rr[u] = r[i + u * S];
+#pragma unroll
+        for (int j = 1; j <= M; j++)
+#pragma unroll
+            for (int u = 0; u < U; u++) qq[j - 1][u] = (j <= nprev) ? qs[j - 1][i + u * S] : 0.0;
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            v[0] += rr[u] * zz[u];
+#pragma unroll
+            for (int j = 1; j <= M; j++) v[j] += zz[u] * qq[j - 1][u];
+        }
+    }
+    for (; i < n; i += S) {
+        const double zi = double(z[i]);
+        v[0] += r[i] * zi;
+#pragma unroll
+        for (int j = 1; j <= M; j++)
+            if (j <= nprev) v[j] += zi * qs[j - 1][i];
+    }
+    grid_reduce<M + 1>(v, partials, ticket, [sc](double* t) {
+        sc->s_old = sc->s;
+        sc->s = t[0];
+#pragma unroll
+        for (int j = 1; j <= M; j++) sc->tj[j - 1] = t[j];
+    });
+}
+
+// p_k = z - sum_j (tj[j-1] / pqh[(k-j) mod M]) p_{k-j}
+template <typename TZ, int M>
+__global__ void fcg_update_p_kernel(int n, const TZ* __restrict__ z, const double* __restrict__ ph,
+                                    double* __restrict__ p, const KScalars* sc) {
+    const int k = sc->iter;
+    const int nprev = k < M ? k : M;
+    double c[M];
+    const double* ps[M];
+#pragma unroll
+    for (int j = 1; j <= M; j++) {
+        const int slot = (k - j + M * kFcgMax) % M;
+        c[j - 1] = (j <= nprev) ? sc->tj[j - 1] / sc->pqh[slot] : 0.0;
+        ps[j - 1] = ph + (size_t)slot * n;
+    }
+    constexpr int U = (M <= 3) ? 4 : 2;
+    const long S = (long)gridDim.x * blockDim.x;
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + (U - 1) * S < n; i += U * S) {
+        double pp[U], hh[M][U];
+#pragma unroll
+        for (int u = 0; u < U; u++) pp[u] = double(z[i + u * S]);
+#pragma unroll
+        for (int j = 1; j <= M; j++)
+#pragma unroll
+            for (int u = 0; u < U; u++) hh[j - 1][u] = (j <= nprev) ? ps[j - 1][i + u * S] : 0.0;
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+#pragma unroll
+            for (int j = 1; j <= M; j++) pp[u] -= c[j - 1] * hh[j - 1][u];
+            p[i + u * S] = pp[u];
+        }
+    }
+    for (; i < n; i += S) {
+        double pi = double(z[i]);
+#pragma unroll
+        for (int j = 1; j <= M; j++)
+            if (j <= nprev) pi -= c[j - 1] * ps[j - 1][i];
+        p[i] = pi;
+    }
+}
+
+// alpha = s / (p.q); x += alpha p; r -= alpha q; rr = r.r.  With a direction history (hm > 0) p and
+// q are also stored in slot iter mod hm of the rings ph, qh, and p.q in sc->pqh.
 __global__ void __launch_bounds__(kThreads) update_xr_kernel(int n, double* __restrict__ x, double* __restrict__ r,
                                                              const double* __restrict__ p,
                                                              const double* __restrict__ q, double* partials,
-                                                             unsigned* ticket, KScalars* sc) {
+                                                             unsigned* ticket, KScalars* sc, int hm,
+                                                             double* __restrict__ ph, double* __restrict__ qh) {
     const double alpha = sc->s / sc->pq;
+    double* hp = nullptr;
+    double* hq = nullptr;
+    if (hm > 0) {
+        const size_t slot = (size_t)(sc->iter % hm);
+        hp = ph + slot * n;
+        hq = qh + slot * n;
+    }
     double v[1] = {0.0};
     const long S = (long)gridDim.x * blockDim.x;
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -589,16 +795,29 @@ __global__ void __launch_bounds__(kThreads) update_xr_kernel(int n, double* __re
             r[i + u * S] = ri;
             v[0] += ri * ri;
         }
+        if (hp) {
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                hp[i + u * S] = pp[u];
+                hq[i + u * S] = qq[u];
+            }
+        }
     }
     for (; i < n; i += S) {
-        x[i] += alpha * p[i];
-        const double ri = r[i] - alpha * q[i];
+        const double pi = p[i], qi = q[i];
+        x[i] += alpha * pi;
+        const double ri = r[i] - alpha * qi;
         r[i] = ri;
         v[0] += ri * ri;
+        if (hp) {
+            hp[i] = pi;
+            hq[i] = qi;
+        }
     }
-    grid_reduce<1>(v, partials, ticket, [sc, alpha](double* t) {
+    grid_reduce<1>(v, partials, ticket, [sc, alpha, hm](double* t) {
         sc->rr = t[0];
         sc->alpha = alpha;
+        if (hm > 0) sc->pqh[sc->iter % hm] = sc->pq;
         sc->iter += 1;
     });
 }
@@ -915,6 +1134,13 @@ struct DCsr {
     double* v64 = nullptr;
     float* v32 = nullptr;
     int* rowmap = nullptr;          // row of each position (-1 = padding), null = natural order
+    // SELL-32 in quads with 16-bit offsets (sellq_kernel), for the FP32 passes in natural order; null
+    // when the matrix is colour-grouped, uses the lane-group layout, or a slice's columns do not fit
+    int* q_sptr = nullptr;
+    int2* q_base = nullptr;
+    uint2* q_col = nullptr;
+    float4* q_val = nullptr;
+    long q_padded = 0;
     std::vector<int> group_slice;   // colour c occupies slices [group_slice[c], group_slice[c+1])
     // CSR-vector layout (lanes > 0): CSR arrays and, for colour groups, the rows of each colour
     int lanes = 0;
@@ -1047,6 +1273,92 @@ SellHost make_sell(const lina::Csr& A, int ncols, const std::vector<std::vector<
 // column of its rows, base.y = the smallest column beyond base.x + 32767 (base.x if none).  Fails
 // (false) if some slice has a column beyond both windows.  Entries of padding positions (rows past
 // the end, or -1 in the colour order) are never read and hold 0.
+// The quad layout of sellq_kernel for a natural-order matrix: pos[k] receives each CSR entry's stored
+// position (-1 for an explicit zero whose column lies outside the operand, stored as padding).  False
+// when some slice's columns do not fit two windows of 32,768.
+struct QuadHost {
+    std::vector<int> sptr;
+    std::vector<int2> base;
+    std::vector<unsigned short> col;  // four per group
+    std::vector<float> val;
+    std::vector<int> pos;
+};
+
+bool make_quads(const lina::Csr& A, int ncols, QuadHost& Q) {
+    const int n = A.n, ns = (n + 31) / 32;
+    Q.sptr.assign(ns + 1, 0);
+    for (int s = 0; s < ns; s++) {
+        int len = 0;
+        for (int l = 0; l < 32 && 32 * s + l < n; l++) len = std::max(len, A.ptr[32 * s + l + 1] - A.ptr[32 * s + l]);
+        len = (len + 3) / 4 * 4;
+        if ((long)Q.sptr[s] + 32L * len > (long)INT_MAX) return false;
+        Q.sptr[s + 1] = Q.sptr[s] + 32 * len;
+    }
+    const size_t total = (size_t)Q.sptr[ns];
+    Q.col.assign(total, 0);
+    Q.val.assign(total, 0.f);
+    Q.base.assign(ns, make_int2(0, 0));
+    Q.pos.assign(A.nnz(), -1);
+    int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
+    for (int s = 0; s < ns; s++) {
+        const size_t p0 = (size_t)Q.sptr[s];
+        const int len = (Q.sptr[s + 1] - Q.sptr[s]) / 32;
+        // the two 16-bit windows of the slice, from its rows' columns inside the operand
+        int lo = INT_MAX, hi = INT_MAX;
+        for (int l = 0; l < 32 && 32 * s + l < n; l++) {
+            const int r = 32 * s + l;
+            for (int p = A.ptr[r]; p < A.ptr[r + 1]; p++)
+                if (A.col[p] < ncols) lo = std::min(lo, A.col[p]);
+        }
+        if (lo == INT_MAX) lo = 0;
+        for (int l = 0; l < 32 && 32 * s + l < n; l++) {
+            const int r = 32 * s + l;
+            for (int p = A.ptr[r]; p < A.ptr[r + 1]; p++)
+                if (A.col[p] < ncols && (long)A.col[p] - lo > 32767) hi = std::min(hi, A.col[p]);
+        }
+        if (hi == INT_MAX) hi = lo;
+        Q.base[s] = make_int2(lo, hi);
+        auto code = [&](int c, int& out) {
+            if ((long)c - lo <= 32767) {
+                out = c - lo;
+                return true;
+            }
+            if (c >= hi && (long)c - hi <= 32767) {
+                out = 0x8000 | (c - hi);
+                return true;
+            }
+            return false;
+        };
+        for (int l = 0; l < 32; l++) {
+            const int r = 32 * s + l;
+            const bool valid = r < n;
+            const int rl = valid ? A.ptr[r + 1] - A.ptr[r] : 0;
+            int pad = lo;
+            for (int k = 0; k < rl; k++)
+                if (A.col[A.ptr[r] + k] < ncols) {
+                    pad = A.col[A.ptr[r] + k];
+                    break;
+                }
+            for (int k = 0; k < len; k++) {
+                const size_t q = p0 + (size_t)128 * (k / 4) + 4 * (size_t)l + (k % 4);
+                int c = pad;
+                float v = 0.f;
+                if (k < rl && A.col[A.ptr[r] + k] < ncols) {
+                    c = A.col[A.ptr[r] + k];
+                    v = (float)A.val[A.ptr[r] + k];
+                    Q.pos[A.ptr[r] + k] = (int)q;
+                }
+                int e = 0;
+                if (!code(c, e)) bad = 1;
+                Q.col[q] = (unsigned short)e;
+                Q.val[q] = v;
+            }
+        }
+    }
+    return !bad;
+}
+
 bool encode_sell16(const SellHost& S, int nrows, std::vector<unsigned short>& c16, std::vector<int2>& base) {
     const int ns = (int)S.sptr.size() - 1;
     c16.assign(S.col.size(), 0);
@@ -1147,12 +1459,17 @@ struct lina_gpu_amg {
     bool upd_built = false;
     long upd_nnz = 0;
     int *upd_posA = nullptr, *upd_posAcol = nullptr, *upd_diagpos = nullptr, *upd_ptr = nullptr;
+    int* upd_posQ = nullptr;  // quad-layout positions of the finest matrix's entries (when it has that layout)
     unsigned char* upd_isolated = nullptr;
     double* upd_val = nullptr;  // staging for host values
     // Krylov work
     double *kr = nullptr, *kz = nullptr, *kp = nullptr, *kq = nullptr, *kx = nullptr, *kb = nullptr,
            *kt = nullptr;
     float* kz32 = nullptr;
+    // truncated flexible CG: directions kept (0: the precision's default), and their rings
+    int fcg_m = 0;
+    int hist_m = 0;  // slots allocated in kph / kqh
+    double *kph = nullptr, *kqh = nullptr;
     double* partials = nullptr;
     unsigned* ticket = nullptr;
     KScalars* sc = nullptr;
@@ -1163,7 +1480,7 @@ struct lina_gpu_amg {
     std::vector<void*> allocations;
     // CUDA graph of one PCG iteration inside a device-side while loop
     cudaGraphExec_t gexec = nullptr;
-    int g_prec = -1, g_smoother = -1, g_flexible = -1;
+    int g_prec = -1, g_smoother = -1, g_flexible = -1, g_history = -1;
     double g_omega = 0.0;
     long g_kernels = 0;  // kernels per captured iteration
     void drop_graph() {
@@ -1210,7 +1527,7 @@ struct lina_gpu_amg {
     // pos_out (optional): the stored position of every CSR entry (-1: not stored), empty for the
     // lane-group layout, whose positions are the CSR order
     int upload_csr(DCsr& d, const lina::Csr& c, const std::vector<std::vector<int>>* groups = nullptr,
-                   std::vector<int>* pos_out = nullptr) {
+                   std::vector<int>* pos_out = nullptr, std::vector<int>* qpos_out = nullptr) {
         d = DCsr();
         d.n = c.n;
         d.ncols = c.ncols;
@@ -1295,6 +1612,19 @@ struct lina_gpu_amg {
         if (groups) {
             if ((rc = upload(&d.rowmap, S.rowmap.data(), S.rowmap.size()))) return rc;
         }
+        // FP32 passes in natural order read the quad layout (sellq_kernel) where the columns fit 16 bits
+        QuadHost Q;
+        if (!groups && g_sell_bits == 16 && g_quads && make_quads(c, ncols, Q)) {
+            if ((rc = upload(&d.q_sptr, Q.sptr.data(), Q.sptr.size()))) return rc;
+            if ((rc = upload(&d.q_base, Q.base.data(), Q.base.size()))) return rc;
+            if ((rc = alloc(&d.q_col, Q.col.size() / 4))) return rc;
+            if ((rc = alloc(&d.q_val, Q.val.size() / 4))) return rc;
+            CK(cudaMemcpyAsync(d.q_col, Q.col.data(), Q.col.size() * sizeof(unsigned short), cudaMemcpyHostToDevice,
+                               stream));
+            CK(cudaMemcpyAsync(d.q_val, Q.val.data(), Q.val.size() * sizeof(float), cudaMemcpyHostToDevice, stream));
+            d.q_padded = (long)Q.val.size();
+            if (qpos_out) qpos_out->swap(Q.pos);
+        }
         // the host copies must outlive the asynchronous uploads
         return cudaStreamSynchronize(stream) == cudaSuccess ? 0 : LINA_GPU_ECUDA;
     }
@@ -1330,6 +1660,14 @@ struct lina_gpu_amg {
         // natural order: rows of this range are [32 slice0, n); colour order: the row map marks padding
         const int nrows = rm ? m.n : m.n - 32 * slice0;
         const int* sp = m.sptr + slice0;
+        if constexpr (sizeof(TX) == 4 && (MODE == M_SPMV || MODE == M_RESID || MODE == M_JACOBI || MODE == M_ADD)) {
+            if (m.q_val && !m.rowmap && slice0 == 0 && 32 * slice1 >= m.n) {
+                sellq_kernel<MODE><<<grid, kThreads, 0, stream>>>(m.n, m.q_sptr, m.q_base, m.q_col, m.q_val,
+                                                                  (const float*)x, (float*)y, (const float*)b,
+                                                                  (const float*)dinv, (float)w, (const float*)z);
+                return;
+            }
+        }
         if (sizeof(TX) == 4 && m.col16) {
             const int2* sb = m.sbase + slice0;
             if (m.long_rows)
@@ -1725,11 +2063,71 @@ struct lina_gpu_amg {
         if (beta_mode >= 0) return beta_mode;
         return opt.precision == LINA_PREC_MIXED ? 1 : 0;
     }
+    // directions kept by the Krylov loop: FCG(m) for m >= 2 (mixed precision by default, where the FP32
+    // V-cycle's rounding makes the preconditioner vary), 1 for the two-term recurrences above
+    int history() const {
+        if (beta_mode >= 0) return 1;  // an explicitly chosen two-term recurrence
+        if (fcg_m > 0) return fcg_m;
+        return opt.precision == LINA_PREC_MIXED ? kFcgDefault : 1;
+    }
+    static constexpr int kFcgDefault = 4;
+    // the rings of kept directions (allocated before any capture)
+    int ensure_history() {
+        const int m = history();
+        if (m < 2 || hist_m >= m) return 0;
+        const size_t n = (size_t)lv[depth - 1].n;
+        int rc;
+        if ((rc = alloc(&kph, (size_t)m * n))) return rc;
+        if ((rc = alloc(&kqh, (size_t)m * n))) return rc;
+        hist_m = m;
+        return 0;
+    }
+    template <int M>
+    void issue_fcg_dots(int n, bool mixed, int gr) {
+        if (mixed)
+            go(fcg_dot_kernel<float, M>, gr, stream, n, (const double*)kr, (const float*)kz32, (const double*)kqh,
+               partials, ticket, sc);
+        else
+            go(fcg_dot_kernel<double, M>, gr, stream, n, (const double*)kr, (const double*)kz, (const double*)kqh,
+               partials, ticket, sc);
+    }
+    template <int M>
+    void issue_fcg_p(int n, bool mixed, int gv) {
+        if (mixed)
+            go(fcg_update_p_kernel<float, M>, gv, stream, n, (const float*)kz32, (const double*)kph, kp,
+               (const KScalars*)sc);
+        else
+            go(fcg_update_p_kernel<double, M>, gv, stream, n, (const double*)kz, (const double*)kph, kp,
+               (const KScalars*)sc);
+    }
     void issue_iteration(int n, bool precon, bool time_it) {
         const bool mixed = (opt.precision == LINA_PREC_MIXED);
         const int flexible = flexible_beta();
         const int gr = grid_red(n), gv = grid_for(n, kThreads);
         if (precon) precondition(kr, kz, time_it);
+        const int m = history();
+        if (m >= 2 && hist_m >= m) {
+            switch (m) {
+#define LINA_FCG_CASE(MM)              \
+    case MM:                           \
+        issue_fcg_dots<MM>(n, mixed, gr); \
+        issue_fcg_p<MM>(n, mixed, gv);  \
+        break;
+                LINA_FCG_CASE(2)
+                LINA_FCG_CASE(3)
+                LINA_FCG_CASE(4)
+                LINA_FCG_CASE(5)
+                LINA_FCG_CASE(6)
+                LINA_FCG_CASE(7)
+                default:
+                    LINA_FCG_CASE(8)
+#undef LINA_FCG_CASE
+            }
+            csr<double, M_DOT>(krylov_matrix(), kp, kq);
+            go(update_xr_kernel, gr, stream, n, kx, kr, (const double*)kp, (const double*)kq, partials, ticket, sc,
+               m, kph, kqh);
+            return;
+        }
         if (mixed)
             go(dot_rz_kernel<float>, gr, stream, n, (const double*)kr, (const float*)kz32, (const double*)kq, flexible,
                partials, ticket, sc);
@@ -1741,13 +2139,14 @@ struct lina_gpu_amg {
         else
             go(update_p_kernel<double>, gv, stream, n, (const double*)kz, kp, flexible, sc);
         csr<double, M_DOT>(krylov_matrix(), kp, kq);
-        go(update_xr_kernel, gr, stream, n, kx, kr, (const double*)kp, (const double*)kq, partials, ticket, sc);
+        go(update_xr_kernel, gr, stream, n, kx, kr, (const double*)kp, (const double*)kq, partials, ticket, sc, 0,
+           (double*)nullptr, (double*)nullptr);
     }
 
     // capture issue_iteration + the loop test into a while-loop graph (cached per configuration)
     int ensure_graph(int n) {
         if (gexec && g_prec == opt.precision && g_smoother == opt.smoother && g_omega == opt.omega &&
-            g_flexible == flexible_beta())
+            g_flexible == flexible_beta() && g_history == history())
             return 0;
         drop_graph();
         cudaGraph_t g = nullptr;
@@ -1788,6 +2187,7 @@ struct lina_gpu_amg {
         g_smoother = opt.smoother;
         g_omega = opt.omega;
         g_flexible = flexible_beta();
+        g_history = history();
         return 0;
     }
 };
@@ -1875,7 +2275,7 @@ int upload_hierarchy(lina_gpu_amg* h) {
     if ((rc = h->alloc(&h->kb, nf))) return rc;
     if ((rc = h->alloc(&h->kt, nf))) return rc;
     if ((rc = h->alloc(&h->kz32, nf))) return rc;
-    if ((rc = h->alloc(&h->partials, 2 * kMaxBlocks))) return rc;
+    if ((rc = h->alloc(&h->partials, (kFcgMax + 1) * kMaxBlocks))) return rc;
     if ((rc = h->alloc(&h->ticket, 4))) return rc;
     if ((rc = h->alloc(&h->sc, 1))) return rc;
     if ((rc = h->alloc(&h->hscal, 2))) return rc;
@@ -1969,6 +2369,11 @@ int lina_gpu_set_layout(int layout) {
         return LINA_GPU_EINVAL;
     }
     g_layout = layout;
+    return 0;
+}
+
+int lina_gpu_set_sell_quads(int on) {
+    g_quads = on ? 1 : 0;
     return 0;
 }
 
@@ -2147,7 +2552,12 @@ int lina_gpu_amg_recompute(lina_gpu_amg* h, int n, const int* rowptr, const int*
     for (void* p : h->allocations) cudaFree(p);
     h->allocations.clear();
     h->dev_bytes = 0;
+    // every pointer into the freed allocations is rebuilt on demand: the update maps and the Krylov
+    // direction history (upload_hierarchy below re-creates the levels and the Krylov vectors)
     h->upd_built = false;
+    h->upd_posQ = nullptr;
+    h->kph = h->kqh = nullptr;
+    h->hist_m = 0;
     h->Aorig = DCsr();
     int rc = upload_hierarchy(h);
     if (rc) return rc;
@@ -2174,6 +2584,14 @@ int build_update_maps(lina_gpu_amg* h) {
     int rc;
     std::vector<int> posA = layout_positions(A, nullptr);
     if ((rc = h->upload(&h->upd_posA, posA.data(), posA.size()))) return rc;
+    if (h->lv[f].A.q_val) {
+        QuadHost Q;
+        if (!make_quads(A, A.ncols > 0 ? A.ncols : A.n, Q)) {
+            set_err("quad layout positions of the finest matrix could not be rebuilt");
+            return LINA_GPU_ESETUP;
+        }
+        if ((rc = h->upload(&h->upd_posQ, Q.pos.data(), Q.pos.size()))) return rc;
+    }
     {
         std::vector<int> colour;
         const int nc = lina::greedy_colouring(A, colour);
@@ -2223,7 +2641,8 @@ int lina_gpu_amg_update_values(lina_gpu_amg* h, const double* val, int flags) {
         v = h->upd_val;
     }
     go(update_values_kernel, grid_for(h->upd_nnz, kThreads), h->stream, h->upd_nnz, v, (const int*)h->upd_posA,
-       (const int*)h->upd_posAcol, L.A.v64, L.A.v32, L.Acol.v64, L.Acol.v32);
+       (const int*)h->upd_posAcol, L.A.v64, L.A.v32, L.Acol.v64, L.Acol.v32, (const int*)h->upd_posQ,
+       reinterpret_cast<float*>(L.A.q_val));
     go(update_diag_kernel, grid_for(L.n, kThreads), h->stream, L.n, v, (const int*)h->upd_ptr,
        (const int*)h->upd_diagpos, (const unsigned char*)h->upd_isolated, L.dinv64, L.dinv32, h->isoinv);
     CK(cudaGetLastError());
@@ -2245,6 +2664,16 @@ int lina_gpu_amg_set_smoother(lina_gpu_amg* h, int smoother, double omega, int p
     h->opt.smoother = smoother;
     h->opt.omega = omega;
     h->opt.precision = precision;
+    h->drop_graph();
+    return 0;
+}
+
+int lina_gpu_amg_set_fcg_history(lina_gpu_amg* h, int m) {
+    if (!h || m < 0 || m > kFcgMax) {
+        set_err("lina_gpu_amg_set_fcg_history: m must be 0..%d", kFcgMax);
+        return LINA_GPU_EINVAL;
+    }
+    h->fcg_m = m;
     h->drop_graph();
     return 0;
 }
@@ -2435,6 +2864,7 @@ int lina_gpu_pcg(lina_gpu_amg* h, const double* b_in, double* x_out, double tol,
         // or as a captured CUDA graph whose while-loop node repeats the iteration
         // on the device until the residual test passes.
         const bool use_graph = !time_it && !(flags & LINA_PCG_HOST_LOOP);
+        if (int rc = h->ensure_history()) return rc;
         int it = 0;
         int restarts = 0;
         int dev_iter = 0;  // the device's iteration counter (reset on restart)
@@ -2589,8 +3019,8 @@ struct lina_gpu_matrix {
     // for lina_gpu_matrix_update_values: stored position of each CSR entry (host until first use),
     // the last diagonal entry of each row, staging for new values
     long nnz = 0;
-    std::vector<int> pos_host, diag_host;
-    int *pos = nullptr, *diagpos = nullptr;
+    std::vector<int> pos_host, diag_host, qpos_host;
+    int *pos = nullptr, *diagpos = nullptr, *qpos = nullptr;
     double* stage = nullptr;
 };
 
@@ -2599,12 +3029,17 @@ namespace {
 // new values on the stored pattern: SELL (or CSR) values in both precisions and the inverse diagonal
 // (the last diagonal entry of a row, 0 where it is absent or zero, as at creation)
 __global__ void matrix_values_kernel(long nnz, const double* __restrict__ val, const int* __restrict__ pos,
-                                     double* __restrict__ v64, float* __restrict__ v32) {
+                                     double* __restrict__ v64, float* __restrict__ v32, const int* __restrict__ qpos,
+                                     float* __restrict__ q32) {
     for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (long)gridDim.x * blockDim.x) {
         const int p = pos ? pos[k] : (int)k;
         if (p >= 0) {
             v64[p] = val[k];
             v32[p] = float(val[k]);
+        }
+        if (qpos) {
+            const int q = qpos[k];
+            if (q >= 0) q32[q] = float(val[k]);
         }
     }
 }
@@ -2666,7 +3101,7 @@ int lina_gpu_matrix_create(int n, int ncols, const int* rowptr, const int* col, 
             }
         dinv32[i] = (float)dinv[i];
     }
-    int rc = h->upload_csr(m->A, c, nullptr, &m->pos_host);
+    int rc = h->upload_csr(m->A, c, nullptr, &m->pos_host, &m->qpos_host);
     if (!rc) rc = h->upload(&m->dinv64, dinv.data(), dinv.size());
     if (!rc) rc = h->upload(&m->dinv32, dinv32.data(), dinv32.size());
     if (!rc) rc = h->alloc(&h->partials, 2 * kMaxBlocks);
@@ -2693,11 +3128,13 @@ int lina_gpu_matrix_update_values(lina_gpu_matrix* m, const double* val, int fla
     int rc = 0;
     if (!m->diagpos) {
         if (!m->pos_host.empty()) rc = h->upload(&m->pos, m->pos_host.data(), m->pos_host.size());
+        if (!rc && !m->qpos_host.empty()) rc = h->upload(&m->qpos, m->qpos_host.data(), m->qpos_host.size());
         if (!rc) rc = h->upload(&m->diagpos, m->diag_host.data(), m->diag_host.size());
         if (!rc && !(flags & LINA_PCG_DEVICE_PTRS)) rc = h->alloc(&m->stage, (size_t)m->nnz);
         if (!rc && cudaStreamSynchronize(h->stream) != cudaSuccess) rc = LINA_GPU_ECUDA;
         if (rc) return rc;
         m->pos_host = std::vector<int>();
+        m->qpos_host = std::vector<int>();
     }
     const double* v = val;
     if (!(flags & LINA_PCG_DEVICE_PTRS)) {
@@ -2706,7 +3143,7 @@ int lina_gpu_matrix_update_values(lina_gpu_matrix* m, const double* val, int fla
         v = m->stage;
     }
     go(matrix_values_kernel, grid_for(m->nnz, kThreads), h->stream, m->nnz, v, (const int*)m->pos, m->A.v64,
-       m->A.v32);
+       m->A.v32, (const int*)m->qpos, reinterpret_cast<float*>(m->A.q_val));
     go(matrix_dinv_kernel, grid_for(m->A.n, kThreads), h->stream, m->A.n, v, (const int*)m->diagpos, m->dinv64,
        m->dinv32);
     CK(cudaGetLastError());
@@ -2765,14 +3202,14 @@ int lina_gpu_matrix_rows(const lina_gpu_matrix* m) { return m ? m->A.n : 0; }
 
 int lina_gpu_matrix_index_bits(const lina_gpu_matrix* m) {
     if (!m || m->A.lanes > 0) return 0;
-    return m->A.col16 ? 16 : 32;
+    return (m->A.col16 || m->A.q_val) ? 16 : 32;
 }
 
 int lina_gpu_amg_depth(const lina_gpu_amg* h) { return h ? h->depth : 0; }
 
 int lina_gpu_level_index_bits(const lina_gpu_amg* h, int level, int* A_bits, int* P_bits, int* R_bits) {
     if (!h || h->host_only || level < 0 || level >= (int)h->lv.size()) return LINA_GPU_EINVAL;
-    auto bits = [](const DCsr& d) { return d.lanes > 0 || !d.col ? 0 : (d.col16 ? 16 : 32); };
+    auto bits = [](const DCsr& d) { return d.lanes > 0 || !d.col ? 0 : ((d.col16 || d.q_val) ? 16 : 32); };
     const DLevel& L = h->lv[level];
     if (A_bits) *A_bits = bits(L.A);
     if (P_bits) *P_bits = level > 0 ? bits(L.P) : 0;
@@ -2930,6 +3367,8 @@ int build_batch_graph(lina_gpu_batch* B) {
         const int n = h->lv[h->depth - 1].n;
         const bool mixed = (h->opt.precision == LINA_PREC_MIXED);
         const int gr = grid_red(n);
+        h->beta_mode = -1;
+        if ((rc = h->ensure_history())) break;
         cudaGraph_t gstart = nullptr, gfin = nullptr;
         rc = capture_on(h, &gstart, &B->k_start[s], [&] {
             cudaMemsetAsync(h->kx, 0, (size_t)n * sizeof(double), h->stream);
@@ -2974,7 +3413,7 @@ int build_batch_graph(lina_gpu_batch* B) {
                                               cudaStreamCaptureModeRelaxed);
         if (e == cudaSuccess) {
             const unsigned long long before = g_launches;
-            h->beta_mode = -1;  // the precision's default beta
+            h->beta_mode = -1;  // the precision's default recurrence
             h->issue_iteration(n, true, false);
             loop_cond_kernel<<<1, 1, 0, h->stream>>>(hd, h->sc);
             B->k_iter[s] = (long)(g_launches - before) + 1;

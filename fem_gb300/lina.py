@@ -107,6 +107,7 @@ def lib():
         "lina_gpu_amg_save": (C.c_int, [vp, C.c_char_p]),
         "lina_gpu_amg_load": (C.c_int, [C.c_char_p, C.POINTER(AmgOptions), C.c_int, C.POINTER(vp)]),
         "lina_gpu_amg_set_smoother": (C.c_int, [vp, C.c_int, C.c_double, C.c_int]),
+        "lina_gpu_amg_set_fcg_history": (C.c_int, [vp, C.c_int]),
         "lina_gpu_pcg": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, C.POINTER(SolveInfo)]),
         "lina_gpu_batch_create": (C.c_int, [C.c_int, C.POINTER(vp), C.c_int, C.POINTER(vp)]),
         "lina_gpu_batch_solve": (C.c_int, [vp, C.POINTER(vp), C.POINTER(vp), C.c_double, C.c_int, C.c_int,
@@ -131,6 +132,7 @@ def lib():
         "lina_gpu_set_layout": (C.c_int, [C.c_int]),
         "lina_gpu_set_fused_rows": (C.c_int, [C.c_int]),
         "lina_gpu_set_sell_index_bits": (C.c_int, [C.c_int]),
+        "lina_gpu_set_sell_quads": (C.c_int, [C.c_int]),
         "lina_gpu_matrix_index_bits": (C.c_int, [vp]),
         "lina_gpu_level_index_bits": (C.c_int, [vp, C.c_int, ip, ip, ip]),
         "lina_gpu_last_error": (C.c_char_p, []),
@@ -295,6 +297,12 @@ def set_sell_index_bits(bits: int):
     """16 (the default): SELL-32 matrices with long rows uploaded afterwards also get 16-bit column
     offsets (two bases per slice, where the columns fit), read by FP32 passes; 32: int columns only."""
     _check(lib().lina_gpu_set_sell_index_bits(int(bits)), "set SELL index bits")
+
+
+def set_sell_quads(on):
+    """FP32 passes over natural-order SELL-32 matrices uploaded afterwards read the quad layout (1) or
+    the one-entry layout (0); identical results."""
+    _check(lib().lina_gpu_set_sell_quads(int(on)), "set quads")
 
 
 def dot(a: "DeviceArray", b: "DeviceArray") -> float:
@@ -678,6 +686,10 @@ class AMG:
 
     def set_smoother(self, smoother, omega, precision):
         _check(lib().lina_gpu_amg_set_smoother(self.h, smoother, omega, precision), "set smoother")
+
+    def set_fcg_history(self, m):
+        """Directions kept by the flexible CG (0 default: FCG(4) mixed, CG FP64; 1 two-term; 2..8 FCG(m))."""
+        _check(lib().lina_gpu_amg_set_fcg_history(self.h, m), "set FCG history")
 
     def update_values(self, data=None, device_ptr=None):
         """New finest values on the creation pattern (lina_gpu_amg_update_values): a host array, or a

@@ -177,11 +177,35 @@ def poisson_p1(m: int, seed: int = 0) -> CSRSystem:
                      meta={"kind": "poisson_p1", "m": m, "seed": seed, "n_boundary": len(bnd)})
 
 
+_LN2_HI = 6.93147180369123816490e-01  # ln 2 split so that k * _LN2_HI is exact for |k| < 2^20
+_LN2_LO = 1.90821492927058770002e-10
+_INV_LN2 = 1.44269504088896338700e+00
+
+
+def portable_exp(x: np.ndarray) -> np.ndarray:
+    """exp(x) for |x| < 700 from IEEE basic operations only, so that every host computes the same bits.
+
+    Library exponentials (numpy's vectorised loops, libm) may round the last bit differently on x86 and
+    Arm hosts; the benchmark's systems are generated on both, and their AMG hierarchies are compared
+    bit for bit.  Cody-Waite reduction x = k ln2 + r (|r| <= ln2 / 2, ln 2 in two parts), the Taylor
+    series of exp(r) to degree 14 (truncation below 1e-18 relative) by Horner's rule, then 2^k.
+    Accurate to about 2 ulp.
+    """
+    x = np.asarray(x, dtype=np.float64)
+    k = np.rint(x * _INV_LN2)
+    r = (x - k * _LN2_HI) - k * _LN2_LO
+    p = np.full_like(r, 1.0)
+    for j in range(14, 0, -1):
+        p = p * (r / j) + 1.0
+    return np.ldexp(p, k.astype(np.int64))
+
+
 def notch_damage(m: int, ell: float | None = None) -> np.ndarray:
     """Per-element damage d = exp(-dist/ell) to the notch (0,0.5)-(0.5,0.5).
 
     Returned as [2, (m-1)^2] (lower, upper triangle of each cell) evaluated at
-    the triangle centroids; ``ell`` defaults to 2h.
+    the triangle centroids; ``ell`` defaults to 2h.  The exponential is
+    ``portable_exp``: the same bits on every host.
     """
     h = 1.0 / (m - 1)
     if ell is None:
@@ -194,7 +218,7 @@ def notch_damage(m: int, ell: float | None = None) -> np.ndarray:
         cy = (rr.ravel() + np.mean([dr for (dr, dc) in tri])) * h
         dx = np.where(cx > 0.5, cx - 0.5, 0.0)
         dist = np.sqrt(dx * dx + (cy - 0.5) ** 2)
-        out.append(np.exp(-dist / ell))
+        out.append(portable_exp(-dist / ell))
     return np.stack(out)
 
 

@@ -124,6 +124,13 @@ int lina_gpu_amg_save(const lina_gpu_amg* h, const char* dir);
 int lina_gpu_amg_load(const char* dir, const lina_gpu_amg_options* opt, int host_only, lina_gpu_amg** out);
 /* change smoother, relaxation or precision of an existing hierarchy */
 int lina_gpu_amg_set_smoother(lina_gpu_amg* h, int smoother, double omega, int precision);
+/* Krylov directions kept by lina_gpu_pcg and the batch solves (no reference counterpart): m >= 2 runs the
+   truncated flexible CG FCG(m) of Notay, which makes every new direction A-orthogonal to the last m
+   (robust to the slight variation of the FP32 V-cycle between applications); m = 1 the two-term
+   recurrences (flexible beta in mixed precision, the reference's beta in FP64); 0 (default) FCG(4) in mixed
+   precision and the reference's CG in FP64.  Up to 8.  The LINA_PCG_BETA_* flags select the two-term
+   recurrence for one call.  FCG(m) keeps 2 m extra FP64 vectors on the device. */
+int lina_gpu_amg_set_fcg_history(lina_gpu_amg* h, int m);
 
 /* AMG-preconditioned CG on the hierarchy's finest matrix (pcg, LinA/PCGS.c:163). */
 int lina_gpu_pcg(lina_gpu_amg* h, const double* b, double* x, double tol, int max_iter,
@@ -404,6 +411,11 @@ int lina_gpu_set_fused_rows(int max_rows);
    bytes less per stored entry), FP64 passes the int columns.  32: int columns only.  The results
    are identical. */
 int lina_gpu_set_sell_index_bits(int bits);
+/* 1 (default): SELL-32 matrices in natural row order uploaded afterwards (with 16-bit indices enabled)
+   also get the quad layout, in which every lane holds four consecutive entries of its row (one 16-byte
+   value load and one 8-byte index load), and their FP32 passes read it; 0: FP32 passes read the
+   one-entry SELL-32 layout.  The results are identical. */
+int lina_gpu_set_sell_quads(int on);
 
 const char* lina_gpu_last_error(void);
 

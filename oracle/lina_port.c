@@ -224,6 +224,36 @@ int port_amg_finalize(port_amg* h) {
     return 0;
 }
 
+int port_amg_level_info(const port_amg* h, int l, int* n, long* nnz_A, long* nnz_P, long* nnz_R) {
+    if (!h || l < 0 || l >= h->depth) return -1;
+    const level_t* L = &h->lv[l];
+    *n = L->n;
+    *nnz_A = L->A.ptr ? L->A.ptr[L->n] : 0;
+    *nnz_P = (l > 0 && L->P.ptr) ? L->P.ptr[L->n] : 0;
+    *nnz_R = (l > 0 && L->R.ptr) ? L->R.ptr[L->R.n] : 0;
+    return 0;
+}
+
+static void csr_out(const csr_t* m, int* ptr, int* col, double* val) {
+    if (!m->ptr) return;
+    if (ptr) memcpy(ptr, m->ptr, (m->n + 1) * sizeof(int));
+    if (col) memcpy(col, m->col, m->ptr[m->n] * sizeof(int));
+    if (val) memcpy(val, m->val, m->ptr[m->n] * sizeof(double));
+}
+
+int port_amg_level_export(const port_amg* h, int l, int* labels, int* A_ptr, int* A_col, double* A_val,
+                          int* P_ptr, int* P_col, double* P_val, int* R_ptr, int* R_col, double* R_val) {
+    if (!h || l < 0 || l >= h->depth) return -1;
+    const level_t* L = &h->lv[l];
+    csr_out(&L->A, A_ptr, A_col, A_val);
+    if (l > 0) {
+        if (labels) memcpy(labels, L->labels, L->n * sizeof(int));
+        csr_out(&L->P, P_ptr, P_col, P_val);
+        csr_out(&L->R, R_ptr, R_col, R_val);
+    }
+    return 0;
+}
+
 void port_amg_free(port_amg* h) {
     if (!h) return;
     for (int l = 0; l < h->depth; l++) {

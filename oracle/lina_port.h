@@ -38,6 +38,18 @@ int port_amg_set_level(port_amg* h, int l, int n, const int* A_ptr, const int* A
                        const int* labels, const int* P_ptr, const int* P_col, const double* P_val,
                        const int* R_ptr, const int* R_col, const double* R_val, int nc);
 int port_amg_finalize(port_amg* h);      /* colourings and the coarsest LU */
+/* AMG_setup (LinA/Multigrid.c:1613-1754) restated (amg_setup_port.c): builds every level of a handle
+   from port_amg_new from the finest matrix (CSR, sorted columns) and finalizes it.  coarsening: 1
+   aggressive (finest level only), 2 standard.  0, or a negative code: -1 bad argument, -3 a negative
+   diagonal (the restated solve does not apply the reference's row signs), -4 inconsistent coarse
+   count, -5 a zero diagonal in the interpolation, -6 an erroneous coarse matrix (the reference aborts
+   on the last two), -2 a zero pivot in the coarsest factorisation. */
+int port_amg_setup(port_amg* h, int n, const int* ptr, const int* col, const double* val, int dof, int depth,
+                   int coarsening, double eps_minus, double eps_plus, double matrix_tol);
+/* sizes and host copies of a level (any output pointer may be NULL) */
+int port_amg_level_info(const port_amg* h, int l, int* n, long* nnz_A, long* nnz_P, long* nnz_R);
+int port_amg_level_export(const port_amg* h, int l, int* labels, int* A_ptr, int* A_col, double* A_val,
+                          int* P_ptr, int* P_col, double* P_val, int* R_ptr, int* R_col, double* R_val);
 void port_amg_free(port_amg* h);
 int port_amg_colouring(const port_amg* h, int l, int* colour);
 

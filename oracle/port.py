@@ -7,6 +7,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+from types import SimpleNamespace
 
 import numpy as np
 
@@ -37,6 +38,11 @@ def lib():
         "port_pcg": (C.c_int, [vp, dp, dp, C.c_double, C.c_int, C.c_int, C.c_double, dp]),
         "port_spmv": (None, [vp, C.c_int, dp, dp]),
         "port_ilu0": (C.c_int, [C.c_int, ip, ip, dp, dp]),
+        "port_amg_setup": (C.c_int, [vp, C.c_int, ip, ip, dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                     C.c_double]),
+        "port_amg_level_info": (C.c_int, [vp, C.c_int, ip, C.POINTER(C.c_long), C.POINTER(C.c_long),
+                                          C.POINTER(C.c_long)]),
+        "port_amg_level_export": (C.c_int, [vp, C.c_int, ip, ip, ip, dp, ip, ip, dp, ip, ip, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -98,6 +104,52 @@ class PortAMG:
         if rc:
             raise RuntimeError(f"port_amg_finalize failed ({rc})")
         self.n = len(levels[-1]["A"][0]) - 1
+
+    @classmethod
+    def setup(cls, system, depth, coarsening=2, matrix_tol=0.1, smoother=MC_SOR, omega=1.0, nu=2, nu_finest=2,
+              eps_minus=0.3, eps_plus=0.5):
+        """AMG_setup restated in C (amg_setup_port.c) on a CSR system (indptr, indices, data, dof):
+        the hierarchy is built by the oracle itself, without the GPU library."""
+        self = cls.__new__(cls)
+        self.depth = depth
+        self._keep = []
+        self.h = lib().port_amg_new(depth, smoother, omega, nu, nu_finest)
+        ptr = np.ascontiguousarray(system.indptr, dtype=np.int32)
+        col = np.ascontiguousarray(system.indices, dtype=np.int32)
+        val = np.ascontiguousarray(system.data, dtype=np.float64)
+        rc = lib().port_amg_setup(self.h, len(ptr) - 1, _ip(ptr), _ip(col), _dp(val), int(system.dof), depth,
+                                  coarsening, eps_minus, eps_plus, matrix_tol)
+        if rc:
+            raise RuntimeError(f"port_amg_setup failed ({rc})")
+        self.n = len(ptr) - 1
+        return self
+
+    def level_sizes(self, l):
+        n, a, p, r = C.c_int(), C.c_long(), C.c_long(), C.c_long()
+        if lib().port_amg_level_info(self.h, l, C.byref(n), C.byref(a), C.byref(p), C.byref(r)):
+            raise IndexError(l)
+        return n.value, a.value, p.value, r.value
+
+    def sizes(self):
+        return [self.level_sizes(l)[0] for l in range(self.depth)]
+
+    def level(self, l):
+        """Host copy of level l: an object with A, P, R (CSR triples) and labels (None on level 0)."""
+        n, na, np_, nr = self.level_sizes(l)
+        A = (np.zeros(n + 1, np.int32), np.zeros(max(na, 1), np.int32), np.zeros(max(na, 1)))
+        lab = P = R = None
+        if l > 0:
+            nc = self.level_sizes(l - 1)[0]
+            lab = np.zeros(n, np.int32)
+            P = (np.zeros(n + 1, np.int32), np.zeros(max(np_, 1), np.int32), np.zeros(max(np_, 1)))
+            R = (np.zeros(nc + 1, np.int32), np.zeros(max(nr, 1), np.int32), np.zeros(max(nr, 1)))
+        Pp = (_ip(P[0]), _ip(P[1]), _dp(P[2])) if P else (None, None, None)
+        Rp = (_ip(R[0]), _ip(R[1]), _dp(R[2])) if R else (None, None, None)
+        if lib().port_amg_level_export(self.h, l, _ip(lab), _ip(A[0]), _ip(A[1]), _dp(A[2]), *Pp, *Rp):
+            raise IndexError(l)
+        return SimpleNamespace(n=n, A=(A[0], A[1][:na], A[2][:na]), labels=lab,
+                               P=(P[0], P[1][:np_], P[2][:np_]) if P else None,
+                               R=(R[0], R[1][:nr], R[2][:nr]) if R else None)
 
     def vcycle(self, r):
         rr = np.ascontiguousarray(r, dtype=np.float64)

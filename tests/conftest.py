@@ -42,6 +42,8 @@ def golden_cases(kind="hierarchy"):
         g = np.load(f)
         if "digest" not in g.files and "L0_A_ptr" not in g.files:
             continue  # not a linear-system fixture (reflective Newton quadratics)
+        if "sample_index" in g.files:
+            continue  # a configuration-size digest (tests/test_config_parity.py), without the system itself
         has_h = "L0_A_ptr" in g.files
         if (kind == "hierarchy") == has_h:
             out.append(os.path.basename(f)[:-4])

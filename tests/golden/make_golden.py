@@ -54,6 +54,16 @@ SMOOTHERS = {
 }
 TOL = 1e-8
 MAX_IT = 500
+# configuration-size systems, stored as digests (per-level SHA-256 of the hierarchy, iteration
+# counts, norms and a fixed subsample of each solution; tests/golden/digest.py): the 2.1M-unknown
+# degraded elasticity system of the benchmark (standard coarsening, depth 10) and the 66,049-unknown
+# Poisson system (aggressive coarsening, depth 6, lexicographic SOR with omega 1)
+DIGEST_CASES = {
+    "elast1025_digest": (lambda: problems.elasticity_p1(1025), 10, ref.STANDARD, ("jacobi", "refsor")),
+    "poisson257_digest": (lambda: problems.poisson_p1(257, seed=0), 6, ref.AGGRESSIVE, ("refsor", "jacobi", "mcsor")),
+}
+# the AT2 damage step at 1025 x 1025 nodes (1.05M unknowns) by reflective Newton, stored as a digest
+RN_DIGEST_CASES = {"at2_1025_rn_digest": lambda: problems.at2_damage(1025)}
 # bound-constrained damage quadratics solved by reflective_newton (LinA/reflective_newton.c:660)
 RN_CASES = {
     "damage65_rn": lambda: problems.damage_qp(65),
@@ -141,6 +151,70 @@ def make_solve_case(name):
         out[f"pcg_{sname}_res"] = np.float64(res)
     x, it, res = amg.pcg(s.b, 1e-13, 2000, ref.SMOOTHER_MC_SOR, 1.0)
     out["x_tight"] = x
+    return out
+
+
+def make_digest_case(name):
+    import time
+    from tests.golden import digest as D
+    factory, depth, coarsening, smoothers = DIGEST_CASES[name]
+    s = factory()
+    t0 = time.perf_counter()
+    amg = ref.RefAMG(s, depth, 2, 2, coarsening)
+    t_setup = time.perf_counter() - t0
+    idx = D.sample_index(s.n)
+    out = {"n": np.int64(s.n), "dof": np.int64(s.dof), "depth": np.int64(depth),
+           "coarsening": np.int64(coarsening), "digest": np.array(system_digest(s)),
+           "sizes": np.array(amg.sizes(), dtype=np.int64), "sample_index": idx,
+           "ref_setup_s": np.float64(t_setup)}
+    for k, v in D.level_digest(amg.level, depth).items():
+        out[f"sha_{k}"] = np.array(v)
+    bn = np.linalg.norm(s.b)
+    import scipy.sparse as sp
+    A = sp.csr_matrix((s.data, s.indices, s.indptr), shape=(s.n, s.n))
+    for sname in smoothers:
+        kind, omega = SMOOTHERS[sname]
+        t0 = time.perf_counter()
+        x, it, res = amg.pcg(s.b, TOL, MAX_IT, kind, omega)
+        out[f"pcg_{sname}_s"] = np.float64(time.perf_counter() - t0)
+        out[f"pcg_{sname}_it"] = np.int64(it)
+        out[f"pcg_{sname}_res"] = np.float64(res)
+        out[f"pcg_{sname}_norm"] = np.float64(np.linalg.norm(x))
+        out[f"pcg_{sname}_true_rel"] = np.float64(np.linalg.norm(s.b - A @ x) / bn)
+        out[f"pcg_{sname}_xs"] = x[idx]
+        print(f"  {name} {sname}: {it} iterations, {out[f'pcg_{sname}_s']:.1f} s", flush=True)
+    # an accurate FP64 solution (tolerance 1e-13 in the reference's rule) for error bars
+    kind, omega = SMOOTHERS[smoothers[0]]
+    x, it, res = amg.pcg(s.b, 1e-13, 4000, kind, omega)
+    out["tight_it"] = np.int64(it)
+    out["tight_norm"] = np.float64(np.linalg.norm(x))
+    out["tight_xs"] = x[idx]
+    if s.n <= 100_000:
+        out["x_tight"] = x
+    return out
+
+
+def make_rn_digest_case(name):
+    import time
+    from tests.golden import digest as D
+    q = RN_DIGEST_CASES[name]()
+    idx = D.sample_index(q.n)
+    out = {"n": np.int64(q.n), "sample_index": idx,
+           "digest": np.array(system_digest(q))}
+    for sname, code in RN_SOLVERS.items():
+        if code != 5:
+            continue
+        t0 = time.perf_counter()
+        x, it = ref.reflective_newton_qp(q, solver=code, max_iter=50, eps=1e-8, bi_eps=1e-8)
+        out[f"rn_{sname}_s"] = np.float64(time.perf_counter() - t0)
+        out[f"rn_{sname}_it"] = np.int64(it)
+        out[f"rn_{sname}_norm"] = np.float64(np.linalg.norm(x))
+        out[f"rn_{sname}_xs"] = x[idx]
+        out[f"rn_{sname}_min"] = np.float64(x.min())
+        out[f"rn_{sname}_max"] = np.float64(x.max())
+        lo, up = q.meta["lower"], q.meta["upper"]
+        out[f"rn_{sname}_at_lower"] = np.int64(np.sum(np.abs(x - lo) <= 1e-10))
+        out[f"rn_{sname}_at_upper"] = np.int64(np.sum(np.abs(x - up) <= 1e-10))
     return out
 
 
@@ -376,6 +450,21 @@ def main():
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **data)
         print(f"{path}: loss {float(data['loss']):.6e}, pcg iterations (target, forward, adjoint) {list(data['it'])}")
+    for name in DIGEST_CASES:
+        if name not in only:  # minutes of reference time: generated only when named
+            continue
+        data = make_digest_case(name)
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **data)
+        print(f"{path}: sizes {list(data['sizes'])}, setup {float(data['ref_setup_s']):.1f} s, pcg iterations "
+              + ", ".join(f"{k}={int(data[f'pcg_{k}_it'])}" for k in DIGEST_CASES[name][3]))
+    for name in RN_DIGEST_CASES:
+        if name not in only:
+            continue
+        data = make_rn_digest_case(name)
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **data)
+        print(f"{path}: reflective Newton iterations {int(data['rn_umf_bicgstab_ilu_it'])}")
     for name in RN_CASES:
         if only and name not in only:
             continue

@@ -18,10 +18,13 @@ pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not gpu_available(), reason="n
 
 @pytest.fixture
 def bits():
+    """The one-entry SELL-32 layout (quads off; tests/test_sell_quads.py covers the quad layout)."""
     def set_bits(b):
         lina.set_sell_index_bits(b)
+    lina.set_sell_quads(0)
     yield set_bits
     lina.set_sell_index_bits(16)
+    lina.set_sell_quads(1)
     lina.set_layout(lina.LAYOUT_AUTO)
 
 
