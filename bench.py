@@ -190,6 +190,54 @@ def cpu_baseline(args, s, depth, omega):
     return rec, x
 
 
+def reference_api_e2e(args, s, depth, omega, world):
+    """Solves through the drop-in LinA API on host arrays: AMG_setup on the row-list matrix, PCG_default,
+    PCG_set_AMG_data, PCG_set_precon(PCG_AMG_vcycle_precon) and pcg (which then runs on the device), mixed
+    precision, the reference's stopping rule ||r|| / ||M^-1 r0|| <= tol.  Each step is one pcg call from
+    X = 0 with host B and X (their copies to and from the device inside the call)."""
+    from fem_gb300 import lina
+    L = lina.dropin()
+    A = lina.RowListView(s.indptr, s.indices, s.data)
+    L.AMG_print_info(0)
+    L.AMG_set_matrix_tolerance(args.matrix_tol)
+    L.AMG_set_SOR_relaxation_coeff(omega)
+    sm = L.AMG_damped_Jacobi_smoother if args.smoother == "jacobi" else L.AMG_SOR_smoother
+    L.AMG_set_smoother(ctypes.cast(sm, ctypes.c_void_p))
+    L.AMG_gpu_set_precision(1)
+    coarsening = 2  # STANDARD
+    t0 = time.perf_counter()
+    data = L.AMG_setup(A.ref, int(s.dof), depth, 2, 2, coarsening, 0, 1, None, None)
+    setup_s = time.perf_counter() - t0
+    if not data:
+        raise RuntimeError("AMG_setup through the drop-in API failed")
+    L.PCG_default(A.ref, None, None)
+    L.PCG_set_AMG_data(data)
+    L.PCG_set_precon(ctypes.cast(L.PCG_AMG_vcycle_precon, ctypes.c_void_p))
+    b = np.ascontiguousarray(s.b, dtype=np.float64)
+    x = np.zeros(s.n)
+    dp = ctypes.POINTER(ctypes.c_double)
+    bp, xp = b.ctypes.data_as(dp), x.ctypes.data_as(dp)
+    times, its = [], []
+    for k in range(args.warmup + args.steps):
+        x[:] = 0.0
+        t0 = time.perf_counter()
+        it = L.pcg(xp, bp, s.n, args.tol, 2000)
+        dt = time.perf_counter() - t0
+        if it < 0:
+            raise RuntimeError("pcg through the drop-in API failed")
+        if k >= args.warmup:
+            times.append(dt)
+            its.append(it)
+    trr = float(np.linalg.norm(s.b - _csr_matvec(s)(x)) / np.linalg.norm(s.b))
+    L.AMG_free_data(data)
+    value = world * len(times) / max_over_ranks(sum(times), world)
+    return {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 16 * s.n, "d2h_bytes_per_step": 8 * s.n,
+            "api": "AMG_setup + PCG_default + PCG_set_AMG_data + PCG_set_precon(PCG_AMG_vcycle_precon) + pcg on host "
+                   "arrays (drop-in LinA API), mixed precision",
+            "stop_rule": f"reference: ||r|| / ||M^-1 r0|| <= {args.tol:g}", "iterations": its,
+            "true_rel_residual": trr, "pcg_residuum": float(L.get_pcg_residuum()), "setup_s": setup_s}
+
+
 def reference_digest(m):
     """The reference's own results for the benchmark system, if committed (tests/golden)."""
     path = os.path.join(ROOT, "tests", "golden", f"elast{m}_digest.npz")
@@ -262,6 +310,8 @@ def run_gb300(args, rank, world, local):
         if k >= args.warmup:
             e2e_ms.append(t)
     e2e_value = world * len(e2e_ms) / (max_over_ranks(sum(e2e_ms), world) / 1e3)
+    # end to end through the reference-facing drop-in API, as crack.c / FEM2D would call it
+    api = reference_api_e2e(args, s, depth, omega, world)
 
     # the same GPU's plain FP64 path on the same hierarchy
     fp64 = None
@@ -322,7 +372,9 @@ def run_gb300(args, rank, world, local):
         "parallelism": "replicas" if world > 1 else "single GPU", "sell_index_bits": args.sell_bits,
         "iterations": it_mixed, "restarts": max(i.restarts for i in infos), "true_rel_residual": trr,
         "dofs_per_s": value * n, "setup_s": setup_s, "parity": parity,
-        "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},
+        "e2e": api,
+        "e2e_c_abi": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
+                      "api": "lina_gpu_pcg with pinned host buffers, relative rule"},
         "gpu_launches": int(launches),
         "fp64_gpu": fp64,
         "mixed_vs_fp64": (value / fp64["value"]) if fp64 else None,

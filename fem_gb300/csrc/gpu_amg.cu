@@ -43,6 +43,7 @@ int g_fused_rows = 24576;
 // per slice, where every slice's columns fit), read by FP32 passes; 32: int columns only
 int g_sell_bits = 16;
 int g_quads = 1;  // FP32 passes read the quad layout (sellq_kernel); 0 keeps the one-entry SELL layout
+int g_pdl = 1;    // programmatic dependent launch of the solve kernels (launch())
 
 void set_err(const char* fmt, ...) {
     char buf[512];
@@ -68,6 +69,17 @@ constexpr int kGridCap = 152 * 12;    // grid-stride cap: 152 SMs x 12 blocks of
 constexpr int kReduceGrid = 152 * 4;  // streaming reductions: half a wave, four strides per loop trip
 
 // ---------------------------------------------------------------- reductions
+// Programmatic dependent launch: kernels of the solve are launched with programmatic stream
+// serialisation.  Each kernel first waits, before any access to global memory, until the previous grid
+// has completed and its writes are visible, then lets the next kernel's blocks be scheduled: they take
+// the SMs this grid's finishing blocks free and wait there, so the launch gap between the many short
+// kernels of a V-cycle is hidden.  Both instructions are no-ops for a kernel launched without the
+// attribute.
+__device__ __forceinline__ void pdl_wait() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -148,10 +160,18 @@ struct KScalars {
 
 // p.q from the block partials of an SpMV+dot launch, summed in block order by one block
 __global__ void dot_finish_kernel(int nparts, const double* __restrict__ partials, KScalars* sc) {
+    pdl_wait();
     __shared__ double sm[32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    double x = 0.0;
-    for (int i = threadIdx.x; i < nparts; i += blockDim.x) x += partials[i];
+    // eight independent loads per thread per trip (the partials sit in L2), combined in a fixed order
+    double a[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    int i = threadIdx.x;
+    for (; i + 7 * (int)blockDim.x < nparts; i += 8 * blockDim.x) {
+#pragma unroll
+        for (int u = 0; u < 8; u++) a[u] += partials[i + u * blockDim.x];
+    }
+    for (; i < nparts; i += blockDim.x) a[0] += partials[i];
+    double x = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
     x = warp_sum(x);
     if (lane == 0) sm[wid] = x;
     __syncthreads();
@@ -165,6 +185,7 @@ __global__ void dot_finish_kernel(int nparts, const double* __restrict__ partial
 // last node of the graph-captured iteration: continue the device-side loop
 // while the residual test fails and the iteration budget lasts
 __global__ void loop_cond_kernel(cudaGraphConditionalHandle handle, const KScalars* sc) {
+    pdl_wait();
     const double rel = sqrt(sc->rr) / sc->r0;
     const bool more = isfinite(rel) && rel > sc->tol && sc->iter < sc->maxit;
     cudaGraphSetConditional(handle, more ? 1u : 0u);
@@ -206,6 +227,7 @@ __global__ void __launch_bounds__(kThreads) sell_kernel(int npos, int nrows, con
                                                         const TX* x, TX* y, const TX* __restrict__ b,
                                                         const TX* __restrict__ dinv, TX w, const TX* z,
                                                         double* partials, unsigned* ticket, KScalars* sc) {
+    pdl_wait();
     double dot = 0.0;
     // grid-stride over slice positions (npos is a multiple of 32, so warps stay whole); positions
     // past the last row (natural order) or marked -1 (colour order) are padding
@@ -325,6 +347,7 @@ __global__ void __launch_bounds__(kThreads, 5) sellq_kernel(int n, const int* __
                                                             float* y, const float* __restrict__ b,
                                                             const float* __restrict__ dinv, float w,
                                                             const float* z) {
+    pdl_wait();
     const int npos = ((n + 31) >> 5) << 5;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < npos; t += gridDim.x * blockDim.x) {
         const int i = t;
@@ -405,6 +428,7 @@ __global__ void __launch_bounds__(kThreads) csrv_kernel(int nrows, const int* __
                                                         const TX* __restrict__ b, const TX* __restrict__ dinv, TX w,
                                                         const TX* z, double* partials, unsigned* ticket,
                                                         KScalars* sc) {
+    pdl_wait();
     const int lane = threadIdx.x & 31;
     const int sub = lane & (S - 1);
     const long warp_global = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -462,6 +486,7 @@ template <typename TB, typename TX>
 __global__ void jacobi_first_kernel(int n, const TB* __restrict__ b, const double* __restrict__ sign,
                                     const TX* __restrict__ dinv, const double* __restrict__ isoinv, TX w,
                                     TX* __restrict__ x, TX* __restrict__ bout) {
+    pdl_wait();
     const long S = (long)gridDim.x * blockDim.x;
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     auto one = [&](long k, double bd, TX di, double iso) {
@@ -489,6 +514,7 @@ __global__ void jacobi_first_kernel(int n, const TB* __restrict__ b, const doubl
 template <typename TB, typename TX>
 __global__ void init_x_kernel(int n, const TB* __restrict__ b, const double* __restrict__ sign,
                               const double* __restrict__ isoinv, TX* __restrict__ x, TX* __restrict__ bout) {
+    pdl_wait();
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
         double bd = double(b[i]);
         if (sign) bd *= sign[i];
@@ -502,6 +528,7 @@ template <typename TX>
 __global__ void coarse_gather_kernel(int n, const TX* __restrict__ b, const int* __restrict__ inblock,
                                      const int* __restrict__ blockpos, const double* __restrict__ dginv,
                                      double* __restrict__ bblk, TX* __restrict__ x) {
+    pdl_wait();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         if (inblock[i])
             bblk[blockpos[i]] = double(b[i]);
@@ -514,6 +541,7 @@ __global__ void coarse_gather_kernel(int n, const TX* __restrict__ b, const int*
 template <typename TX>
 __global__ void coarse_gemv_kernel(int m, const double* __restrict__ inv, const double* __restrict__ bblk,
                                    const int* __restrict__ brows, TX* __restrict__ x) {
+    pdl_wait();
     const int lane = threadIdx.x & 31;
     for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < m;
          r += ((long)gridDim.x * blockDim.x) >> 5) {
@@ -527,21 +555,25 @@ __global__ void coarse_gemv_kernel(int m, const double* __restrict__ inv, const 
 
 template <typename TA, typename TB>
 __global__ void convert_kernel(long n, const TA* __restrict__ a, TB* __restrict__ b) {
+    pdl_wait();
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) b[i] = TB(a[i]);
 }
 
 __global__ void scale_kernel(long n, double* __restrict__ v, const double* __restrict__ f, int invert) {
+    pdl_wait();
     double s = invert ? 1.0 / (*f) : (*f);
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) v[i] *= s;
 }
 
 // AMG_solve helpers: b = signs * F, the isolated-row fix x_i = b_i / a_i, x += z
 __global__ void mul_kernel(int n, double* __restrict__ b, const double* __restrict__ f) {
+    pdl_wait();
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) b[i] *= f[i];
 }
 
 __global__ void fix_isolated_kernel(int n, const double* __restrict__ b, const double* __restrict__ isoinv,
                                     double* __restrict__ x) {
+    pdl_wait();
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
         if (isoinv[i] != 0.0) x[i] = b[i] * isoinv[i];
 }
@@ -552,6 +584,7 @@ __global__ void update_values_kernel(long nnz, const double* __restrict__ val, c
                                      const int* __restrict__ posAcol, double* __restrict__ a64,
                                      float* __restrict__ a32, double* __restrict__ c64, float* __restrict__ c32,
                                      const int* __restrict__ posQ, float* __restrict__ q32) {
+    pdl_wait();
     for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (long)gridDim.x * blockDim.x) {
         const double v = val[k];
         const int p = posA[k];
@@ -577,6 +610,7 @@ __global__ void update_diag_kernel(int n, const double* __restrict__ val, const 
                                    const int* __restrict__ diagpos, const unsigned char* __restrict__ isolated,
                                    double* __restrict__ dinv64, float* __restrict__ dinv32,
                                    double* __restrict__ isoinv) {
+    pdl_wait();
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
         const int dp = diagpos[i];
         const double d = dp >= 0 ? val[dp] : 0.0;
@@ -596,6 +630,7 @@ __global__ void update_diag_kernel(int n, const double* __restrict__ val, const 
 
 template <typename TZ>
 __global__ void add_kernel(int n, double* __restrict__ x, const TZ* __restrict__ z) {
+    pdl_wait();
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
         x[i] += double(z[i]);
 }
@@ -611,6 +646,7 @@ __global__ void __launch_bounds__(kThreads) dot_rz_kernel(int n, const double* _
                                                           const TZ* __restrict__ z, const double* __restrict__ q,
                                                           int flexible, double* partials, unsigned* ticket,
                                                           KScalars* sc) {
+    pdl_wait();
     double v[2] = {0.0, 0.0};
     const long S = (long)gridDim.x * blockDim.x;
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -644,6 +680,7 @@ __global__ void __launch_bounds__(kThreads) dot_rz_kernel(int n, const double* _
 template <typename TZ>
 __global__ void update_p_kernel(int n, const TZ* __restrict__ z, double* __restrict__ p, int flexible,
                                 KScalars* sc) {
+    pdl_wait();
     const bool first = (sc->iter == 0);
     double beta = 0.0;
     if (!first) beta = flexible ? (-sc->alpha * sc->t / sc->s_old) : (sc->s / sc->s_old);
@@ -674,9 +711,10 @@ __global__ void update_p_kernel(int n, const TZ* __restrict__ z, double* __restr
 
 // s_old = s; s = r.z; tj[j-1] = z.q_{k-j}, j = 1..min(k, M)
 template <typename TZ, int M>
-__global__ void __launch_bounds__(kThreads) fcg_dot_kernel(int n, const double* __restrict__ r,
+__global__ void __launch_bounds__(kThreads, 4) fcg_dot_kernel(int n, const double* __restrict__ r,
                                                            const TZ* __restrict__ z, const double* __restrict__ qh,
                                                            double* partials, unsigned* ticket, KScalars* sc) {
+    pdl_wait();
     const int k = sc->iter;
     const int nprev = k < M ? k : M;
     const double* qs[M];
@@ -722,8 +760,9 @@ __global__ void __launch_bounds__(kThreads) fcg_dot_kernel(int n, const double* 
 
 // p_k = z - sum_j (tj[j-1] / pqh[(k-j) mod M]) p_{k-j}
 template <typename TZ, int M>
-__global__ void fcg_update_p_kernel(int n, const TZ* __restrict__ z, const double* __restrict__ ph,
+__global__ void __launch_bounds__(kThreads, 4) fcg_update_p_kernel(int n, const TZ* __restrict__ z, const double* __restrict__ ph,
                                     double* __restrict__ p, const KScalars* sc) {
+    pdl_wait();
     const int k = sc->iter;
     const int nprev = k < M ? k : M;
     double c[M];
@@ -768,6 +807,7 @@ __global__ void __launch_bounds__(kThreads) update_xr_kernel(int n, double* __re
                                                              const double* __restrict__ q, double* partials,
                                                              unsigned* ticket, KScalars* sc, int hm,
                                                              double* __restrict__ ph, double* __restrict__ qh) {
+    pdl_wait();
     const double alpha = sc->s / sc->pq;
     double* hp = nullptr;
     double* hq = nullptr;
@@ -825,6 +865,7 @@ __global__ void __launch_bounds__(kThreads) update_xr_kernel(int n, double* __re
 template <typename T>
 __global__ void __launch_bounds__(kThreads) norm2_kernel(int n, const T* __restrict__ v, double* partials,
                                                          unsigned* ticket, KScalars* sc) {
+    pdl_wait();
     double a[1] = {0.0};
     const long S = (long)gridDim.x * blockDim.x;
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1087,6 +1128,7 @@ __device__ __forceinline__ void fused_sweeps(const FusedStep& st, TX* xs, const 
 // dynamic shared memory of a block: a copy of x (n entries)
 template <typename TX, bool PRE>
 __global__ void __launch_bounds__(kFuseThreads, 1) fused_step_kernel(const FusedStep st) {
+    pdl_wait();
     extern __shared__ __align__(16) unsigned char fused_smem[];
     const cg::cluster_group cl = cg::this_cluster();
     TX* xs = reinterpret_cast<TX*>(fused_smem);
@@ -1413,10 +1455,32 @@ struct DLevel {
 
 // every non-CSR launch goes through here so that the library can report how many
 // kernels it issued
+// Every kernel of this file starts with pdl_wait(), so it may be launched with programmatic stream
+// serialisation (g_pdl, default on): its blocks start while the previous kernel drains, which hides most
+// of the launch gap between the many short kernels of a V-cycle.
+template <typename... KA, typename... A>
+void launch(void (*k)(KA...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, A... a) {
+    g_launches++;
+    if (g_pdl) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = grid;
+        cfg.blockDim = block;
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = st;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        cudaLaunchKernelEx(&cfg, k, static_cast<KA>(a)...);
+    } else {
+        k<<<grid, block, smem, st>>>(a...);
+    }
+}
+
 template <typename... KA, typename... A>
 void go(void (*k)(KA...), int grid, cudaStream_t st, A... a) {
-    g_launches++;
-    k<<<grid, kThreads, 0, st>>>(a...);
+    launch(k, dim3(grid), dim3(kThreads), 0, st, a...);
 }
 
 int grid_for(long items, int per_block) {
@@ -1580,6 +1644,9 @@ struct lina_gpu_amg {
                 d.group_row.push_back(c.n);
             }
             d.group_slice.assign(1, 0);
+            // mid-size levels: FP32 passes in natural order read the quad layout (measured on the 34k-row
+            // level of the 2.1M-dof elasticity hierarchy: 8-10 us per sweep against 12 us in lane groups)
+            if (!groups && c.n >= kQuadMinRows && (rc = upload_quads(d, c, ncols, qpos_out))) return rc;
             return cudaStreamSynchronize(stream) == cudaSuccess ? 0 : LINA_GPU_ECUDA;
         }
         SellHost S = make_sell(c, ncols, groups);
@@ -1613,19 +1680,28 @@ struct lina_gpu_amg {
             if ((rc = upload(&d.rowmap, S.rowmap.data(), S.rowmap.size()))) return rc;
         }
         // FP32 passes in natural order read the quad layout (sellq_kernel) where the columns fit 16 bits
-        QuadHost Q;
-        if (!groups && g_sell_bits == 16 && g_quads && make_quads(c, ncols, Q)) {
-            if ((rc = upload(&d.q_sptr, Q.sptr.data(), Q.sptr.size()))) return rc;
-            if ((rc = upload(&d.q_base, Q.base.data(), Q.base.size()))) return rc;
-            if ((rc = alloc(&d.q_col, Q.col.size() / 4))) return rc;
-            if ((rc = alloc(&d.q_val, Q.val.size() / 4))) return rc;
-            CK(cudaMemcpyAsync(d.q_col, Q.col.data(), Q.col.size() * sizeof(unsigned short), cudaMemcpyHostToDevice,
-                               stream));
-            CK(cudaMemcpyAsync(d.q_val, Q.val.data(), Q.val.size() * sizeof(float), cudaMemcpyHostToDevice, stream));
-            d.q_padded = (long)Q.val.size();
-            if (qpos_out) qpos_out->swap(Q.pos);
-        }
+        if (!groups && (rc = upload_quads(d, c, ncols, qpos_out))) return rc;
         // the host copies must outlive the asynchronous uploads
+        return cudaStreamSynchronize(stream) == cudaSuccess ? 0 : LINA_GPU_ECUDA;
+    }
+
+    // the quad layout of a natural-order matrix, where enabled and its columns fit 16-bit offsets (the
+    // matrix keeps its other layout for FP64 passes); synchronises before the host copy is released
+    static constexpr int kQuadMinRows = 20000;
+    int upload_quads(DCsr& d, const lina::Csr& c, int ncols, std::vector<int>* qpos_out) {
+        if (g_sell_bits != 16 || !g_quads) return 0;
+        QuadHost Q;
+        if (!make_quads(c, ncols, Q)) return 0;
+        int rc;
+        if ((rc = upload(&d.q_sptr, Q.sptr.data(), Q.sptr.size()))) return rc;
+        if ((rc = upload(&d.q_base, Q.base.data(), Q.base.size()))) return rc;
+        if ((rc = alloc(&d.q_col, Q.col.size() / 4))) return rc;
+        if ((rc = alloc(&d.q_val, Q.val.size() / 4))) return rc;
+        CK(cudaMemcpyAsync(d.q_col, Q.col.data(), Q.col.size() * sizeof(unsigned short), cudaMemcpyHostToDevice,
+                           stream));
+        CK(cudaMemcpyAsync(d.q_val, Q.val.data(), Q.val.size() * sizeof(float), cudaMemcpyHostToDevice, stream));
+        d.q_padded = (long)Q.val.size();
+        if (qpos_out) qpos_out->swap(Q.pos);
         return cudaStreamSynchronize(stream) == cudaSuccess ? 0 : LINA_GPU_ECUDA;
     }
 
@@ -1662,33 +1738,31 @@ struct lina_gpu_amg {
         const int* sp = m.sptr + slice0;
         if constexpr (sizeof(TX) == 4 && (MODE == M_SPMV || MODE == M_RESID || MODE == M_JACOBI || MODE == M_ADD)) {
             if (m.q_val && !m.rowmap && slice0 == 0 && 32 * slice1 >= m.n) {
-                sellq_kernel<MODE><<<grid, kThreads, 0, stream>>>(m.n, m.q_sptr, m.q_base, m.q_col, m.q_val,
-                                                                  (const float*)x, (float*)y, (const float*)b,
-                                                                  (const float*)dinv, (float)w, (const float*)z);
+                g_launches--;  // counted by launch()
+                launch(sellq_kernel<MODE>, dim3(grid), dim3(kThreads), 0, stream, m.n, (const int*)m.q_sptr,
+                       (const int2*)m.q_base, (const uint2*)m.q_col, (const float4*)m.q_val, (const float*)x,
+                       (float*)y, (const float*)b, (const float*)dinv, (float)w, (const float*)z);
                 return;
             }
         }
+        g_launches--;  // counted by launch()
+        const dim3 gd(grid), bd(kThreads);
         if (sizeof(TX) == 4 && m.col16) {
             const int2* sb = m.sbase + slice0;
             if (m.long_rows)
-                sell_kernel<TV, TX, MODE, true, unsigned short><<<grid, kThreads, 0, stream>>>(
-                    npos, nrows, rm, sp, sb, m.col16, val, x, y, b, dinv, w, z, partials, ticket, sc);
+                launch(sell_kernel<TV, TX, MODE, true, unsigned short>, gd, bd, 0, stream, npos, nrows, rm, sp, sb,
+                       (const unsigned short*)m.col16, val, x, y, b, dinv, w, z, partials, ticket, sc);
             else
-                sell_kernel<TV, TX, MODE, false, unsigned short><<<grid, kThreads, 0, stream>>>(
-                    npos, nrows, rm, sp, sb, m.col16, val, x, y, b, dinv, w, z, partials, ticket, sc);
+                launch(sell_kernel<TV, TX, MODE, false, unsigned short>, gd, bd, 0, stream, npos, nrows, rm, sp, sb,
+                       (const unsigned short*)m.col16, val, x, y, b, dinv, w, z, partials, ticket, sc);
         } else if (m.long_rows) {
-            sell_kernel<TV, TX, MODE, true, int><<<grid, kThreads, 0, stream>>>(npos, nrows, rm, sp, nullptr, m.col,
-                                                                                 val, x, y, b, dinv, w, z, partials,
-                                                                                 ticket, sc);
+            launch(sell_kernel<TV, TX, MODE, true, int>, gd, bd, 0, stream, npos, nrows, rm, sp, (const int2*)nullptr,
+                   (const int*)m.col, val, x, y, b, dinv, w, z, partials, ticket, sc);
         } else {
-            sell_kernel<TV, TX, MODE, false, int><<<grid, kThreads, 0, stream>>>(npos, nrows, rm, sp, nullptr, m.col,
-                                                                                  val, x, y, b, dinv, w, z, partials,
-                                                                                  ticket, sc);
+            launch(sell_kernel<TV, TX, MODE, false, int>, gd, bd, 0, stream, npos, nrows, rm, sp, (const int2*)nullptr,
+                   (const int*)m.col, val, x, y, b, dinv, w, z, partials, ticket, sc);
         }
-        if (MODE == M_DOT) {
-            g_launches++;
-            dot_finish_kernel<<<1, kThreads, 0, stream>>>(grid, partials, sc);
-        }
+        if (MODE == M_DOT) launch(dot_finish_kernel, dim3(1), dim3(1024), 0, stream, grid, (const double*)partials, sc);
     }
 
     template <typename TV, typename TX, int MODE>
@@ -1696,16 +1770,24 @@ struct lina_gpu_amg {
                        const TX* dinv, TX w, const TX* z) {
         const int nrows = r1 - r0;
         if (nrows <= 0) return;
+        if constexpr (sizeof(TX) == 4 && (MODE == M_SPMV || MODE == M_RESID || MODE == M_JACOBI || MODE == M_ADD)) {
+            if (m.q_val && !m.rows && r0 == 0 && r1 == m.n) {
+                const int grid = (((m.n + 31) / 32) * 32 + kThreads - 1) / kThreads;
+                launch(sellq_kernel<MODE>, dim3(grid), dim3(kThreads), 0, stream, m.n, (const int*)m.q_sptr,
+                       (const int2*)m.q_base, (const uint2*)m.q_col, (const float4*)m.q_val, (const float*)x,
+                       (float*)y, (const float*)b, (const float*)dinv, (float)w, (const float*)z);
+                return;
+            }
+        }
         const int S = m.lanes;
         long grid = ((long)nrows * S + kThreads - 1) / kThreads;
         if (MODE == M_DOT && grid > kMaxBlocks) grid = kMaxBlocks;
         if (grid > (1L << 30)) grid = 1L << 30;
         const int* rl = m.rows ? m.rows + r0 : nullptr;
-        g_launches++;
 #define LINA_CSRV_CASE(SS)                                                                                       \
     case SS:                                                                                                     \
-        csrv_kernel<TV, TX, SS, MODE><<<(int)grid, kThreads, 0, stream>>>(nrows, rl, m.ptr, m.col, val, x, y, b, \
-                                                                          dinv, w, z, partials, ticket, sc);     \
+        launch(csrv_kernel<TV, TX, SS, MODE>, dim3((int)grid), dim3(kThreads), 0, stream, nrows, rl,              \
+               (const int*)m.ptr, (const int*)m.col, val, x, y, b, dinv, w, z, partials, ticket, sc);             \
         break;
         switch (S) {
             LINA_CSRV_CASE(4)
@@ -1715,10 +1797,7 @@ struct lina_gpu_amg {
                 LINA_CSRV_CASE(32)
         }
 #undef LINA_CSRV_CASE
-        if (MODE == M_DOT) {
-            g_launches++;
-            dot_finish_kernel<<<1, kThreads, 0, stream>>>((int)grid, partials, sc);
-        }
+        if (MODE == M_DOT) launch(dot_finish_kernel, dim3(1), dim3(1024), 0, stream, (int)grid, (const double*)partials, sc);
     }
 
     // all rows of m (natural order)
@@ -2070,7 +2149,7 @@ struct lina_gpu_amg {
         if (fcg_m > 0) return fcg_m;
         return opt.precision == LINA_PREC_MIXED ? kFcgDefault : 1;
     }
-    static constexpr int kFcgDefault = 4;
+    static constexpr int kFcgDefault = 6;
     // the rings of kept directions (allocated before any capture)
     int ensure_history() {
         const int m = history();
@@ -2369,6 +2448,11 @@ int lina_gpu_set_layout(int layout) {
         return LINA_GPU_EINVAL;
     }
     g_layout = layout;
+    return 0;
+}
+
+int lina_gpu_set_pdl(int on) {
+    g_pdl = on ? 1 : 0;
     return 0;
 }
 
@@ -3031,6 +3115,7 @@ namespace {
 __global__ void matrix_values_kernel(long nnz, const double* __restrict__ val, const int* __restrict__ pos,
                                      double* __restrict__ v64, float* __restrict__ v32, const int* __restrict__ qpos,
                                      float* __restrict__ q32) {
+    pdl_wait();
     for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (long)gridDim.x * blockDim.x) {
         const int p = pos ? pos[k] : (int)k;
         if (p >= 0) {
@@ -3046,6 +3131,7 @@ __global__ void matrix_values_kernel(long nnz, const double* __restrict__ val, c
 
 __global__ void matrix_dinv_kernel(int n, const double* __restrict__ val, const int* __restrict__ diagpos,
                                    double* __restrict__ d64, float* __restrict__ d32) {
+    pdl_wait();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int p = diagpos[i];
         const double d = (p >= 0 && val[p] != 0.0) ? 1.0 / val[p] : 0.0;
@@ -3307,10 +3393,14 @@ struct BatchLimits {
     int pad;
 };
 
-__global__ void save_norm_kernel(KScalars* sc) { sc->aux = sc->norm2; }
+__global__ void save_norm_kernel(KScalars* sc) {
+    pdl_wait();
+    sc->aux = sc->norm2;
+}
 
 // sc->norm2 holds r0^2 (||b||^2 or ||M^-1 b||^2); the loop runs when r0 is a positive number
 __global__ void batch_start_kernel(cudaGraphConditionalHandle hd, KScalars* sc, const BatchLimits* lim) {
+    pdl_wait();
     const double r0 = sqrt(sc->norm2);
     sc->r0 = r0;
     sc->tol = lim->tol;

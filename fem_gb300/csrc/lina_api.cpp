@@ -681,6 +681,8 @@ int gpu_precision = LINA_PREC_FP64;
 void (*amg_smoother)(sparse_matrix*, double*, double*, int*, double, int, int, int) = nullptr;
 
 std::unordered_map<amg_system_info*, lina_gpu_amg*> g_amg;
+// the caller's matrix each hierarchy was built from (AMG_setup, AMG_recompute_coarse_matrices)
+std::unordered_map<amg_system_info*, const sparse_matrix*> g_amg_source;
 
 // the GPU smoother standing for the installed smoother function
 bool gpu_smoother(int* kind, double* omega) {
@@ -898,6 +900,7 @@ amg_system_info* AMG_setup(sparse_matrix* A, int deg_of_freedom, int depth, int 
         if (get_diag(A, i) < 0) S->Values[i][0] = -1.;
     I->Signs = S;
     g_amg[I] = h;
+    g_amg_source[I] = A;
     return I;
 }
 
@@ -960,6 +963,7 @@ void AMG_recompute_coarse_matrices(amg_system_info* Info, sparse_matrix* New_mat
     }
     free_info_levels(Info);
     fill_info_levels(Info, it->second);
+    g_amg_source[Info] = New_matrix;
 }
 
 void AMG_free_data(amg_system_info* Data) {
@@ -968,6 +972,7 @@ void AMG_free_data(amg_system_info* Data) {
         lina_gpu_amg_destroy(it->second);
         g_amg.erase(it);
     }
+    g_amg_source.erase(Data);
     free_info_levels(Data);
     if (Data->Signs) { free_sparse(Data->Signs); }
     free(Data->Coarse_A);
@@ -1051,6 +1056,19 @@ bool apply_matmult(MatMult f, sparse_matrix* own, int n, const double* x, double
 // Z = M^-1 R; the AMG preconditioners warm-start from the incoming Z like
 // AMG_solve does on the host (PCGS.c:114, BiCGStab.c:84)
 int apply_precon(Precon f, int n, const double* r, double* z, amg_statistics* stat) {
+    if (f == PCG_AMG_vcycle_precon) {
+        auto it = g_amg.find(pcg_amg_data);
+        int kind;
+        double omega;
+        if (it == g_amg.end() || !gpu_smoother(&kind, &omega)) return -1;
+        lina_gpu_amg_set_smoother(it->second, kind, omega, gpu_precision);
+        if (!lina::dev::zero(z, n)) return -1;
+        lina::dev::sync();
+        int iters = 0;
+        double rel = 0;
+        int rc = lina_gpu_amg_solve(it->second, r, z, 0.0, 1, LINA_PCG_DEVICE_PTRS, &iters, &rel);
+        return (rc != 0 && rc != LINA_GPU_EBREAKDOWN) ? -1 : iters;
+    }
     amg_system_info* data = nullptr;
     if (f == PCG_AMG_precon) data = pcg_amg_data;
     if (f == BI_AMG_precon) data = bi_amg_data;
@@ -1106,18 +1124,25 @@ int bi_max_iter = 1000;  // BiCGStab.c:12
 double bi_eps = 1e-8;    // :13
 int bi_info = YES;       // :14
 
+// Work vectors of the drop-in Krylov loops, kept between calls (grown when a larger system comes) so
+// that a caller solving repeatedly does not pay device allocations on every call.
 struct DevVecs {
     std::vector<double*> v;
-    explicit DevVecs(int count, int n) : v(count, nullptr) {
-        for (auto& p : v) p = lina::dev::alloc(n);
+    DevVecs(int count, int n) {
+        static std::vector<double*> cache;
+        static int cache_n = 0;
+        if (n > cache_n) {
+            for (auto p : cache) lina::dev::release(p);
+            cache.clear();
+            cache_n = n;
+        }
+        while ((int)cache.size() < count) cache.push_back(lina::dev::alloc(cache_n));
+        v.assign(cache.begin(), cache.begin() + count);
     }
     bool ok() const {
         for (auto p : v)
             if (!p) return false;
         return true;
-    }
-    ~DevVecs() {
-        for (auto p : v) lina::dev::release(p);
     }
 };
 
@@ -1176,6 +1201,29 @@ int PCG_AMG_precon(int n, double* Y, double* X) {
     return AMG_solve(pcg_amg_data, Y, X, nullptr);
 }
 
+// One V-cycle of the hierarchy set by PCG_set_AMG_data (or PCG_set_AMG_preconditioner) from the zero
+// guess: Z = M^-1 R with the isolated-row fix.  No counterpart in the reference (whose PCG_AMG_precon
+// warm-starts AMG_solve from the incoming Z and repeats V-cycles to AMG_eps); installed with
+// PCG_set_precon it makes pcg run entirely on the device (see pcg).
+int PCG_AMG_vcycle_precon(int n, double* R, double* Z) {
+    auto it = g_amg.find(pcg_amg_data);
+    if (it == g_amg.end()) {
+        fprintf(stderr, "LinA-GB300: PCG_AMG_vcycle_precon without AMG data (PCG_set_AMG_data)\n");
+        return -1;
+    }
+    for (int i = 0; i < n; i++) Z[i] = 0.0;
+    const int save_it = amg_max_iter;
+    const double save_eps = amg_eps;
+    amg_max_iter = 1;
+    amg_eps = 0.0;
+    const int k = AMG_solve(pcg_amg_data, R, Z, nullptr);
+    amg_max_iter = save_it;
+    amg_eps = save_eps;
+    return k;
+}
+
+void PCG_set_AMG_data(amg_system_info* data) { pcg_amg_data = data; }
+
 void PCG_set_AMG_preconditioner(sparse_matrix* A, int num_fields, int depth) {
     AMG_print_info(NO);
     AMG_set_SOR_relaxation_coeff(1.6);
@@ -1186,8 +1234,43 @@ void PCG_set_AMG_preconditioner(sparse_matrix* A, int num_fields, int depth) {
     PCG_set_precon(PCG_AMG_precon);
 }
 
+namespace {
+// pcg with the library's operator and the zero-guess V-cycle: the whole loop on the device as the
+// captured graph of lina_gpu_pcg, with the reference's stopping rule ||R|| / ||M^-1 R_0||, B and X scaled
+// by 1/||B|| during the solve, X the initial guess, and the closing preconditioner application that
+// gives get_pcg_residuum.  -2 when the fast path does not apply.
+int pcg_on_device(double* X, double* B, int n, double tol, int max_iter) {
+    if (pcg_precon != PCG_AMG_vcycle_precon || pcg_mat_multi != PCG_mult || !pcg_default_A) return -2;
+    auto it = g_amg.find(pcg_amg_data);
+    auto src = g_amg_source.find(pcg_amg_data);
+    if (it == g_amg.end() || src == g_amg_source.end() || src->second != pcg_default_A || pcg_default_A->size != n)
+        return -2;
+    int kind;
+    double omega;
+    if (!gpu_smoother(&kind, &omega)) return -2;
+    lina_gpu_amg_set_smoother(it->second, kind, omega, gpu_precision);
+    lina_gpu_solve_info info;
+    const int rc = lina_gpu_pcg(it->second, B, X, tol, max_iter < 1 ? 1 : max_iter, LINA_STOP_REFERENCE,
+                                LINA_PCG_USE_X0 | LINA_PCG_NORMALIZE | LINA_PCG_FINAL_PRECON, &info);
+    if (rc == LINA_GPU_EBREAKDOWN || std::isnan(info.pcg_residuum)) {
+        printf("Fehler bei PCG: nan -> Abbruch\n");
+        pcg_res = info.pcg_residuum;
+        return -1;
+    }
+    if (rc != 0 && rc != LINA_GPU_ENOCONV) {
+        fprintf(stderr, "LinA-GB300: pcg failed: %s\n", lina_gpu_last_error());
+        return -1;
+    }
+    if (info.iterations >= max_iter) printf("Warnung: maximale Anzahl von %d Iterationen erreicht\n", info.iterations);
+    pcg_res = info.pcg_residuum;
+    return info.iterations;
+}
+}  // namespace
+
 // pcg (PCGS.c:163-233) with every vector on the GPU
 int pcg(double* X, double* B, int n, double tol, int max_iter) {
+    const int fast = pcg_on_device(X, B, n, tol, max_iter);
+    if (fast != -2) return fast;
     DevVecs d(7, n);
     if (!d.ok()) {
         fprintf(stderr, "LinA-GB300: pcg: device allocation failed\n");

@@ -133,6 +133,7 @@ def lib():
         "lina_gpu_set_fused_rows": (C.c_int, [C.c_int]),
         "lina_gpu_set_sell_index_bits": (C.c_int, [C.c_int]),
         "lina_gpu_set_sell_quads": (C.c_int, [C.c_int]),
+        "lina_gpu_set_pdl": (C.c_int, [C.c_int]),
         "lina_gpu_matrix_index_bits": (C.c_int, [vp]),
         "lina_gpu_level_index_bits": (C.c_int, [vp, C.c_int, ip, ip, ip]),
         "lina_gpu_last_error": (C.c_char_p, []),
@@ -297,6 +298,11 @@ def set_sell_index_bits(bits: int):
     """16 (the default): SELL-32 matrices with long rows uploaded afterwards also get 16-bit column
     offsets (two bases per slice, where the columns fit), read by FP32 passes; 32: int columns only."""
     _check(lib().lina_gpu_set_sell_index_bits(int(bits)), "set SELL index bits")
+
+
+def set_pdl(on):
+    """Programmatic dependent launch of the solve kernels (1, default) or plain stream order (0)."""
+    _check(lib().lina_gpu_set_pdl(int(on)), "set PDL")
 
 
 def set_sell_quads(on):
@@ -688,7 +694,7 @@ class AMG:
         _check(lib().lina_gpu_amg_set_smoother(self.h, smoother, omega, precision), "set smoother")
 
     def set_fcg_history(self, m):
-        """Directions kept by the flexible CG (0 default: FCG(4) mixed, CG FP64; 1 two-term; 2..8 FCG(m))."""
+        """Directions kept by the flexible CG (0 default: FCG(6) mixed, CG FP64; 1 two-term; 2..8 FCG(m))."""
         _check(lib().lina_gpu_amg_set_fcg_history(self.h, m), "set FCG history")
 
     def update_values(self, data=None, device_ptr=None):
@@ -864,3 +870,60 @@ class ElasticAdjoint:
             self.close()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------- the drop-in LinA API (include/*.h)
+class SparseMatrix(C.Structure):
+    """The reference's row-list sparse_matrix (LinA/linear_algebra.h:29-34)."""
+    _fields_ = [("Values", C.POINTER(C.POINTER(C.c_double))), ("Indices", C.POINTER(C.POINTER(C.c_int))),
+                ("Len", C.POINTER(C.c_int)), ("size", C.c_int)]
+
+
+class RowListView:
+    """A sparse_matrix whose rows point into the arrays of a CSR matrix (no copy): what a caller of the
+    drop-in API hands to AMG_setup, PCG_default and friends.  Read-only use: the library functions that
+    would grow or free rows must not be called on it."""
+
+    def __init__(self, indptr, indices, data):
+        self.ptr = np.ascontiguousarray(indptr, dtype=np.int64)
+        self.col = np.ascontiguousarray(indices, dtype=np.int32)
+        self.val = np.ascontiguousarray(data, dtype=np.float64)
+        n = len(self.ptr) - 1
+        self.len = np.ascontiguousarray(np.diff(self.ptr), dtype=np.int32)
+        self.vrows = (self.val.ctypes.data + 8 * self.ptr[:-1]).astype(np.uint64)
+        self.crows = (self.col.ctypes.data + 4 * self.ptr[:-1]).astype(np.uint64)
+        self.m = SparseMatrix(C.cast(self.vrows.ctypes.data, C.POINTER(C.POINTER(C.c_double))),
+                              C.cast(self.crows.ctypes.data, C.POINTER(C.POINTER(C.c_int))),
+                              C.cast(self.len.ctypes.data, C.POINTER(C.c_int)), n)
+
+    @property
+    def ref(self):
+        return C.byref(self.m)
+
+
+def dropin():
+    """The library with the signatures of the drop-in functions used from Python (AMG, PCG)."""
+    L = lib()
+    if getattr(L, "_dropin_ready", False):
+        return L
+    vp, dp = C.c_void_p, C.POINTER(C.c_double)
+    sig = {
+        "AMG_setup": (vp, [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp]),
+        "AMG_free_data": (None, [vp]),
+        "AMG_set_smoother": (None, [vp]),
+        "AMG_set_SOR_relaxation_coeff": (None, [C.c_double]),
+        "AMG_set_matrix_tolerance": (None, [C.c_double]),
+        "AMG_gpu_set_precision": (None, [C.c_int]),
+        "AMG_print_info": (None, [C.c_int]),
+        "PCG_default": (None, [vp, vp, vp]),
+        "PCG_set_AMG_data": (None, [vp]),
+        "PCG_set_precon": (None, [vp]),
+        "pcg": (C.c_int, [dp, dp, C.c_int, C.c_double, C.c_int]),
+        "get_pcg_residuum": (C.c_double, []),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    L._dropin_ready = True
+    return L

@@ -92,6 +92,17 @@ amg_system_info* AMG_setup(sparse_matrix* A, int AMG_deg_of_freedom, int depth, 
 int* AMG_default_iterations(int depth);
 void AMG_print_info(int s);
 void AMG_free_data(amg_system_info* Data);
+
+/* Extensions without a counterpart in the reference.  PCG_set_AMG_data selects the hierarchy (from
+   AMG_setup) that PCG_AMG_vcycle_precon applies: one V-cycle from the zero guess, Z = M^-1 R (AMG_solve
+   with one cycle and a zeroed Z).  When a caller installs PCG_default(A, ...) (the operator PCG_mult)
+   and PCG_set_precon(PCG_AMG_vcycle_precon) for a hierarchy built by AMG_setup from the same A (the same
+   pointer, unchanged since AMG_setup or AMG_recompute_coarse_matrices), pcg runs its whole loop on the
+   GPU as one captured graph: the reference's stopping rule ||R|| / ||M^-1 R_0||, X as initial guess,
+   get_pcg_residuum as the reference defines it; in mixed precision (AMG_gpu_set_precision(1)) the
+   iteration is the truncated flexible CG of lina_gpu_pcg. */
+void PCG_set_AMG_data(amg_system_info* data);
+int PCG_AMG_vcycle_precon(int n, double* R, double* Z);
 void AMG_set_SOR_relaxation_coeff(double alpha);
 void set_connection_thresholds(double negative, double positive);
 

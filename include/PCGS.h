@@ -33,6 +33,9 @@ void PCG_mult(int n, double* y, double* z);
 int PCG_preconlr(int n, double* z, double* w);
 int PCG_AMG_precon(int n, double* Y, double* X);
 
+/* PCG_set_AMG_data and PCG_AMG_vcycle_precon (extensions for pcg on the device) are declared in
+   Multigrid.h, after the hierarchy type. */
+
 #ifdef __cplusplus
 }
 #endif

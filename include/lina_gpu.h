@@ -127,7 +127,7 @@ int lina_gpu_amg_set_smoother(lina_gpu_amg* h, int smoother, double omega, int p
 /* Krylov directions kept by lina_gpu_pcg and the batch solves (no reference counterpart): m >= 2 runs the
    truncated flexible CG FCG(m) of Notay, which makes every new direction A-orthogonal to the last m
    (robust to the slight variation of the FP32 V-cycle between applications); m = 1 the two-term
-   recurrences (flexible beta in mixed precision, the reference's beta in FP64); 0 (default) FCG(4) in mixed
+   recurrences (flexible beta in mixed precision, the reference's beta in FP64); 0 (default) FCG(6) in mixed
    precision and the reference's CG in FP64.  Up to 8.  The LINA_PCG_BETA_* flags select the two-term
    recurrence for one call.  FCG(m) keeps 2 m extra FP64 vectors on the device. */
 int lina_gpu_amg_set_fcg_history(lina_gpu_amg* h, int m);
@@ -416,6 +416,11 @@ int lina_gpu_set_sell_index_bits(int bits);
    value load and one 8-byte index load), and their FP32 passes read it; 0: FP32 passes read the
    one-entry SELL-32 layout.  The results are identical. */
 int lina_gpu_set_sell_quads(int on);
+/* 1 (default): the solve's kernels are launched with programmatic dependent launch (each kernel waits
+   for the previous grid before touching memory, and its blocks are scheduled while that grid drains);
+   0: ordinary stream order.  Takes effect for launches issued afterwards (a hierarchy's captured solve
+   graph keeps the choice it was captured with).  The results are identical. */
+int lina_gpu_set_pdl(int on);
 
 const char* lina_gpu_last_error(void);
 

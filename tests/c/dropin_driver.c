@@ -9,6 +9,9 @@
  *            int32 indptr[n+1], int32 indices[nnz], float64 data[nnz], float64 b[n]
  *   modes  : "vcycle-pcg"  pcg with a caller-defined preconditioner running one
  *                          V-cycle from a zero guess through AMG_solve
+ *            "device-pcg"  PCG_default + PCG_set_AMG_data + PCG_AMG_vcycle_precon: the same
+ *                          preconditioner as the library's, pcg on the device
+ *            "device-pcg-clone"  the same with a copy of A as operator (host-driven loop)
  *            "stock"       PCG_default + PCG_set_AMG_preconditioner + pcg
  *            "amgsolve"    AMG_solve alone to 1e-8 (at most 200 V-cycles)
  *   out.bin: int32 iterations, float64 residuum, float64 x[n]
@@ -76,6 +79,22 @@ int main(int argc, char** argv) {
         PCG_set_precon(vcycle_precon);
         it = pcg(x, b, n, 1e-8, 500);
         res = get_pcg_residuum();
+        AMG_free_data(amg);
+        free(amg);
+    } else if (!strcmp(argv[1], "device-pcg") || !strcmp(argv[1], "device-pcg-clone")) {
+        /* the library's zero-guess V-cycle preconditioner: the whole pcg loop runs on the device; with
+           a copy of A as the operator the same preconditioner runs inside the host-driven loop */
+        AMG_set_SOR_relaxation_coeff(omega);
+        amg = AMG_setup(A, dof, depth, 2, 2, coarsening, STAND_ALONE, DIRECT, NULL, NULL);
+        sparse_matrix* op = !strcmp(argv[1], "device-pcg") ? A : clone(A);
+        PCG_default(op, NULL, NULL);
+        PCG_set_AMG_data(amg);
+        PCG_set_precon(PCG_AMG_vcycle_precon);
+        it = pcg(x, b, n, 1e-8, 500);
+        res = get_pcg_residuum();
+        if (op != A) {
+            free_sparse(op);
+        }
         AMG_free_data(amg);
         free(amg);
     } else if (!strcmp(argv[1], "stock")) {

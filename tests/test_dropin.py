@@ -67,6 +67,23 @@ def test_pcg_with_caller_vcycle_preconditioner(driver, tmp_path, name, smoother,
 
 
 @pytest.mark.parametrize("name", golden_cases("hierarchy"))
+@pytest.mark.parametrize("smoother,code,omega", [("jacobi", 2, 0.6), ("mcsor", 0, 1.0)])
+@pytest.mark.parametrize("mode", ["device-pcg", "device-pcg-clone"])
+@pytest.mark.gpu
+@pytest.mark.skipif(not gpu_available(), reason="no CUDA device")
+def test_pcg_with_library_vcycle_preconditioner(driver, tmp_path, name, smoother, code, omega, mode):
+    """PCG_set_AMG_data + PCG_AMG_vcycle_precon: pcg on the device (device-pcg) or driven from the host
+    with the preconditioner on the device (device-pcg-clone) reproduces the reference's pcg with a
+    one-V-cycle zero-guess preconditioner: iterations within 1, solution within 1e-9."""
+    g = load_golden(name)
+    s = system_for(name)
+    it, res, x = run_driver(driver, tmp_path, mode, s, int(g["depth"]), int(g["coarsening"]), code, omega)
+    assert abs(it - int(g[f"pcg_{smoother}_it"])) <= 1
+    assert rel(x, g[f"pcg_{smoother}_x"]) < 1e-9
+    assert res == pytest.approx(float(g[f"pcg_{smoother}_res"]), rel=1e-3)
+
+
+@pytest.mark.parametrize("name", golden_cases("hierarchy"))
 @pytest.mark.gpu
 @pytest.mark.skipif(not gpu_available(), reason="no CUDA device")
 def test_stock_amg_preconditioner(driver, tmp_path, name):
