@@ -837,7 +837,7 @@ bool square_clean(Csr& A) {
 // than one nonzero form a dense block factorised without pivoting; the other
 // rows are solved by their diagonal.  The block is stored as its inverse so
 // that the GPU coarse solve is one dense matrix-vector product.
-bool coarse_factor(const Csr& A, CoarseSolver& cs, std::string& err) {
+bool coarse_factor(const Csr& A, CoarseSolver& cs, std::string& err, int device_min_rows) {
     int n = A.n;
     cs = CoarseSolver();
     cs.n = n;
@@ -865,6 +865,11 @@ bool coarse_factor(const Csr& A, CoarseSolver& cs, std::string& err) {
             int J = map[A.col[p]];
             if (J >= 0) M[(size_t)I * m + J] = A.val[p];
         }
+    }
+    if (device_min_rows > 0 && m >= device_min_rows) {  // inverted on the GPU at upload (gpu_coarse.cu)
+        cs.inv = std::move(M);
+        cs.inverted = false;
+        return true;
     }
     // in-place Gauss-Jordan inversion without pivoting (the reference's LU does not pivot)
     std::vector<double>& X = M;
@@ -1095,7 +1100,7 @@ bool amg_setup_host(const Csr& Ain, const AmgParams& p, HostHierarchy& h) {
                     L.A.n, (long long)L.A.nnz(), secs(t0, t1), secs(t1, t2), secs(t2, t3), secs(t3, t4));
     }
     auto tc = now();
-    bool ok = coarse_factor(h.lv[0].A, h.coarse, h.error);
+    bool ok = coarse_factor(h.lv[0].A, h.coarse, h.error, p.coarse_device_rows);
     if (timing) fprintf(stderr, "coarsest n=%d block=%zu: %.2fs\n", h.lv[0].A.n, h.coarse.block_rows.size(), secs(tc, now()));
     return ok;
 }
@@ -1119,7 +1124,7 @@ bool amg_recompute_host(HostHierarchy& h, const Csr& A) {
             return false;
         }
     }
-    return coarse_factor(h.lv[0].A, h.coarse, h.error);
+    return coarse_factor(h.lv[0].A, h.coarse, h.error, h.params.coarse_device_rows);
 }
 
 // ---------------------------------------------------------------- hierarchy files
@@ -1224,7 +1229,7 @@ bool amg_save_host(const HostHierarchy& h, const std::string& dir, std::string& 
     return ok;
 }
 
-bool amg_load_host(const std::string& dir, HostHierarchy& h) {
+bool amg_load_host(const std::string& dir, HostHierarchy& h, int coarse_device_rows) {
     h = HostHierarchy();
     FILE* f = fopen((dir + "/hierarchy.txt").c_str(), "r");
     if (!f) {
@@ -1271,7 +1276,8 @@ bool amg_load_host(const std::string& dir, HostHierarchy& h) {
         h.error = "the hierarchy files in " + dir + " are missing or inconsistent";
         return false;
     }
-    return coarse_factor(h.lv[0].A, h.coarse, h.error);
+    h.params.coarse_device_rows = coarse_device_rows;
+    return coarse_factor(h.lv[0].A, h.coarse, h.error, coarse_device_rows);
 }
 
 }  // namespace lina

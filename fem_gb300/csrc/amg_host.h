@@ -39,6 +39,8 @@ struct AmgParams {
     double eps_plus = 0.5;
     double matrix_tol = 0.1;      // interpolation truncation (Multigrid.c:37)
     bool gpu_products = false;    // Galerkin products on the GPU (same results; host if it fails)
+    int coarse_device_rows = 0;   // coarsest dense blocks of at least this many rows are left for the GPU
+                                  // to invert (gpu_coarse.cu); 0: always inverted on the host
 };
 
 struct HostLevel {
@@ -53,7 +55,9 @@ struct HostLevel {
 struct CoarseSolver {
     int n = 0;                      // coarsest level size
     std::vector<int> block_rows;    // rows with more than one nonzero (dense block)
-    std::vector<double> inv;        // dense inverse of the block, row-major, m x m
+    std::vector<double> inv;        // dense inverse of the block, row-major, m x m (the block itself when
+                                    // inverted is false: the GPU inverts it at upload)
+    bool inverted = true;
     std::vector<double> diag_inv;   // 1/a_ii for rows outside the block (0 inside)
     std::vector<int> in_block;      // 1 if row is part of the dense block
 };
@@ -88,7 +92,8 @@ bool spgemm_gpu(const Csr& A, const Csr& B, Csr& C, std::string& err);
 bool write_csr_file(const std::string& path, const Csr& A);
 bool read_csr_file(const std::string& path, Csr& A, int ncols);
 bool amg_save_host(const HostHierarchy& h, const std::string& dir, std::string& err);
-bool amg_load_host(const std::string& dir, HostHierarchy& h);
+// coarse_device_rows: as AmgParams::coarse_device_rows for the reloaded coarsest block
+bool amg_load_host(const std::string& dir, HostHierarchy& h, int coarse_device_rows = 0);
 
 // PMIS labels on the GPU (gpu_pmis.cu) from the strong-connection sets S (sptr, sidx) and their
 // transpose T: label holds kIsolated / kCoarse for the points decided beforehand and kUndecided

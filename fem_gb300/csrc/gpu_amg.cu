@@ -29,6 +29,10 @@
 #include "gpu_ops.h"
 #include "lina_gpu.h"
 
+namespace lina {
+int dense_inverse(int m, double* a_dev, int method, cudaStream_t st, int* err_dev, std::string& msg);
+}
+
 namespace {
 
 std::string g_err;
@@ -44,6 +48,8 @@ int g_fused_rows = 24576;
 int g_sell_bits = 16;
 int g_quads = 1;  // FP32 passes read the quad layout (sellq_kernel); 0 keeps the one-entry SELL layout
 int g_pdl = 1;    // programmatic dependent launch of the solve kernels (launch())
+int g_coarse_device_rows = 256;      // coarsest blocks of this many rows or more are inverted on the GPU
+int g_dense_method = LINA_DENSE_SIMT;  // their rank-32 updates: FP64 CUDA cores or FP64 tensor cores
 
 void set_err(const char* fmt, ...) {
     char buf[512];
@@ -2322,6 +2328,15 @@ int upload_hierarchy(lina_gpu_amg* h) {
     if ((rc = h->upload(&h->c_inblock, cs.in_block.data(), cs.in_block.size()))) return rc;
     if ((rc = h->upload(&h->c_blockpos, blockpos.data(), blockpos.size()))) return rc;
     if ((rc = h->upload(&h->c_inv, cs.inv.data(), cs.inv.size()))) return rc;
+    if (!cs.inverted) {  // a large block: inverted in place on the device
+        int* err = nullptr;
+        if ((rc = h->alloc(&err, 1))) return rc;
+        std::string msg;
+        if ((rc = lina::dense_inverse(h->cm, h->c_inv, g_dense_method, h->stream, err, msg))) {
+            set_err("%s", msg.c_str());
+            return rc;
+        }
+    }
     if ((rc = h->upload(&h->c_dginv, cs.diag_inv.data(), cs.diag_inv.size()))) return rc;
     if ((rc = h->alloc(&h->c_bblk, std::max(h->cm, 1)))) return rc;
     // finest extras
@@ -2451,6 +2466,16 @@ int lina_gpu_set_layout(int layout) {
     return 0;
 }
 
+int lina_gpu_set_coarse_inverse(int min_rows, int method) {
+    if (min_rows < 0 || (method != LINA_DENSE_SIMT && method != LINA_DENSE_DMMA)) {
+        set_err("lina_gpu_set_coarse_inverse: invalid argument");
+        return LINA_GPU_EINVAL;
+    }
+    g_coarse_device_rows = min_rows;
+    g_dense_method = method;
+    return 0;
+}
+
 int lina_gpu_set_pdl(int on) {
     g_pdl = on ? 1 : 0;
     return 0;
@@ -2509,6 +2534,7 @@ static int amg_create_impl(int n, const int* rowptr, const int* col, const doubl
     p.eps_plus = opt->eps_plus;
     p.matrix_tol = opt->matrix_tol;
     p.gpu_products = !host_only;  // the Galerkin products on the GPU (bit-identical to the host's)
+    p.coarse_device_rows = host_only ? 0 : g_coarse_device_rows;
     if (!lina::amg_setup_host(csr_from(n, rowptr, col, val), p, h->host)) {
         set_err("AMG setup: %s", h->host.error.c_str());
         delete h;
@@ -2574,7 +2600,7 @@ int lina_gpu_amg_load(const char* dir, const lina_gpu_amg_options* opt, int host
     }
     *out = nullptr;
     lina_gpu_amg* h = new lina_gpu_amg();
-    if (!lina::amg_load_host(dir, h->host)) {
+    if (!lina::amg_load_host(dir, h->host, host_only ? 0 : g_coarse_device_rows)) {
         set_err("AMG load: %s", h->host.error.c_str());
         delete h;
         return LINA_GPU_EINVAL;

@@ -27,7 +27,13 @@ def main():
     ap.add_argument("--depth", type=int, default=10)
     ap.add_argument("--matrix-tol", type=float, default=0.1)
     ap.add_argument("--sell-bits", type=int, default=16, choices=[16, 32], help="SELL-32 column-index width")
+    ap.add_argument("--dense-inverse", type=str, default="",
+                    help="comma-separated sizes m: time the device inverse of a dense m x m block with FP64 CUDA "
+                         "cores and with FP64 tensor cores instead")
     args = ap.parse_args()
+    if args.dense_inverse:
+        dense_inverse(int(v) for v in args.dense_inverse.split(","))
+        return
     lina.set_sell_index_bits(args.sell_bits)
     s = problems.elasticity_p1(args.m)
     if args.level >= 0:
@@ -54,6 +60,25 @@ def main():
     out.update(level=args.level, n=n, nnz=int(ip[-1]), padded=int(M.padded_entries),
                index_bits=M.index_bits())
     print(out)
+
+
+def dense_inverse(sizes, reps=3):
+    """Blocked Gauss-Jordan inverse of diagonally dominant m x m blocks: device time per inverse with the
+    rank-32 updates on FP64 CUDA cores (SIMT) and on FP64 tensor cores (DMMA); 2 m^3 flops each."""
+    for m in sizes:
+        rng = np.random.default_rng(m)
+        a = rng.uniform(-1, 1, (m, m))
+        a += np.diag(np.abs(a).sum(axis=1) + 1.0)
+        row = {"m": m}
+        for name, method in (("simt", lina.DENSE_SIMT), ("dmma", lina.DENSE_DMMA)):
+            ts = []
+            for _ in range(reps):
+                d = lina.DeviceArray.from_host(a.ravel())
+                ts.append(lina.dense_inverse_device(d, m, method))
+            ms = min(ts)
+            row[f"{name}_ms"] = ms
+            row[f"{name}_tflops"] = 2.0 * m ** 3 / (ms * 1e-3) / 1e12
+        print(row, flush=True)
 
 
 if __name__ == "__main__":

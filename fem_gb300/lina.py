@@ -134,6 +134,8 @@ def lib():
         "lina_gpu_set_sell_index_bits": (C.c_int, [C.c_int]),
         "lina_gpu_set_sell_quads": (C.c_int, [C.c_int]),
         "lina_gpu_set_pdl": (C.c_int, [C.c_int]),
+        "lina_gpu_dense_inverse": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
+        "lina_gpu_set_coarse_inverse": (C.c_int, [C.c_int, C.c_int]),
         "lina_gpu_matrix_index_bits": (C.c_int, [vp]),
         "lina_gpu_level_index_bits": (C.c_int, [vp, C.c_int, ip, ip, ip]),
         "lina_gpu_last_error": (C.c_char_p, []),
@@ -298,6 +300,22 @@ def set_sell_index_bits(bits: int):
     """16 (the default): SELL-32 matrices with long rows uploaded afterwards also get 16-bit column
     offsets (two bases per slice, where the columns fit), read by FP32 passes; 32: int columns only."""
     _check(lib().lina_gpu_set_sell_index_bits(int(bits)), "set SELL index bits")
+
+
+DENSE_SIMT, DENSE_DMMA = 0, 1
+
+
+def dense_inverse_device(a: "DeviceArray", m, method=DENSE_SIMT):
+    """In-place inverse of the m x m row-major matrix in a (device) by blocked Gauss-Jordan without
+    pivoting; returns the device time in ms."""
+    ms = C.c_double()
+    _check(lib().lina_gpu_dense_inverse(C.c_int(m), C.c_void_p(a.ptr), method, C.byref(ms)), "dense inverse")
+    return ms.value
+
+
+def set_coarse_inverse(min_rows, method=DENSE_SIMT):
+    """Coarsest blocks of min_rows rows or more inverted on the GPU (0: host) with method."""
+    _check(lib().lina_gpu_set_coarse_inverse(int(min_rows), int(method)), "set coarse inverse")
 
 
 def set_pdl(on):

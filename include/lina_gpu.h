@@ -422,6 +422,21 @@ int lina_gpu_set_sell_quads(int on);
    graph keeps the choice it was captured with).  The results are identical. */
 int lina_gpu_set_pdl(int on);
 
+/* Dense inverse of a row-major m x m matrix in device memory, in place, by blocked Gauss-Jordan
+   elimination without pivoting (the elimination order of the reference's dense LU,
+   LinA/linear_algebra.c:2909, so it exists exactly when that factorisation does).  method selects the
+   arithmetic of the rank-32 updates, which carry 2 m^3 flops: LINA_DENSE_SIMT on the FP64 CUDA cores,
+   LINA_DENSE_DMMA on the FP64 tensor cores (mma.sync m8n8k4).  *ms (may be NULL) receives the device
+   time.  LINA_GPU_ESETUP on a zero pivot.  The coarsest AMG block is inverted this way at set-up and
+   recompute when it has at least the rows set by lina_gpu_set_coarse_inverse (default 256, SIMT);
+   smaller blocks are inverted on the host. */
+#define LINA_DENSE_SIMT 0
+#define LINA_DENSE_DMMA 1
+int lina_gpu_dense_inverse(int m, double* a_dev, int method, double* ms);
+/* coarsest blocks of min_rows rows or more are inverted on the GPU with method (0: always on the host);
+   hierarchies created or recomputed afterwards */
+int lina_gpu_set_coarse_inverse(int min_rows, int method);
+
 const char* lina_gpu_last_error(void);
 
 #ifdef __cplusplus

@@ -39,6 +39,8 @@ CASES = {
     "poisson33_std": (lambda: problems.poisson_p1(33, seed=0), 4, ref.STANDARD),
     "elast17_aggr": (lambda: problems.elasticity_p1(17), 3, ref.AGGRESSIVE),
     "elast17_std": (lambda: problems.elasticity_p1(17), 3, ref.STANDARD),
+    # two levels: a coarsest dense block of about 2,000 rows (the GPU inverts it at set-up)
+    "poisson65_d2": (lambda: problems.poisson_p1(65, seed=0), 2, ref.STANDARD),
 }
 # larger systems for which only the solves are stored (the input is regenerated
 # by fem_gb300.problems and checked against the stored digest)
