@@ -48,6 +48,7 @@ int g_fused_rows = 24576;
 int g_sell_bits = 16;
 int g_quads = 1;  // FP32 passes read the quad layout (sellq_kernel); 0 keeps the one-entry SELL layout
 int g_pdl = 1;    // programmatic dependent launch of the solve kernels (launch())
+long g_mem_limit = 0;  // device bytes one handle may hold (0: no limit), lina_gpu_set_device_memory_limit
 int g_coarse_device_rows = 256;      // coarsest blocks of this many rows or more are inverted on the GPU
 int g_dense_method = LINA_DENSE_SIMT;  // their rank-32 updates: FP64 CUDA cores or FP64 tensor cores
 
@@ -1577,6 +1578,12 @@ struct lina_gpu_amg {
     template <typename T>
     int alloc(T** p, size_t count) {
         if (count == 0) count = 1;
+        if (g_mem_limit > 0 && dev_bytes + (long)(count * sizeof(T)) > g_mem_limit) {
+            set_err("cudaMalloc(%zu bytes) refused: the handle's device-memory limit of %ld bytes "
+                    "(lina_gpu_set_device_memory_limit) would be exceeded", count * sizeof(T), g_mem_limit);
+            *p = nullptr;
+            return LINA_GPU_ECUDA;
+        }
         cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
         if (e != cudaSuccess) {
             set_err("cudaMalloc(%zu bytes) failed: %s", count * sizeof(T), cudaGetErrorString(e));
@@ -2473,6 +2480,15 @@ int lina_gpu_set_coarse_inverse(int min_rows, int method) {
     }
     g_coarse_device_rows = min_rows;
     g_dense_method = method;
+    return 0;
+}
+
+int lina_gpu_set_device_memory_limit(long bytes) {
+    if (bytes < 0) {
+        set_err("lina_gpu_set_device_memory_limit: negative limit");
+        return LINA_GPU_EINVAL;
+    }
+    g_mem_limit = bytes;
     return 0;
 }
 

@@ -1533,3 +1533,103 @@ int lina_gpu_bicgstab(lina_gpu_matrix* Am, lina_gpu_ilu* ilu, int ilu_precision,
 }
 
 }  // extern "C"
+
+// ============================================================ local solvers for the caller's solver slots
+// The reference's callers hand a whole linear solve to a function int f(sparse_matrix* A, double* X,
+// double* b): reflective_newton's RN_set_local_solver slot (reflective_newton.c:308), active_set_solver's
+// Solver (linear_algebra.c:4995), and Crack/crack.c's UMFPACK wrapper multifrontal_solver (:5424, used by
+// the elastic step :9340 and, through multifrontal_solver_AS, the chemical step's active-set solver
+// :9250).  These two functions fill such slots on the GPU.  They return POSITIVE_DEFINITE (1) when the
+// solve reached its tolerance and INDEFINITE (0) otherwise, the convention of the RN slot.
+namespace {
+
+struct SpdCache {
+    lina_gpu_amg* h = nullptr;
+    int n = 0;
+    uint64_t pattern = 0;
+    int dof = 0;
+} g_spd;
+
+uint64_t pattern_fingerprint(const sparse_matrix* A) {
+    uint64_t h = 1469598103934665603ull ^ (uint64_t)A->size;
+    for (int i = 0; i < A->size; i++) {
+        h = (h ^ (uint64_t)A->Len[i]) * 1099511628211ull;
+        for (int k = 0; k < A->Len[i]; k++) h = (h ^ (uint64_t)(uint32_t)A->Indices[i][k]) * 1099511628211ull;
+    }
+    return h;
+}
+
+// levels of the hierarchy for an n-row system: coarsen until a few thousand rows remain
+int spd_depth(int n) {
+    int d = 1;
+    for (double m = n; m > 4000.0 && d < 12; m /= 2.6) d++;
+    return d < 2 ? 2 : d;
+}
+
+}  // namespace
+
+extern "C" {
+
+/* A X = b for symmetric positive definite A (an elasticity or reaction-diffusion step, the scaled Newton
+   matrix of reflective_newton) by AMG-preconditioned CG on the GPU: standard coarsening with the unknowns
+   per node of AMG_set_deg_of_freedom, mixed precision, X as initial guess, to ||b - A X|| <= 1e-10 ||b||.
+   The hierarchy is kept between calls and rebuilt only when A's pattern changes; new values on the same
+   pattern recompute its coarse levels (AMG_recompute_coarse_matrices). */
+int LinA_gpu_spd_solver(sparse_matrix* A, double* X, double* b) {
+    if (!A || !X || !b || A->size <= 0) return INDEFINITE;
+    CsrCopy c = to_csr(A);
+    const uint64_t pat = pattern_fingerprint(A);
+    int rc = 0;
+    if (g_spd.h && g_spd.n == c.n && g_spd.pattern == pat && g_spd.dof == amg_dof) {
+        rc = lina_gpu_amg_recompute(g_spd.h, c.n, c.ptr.data(), c.col.data(), c.val.data());
+    } else {
+        if (g_spd.h) lina_gpu_amg_destroy(g_spd.h);
+        g_spd = SpdCache();
+        lina_gpu_amg_options o;
+        lina_gpu_default_options(&o);
+        o.dof = amg_dof > 0 && c.n % amg_dof == 0 ? amg_dof : 1;
+        o.depth = spd_depth(c.n);
+        o.coarsening = LINA_STANDARD;
+        o.smoother = LINA_SMOOTHER_JACOBI;
+        o.omega = 0.6;
+        o.precision = LINA_PREC_MIXED;
+        rc = lina_gpu_amg_create(c.n, c.ptr.data(), c.col.data(), c.val.data(), &o, &g_spd.h);
+        if (rc == 0) {
+            g_spd.n = c.n;
+            g_spd.pattern = pat;
+            g_spd.dof = amg_dof;
+        } else {
+            g_spd.h = nullptr;
+        }
+    }
+    if (rc != 0) {
+        fprintf(stderr, "LinA-GB300: LinA_gpu_spd_solver: set-up failed: %s\n", lina_gpu_last_error());
+        return INDEFINITE;
+    }
+    lina_gpu_solve_info info;
+    rc = lina_gpu_pcg(g_spd.h, b, X, 1e-10, 5000, LINA_STOP_RELATIVE, LINA_PCG_USE_X0, &info);
+    return rc == 0 ? POSITIVE_DEFINITE : INDEFINITE;
+}
+
+/* A X = b for a general square A (nonsymmetric, or the indefinite KKT systems active_set_solver builds)
+   by restarted GMRES(30) on the GPU with ILU(0) of A as right preconditioner (none where the incomplete
+   factorisation meets a zero pivot), X as initial guess, to a relative residual of 1e-10. */
+int LinA_gpu_general_solver(sparse_matrix* A, double* X, double* b) {
+    if (!A || !X || !b || A->size <= 0) return INDEFINITE;
+    lina_gpu_matrix* m = device_matrix(A);
+    if (!m) return INDEFINITE;
+    CsrCopy c = to_csr(A);
+    lina_gpu_ilu* ilu = nullptr;
+    if (lina_gpu_ilu_create_from_matrix(c.n, c.ptr.data(), c.col.data(), c.val.data(), &ilu) != 0) ilu = nullptr;
+    lina_gpu_solve_info info;
+    // GMRES works on the preconditioned unknown y (x = B_r y); start from y = 0 and return x
+    std::vector<double> y(c.n, 0.0);
+    int rc = lina_gpu_gmres(m, ilu, nullptr, LINA_PREC_FP64, b, y.data(), 1e-10, 30, 20000, 1,
+                            LINA_GMRES_APPLY_PRECON, &info);
+    if (ilu) lina_gpu_ilu_destroy(ilu);
+    if (rc != 0 && rc != LINA_GPU_ENOCONV) return INDEFINITE;
+    for (int i = 0; i < c.n; i++) X[i] = y[i];
+    return rc == 0 ? POSITIVE_DEFINITE : INDEFINITE;
+}
+
+}  // extern "C"

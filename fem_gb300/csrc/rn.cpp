@@ -534,16 +534,28 @@ bool subspace_min_dev(lina_gpu_matrix* A, int n, const double* b, const double* 
     return true;
 }
 
-// Largest-magnitude eigenpair by power iteration (power_method, linear_algebra.c:4802), and the
-// direction of most negative curvature via the shifted operator A - shift I
-// (get_neg_curvature_direction, :4849).  The reference starts from a time-seeded random vector;
-// here the start vector is a fixed pseudo-random one so that runs repeat.
+// Largest-magnitude eigenpair by power iteration (power_method, linear_algebra.c:4802-4823): x <- A x (or
+// (A - shift I) x), eigenvalue estimate x_new . x_old, x normalised, until the estimate changes by at most
+// eps times the operator's mean absolute row sum (matrix_norm, :3441, of the shifted matrix for the
+// shifted run).  prev is the estimate before the first step: the reference's second run starts from the
+// caller's 0; its first run reads an unset value, for which at least two steps are taken here.
 int power_iteration(lina_gpu_matrix* A, const CsrCopy& Ac, double shift, double* x, double* tmp, int n, int max_iter,
-                    double eps, double* eig) {
+                    double eps, double prev0, bool two_steps, double* eig) {
     double q = 0;
-    for (double v : Ac.val) q += fabs(v);
+    for (int i = 0; i < n; i++) {
+        bool diag = false;
+        for (int p = Ac.ptr[i]; p < Ac.ptr[i + 1]; p++) {
+            if (Ac.col[p] == i) {
+                diag = true;
+                q += fabs(Ac.val[p] - shift);
+            } else {
+                q += fabs(Ac.val[p]);
+            }
+        }
+        if (!diag && shift != 0) q += fabs(shift);
+    }
     q /= n;
-    double prev, lambda = 0;
+    double prev, lambda = prev0;
     int i = 0;
     double r;
     do {
@@ -556,24 +568,76 @@ int power_iteration(lina_gpu_matrix* A, const CsrCopy& Ac, double shift, double*
         lina::dev::scal(x, 1. / sqrt(lina::dev::dot(x, x, n)), n);
         r = fabs(lambda - prev) / q;
         i++;
-    } while ((r > eps || i == 1) && i < max_iter);
+    } while ((r > eps || (two_steps && i == 1)) && i < max_iter);
     *eig = lambda;
     return i == max_iter ? 0 : i;
 }
 
-void fixed_random_unit(double* x, int n, std::vector<double>& host) {
-    uint64_t s = 0x2545F4914F6CDD1Dull;
+// set_random_normal_vector (linear_algebra.c:4823-4828): rand() / RAND_MAX after srand, normalised.  The
+// reference seeds with time(NULL); the library seeds with kRnSeed so that runs repeat (the reference run
+// with time() returning kRnSeed draws the same vector).
+constexpr unsigned kRnSeed = 1;
+void seeded_random_unit(double* x, int n, std::vector<double>& host) {
+    srand(kRnSeed);
+    for (int i = 0; i < n; i++) host[i] = (double)rand() / RAND_MAX;
     double nrm = 0;
-    for (int i = 0; i < n; i++) {
-        s ^= s << 13;
-        s ^= s >> 7;
-        s ^= s << 17;
-        host[i] = (double)(s >> 11) / 9007199254740992.0;
-        nrm += host[i] * host[i];
-    }
+    for (int i = 0; i < n; i++) nrm += host[i] * host[i];
     nrm = sqrt(nrm);
     for (int i = 0; i < n; i++) host[i] /= nrm;
     lina::dev::h2d(x, host.data(), n);
+}
+
+// RN_CHOLESKY (reflective_newton.c:332-338): the complete Cholesky factor C of M by cholesky_factorization
+// (linear_algebra.c:2966-2983; dense, row by row, INDEFINITE when a diagonal square is negative), then
+// L_triang_invert with C and U_triang_invert with C^T (:2008-2043) on v; the products of each row are
+// subtracted in column order.  Dense: O(n^3) work and n^2 memory, as in the reference.
+int cholesky_solve(const CsrCopy& M, int n, std::vector<double>& v) {
+    std::vector<double> C((size_t)n * n, 0.0), A((size_t)n * n, 0.0);
+    for (int i = 0; i < n; i++)
+        for (int p = M.ptr[i]; p < M.ptr[i + 1]; p++) A[(size_t)i * n + M.col[p]] = M.val[p];
+    for (int i = 0; i < n; i++) {
+        double* ci = &C[(size_t)i * n];
+        for (int j = 0; j < i; j++) {
+            const double* cj = &C[(size_t)j * n];
+            double s = A[(size_t)i * n + j];
+            for (int k = 0; k < j; k++) s -= ci[k] * cj[k];
+            ci[j] = s / cj[j];
+        }
+        double d = A[(size_t)i * n + i];
+        for (int k = 0; k < i; k++) d -= ci[k] * ci[k];
+        if (d < 0) return INDEFINITE;
+        ci[i] = sqrt(d);
+    }
+    // forward: C y = v (rows of C in column order, the diagonal last)
+    std::vector<double> b(v);
+    double diag = 0;
+    for (int i = 0; i < n; i++) {
+        double sum = b[i];
+        for (int j = 0; j <= i; j++) {
+            const double c = C[(size_t)i * n + j];
+            if (c == 0.0) continue;  // not stored in the reference's sparse factor
+            if (j != i)
+                sum -= c * v[j];
+            else
+                diag = c;
+        }
+        v[i] = sum / diag;
+    }
+    // backward: C^T x = y (row i of C^T holds C[j][i], j >= i, in column order)
+    b = v;
+    for (int i = n - 1; i >= 0; i--) {
+        double sum = b[i];
+        for (int j = i; j < n; j++) {
+            const double c = C[(size_t)j * n + i];
+            if (c == 0.0) continue;
+            if (j != i)
+                sum -= c * v[j];
+            else
+                diag = c;
+        }
+        v[i] = sum / diag;
+    }
+    return POSITIVE_DEFINITE;
 }
 
 sparse_matrix* row_list_M(Ctx& c) {
@@ -651,6 +715,13 @@ bool get_subspace(Ctx& c) {
             lina::dev::h2d(c.V2, c.hA.data(), n);
             break;
         }
+        case RN_CHOLESKY: {
+            iter = 1;
+            lina::dev::d2h(c.hA.data(), c.V2, n);
+            rn_status = cholesky_solve(c.Mc, n, c.hA);
+            if (rn_status != INDEFINITE) lina::dev::h2d(c.V2, c.hA.data(), n);
+            break;
+        }
         default:
             printf("Reflective Newton: local solver %d is not available in the GPU library\n", rn_solver_type);
             rn_status = INDEFINITE;
@@ -658,10 +729,12 @@ bool get_subspace(Ctx& c) {
     if (rn_status == INDEFINITE) {
         stats.number_neg_curv++;
         double shift = 0, curv = 0;
-        fixed_random_unit(c.V2, n, c.hA);
-        power_iteration(c.Mdev, c.Mc, 0.0, c.V2, c.T, n, 1000, eig_eps, &shift);
-        fixed_random_unit(c.V2, n, c.hA);
-        int it = power_iteration(c.Mdev, c.Mc, shift, c.V2, c.T, n, eig_iter, eig_eps, &curv);
+        // get_neg_curvature_direction (linear_algebra.c:4849-4866): the largest-magnitude eigenvalue, then
+        // the shifted iteration from the same start vector towards the most negative curvature
+        seeded_random_unit(c.V2, n, c.hA);
+        power_iteration(c.Mdev, c.Mc, 0.0, c.V2, c.T, n, 1000, eig_eps, 0.0, true, &shift);
+        seeded_random_unit(c.V2, n, c.hA);
+        int it = power_iteration(c.Mdev, c.Mc, shift, c.V2, c.T, n, eig_iter, eig_eps, curv, false, &curv);
         curv += shift;
         stats.average_eig_iter += it;
         if (curv >= 0) {

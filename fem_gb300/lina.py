@@ -134,6 +134,7 @@ def lib():
         "lina_gpu_set_sell_index_bits": (C.c_int, [C.c_int]),
         "lina_gpu_set_sell_quads": (C.c_int, [C.c_int]),
         "lina_gpu_set_pdl": (C.c_int, [C.c_int]),
+        "lina_gpu_set_device_memory_limit": (C.c_int, [C.c_long]),
         "lina_gpu_dense_inverse": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
         "lina_gpu_set_coarse_inverse": (C.c_int, [C.c_int, C.c_int]),
         "lina_gpu_matrix_index_bits": (C.c_int, [vp]),
@@ -316,6 +317,11 @@ def dense_inverse_device(a: "DeviceArray", m, method=DENSE_SIMT):
 def set_coarse_inverse(min_rows, method=DENSE_SIMT):
     """Coarsest blocks of min_rows rows or more inverted on the GPU (0: host) with method."""
     _check(lib().lina_gpu_set_coarse_inverse(int(min_rows), int(method)), "set coarse inverse")
+
+
+def set_device_memory_limit(nbytes):
+    """Device bytes one handle may allocate (0: no limit); beyond it allocations fail with ECUDA."""
+    _check(lib().lina_gpu_set_device_memory_limit(int(nbytes)), "set memory limit")
 
 
 def set_pdl(on):

@@ -399,6 +399,42 @@ def _smooth_field(m, seed, modes=4):
     return u
 
 
+def indefinite_qp(m: int, shift: float = 0.5, seed: int = 0) -> CSRSystem:
+    """A bound-constrained quadratic with an indefinite Hessian on an m x m grid (one unknown per node).
+
+    ``H = K - shift I`` with K the graph Laplacian of the 5-point grid (diagonal = number of neighbours,
+    -1 per neighbour; eigenvalues in [0, 8]), so the smooth modes below ``shift`` have negative
+    curvature; ``b`` i.i.d. uniform in [-1/2, 1/2] from ``default_rng(seed)``; bounds 0 <= x <= 1, start at
+    the midpoint 1/2.  Reflective Newton meets an indefinite scaled matrix here and takes the
+    direction of negative curvature (get_neg_curvature_direction).  meta: lower, upper, x0.
+    """
+    n = m * m
+    r = np.arange(n) // m
+    c = np.arange(n) % m
+    rows, cols, vals = [], [], []
+    deg = np.zeros(n)
+    for dr, dc in ((-1, 0), (1, 0), (0, -1), (0, 1)):
+        ok = (r + dr >= 0) & (r + dr < m) & (c + dc >= 0) & (c + dc < m)
+        i = np.nonzero(ok)[0]
+        j = (r[i] + dr) * m + (c[i] + dc)
+        rows.append(i)
+        cols.append(j)
+        vals.append(-np.ones(len(i)))
+        deg[i] += 1.0
+    rows.append(np.arange(n))
+    cols.append(np.arange(n))
+    vals.append(deg - shift)
+    rows, cols, vals = np.concatenate(rows), np.concatenate(cols), np.concatenate(vals)
+    order = np.lexsort((cols, rows))
+    rows, cols, vals = rows[order], cols[order], vals[order]
+    indptr = np.zeros(n + 1, dtype=np.int32)
+    np.add.at(indptr, rows + 1, 1)
+    indptr = np.cumsum(indptr).astype(np.int32)
+    b = np.random.default_rng(seed).uniform(-0.5, 0.5, n)
+    return CSRSystem(n, indptr, cols.astype(np.int32), vals.astype(np.float64), b, dof=1,
+                     meta={"lower": np.zeros(n), "upper": np.ones(n), "x0": np.full(n, 0.5)})
+
+
 def at2_damage(m: int, seed: int = 0, gc: float = 2.7e-3, sigma: float = 1.0, E: float = 210.0,
                nu: float = 0.3) -> CSRSystem:
     """Phase-field damage step of AT2 type on the m x m grid (scalar P1, one unknown per node).

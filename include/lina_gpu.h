@@ -421,6 +421,11 @@ int lina_gpu_set_sell_quads(int on);
    0: ordinary stream order.  Takes effect for launches issued afterwards (a hierarchy's captured solve
    graph keeps the choice it was captured with).  The results are identical. */
 int lina_gpu_set_pdl(int on);
+/* Device bytes that one hierarchy or matrix handle may allocate (0, the default: no limit).  An allocation
+   that would exceed it fails as a failed cudaMalloc does: the call returns LINA_GPU_ECUDA with the reason
+   in lina_gpu_last_error(), frees what the handle holds, and the device stays usable.  For callers with a
+   fixed memory budget, and for tests of the failure paths. */
+int lina_gpu_set_device_memory_limit(long bytes);
 
 /* Dense inverse of a row-major m x m matrix in device memory, in place, by blocked Gauss-Jordan
    elimination without pivoting (the elimination order of the reference's dense LU,

@@ -117,6 +117,17 @@ int active_set_solver(sparse_matrix* A, double* Sol, double* b, sparse_matrix* B
                       int mode, ass_info** solver_info);
 void free_ass_info(ass_info** info);
 
+/* Local solvers on the GPU for the slots that take int f(sparse_matrix* A, double* X, double* b):
+   reflective_newton's RN_set_local_solver, active_set_solver's Solver, and a replacement for
+   Crack/crack.c's UMFPACK wrapper multifrontal_solver.  No counterpart in the reference.  Both return
+   POSITIVE_DEFINITE (1) when the solve reached its tolerance, INDEFINITE (0) otherwise.
+   LinA_gpu_spd_solver: symmetric positive definite A, AMG-preconditioned CG (hierarchy kept between calls,
+   coarse levels recomputed when only the values change), X as initial guess, ||b - A X|| <= 1e-10 ||b||.
+   LinA_gpu_general_solver: any square A (e.g. active-set KKT systems), GMRES(30) with ILU(0) of A (none on
+   a zero pivot), from X = 0, relative residual 1e-10. */
+int LinA_gpu_spd_solver(sparse_matrix* A, double* X, double* b);
+int LinA_gpu_general_solver(sparse_matrix* A, double* X, double* b);
+
 /* ---- incomplete factorisation and triangular solves (linear_algebra.c:1952-2043) ---- */
 int incomplete_LU_factorization(sparse_matrix* A, sparse_matrix* L, sparse_matrix* U);
 void L_triang_invert(sparse_matrix* L, double* x);

@@ -80,6 +80,7 @@ def lib():
         "rs_newton": (C.c_int, [vp, C.c_double, dp, dp, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double]),
         "rs_active_set": (C.c_int, [vp, dp, dp, dp, dp, C.c_int, ip]),
         "rs_reflective_newton_qp": (C.c_int, [vp, dp, dp, dp, dp, C.c_int, C.c_int, C.c_double, C.c_double]),
+        "rs_rn_neg_curv": (C.c_int, []),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -295,6 +296,11 @@ def bicgstab_ilu(sysm, eps=1e-8, max_iter=1000):
     finally:
         lib().rs_silence(0)
     return x, it
+
+
+def rn_neg_curv():
+    """Negative-curvature events of the last reflective_newton run (its statistics)."""
+    return lib().rs_rn_neg_curv()
 
 
 def reflective_newton_qp(qp, solver=5, max_iter=50, eps=1e-8, bi_eps=1e-8):

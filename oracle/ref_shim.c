@@ -394,6 +394,27 @@ static int rs_rn_local_bicgstab_ilu(sparse_matrix* M, double* X, double* b) {
 /* minimise x.H.x/2 + x.b subject to lower <= x <= upper with reflective_newton
    (LinA/reflective_newton.c:660); solver 3 = RN_PCG (ILU-PCG), 5 = BiCGStab+ILU(0) through the
    local-solver slot.  Returns the Newton iterations; x holds the start on entry. */
+/* The reference seeds its negative-curvature search with srand(time(NULL))
+   (set_random_normal_vector, LinA/linear_algebra.c:4823-4828), its only use of time(): inside this
+   library time() returns 1, so a run repeats and draws the start vector the GPU library draws. */
+time_t time(time_t* t) {
+    if (t) *t = 1;
+    return 1;
+}
+
+/* the count of negative-curvature events of the last reflective_newton run (print_RN_statistics) */
+int rs_rn_neg_curv(void) {
+    char buf[4096];
+    FILE* f = fmemopen(buf, sizeof buf, "w");
+    if (!f) return -1;
+    print_RN_statistics(f);
+    fclose(f);
+    buf[sizeof buf - 1] = 0;
+    const char* key = "number of neg. curvature events: ";
+    const char* p = strstr(buf, key);
+    return p ? atoi(p + strlen(key)) : -1;
+}
+
 int rs_reflective_newton_qp(sparse_matrix* H, double* b, double* lower, double* upper, double* x, int solver,
                             int max_iter, double eps, double bi_eps) {
     int n = H->size;

@@ -11,6 +11,7 @@
  *            float64 b[n], float64 lower[n], float64 upper[n], float64 x0[n]
  *   modes  : "gpu"   RN_set_solver(RN_GPU_BICGSTAB_ILU): BiCGStab + ILU(0) on the device
  *            "umf"   RN_set_local_solver with a caller solver running BiCGStab_solve
+ *            "spd"   RN_set_local_solver(LinA_gpu_spd_solver): AMG-PCG on the device
  *                    preconditioned by the ILU(0) of the local matrix (host triangular solves)
  *            "pcg"   RN_set_solver(RN_PCG): ILU-preconditioned pcg
  *   out.bin: int32 iterations, float64 x[n]
@@ -100,6 +101,9 @@ int main(int argc, char** argv) {
         RN_set_solver(RN_GPU_BICGSTAB_ILU);
     } else if (!strcmp(argv[1], "umf")) {
         RN_set_local_solver(local_bicgstab_ilu);
+    } else if (!strcmp(argv[1], "spd")) {
+        /* the library's AMG-PCG local solver in the slot crack.c fills with its UMFPACK wrapper */
+        RN_set_local_solver(LinA_gpu_spd_solver);
     } else if (!strcmp(argv[1], "pcg")) {
         RN_set_local_solver(NULL);
         RN_set_solver(RN_PCG);

@@ -15,6 +15,7 @@
  *                          SMALL_SYSTEM), p1 = GMRES i_max, p2 = Newton steps, q0 = eps
  *            "active"      active_set_solver with identity constraints lower <= x <= upper and
  *                          a dense-LU KKT solver; p0 = max_iter
+ *            "active-gpu"  the same with the library's GMRES + ILU(0) KKT solver on the device
  *   out.bin: int32 r0, int32 r1, int32 r2, float64 d0, float64 x[n]
  *            gmres: iterations, rcode, nomatvec, precision;  newton: steps;
  *            active: iterations, final active count
@@ -124,10 +125,11 @@ int main(int argc, char** argv) {
         Newton_GMRES_options(hdr[3], 1000, 1e-10);
         Newton_set_range(n, lo, up);
         out_i[0] = Newton_solver(A, x, hdr[4], q[0], hdr[2], -1.0);
-    } else if (!strcmp(argv[1], "active")) {
+    } else if (!strcmp(argv[1], "active") || !strcmp(argv[1], "active-gpu")) {
         sparse_matrix* B = sparse_identity(n);
         ass_info* info = NULL;
-        out_i[0] = active_set_solver(A, x, b, B, lo, up, dense_lu, hdr[2], POS_DEFINITE, ASS_DEFAULT, &info);
+        out_i[0] = active_set_solver(A, x, b, B, lo, up, !strcmp(argv[1], "active") ? dense_lu : LinA_gpu_general_solver,
+                                     hdr[2], POS_DEFINITE, ASS_DEFAULT, &info);
         out_i[1] = info->active_size;
         free_ass_info(&info);
         free_sparse(B);

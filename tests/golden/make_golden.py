@@ -72,6 +72,11 @@ RN_CASES = {
     "damage129_rn": lambda: problems.damage_qp(129),
     "at2_65_rn": lambda: problems.at2_damage(65),
 }
+# bound-constrained quadratics with an indefinite Hessian: the local solve reports INDEFINITE and
+# reflective_newton takes the direction of negative curvature; solved with the complete Cholesky local
+# solver (RN_CHOLESKY) and with BiCGStab + ILU(0) in the RN_UMF slot
+INDEF_CASES = {"indef17_rn": lambda: problems.indefinite_qp(17)}
+INDEF_SOLVERS = {"cholesky": 4, "umf_bicgstab_ilu": 5}
 # material identification (adjoint) cases: name -> (grid size m, AMG depth)
 ADJOINT_CASES = {"adjoint65": (65, 5)}
 # gmres / Newton_solver / active_set_solver runs of the reference, one file
@@ -217,6 +222,18 @@ def make_rn_digest_case(name):
         lo, up = q.meta["lower"], q.meta["upper"]
         out[f"rn_{sname}_at_lower"] = np.int64(np.sum(np.abs(x - lo) <= 1e-10))
         out[f"rn_{sname}_at_upper"] = np.int64(np.sum(np.abs(x - up) <= 1e-10))
+    return out
+
+
+def make_indef_case(name):
+    q = INDEF_CASES[name]()
+    out = {"n": np.int64(q.n), "indptr": q.indptr, "indices": q.indices, "data": q.data, "b": q.b,
+           "lower": q.meta["lower"], "upper": q.meta["upper"], "x0": q.meta["x0"]}
+    for sname, code in INDEF_SOLVERS.items():
+        x, it = ref.reflective_newton_qp(q, solver=code, max_iter=50, eps=1e-8, bi_eps=1e-8)
+        out[f"rn_{sname}_x"] = x
+        out[f"rn_{sname}_it"] = np.int64(it)
+        out[f"rn_{sname}_negcurv"] = np.int64(ref.rn_neg_curv())
     return out
 
 
@@ -467,6 +484,14 @@ def main():
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **data)
         print(f"{path}: reflective Newton iterations {int(data['rn_umf_bicgstab_ilu_it'])}")
+    for name in INDEF_CASES:
+        if only and name not in only:
+            continue
+        data = make_indef_case(name)
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **data)
+        print(f"{path}: reflective Newton iterations (negative-curvature events) "
+              + ", ".join(f"{k}={int(data[f'rn_{k}_it'])} ({int(data[f'rn_{k}_negcurv'])})" for k in INDEF_SOLVERS))
     for name in RN_CASES:
         if only and name not in only:
             continue

@@ -160,3 +160,27 @@ def test_row_list_helpers_match_reference():
     Lg, Ug, Lr, Ur = G.sparse_zero(s.n), G.sparse_zero(s.n), R.sparse_zero(s.n), R.sparse_zero(s.n)
     assert G.incomplete_LU_factorization(Ag, Lg, Ug) == R.incomplete_LU_factorization(Ar, Lr, Ur) == 1
     assert _read(Lg) == _read(Lr) and _read(Ug) == _read(Ur)
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not gpu_available(), reason="no CUDA device")
+def test_spd_local_solver_matches_reference():
+    """LinA_gpu_spd_solver (the library's AMG-PCG behind the slot signature int f(A, X, b)) on the 65 x 65
+    elasticity system: the reference's tight solution; a second call with new values on the same pattern
+    (the coarse levels recomputed) solves the scaled system."""
+    g = load_golden("elast65_std_solve")
+    s = system_for("elast65_std_solve")
+    L = lina.dropin()
+    L.LinA_gpu_spd_solver.restype = C.c_int
+    L.LinA_gpu_spd_solver.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    L.AMG_set_deg_of_freedom.argtypes = [C.c_int]
+    L.AMG_set_deg_of_freedom(2)
+    A = lina.RowListView(s.indptr, s.indices, s.data)
+    x = np.zeros(s.n)
+    b = np.ascontiguousarray(s.b)
+    assert L.LinA_gpu_spd_solver(A.ref, x.ctypes.data, b.ctypes.data) == 1
+    assert rel(x, g["x_tight"]) < 1e-6
+    A2 = lina.RowListView(s.indptr, s.indices, 2.0 * s.data)
+    x2 = np.zeros(s.n)
+    assert L.LinA_gpu_spd_solver(A2.ref, x2.ctypes.data, b.ctypes.data) == 1
+    assert rel(x2, 0.5 * g["x_tight"]) < 1e-6

@@ -113,6 +113,18 @@ def test_active_set_matches_reference(driver, tmp_path):
 
 
 @pytest.mark.gpu
+def test_active_set_with_gpu_kkt_solver_matches_reference(driver, tmp_path):
+    """active_set_solver with LinA_gpu_general_solver (GMRES + ILU(0) on the device) solving its KKT
+    systems, in the slot crack.c fills with its UMFPACK wrapper: the reference's active set and solution."""
+    g = load()
+    s = problems.poisson_p1(17, seed=1)
+    ints, _, x = run(driver, tmp_path, "active-gpu", s, [100, 0, 0], [0.0, 0.0], lower=g["active_lower"],
+                     upper=g["active_upper"])
+    assert int(ints[0]) == int(g["active_it"]) and int(ints[1]) == int(g["active_size"])
+    assert rel(x, g["active_x"]) <= SOL_TOL
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("name", list(SYSTEMS))
 @pytest.mark.parametrize("check", [0, 1])
 @pytest.mark.parametrize("mode", ["gmres", "gmres-host"])

@@ -14,7 +14,7 @@ import pytest
 import scipy.sparse as sp
 
 from fem_gb300 import lina, problems
-from tests.conftest import ROOT
+from tests.conftest import ROOT, gpu_available
 
 DRIVER_SRC = os.path.join(ROOT, "tests", "c", "rn_driver.c")
 GOLDEN = os.path.join(ROOT, "tests", "golden")
@@ -107,7 +107,7 @@ def run_rn(driver, tmp_path, mode, g, max_iter=50, eps=1e-8, bi_eps=1e-8):
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", RN_CASES)
 @pytest.mark.parametrize("mode,ref_solver", [("gpu", "umf_bicgstab_ilu"), ("umf", "umf_bicgstab_ilu"),
-                                             ("pcg", "pcg_ilu")])
+                                             ("pcg", "pcg_ilu"), ("spd", "umf_bicgstab_ilu")])
 def test_reflective_newton_matches_reference(driver, tmp_path, name, mode, ref_solver):
     g = load(name)
     it, x = run_rn(driver, tmp_path, mode, g)
@@ -136,3 +136,42 @@ def test_csr_entry_point_matches_reference(name):
     it_ref = int(g["rn_umf_bicgstab_ilu_it"])
     assert abs(it - it_ref) <= it_slack(it_ref), (it, it_ref)
     assert np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref) <= X_TOL
+
+
+def _neg_curv_events(tmp_path):
+    """number_neg_curv of the library's RN statistics, read through print_RN_statistics."""
+    import ctypes as C
+    libc = C.CDLL(None)
+    libc.fopen.restype, libc.fopen.argtypes = C.c_void_p, [C.c_char_p, C.c_char_p]
+    libc.fclose.argtypes = [C.c_void_p]
+    L = lina.lib()
+    L.print_RN_statistics.argtypes = [C.c_void_p]
+    path = str(tmp_path / "rnstat.txt")
+    f = libc.fopen(path.encode(), b"w")
+    L.print_RN_statistics(f)
+    libc.fclose(f)
+    for line in open(path):
+        if line.startswith("number of neg. curvature events:"):
+            return int(line.split(":")[1])
+    return -1
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not gpu_available(), reason="no CUDA device")
+@pytest.mark.parametrize("solver,ref_name", [(4, "cholesky"), (lina.RN_GPU_BICGSTAB_ILU, "umf_bicgstab_ilu")])
+def test_indefinite_quadratic_matches_reference(solver, ref_name, tmp_path):
+    """An indefinite Hessian (grid Laplacian minus 0.5 I, tests/golden/indef17_rn.npz): with the complete
+    Cholesky local solver (RN_CHOLESKY) the scaled matrix is reported INDEFINITE and the step takes the
+    direction of negative curvature found by the shifted power iteration, as in the reference (whose
+    start vector is drawn with the same seed); BiCGStab + ILU(0) solves the indefinite systems as the
+    reference's BiCGStab did.  Minimiser within 1e-6, Newton steps within 10 %, the same number of
+    negative-curvature events."""
+    g = load("indef17_rn")
+    q = problems.indefinite_qp(17)
+    assert np.array_equal(q.data, g["data"]) and np.array_equal(q.b, g["b"])
+    lina.lib().RN_init_statistics()
+    x, it = lina.reflective_newton(q, g["lower"], g["upper"], g["x0"], solver=solver)
+    it_ref = int(g[f"rn_{ref_name}_it"])
+    assert abs(it - it_ref) <= it_slack(it_ref), (it, it_ref)
+    assert np.max(np.abs(x - g[f"rn_{ref_name}_x"])) <= X_TOL
+    assert _neg_curv_events(tmp_path) == int(g[f"rn_{ref_name}_negcurv"])
