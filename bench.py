@@ -64,8 +64,9 @@ def parse():
     p.add_argument("--ref-sor", type=int, default=1,
                    help="reference arm: also time one solve with the reference's lexicographic SOR (1) or not (0)")
     p.add_argument("--no-fp64", action="store_true")
-    p.add_argument("--workload", default="elasticity", choices=["elasticity", "damage", "adjoint", "batch"],
-                   help="elasticity: the headline AMG-PCG solve (default); damage: the reflective-Newton "
+    p.add_argument("--workload", default="elasticity", choices=["elasticity", "poisson", "damage", "adjoint", "batch"],
+                   help="elasticity: the headline AMG-PCG solve (default); poisson: the 257 x 257 P1 Poisson "
+                        "system in FP64 (66,049 unknowns); damage: the reflective-Newton "
                         "damage step on the same mesh; adjoint: the material-identification gradient; "
                         "batch: independent unstructured systems solved in one graph launch")
     p.add_argument("--coarsening", default="standard", choices=["standard", "pmis"],
@@ -401,6 +402,109 @@ def common_line(metric, value, unit, world, steps, warmup, ms, dtype, data, conf
             "clocks": clocks.summary()}
 
 
+def run_poisson(args, rank, world, local):
+    """Plain FP64 AMG-PCG on the P1 Poisson system of a 257 x 257 grid (66,049 unknowns, homogeneous
+    Dirichlet rows, right-hand side uniform in [-1, 1] from seed 0): aggressive coarsening, depth 6, one
+    V-cycle of 2 + 2 multicolour-SOR sweeps (omega 1) per iteration, the reference's stopping rule
+    ||r|| / ||M^-1 r0|| <= 1e-8.  value: device-resident solves; e2e: the drop-in pcg on host arrays; the
+    CPU baseline: the restated reference set-up and pcg with its own lexicographic SOR."""
+    from fem_gb300 import lina, problems
+    from oracle import port
+    m = 257
+    s = problems.poisson_p1(m, seed=0)
+    depth = 6
+    amg = lina.AMG.from_system(s, depth=depth, coarsening=lina.AGGRESSIVE, smoother=lina.SMOOTHER_MC_SOR, omega=1.0,
+                               precision=lina.PREC_FP64)
+    b_dev = lina.DeviceArray.from_host(s.b)
+    x_dev = lina.DeviceArray(s.n)
+    flags = lina.PCG_NORMALIZE | lina.PCG_FINAL_PRECON
+
+    def solve():
+        return amg.pcg_device(b_dev, x_dev, tol=args.tol, max_iter=500, stop=lina.STOP_REFERENCE, flags=flags)
+
+    for _ in range(args.warmup):
+        solve()
+    barrier(world)
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = lina.launches()
+    amg.timer_begin()
+    infos = [solve() for _ in range(args.steps)]
+    ms = max_over_ranks(amg.timer_end(), world)
+    launches = lina.launches() - launches0
+    clocks.stop()
+    x = x_dev.to_host()
+    value = world * args.steps / (ms / 1e3)
+    # the drop-in API on host arrays (FP64, the same smoother)
+    L = lina.dropin()
+    A = lina.RowListView(s.indptr, s.indices, s.data)
+    L.AMG_print_info(0)
+    L.AMG_set_matrix_tolerance(0.1)
+    L.AMG_set_SOR_relaxation_coeff(1.0)
+    L.AMG_set_smoother(ctypes.cast(L.AMG_SOR_smoother, ctypes.c_void_p))
+    L.AMG_gpu_set_precision(0)
+    data = L.AMG_setup(A.ref, 1, depth, 2, 2, 1, 0, 1, None, None)
+    L.PCG_default(A.ref, None, None)
+    L.PCG_set_AMG_data(data)
+    L.PCG_set_precon(ctypes.cast(L.PCG_AMG_vcycle_precon, ctypes.c_void_p))
+    bh = np.ascontiguousarray(s.b)
+    xh = np.zeros(s.n)
+    dp = ctypes.POINTER(ctypes.c_double)
+    times, e2e_its = [], []
+    for k in range(args.warmup + args.steps):
+        xh[:] = 0.0
+        t0 = time.perf_counter()
+        e2e_its.append(L.pcg(xh.ctypes.data_as(dp), bh.ctypes.data_as(dp), s.n, args.tol, 500))
+        if k >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    L.AMG_free_data(data)
+    e2e_value = world * len(times) / max_over_ranks(sum(times), world)
+    # parity against the reference's own digest of this system
+    parity = {}
+    gpath = os.path.join(ROOT, "tests", "golden", "poisson257_digest.npz")
+    if os.path.exists(gpath):
+        g = np.load(gpath)
+        idx = g["sample_index"]
+        xt = g["tight_xs"]
+        parity = {"reference_iterations_mcsor": int(g["pcg_mcsor_it"]),
+                  "reference_iterations_lexicographic_sor": int(g["pcg_refsor_it"]),
+                  "err_vs_ref_tight": float(np.linalg.norm(x[idx] - xt) / np.linalg.norm(xt)),
+                  "err_vs_ref_same_tol": float(np.linalg.norm(x[idx] - g["pcg_mcsor_xs"]) /
+                                               np.linalg.norm(g["pcg_mcsor_xs"]))}
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        t0 = time.perf_counter()
+        P = port.PortAMG.setup(s, depth, 1, 0.1, port.REF_SOR, 1.0, 2, 2)
+        setup_s = time.perf_counter() - t0
+        ts, its = [], []
+        while not ts or (sum(ts) < args.cpu_seconds and len(ts) < 20):
+            t0 = time.perf_counter()
+            _, it, _ = P.pcg(s.b, args.tol, 500, 0)
+            ts.append(time.perf_counter() - t0)
+            its.append(it)
+        cpu = {"value": len(ts) / sum(ts), "unit": "solves/s", "cores": 1, "kind": "port",
+               "sample": f"{len(ts)} whole solves with the reference's lexicographic SOR (serial, as the reference), "
+                         f"{its[0]} PCG iterations each; restated set-up {setup_s:.1f} s (not timed)",
+               "iterations": its[0]}
+    out = common_line("AMG-PCG solves/s at 66k dofs (P1 Poisson 257 x 257, FP64) to the reference's rel-res 1e-8",
+                      value, "solves/s", world, args.steps, args.warmup, ms, "f64",
+                      "synthetic (seeded uniform right-hand side)",
+                      {"workload": f"P1 Poisson {m}x{m} nodes, {s.n} dofs, aggressive coarsening, depth {depth}, "
+                                   "one V-cycle of 2+2 multicolour-SOR sweeps (omega 1) per iteration, stopping "
+                                   f"rule ||r||/||M^-1 r0|| <= {args.tol:g}; inputs resident (fit L2)",
+                       "dofs": s.n, "nnz": int(s.nnz), "amg_depth": depth, "level_sizes": amg.sizes()},
+                      {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": 16 * s.n,
+                       "d2h_bytes_per_step": 8 * s.n, "api": "drop-in AMG_setup + PCG_set_AMG_data + "
+                       "PCG_AMG_vcycle_precon + pcg on host arrays", "iterations": e2e_its[args.warmup:][:3]},
+                      launches, clocks)
+    out["iterations"] = [i.iterations for i in infos]
+    out["parity"] = parity
+    out["roofline"] = None
+    out["cpu_baseline"] = cpu
+    if rank == 0:
+        print(json.dumps(out))
+
+
 def run_damage(args, rank, world, local):
     """Phase-field damage step (AT2 quadratic, 1025 x 1025 nodes, 1.05M unknowns, bounds
     d_prev <= d <= 1) by reflective Newton with the device BiCGStab + mixed-precision ILU(0) local
@@ -698,6 +802,8 @@ def main():
     lina.set_sell_index_bits(args.sell_bits)
     if args.workload == "damage":
         run_damage(args, rank, world, local)
+    elif args.workload == "poisson":
+        run_poisson(args, rank, world, local)
     elif args.workload == "adjoint":
         run_adjoint(args, rank, world, local)
     elif args.workload == "batch":

@@ -165,16 +165,19 @@ def _fd_check(m, n_dirs, seed=0, **opts):
 
 
 def check_fd(fds, ads):
-    """Relative agreement |fd - ad| / |ad| <= FD_TOL on every direction whose derivative is not a
-    cancellation (|ad| at least a tenth of the root mean square over the directions); on the others
-    the difference, which stays at the solves' accuracy, is held to FD_TOL times that mean."""
+    """Relative agreement |fd - ad| / |ad| <= FD_TOL on every direction.  A direction whose derivative
+    cancels to below 1 % of the root mean square over the directions would carry the solves' absolute
+    accuracy as a large relative error; such a direction is named in the output and held to FD_TOL times
+    that mean instead (none of the seeded 513 x 513 directions is one)."""
     rms = np.sqrt(np.mean(ads ** 2))
     err = np.abs(fds - ads)
-    well = np.abs(ads) >= 0.1 * rms
-    rel = err[well] / np.abs(ads[well])
-    assert well.sum() >= 0.8 * len(ads)
-    assert rel.max() <= FD_TOL, rel
-    assert err.max() <= FD_TOL * rms, err / rms
+    rel = err / np.abs(ads)
+    cancel = np.abs(ads) < 0.01 * rms
+    for k in range(len(ads)):
+        print(f"direction {k:2d}: dL/dE.d = {ads[k]: .6e}  central difference {fds[k]: .6e}  relative error "
+              f"{rel[k]:.2e}  |ad|/rms {abs(ads[k]) / rms:.3f}" + ("  (cancellation)" if cancel[k] else ""))
+    assert np.all(rel[~cancel] <= FD_TOL), rel
+    assert np.all(err[cancel] <= FD_TOL * rms), err / rms
     return rel, err / rms
 
 
