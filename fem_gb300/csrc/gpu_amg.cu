@@ -163,6 +163,11 @@ struct KScalars {
     int maxit;
     double tj[kFcgMax];   // z . q_{k-j}, j = 1..m (truncated flexible CG)
     double pqh[kFcgMax];  // p_i . q_i of the kept directions, by history slot i mod m
+    // Scalars derived from the reductions, formed once by the thread that finishes a reduction: FP64
+    // division is slow on GB300, and each of several hundred thousand threads forming its own copy cost
+    // tens of microseconds per kernel
+    double cj[kFcgMax];   // FCG(m) coefficients tj / pqh
+    double alpha_next;    // s / (p.q) for update_xr
 };
 
 // p.q from the block partials of an SpMV+dot launch, summed in block order by one block
@@ -185,7 +190,10 @@ __global__ void dot_finish_kernel(int nparts, const double* __restrict__ partial
     if (wid == 0) {
         double y = (lane < nw) ? sm[lane] : 0.0;
         y = warp_sum(y);
-        if (lane == 0) sc->pq = y;
+        if (lane == 0) {
+            sc->pq = y;
+            sc->alpha_next = sc->s / y;  // the step length of update_xr (unused by other callers)
+        }
     }
 }
 
@@ -568,7 +576,10 @@ __global__ void convert_kernel(long n, const TA* __restrict__ a, TB* __restrict_
 
 __global__ void scale_kernel(long n, double* __restrict__ v, const double* __restrict__ f, int invert) {
     pdl_wait();
-    double s = invert ? 1.0 / (*f) : (*f);
+    __shared__ double sh;
+    if (threadIdx.x == 0) sh = invert ? 1.0 / (*f) : (*f);
+    __syncthreads();
+    const double s = sh;
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) v[i] *= s;
 }
 
@@ -676,10 +687,12 @@ __global__ void __launch_bounds__(kThreads) dot_rz_kernel(int n, const double* _
         v[0] += r[i] * zi;
         if (flexible) v[1] += zi * q[i];
     }
-    grid_reduce<2>(v, partials, ticket, [sc](double* t) {
+    grid_reduce<2>(v, partials, ticket, [sc, flexible](double* t) {
         sc->s_old = sc->s;
         sc->s = t[0];
         sc->t = t[1];
+        // beta of update_p: s/s_old (CG) or -alpha_prev t / s_old (flexible CG); 0 on the first step
+        sc->beta = (sc->iter == 0) ? 0.0 : flexible ? (-sc->alpha * sc->t / sc->s_old) : (sc->s / sc->s_old);
     });
 }
 
@@ -689,9 +702,8 @@ __global__ void update_p_kernel(int n, const TZ* __restrict__ z, double* __restr
                                 KScalars* sc) {
     pdl_wait();
     const bool first = (sc->iter == 0);
-    double beta = 0.0;
-    if (!first) beta = flexible ? (-sc->alpha * sc->t / sc->s_old) : (sc->s / sc->s_old);
-    if (blockIdx.x == 0 && threadIdx.x == 0) sc->beta = beta;
+    const double beta = sc->beta;  // formed by dot_rz_kernel's last block
+    (void)flexible;
     const long S = (long)gridDim.x * blockDim.x;
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (first) {
@@ -757,11 +769,14 @@ __global__ void __launch_bounds__(kThreads, 4) fcg_dot_kernel(int n, const doubl
         for (int j = 1; j <= M; j++)
             if (j <= nprev) v[j] += zi * qs[j - 1][i];
     }
-    grid_reduce<M + 1>(v, partials, ticket, [sc](double* t) {
+    grid_reduce<M + 1>(v, partials, ticket, [sc, k, nprev](double* t) {
         sc->s_old = sc->s;
         sc->s = t[0];
 #pragma unroll
-        for (int j = 1; j <= M; j++) sc->tj[j - 1] = t[j];
+        for (int j = 1; j <= M; j++) {
+            sc->tj[j - 1] = t[j];
+            sc->cj[j - 1] = (j <= nprev) ? t[j] / sc->pqh[(k - j + M * kFcgMax) % M] : 0.0;
+        }
     });
 }
 
@@ -777,7 +792,7 @@ __global__ void __launch_bounds__(kThreads, 4) fcg_update_p_kernel(int n, const 
 #pragma unroll
     for (int j = 1; j <= M; j++) {
         const int slot = (k - j + M * kFcgMax) % M;
-        c[j - 1] = (j <= nprev) ? sc->tj[j - 1] / sc->pqh[slot] : 0.0;
+        c[j - 1] = sc->cj[j - 1];  // formed by fcg_dot_kernel's last block
         ps[j - 1] = ph + (size_t)slot * n;
     }
     constexpr int U = (M <= 3) ? 4 : 2;
@@ -809,13 +824,13 @@ __global__ void __launch_bounds__(kThreads, 4) fcg_update_p_kernel(int n, const 
 
 // alpha = s / (p.q); x += alpha p; r -= alpha q; rr = r.r.  With a direction history (hm > 0) p and
 // q are also stored in slot iter mod hm of the rings ph, qh, and p.q in sc->pqh.
-__global__ void __launch_bounds__(kThreads) update_xr_kernel(int n, double* __restrict__ x, double* __restrict__ r,
+__global__ void __launch_bounds__(kThreads, 4) update_xr_kernel(int n, double* __restrict__ x, double* __restrict__ r,
                                                              const double* __restrict__ p,
                                                              const double* __restrict__ q, double* partials,
                                                              unsigned* ticket, KScalars* sc, int hm,
                                                              double* __restrict__ ph, double* __restrict__ qh) {
     pdl_wait();
-    const double alpha = sc->s / sc->pq;
+    const double alpha = sc->alpha_next;  // s / (p.q), formed by dot_finish_kernel
     double* hp = nullptr;
     double* hq = nullptr;
     if (hm > 0) {
