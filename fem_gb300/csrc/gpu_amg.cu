@@ -508,7 +508,9 @@ __global__ void jacobi_first_kernel(int n, const TB* __restrict__ b, const doubl
         if (sign) bd *= sign[k];
         const TX bi = TX(bd);
         if (bout) bout[k] = bi;
-        x[k] = (iso != 0.0) ? TX(bd * iso) : w * di * bi;
+        // isolated rows have a nonzero inverse, every other row +0.0: tested by its bits (an FP64
+        // comparison per row would take GB300's slow FP64 pipe)
+        x[k] = (__double_as_longlong(iso) != 0) ? TX(bd * iso) : w * di * bi;
     };
     for (; i + 3 * S < n; i += 4 * S) {
         double bb[4], iso[4];

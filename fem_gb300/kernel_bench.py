@@ -2,12 +2,17 @@
 
     python -m fem_gb300.kernel_bench --m 1025 --reps 3              # finest matrix
     python -m fem_gb300.kernel_bench --m 1025 --level 8 --reps 3    # a level of the AMG hierarchy
+    python -m fem_gb300.kernel_bench --m 1025 --solve --reps 2      # whole mixed-precision solves
 
 Builds the degraded plane-strain elasticity matrix (m x m nodes, 2 m^2 unknowns) or, with
 --level, the AMG hierarchy of the benchmark (standard coarsening, depth 10, matrix tolerance
 0.1) on the host, uploads that one matrix as a device matrix in the library's layout, and runs
 `reps` FP32 and `reps` FP64 damped-Jacobi sweeps and SpMVs, so that a profiler can capture them
 in isolation with little device memory in use.
+
+--solve instead builds the benchmark's device hierarchy (damped Jacobi, omega 0.6, mixed precision) and
+runs `reps` AMG-PCG solves to the relative residual 1e-8, each iteration launched from the host rather
+than from the captured graph (a profiler cannot see the kernels of a graph with conditional nodes).
 """
 from __future__ import annotations
 
@@ -30,7 +35,11 @@ def main():
     ap.add_argument("--dense-inverse", type=str, default="",
                     help="comma-separated sizes m: time the device inverse of a dense m x m block with FP64 CUDA "
                          "cores and with FP64 tensor cores instead")
+    ap.add_argument("--solve", action="store_true", help="whole solves, launched iteration by iteration")
     args = ap.parse_args()
+    if args.solve:
+        solve(args)
+        return
     if args.dense_inverse:
         dense_inverse(int(v) for v in args.dense_inverse.split(","))
         return
@@ -60,6 +69,21 @@ def main():
     out.update(level=args.level, n=n, nnz=int(ip[-1]), padded=int(M.padded_entries),
                index_bits=M.index_bits())
     print(out)
+
+
+def solve(args):
+    lina.set_sell_index_bits(args.sell_bits)
+    s = problems.elasticity_p1(args.m)
+    amg = lina.AMG.from_system(s, depth=args.depth, coarsening=lina.STANDARD, smoother=lina.SMOOTHER_JACOBI,
+                               omega=0.6, precision=lina.PREC_MIXED, matrix_tol=args.matrix_tol)
+    b = lina.DeviceArray.from_host(s.b)
+    x = lina.DeviceArray(s.n)
+    for _ in range(args.reps):
+        t0 = time.perf_counter()
+        info = amg.pcg_device(b, x, tol=1e-8, max_iter=2000, stop=lina.STOP_RELATIVE, flags=lina.PCG_HOST_LOOP)
+        print({"iterations": info.iterations, "status": info.status, "ms": (time.perf_counter() - t0) * 1e3,
+               "launches": lina.launches()}, flush=True)
+    amg.close()
 
 
 def dense_inverse(sizes, reps=3):
