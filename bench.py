@@ -402,6 +402,33 @@ def common_line(metric, value, unit, world, steps, warmup, ms, dtype, data, conf
             "clocks": clocks.summary()}
 
 
+def port_threads():
+    """Host threads the OpenMP restatement uses."""
+    return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+
+
+def sweep_roofline(amg, b_dev, x_dev, tol, stop, flags, reps, what):
+    """The smoother sweeps of a hierarchy's level with the most stored entries, timed live: the same solve
+    driven iteration by iteration with CUDA events on the library's stream around every sweep of that
+    level (every colour launch for multicolour SOR), reps solves.  Algorithmic bytes per launch as the
+    library counts them (matrix entries with their column indices, x, b, 1/a_ii and the result; a colour
+    launch carries its share of the sweep).  No ncu capture stands behind these: traffic is null."""
+    from fem_gb300 import lina
+    kinfos = [amg.pcg_device(b_dev, x_dev, tol=tol, max_iter=2000, stop=stop, flags=flags | lina.PCG_TIME_KERNELS)
+              for _ in range(reps)]
+    n = sum(i.smoother_launches for i in kinfos)
+    ms = sum(i.smoother_ms for i in kinfos)
+    if not n or ms <= 0:
+        return None
+    k = kinfos[0]
+    peak, peak_kind = measured_peaks()
+    achieved = k.smoother_bytes / (ms / n / 1e3) / 1e9
+    return {"bound": "hbm", "kernel": f"{what}: smoother launches of level {k.timed_level} ({k.timed_rows} rows, "
+                                      f"{k.timed_entries} stored entries; the level with the most entries)",
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+            "traffic": None, "bytes_per_launch": k.smoother_bytes, "avg_launch_us": ms / n * 1e3, "launches": n}
+
+
 def run_poisson(args, rank, world, local):
     """Plain FP64 AMG-PCG on the P1 Poisson system of a 257 x 257 grid (66,049 unknowns, homogeneous
     Dirichlet rows, right-hand side uniform in [-1, 1] from seed 0): aggressive coarsening, depth 6, one
@@ -499,7 +526,8 @@ def run_poisson(args, rank, world, local):
                       launches, clocks)
     out["iterations"] = [i.iterations for i in infos]
     out["parity"] = parity
-    out["roofline"] = None
+    out["roofline"] = sweep_roofline(amg, b_dev, x_dev, args.tol, lina.STOP_REFERENCE, flags, 3,
+                                     "FP64 multicolour-SOR colour sweeps (the level fits L2)")
     out["cpu_baseline"] = cpu
     if rank == 0:
         print(json.dumps(out))
@@ -534,8 +562,41 @@ def run_damage(args, rank, world, local):
                       {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 8 * 3 * q.n,
                        "d2h_bytes_per_step": 8 * q.n}, launches, clocks)
     out["newton_steps"] = its
-    out["roofline"] = None
+    # dominant kernel: the ILU(0) application (forward + backward triangular solve, FP32) inside every
+    # BiCGStab iteration; timed with CUDA events on the handle's stream, on the ILU(0) of the Hessian
+    # (the Newton systems D H D + diag(|g| J) keep its pattern and level schedule)
+    ilu = lina.ILU(q.n, q.indptr, q.indices, q.data)
+    ms_apply = ilu.time_apply(20, lina.PREC_MIXED)
+    nlev = ilu.levels()[0]
+    by = ilu.apply_bytes(lina.PREC_MIXED)
+    ilu.close()
+    peak, peak_kind = measured_peaks()
+    achieved = by / (ms_apply / 1e3) / 1e9
+    out["roofline"] = {"bound": "hbm", "kernel": f"FP32 ILU(0) application (forward + backward triangular solve, "
+                                                 f"{nlev} levels each way; latency-bound: one block barrier per level)",
+                       "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                       "peak_kind": peak_kind, "traffic": None, "bytes_per_launch": by,
+                       "avg_launch_us": ms_apply * 1e3}
     out["cpu_baseline"] = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import port
+        # one Newton step's local solve as the reference runs it (incomplete_LU_factorization, then
+        # BiCGStab_solve with the ILU(0) preconditioner to 1e-8), restated, serial as the reference
+        t0 = time.perf_counter()
+        f = port.ilu0(q.indptr, q.indices, q.data)
+        t_ilu = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        _, bit, _ = port.bicgstab_ilu(q.indptr, q.indices, q.data, q.b, 1e-8, 1000, factors=f)
+        t_bi = time.perf_counter() - t0
+        steps = int(np.mean(its)) if its else 1
+        t_min = steps * (t_ilu + t_bi)
+        out["cpu_baseline"] = {"value": 1.0 / t_min, "unit": "solves/s", "cores": 1, "kind": "port",
+                               "sample": f"one Newton step's local solve on the AT2 Hessian ({q.n} rows): ILU(0) "
+                                         f"{t_ilu:.2f} s + BiCGStab to 1e-8 ({bit} iterations) {t_bi:.2f} s, the "
+                                         f"reference's algorithm restated and serial as the reference; times "
+                                         f"{steps} Newton steps.  The reflective-Newton host work (assembly of "
+                                         f"D H D + diag(|g| J), line search) is not counted, so the CPU figure "
+                                         f"is an upper bound on the reference's rate"}
     if rank == 0:
         print(json.dumps(out))
 
@@ -583,8 +644,28 @@ def run_adjoint(args, rank, world, local):
                                    f"{len(case['sensor_dof']) // 2} sensor nodes, tol 1e-10", "dofs": n},
                       {"value": value, "unit": "gradients/s", "h2d_bytes_per_step": 8 * len(E),
                        "d2h_bytes_per_step": 8 * (2 * n + len(E))}, launches, clocks)
-    out["roofline"] = None
+    # the assembled system of the timed moduli: the forward and the adjoint solve both run on it (A is
+    # symmetric, so get_transpose(A) = A); the dominant kernel is timed on a hierarchy with the same
+    # options, and the CPU baseline solves it with the restated reference
+    ptr, col, val, b = adj.system()
+    sysm = problems.CSRSystem(n, ptr, col, val, b, dof=2)
+    amg = lina.AMG(n, ptr, col, val, dof=2, **opts)
+    b_dev = lina.DeviceArray.from_host(b)
+    x_dev = lina.DeviceArray(n)
+    out["roofline"] = sweep_roofline(amg, b_dev, x_dev, 1e-10, lina.STOP_RELATIVE, 0, 2,
+                                     "FP32 damped-Jacobi sweeps of the adjoint's hierarchy")
+    amg.close()
     out["cpu_baseline"] = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import port
+        P = port.PortAMG.setup(sysm, opts["depth"], 2, 0.1, port.JACOBI, 0.6, 2, 2)
+        t0 = time.perf_counter()
+        _, it_c, _ = P.pcg(b, 1e-10, 2000, 1)
+        t1 = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 1.0 / (2 * t1), "unit": "gradients/s", "cores": port_threads(),
+                               "kind": "port", "sample": f"one FP64 solve of the system to 1e-10 ({it_c} iterations, "
+                                                         f"{t1:.2f} s) on the restated reference hierarchy, times two "
+                                                         "(forward and adjoint); assembly and gradient not counted"}
     if rank == 0:
         print(json.dumps(out))
 
@@ -673,8 +754,36 @@ def run_batch(args, rank, world, local):
                          "loop_mixed_sum": int(sum(loop_mixed_its))}
     out["worst_true_rel_residual"] = worst
     out["setup_s"] = {"meshes_and_assembly": t_mesh, "amg_setup": t_setup}
-    out["roofline"] = None
+    # the dominant kernel: the colour sweeps of the largest system's level with the most entries
+    big = max(range(len(systems)), key=lambda k: systems[k].nnz)
+    for a in amgs:
+        a.set_smoother(lina.SMOOTHER_MC_SOR, 1.0, lina.PREC_MIXED)
+    out["roofline"] = sweep_roofline(amgs[big], bd[big], lina.DeviceArray(systems[big].n), args.tol,
+                                     lina.STOP_RELATIVE, 0, 2,
+                                     f"FP32 multicolour-SOR colour sweeps of the largest system ({systems[big].n} dofs)")
     out["cpu_baseline"] = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import port
+        # the restated reference on systems taken in plan order until the time bound; the whole batch's
+        # CPU time estimated in proportion to the stored entries
+        t_sum, nnz_done, done, its_c = 0.0, 0, 0, 0
+        for sy in systems:
+            if t_sum >= args.cpu_seconds:
+                break
+            P = port.PortAMG.setup(sy, problems.batch_depth(sy.n), 2, args.batch_matrix_tol, port.MC_SOR, 1.0, 2, 2)
+            t0 = time.perf_counter()
+            _, it_c, _ = P.pcg(sy.b, args.tol, 2000, 1)
+            t_sum += time.perf_counter() - t0
+            nnz_done += sy.nnz
+            done += 1
+            its_c += it_c
+            del P
+        t_all = t_sum * (sum(sy.nnz for sy in systems) / nnz_done)
+        out["cpu_baseline"] = {"value": len(systems) / t_all, "unit": "systems/s", "cores": port_threads(),
+                               "kind": "port", "sample": f"{done} of {len(systems)} systems solved to {args.tol:g} in "
+                                                         f"FP64 ({its_c} PCG iterations, {t_sum:.1f} s) on restated "
+                                                         "reference hierarchies (multicolour SOR, as the batch); "
+                                                         "scaled to the batch by stored entries"}
     if rank == 0:
         print(json.dumps(out))
 

@@ -526,6 +526,11 @@ __global__ void cvt_kernel(long n, const TA* __restrict__ a, TB* __restrict__ b)
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) b[i] = TB(a[i]);
 }
 
+template <typename T>
+__global__ void fill_kernel(long n, T v, T* __restrict__ a) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) a[i] = v;
+}
+
 // one triangular factor as row segments [beg_i, end_i) of shared column and value arrays
 struct Factor {
     int nlev = 0;
@@ -1185,6 +1190,54 @@ int lina_gpu_ilu_apply(lina_gpu_ilu* h, int precision, const double* r_dev, doub
         if (e > 0) cudaMemset(h->err, 0, sizeof(int));
         return LINA_GPU_ECUDA;
     }
+    return 0;
+}
+// reps applications (forward then backward triangular solve, no conversions) on a right-hand side of
+// ones, CUDA events on the handle's stream around them: milliseconds per application
+int lina_gpu_ilu_time_apply(lina_gpu_ilu* h, int precision, int reps, double* ms_per_apply) {
+    if (!h || reps <= 0 || !ms_per_apply) return LINA_GPU_EINVAL;
+    const int n = h->n;
+    const int g = (int)std::min<long>(2048, (n + kT - 1) / kT);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        if (e0) cudaEventDestroy(e0);
+        return LINA_GPU_ECUDA;
+    }
+    if (precision == LINA_PREC_MIXED)
+        fill_kernel<float><<<g, kT, 0, st()>>>(n, 1.0f, h->r32);
+    else
+        fill_kernel<double><<<g, kT, 0, st()>>>(n, 1.0, h->t64);
+    double* r64 = h->t64;
+    double* z64 = nullptr;
+    if (precision != LINA_PREC_MIXED && cudaMalloc(&z64, 2 * (size_t)n * sizeof(double)) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return LINA_GPU_ECUDA;
+    }
+    cudaEventRecord(e0, st());
+    for (int k = 0; k < reps; k++) {
+        if (precision == LINA_PREC_MIXED) {
+            solve<float, float>(h, h->L, h->L.val32, h->L.dinv32, h->r32, h->t32);
+            solve<float, float>(h, h->U, h->U.val32, h->U.dinv32, h->t32, h->z32);
+        } else {
+            solve<double, double>(h, h->L, h->L.val64, h->L.dinv64, r64, z64);
+            solve<double, double>(h, h->U, h->U.val64, h->U.dinv64, z64, z64 + n);
+        }
+    }
+    cudaEventRecord(e1, st());
+    float ms = 0.f;
+    const bool ok = cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (z64) cudaFree(z64);
+    if (!ok || cudaGetLastError() != cudaSuccess) return LINA_GPU_ECUDA;
+    const int e = read_err(h);
+    if (e != 0) {
+        lina::dev::set_error("ILU timing: a wait of the triangular solve ran out");
+        if (e > 0) cudaMemset(h->err, 0, sizeof(int));
+        return LINA_GPU_ECUDA;
+    }
+    *ms_per_apply = ms / reps;
     return 0;
 }
 

@@ -158,6 +158,7 @@ def lib():
         "lina_gpu_wait_probe": (C.c_int, [C.c_int, dp]),
         "lina_gpu_matrix_update_values": (C.c_int, [vp, dp, C.c_int]),
         "lina_gpu_ilu_apply": (C.c_int, [vp, C.c_int, vp, vp]),
+        "lina_gpu_ilu_time_apply": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(C.c_double)]),
         "lina_gpu_dot": (C.c_int, [vp, vp, C.c_long, dp]),
         "lina_gpu_dot_noalloc": (C.c_int, [vp, vp, C.c_long, dp]),
         "lina_gpu_bicgstab": (C.c_int, [vp, vp, C.c_int, vp, vp, C.c_double, C.c_int, C.c_int, C.POINTER(SolveInfo)]),
@@ -444,6 +445,19 @@ class ILU:
         zd = DeviceArray(self.n)
         _check(lib().lina_gpu_ilu_apply(self.h, precision, rd.ptr, zd.ptr), "ILU apply")
         return zd.to_host()
+
+    def time_apply(self, reps=20, precision=PREC_MIXED):
+        """Device milliseconds of one application (forward + backward triangular solve), CUDA events on
+        the handle's stream around reps applications."""
+        ms = C.c_double()
+        _check(lib().lina_gpu_ilu_time_apply(self.h, precision, reps, C.byref(ms)), "ILU timing")
+        return ms.value
+
+    def apply_bytes(self, precision=PREC_MIXED):
+        """Algorithmic bytes of one application: every off-diagonal factor entry's value and column
+        once, and per row and triangular solve its row bounds, 1/diagonal, right-hand side and result."""
+        w = 4 if precision == PREC_MIXED else 8
+        return (w + 4) * (self.nnz - self.n) + 2 * self.n * (8 + 3 * w)
 
     def close(self):
         if getattr(self, "h", None):

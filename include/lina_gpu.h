@@ -217,6 +217,10 @@ int lina_gpu_wait_probe(int limit_us, double* waited_us);
 int lina_gpu_ilu_levels(const lina_gpu_ilu* h, int* nlev_L, int* nlev_U);
 /* z = U^-1 L^-1 r (device vectors, FP64); LINA_PREC_MIXED solves in FP32 */
 int lina_gpu_ilu_apply(lina_gpu_ilu* h, int precision, const double* r_dev, double* z_dev);
+/* device time of one application (forward and backward triangular solve, without the precision
+   conversions of lina_gpu_ilu_apply): reps applications to a right-hand side of ones, timed with CUDA
+   events on the handle's stream; *ms_per_apply = milliseconds per application */
+int lina_gpu_ilu_time_apply(lina_gpu_ilu* h, int precision, int reps, double* ms_per_apply);
 
 /* BiCGStab (BiCGStab_solve, LinA/BiCGStab.c:115-198) on device vectors with A a device matrix and
    the ILU(0) preconditioner (or none if ilu is NULL); stops when ||r|| / ||r0|| <= tol.

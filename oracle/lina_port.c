@@ -511,3 +511,110 @@ int port_ilu0(int n, const int* ptr, const int* col, const double* a, double* f)
     free(ustart);
     return ok;
 }
+
+/* ------------------------------------------------------------------ BiCGStab with ILU(0)
+   The reference's BiCGStab_solve (BiCGStab.c:115-198) with the product sparse_mult (linear_algebra.c:134:
+   each row's products summed in stored order) and the preconditioner of its ILU test drivers: x = y, then
+   L_triang_invert and U_triang_invert (linear_algebra.c:2008-2043) with the factors of
+   incomplete_LU_factorization (:1952).  The reference's L row holds the columns j <= i in ascending order
+   with the diagonal last, its U row (built transposed, then transposed back) the unit diagonal first and
+   the columns j > i ascending; the solves subtract in that order, so on CSR rows with ascending columns
+   the sums here are the reference's.  Vector operations are the reference's serial loops (scalar,
+   vector_add, scalar_mult, euklid_norm: linear_algebra.c:256-316). */
+static void bi_mult(int n, const int* ptr, const int* col, const double* a, const double* y, double* x) {
+    for (int i = 0; i < n; i++) {
+        double sum = 0;
+        for (int p = ptr[i]; p < ptr[i + 1]; p++) sum += a[p] * y[col[p]];
+        x[i] = sum;
+    }
+}
+
+static double bi_scalar(const double* x, const double* y, int n) {
+    double r = 0;
+    for (int i = 0; i < n; i++) r = r + x[i] * y[i];
+    return r;
+}
+
+static void bi_add(double* x, const double* y, double factor, int n) {
+    for (int i = 0; i < n; i++) x[i] += factor * y[i];
+}
+
+static void bi_ilu_apply(int n, const int* ptr, const int* col, const double* f, const double* y, double* x,
+                         double* tmp) {
+    /* L_triang_invert: x_i = (y_i - sum_{j<i} L_ij x_j) / L_ii */
+    for (int i = 0; i < n; i++) tmp[i] = y[i];
+    for (int i = 0; i < n; i++) {
+        double sum = tmp[i], diag = 0;
+        for (int p = ptr[i]; p < ptr[i + 1] && col[p] <= i; p++) {
+            if (col[p] != i)
+                sum -= f[p] * x[col[p]];
+            else
+                diag = f[p];
+        }
+        x[i] = sum / diag;
+    }
+    /* U_triang_invert: unit diagonal first, then the columns j > i */
+    for (int i = 0; i < n; i++) tmp[i] = x[i];
+    for (int i = n - 1; i >= 0; i--) {
+        double sum = tmp[i];
+        for (int p = ptr[i]; p < ptr[i + 1]; p++)
+            if (col[p] > i) sum -= f[p] * x[col[p]];
+        x[i] = sum / 1.0;
+    }
+}
+
+int port_bicgstab_ilu(int n, const int* ptr, const int* col, const double* a, const double* f, const double* b,
+                      double* x, double eps, int max_iter, int use_ilu, double* rel_out) {
+    const double default_eps = 1e-10;
+    double* w = (double*)calloc((size_t)(n > 0 ? n : 1) * 10, sizeof(double));
+    if (!w) return -1;
+    double *S = w, *PS = w + n, *PP = w + 2 * (size_t)n, *APP = w + 3 * (size_t)n, *APS = w + 4 * (size_t)n;
+    double *R = w + 5 * (size_t)n, *R0 = w + 6 * (size_t)n, *P = w + 7 * (size_t)n, *T = w + 8 * (size_t)n;
+    bi_mult(n, ptr, col, a, x, R);
+    bi_add(R, b, -1., n);
+    for (int i = 0; i < n; i++) R[i] *= -1;
+    memcpy(R0, R, (size_t)n * sizeof(double));
+    memcpy(P, R, (size_t)n * sizeof(double));
+    int iter = 0;
+    const double r0 = sqrt(bi_scalar(R, R, n));
+    double r = r0;
+    if (r0 != 0) {
+        do {
+            if (use_ilu)
+                bi_ilu_apply(n, ptr, col, f, P, PP, T);
+            else
+                memcpy(PP, P, (size_t)n * sizeof(double));
+            bi_mult(n, ptr, col, a, PP, APP);
+            const double h = bi_scalar(R, R0, n);
+            const double t = bi_scalar(APP, R0, n);
+            if (t == 0) {
+                (void)default_eps;
+                break;
+            }
+            const double alpha = h / t;
+            memcpy(S, R, (size_t)n * sizeof(double));
+            bi_add(S, APP, -alpha, n);
+            if (use_ilu)
+                bi_ilu_apply(n, ptr, col, f, S, PS, T);
+            else
+                memcpy(PS, S, (size_t)n * sizeof(double));
+            bi_mult(n, ptr, col, a, PS, APS);
+            const double s = bi_scalar(APS, APS, n);
+            if (s == 0) break;
+            const double omega = bi_scalar(APS, S, n) / s;
+            bi_add(x, PP, alpha, n);
+            bi_add(x, PS, omega, n);
+            memcpy(R, S, (size_t)n * sizeof(double));
+            bi_add(R, APS, -omega, n);
+            const double beta = bi_scalar(R, R0, n) * alpha / (h * omega);
+            bi_add(P, APP, -omega, n);
+            for (int i = 0; i < n; i++) P[i] *= beta;
+            bi_add(P, R, 1., n);
+            r = sqrt(bi_scalar(R, R, n));
+            iter++;
+        } while (r / r0 > eps && iter <= max_iter);
+    }
+    if (rel_out) *rel_out = r0 != 0 ? r / r0 : 0.0;
+    free(w);
+    return iter;
+}

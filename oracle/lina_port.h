@@ -62,6 +62,11 @@ int port_pcg(port_amg* h, const double* b, double* x, double tol, int max_iter, 
 void port_spmv(const port_amg* h, int l, const double* x, double* y);
 /* ILU(0) factors on A's pattern (L_ij where j <= i, U_ij where j > i); 1, or 0 on a zero pivot */
 int port_ilu0(int n, const int* ptr, const int* col, const double* a, double* f);
+/* BiCGStab_solve (LinA/BiCGStab.c:115-198) on y = A x with the ILU(0) preconditioner of factors f from
+   port_ilu0 (use_ilu = 0: none); x holds the start and receives the solution.  Returns the iteration
+   count, -1 if memory ran out; *rel_out (if given) = ||R|| / ||R0|| at the end. */
+int port_bicgstab_ilu(int n, const int* ptr, const int* col, const double* a, const double* f, const double* b,
+                      double* x, double eps, int max_iter, int use_ilu, double* rel_out);
 
 #ifdef __cplusplus
 }

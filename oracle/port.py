@@ -38,6 +38,7 @@ def lib():
         "port_pcg": (C.c_int, [vp, dp, dp, C.c_double, C.c_int, C.c_int, C.c_double, dp]),
         "port_spmv": (None, [vp, C.c_int, dp, dp]),
         "port_ilu0": (C.c_int, [C.c_int, ip, ip, dp, dp]),
+        "port_bicgstab_ilu": (C.c_int, [C.c_int, ip, ip, dp, dp, dp, dp, C.c_double, C.c_int, C.c_int, dp]),
         "port_amg_setup": (C.c_int, [vp, C.c_int, ip, ip, dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                      C.c_double]),
         "port_amg_level_info": (C.c_int, [vp, C.c_int, ip, C.POINTER(C.c_long), C.POINTER(C.c_long),
@@ -70,6 +71,24 @@ def ilu0(indptr, indices, data):
     if rc != 1:
         raise ArithmeticError("ILU(0): zero pivot" if rc == 0 else "ILU(0): out of memory")
     return f[:len(col)]
+
+
+def bicgstab_ilu(indptr, indices, data, b, eps=1e-8, max_iter=1000, factors=None, x0=None):
+    """BiCGStab_solve with the ILU(0) preconditioner (the C restatement); returns (x, iterations,
+    ||R|| / ||R0||).  ``factors`` from ilu0() may be passed to skip the factorisation."""
+    ptr = np.ascontiguousarray(indptr, dtype=np.int32)
+    col = np.ascontiguousarray(indices, dtype=np.int32)
+    val = np.ascontiguousarray(data, dtype=np.float64)
+    f = ilu0(ptr, col, val) if factors is None else np.ascontiguousarray(factors, dtype=np.float64)
+    n = len(ptr) - 1
+    x = np.zeros(n) if x0 is None else np.array(x0, dtype=np.float64)
+    bb = np.ascontiguousarray(b, dtype=np.float64)
+    rel = C.c_double()
+    it = lib().port_bicgstab_ilu(n, _ip(ptr), _ip(col), _dp(val), _dp(f), _dp(bb), _dp(x), eps, max_iter, 1,
+                                 C.byref(rel))
+    if it < 0:
+        raise MemoryError("BiCGStab: out of memory")
+    return x, it, rel.value
 
 
 class PortAMG:

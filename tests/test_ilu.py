@@ -241,3 +241,23 @@ def test_gpu_wait_runs_out_and_device_stays_usable():
     ptr, col, val = matrix(g, "nonsym400")
     assert np.array_equal(lina.ILU(400, ptr, col, val).factor_values(), g["nonsym400_f"])
     assert lina.lib().lina_gpu_wait_probe(0, None) == lina.EINVAL
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not gpu_available(), reason="no CUDA device")
+@pytest.mark.parametrize("prec", [lina.PREC_FP64, lina.PREC_MIXED])
+def test_gpu_timed_application_runs_the_solves(prec):
+    """lina_gpu_ilu_time_apply: positive device time, and the handle applies correctly afterwards."""
+    q = problems.at2_damage(65)
+    ilu = lina.ILU(q.n, q.indptr, q.indices, q.data)
+    ms = ilu.time_apply(5, prec)
+    assert 0.0 < ms < 1e3
+    assert ilu.apply_bytes(prec) > 8 * q.n
+    r = np.random.default_rng(0).standard_normal(q.n)
+    f = port.ilu0(q.indptr, q.indices, q.data)
+    A = sp.csr_matrix((f, q.indices, q.indptr), shape=(q.n, q.n))
+    L = sp.tril(A, format="csr")
+    U = sp.triu(A, 1, format="csr") + sp.identity(q.n, format="csr")
+    z_ref = spla.spsolve_triangular(U, spla.spsolve_triangular(L, r, lower=True), lower=False)
+    z = ilu.apply(r, prec)
+    assert np.linalg.norm(z - z_ref) / np.linalg.norm(z_ref) < (1e-12 if prec == lina.PREC_FP64 else 1e-5)

@@ -71,3 +71,27 @@ def test_port_setup_matches_live_reference(case):
             assert np.array_equal(a.labels, b.labels), f"labels level {l}"
             assert _same(a.P, b.P), f"P level {l}"
             assert _same(a.R, b.R), f"R level {l}"
+
+
+@pytest.mark.parametrize("name", golden_cases("hierarchy"))
+def test_port_bicgstab_ilu_matches_reference(name):
+    """The restated BiCGStab with ILU(0) (the damage workload's CPU baseline) reproduces the reference's
+    BiCGStab_solve with its ILU(0) preconditioner bit for bit: iterations and solution."""
+    g = load_golden(name)
+    s = system_for(name)
+    x, it, rel = port.bicgstab_ilu(s.indptr, s.indices, s.data, s.b, 1e-8, 1000)
+    assert it == int(g["bicgstab_ilu_it"])
+    assert np.array_equal(x, g["bicgstab_ilu_x"])
+    assert rel <= 1e-8
+
+
+@pytest.mark.skipif(not ref.available(), reason="reference library not built here (needs the reference tree)")
+def test_port_bicgstab_ilu_matches_live_reference():
+    """The same at a size beyond the goldens: the AT2 damage Hessian on a 129 x 129 mesh, whose
+    factor rows mix short and long patterns."""
+    from fem_gb300 import problems
+    q = problems.at2_damage(129)
+    xr, itr = ref.bicgstab_ilu(q, 1e-8, 1000)
+    x, it, _ = port.bicgstab_ilu(q.indptr, q.indices, q.data, q.b, 1e-8, 1000)
+    assert it == itr
+    assert np.array_equal(x, xr)
