@@ -370,3 +370,63 @@ def greedy_colouring(n, indptr, indices, data):
     col = np.zeros(n, dtype=np.int32)
     nc = lib().rs_greedy_colouring(M.ptr, _ip(col))
     return nc, col
+
+
+# ------------------------------------------------------------------ FEM2D P1 assembly (oracle/fem2d_shim.c)
+FEM2D_PATH = os.path.join(HERE, "_ref", "libFEM2D_ref.so")
+_fem2d = None
+
+
+def fem2d_available() -> bool:
+    if not os.path.exists(FEM2D_PATH):
+        return False
+    try:
+        fem2d_lib()
+    except OSError:
+        return False
+    return True
+
+
+def fem2d_lib():
+    global _fem2d
+    if _fem2d is None:
+        L = C.CDLL(FEM2D_PATH)
+        ip, dp = C.POINTER(C.c_int), C.POINTER(C.c_double)
+        L.fs_p1_assemble.restype = C.c_long
+        L.fs_p1_assemble.argtypes = [C.c_int, C.c_int, dp, ip, ip, C.c_double, C.c_double, ip, ip, dp, C.c_long]
+        _fem2d = L
+    return _fem2d
+
+
+def mesh_neighbours(n_nodes, tri):
+    """Neighbour lists of a triangle mesh (each node's adjacent nodes, ascending) as (ptr, nb)."""
+    tri = np.asarray(tri, dtype=np.int64)
+    e = np.concatenate([tri[:, [0, 1]], tri[:, [1, 2]], tri[:, [2, 0]]])
+    e = np.concatenate([e, e[:, ::-1]])
+    e = np.unique(e, axis=0)
+    ptr = np.zeros(n_nodes + 1, np.int32)
+    np.add.at(ptr, e[:, 0] + 1, 1)
+    return np.cumsum(ptr).astype(np.int32), np.ascontiguousarray(e[:, 1], dtype=np.int32)
+
+
+def p1_assemble(xy, tri, kind="laplace", E=210.0, nu=0.3):
+    """The reference's P1 assembly on the mesh (FEM2D set_matrix_Aij_11_2D): kind "laplace" the Laplacian
+    with coefficient 1 (insert_A_bbV), n x n; kind "elastic" plane-strain elasticity with Young's modulus
+    E and Poisson ratio nu, combined as crack.c does, 2n x 2n with the components blocked.  Returns
+    (indptr, indices, data) with ascending columns."""
+    L = fem2d_lib()
+    xy = np.ascontiguousarray(xy, dtype=np.float64)
+    n = len(xy)
+    nptr, nb = mesh_neighbours(n, tri)
+    k = 1 if kind == "laplace" else 2
+    lam = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu))
+    mu = E / (2.0 * (1.0 + nu))
+    rows = n * k
+    nnz = L.fs_p1_assemble(k, n, _dp(xy), _ip(nptr), _ip(nb), lam, mu, None, None, None, 0)
+    if nnz < 0:
+        raise MemoryError("FEM2D assembly: out of memory")
+    ptr = np.zeros(rows + 1, np.int32)
+    col = np.zeros(max(nnz, 1), np.int32)
+    val = np.zeros(max(nnz, 1))
+    L.fs_p1_assemble(k, n, _dp(xy), _ip(nptr), _ip(nb), lam, mu, _ip(ptr), _ip(col), _dp(val), nnz)
+    return ptr, col[:nnz], val[:nnz]

@@ -14,7 +14,8 @@ pcg solves (LinA/PCGS.c:163) with the smoothers the GPU library implements
 reference's own lexicographic SOR.  For bound-constrained damage quadratics
 it records the minimiser and iteration count of reflective_newton with two
 of the reference's local solvers; and for a material-identification case the
-forward solutions and the adjoint solved with the reference's transpose of A.
+forward solutions and the adjoint solved with the reference's transpose of A.  The P1 assembly
+fixture records FEM2D's own stiffness matrices (``make -C oracle fem2d``) on stored meshes.
 Tests compare the GPU library against
 these files on machines where the reference is absent.
 """
@@ -433,10 +434,36 @@ def make_solvers():
     return out
 
 
+P1_FILE = "p1_fem2d"
+# meshes of the P1 assembly fixture: structured grids of the elasticity benchmark and seeded Delaunay
+# meshes of the batched workload (stored with the file: scipy's triangulation may differ between hosts)
+P1_MESHES = {"grid17": lambda: problems.elastic_mesh(17)[:2], "delaunay600": lambda: problems.delaunay_mesh(600, 5)}
+
+
+def make_p1():
+    """The reference's own P1 assembly (FEM2D set_matrix_Aij_11_2D, oracle/fem2d_shim.c): the Laplacian
+    with coefficient 1 and plane-strain elasticity (E 210, nu 0.3, assembled as crack.c does) on each
+    mesh."""
+    out = {}
+    for name, mk in P1_MESHES.items():
+        xy, tri = mk()
+        out[f"{name}_xy"] = np.asarray(xy, dtype=np.float64)
+        out[f"{name}_tri"] = np.asarray(tri, dtype=np.int32)
+        for kind in ("laplace", "elastic"):
+            ptr, col, val = ref.p1_assemble(xy, tri, kind, 210.0, 0.3)
+            out[f"{name}_{kind}_ptr"], out[f"{name}_{kind}_col"], out[f"{name}_{kind}_val"] = ptr, col, val
+    return out
+
+
 def main():
     only = sys.argv[1:]
     if not ref.available():
         sys.exit("oracle/_ref/libLinA_ref.so is missing: run `make -C oracle ref` where the reference tree exists")
+    if (not only or P1_FILE in only) and ref.fem2d_available():
+        data = make_p1()
+        path = os.path.join(HERE, f"{P1_FILE}.npz")
+        np.savez_compressed(path, **data)
+        print(f"{path}: " + ", ".join(f"{k[:-4]} {len(v)} entries" for k, v in data.items() if k.endswith("_val")))
     if not only or "spgemm" in only:
         data = make_spgemm()
         path = os.path.join(HERE, "spgemm.npz")

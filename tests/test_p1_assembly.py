@@ -1,15 +1,67 @@
 """P1 assembly on the GPU (lina_gpu_p1_*): the scalar Laplacian and plane-strain elasticity with
 per-element coefficients, straight into CSR.
 
-Oracle: the numpy element assembly of fem_gb300.problems (structured grids and the seeded Delaunay
-meshes of the batched workload) to rounding, and the library's host assembly bit for bit.
+Oracle: the reference's own assembly, FEM2D/FEM2D.c set_matrix_Aij_11_2D with its element integrals
+(tests/golden/p1_fem2d.npz, made by tests/golden/make_golden.py from the reference built by
+`make -C oracle fem2d`, and live where that library is built): the same pattern, values to rounding
+(bit for bit for the Laplacian on structured grids); the numpy element assembly of
+fem_gb300.problems; and the library's host assembly bit for bit on the device.
 """
+import os
+
 import numpy as np
 import pytest
 import scipy.sparse as sp
 
 from fem_gb300 import lina, problems
-from tests.conftest import gpu_available
+from oracle import ref
+from tests.conftest import ROOT, gpu_available
+
+P1_GOLDEN = os.path.join(ROOT, "tests", "golden", "p1_fem2d.npz")
+# max |difference| / max |entry| against the reference's assembly: the entries of a node's fan of
+# triangles are summed in another order on irregular meshes (observed up to 5e-15)
+P1_TOL = 1e-13
+P1_KINDS = {"laplace": lina.P1_LAPLACE, "elastic": lina.P1_ELASTIC}
+
+
+def _p1_golden():
+    with np.load(P1_GOLDEN) as z:
+        return {k: z[k] for k in z.files}
+
+
+def _coef(kind, n_elems):
+    """coefficient 1 (Laplacian), Young's modulus 210 (elasticity, nu 0.3), as in the fixture"""
+    return np.ones(n_elems) if kind == "laplace" else np.full(n_elems, 210.0)
+
+
+def _check_against(got, want, bitwise=False):
+    ptr, col, val = got
+    wp, wc, wv = want
+    assert np.array_equal(ptr, wp) and np.array_equal(col, wc), "pattern differs from the reference's"
+    err = np.abs(val - wv).max() / np.abs(wv).max()
+    assert err <= P1_TOL, err
+    if bitwise:
+        assert np.array_equal(val, wv)
+
+
+@pytest.mark.parametrize("mesh", ["grid17", "delaunay600"])
+@pytest.mark.parametrize("kind", ["laplace", "elastic"])
+def test_host_assembly_matches_reference_fem2d(mesh, kind):
+    g = _p1_golden()
+    xy, tri = g[f"{mesh}_xy"], g[f"{mesh}_tri"]
+    ptr, col, val, _ = lina.p1_assemble_host(P1_KINDS[kind], xy, tri, _coef(kind, len(tri)), nu=0.3)
+    _check_against((ptr, col, val), (g[f"{mesh}_{kind}_ptr"], g[f"{mesh}_{kind}_col"], g[f"{mesh}_{kind}_val"]),
+                   bitwise=(mesh == "grid17" and kind == "laplace"))
+
+
+@pytest.mark.skipif(not ref.fem2d_available(), reason="reference FEM2D not built here (needs the reference tree)")
+@pytest.mark.parametrize("mesh", ["grid65", "delaunay5000"])
+@pytest.mark.parametrize("kind", ["laplace", "elastic"])
+def test_host_assembly_matches_live_reference_fem2d(mesh, kind):
+    xy, tri = problems.elastic_mesh(65)[:2] if mesh == "grid65" else problems.delaunay_mesh(5000, 21)
+    ptr, col, val, _ = lina.p1_assemble_host(P1_KINDS[kind], xy, tri, _coef(kind, len(tri)), nu=0.3)
+    _check_against((ptr, col, val), ref.p1_assemble(xy, tri, kind, 210.0, 0.3),
+                   bitwise=(mesh == "grid65" and kind == "laplace"))
 
 
 def csr(ptr, col, val, n):
@@ -124,3 +176,17 @@ def test_device_assembly_feeds_the_solver():
     A2 = csr(ptr, col, val2, len(b2))
     assert info.status == 0
     assert np.linalg.norm(b2 - A2 @ x) / np.linalg.norm(b2) <= 1e-8
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not gpu_available(), reason="no CUDA device")
+@pytest.mark.parametrize("mesh", ["grid17", "delaunay600"])
+@pytest.mark.parametrize("kind", ["laplace", "elastic"])
+def test_device_assembly_matches_reference_fem2d(mesh, kind):
+    g = _p1_golden()
+    xy, tri = g[f"{mesh}_xy"], g[f"{mesh}_tri"]
+    asm = lina.P1Assembly(P1_KINDS[kind], xy, tri, 0.3)
+    asm.assemble(_coef(kind, len(tri)))
+    ptr, col, val, _ = asm.system()
+    _check_against((ptr, col, val), (g[f"{mesh}_{kind}_ptr"], g[f"{mesh}_{kind}_col"], g[f"{mesh}_{kind}_val"]),
+                   bitwise=(mesh == "grid17" and kind == "laplace"))
