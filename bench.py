@@ -673,9 +673,11 @@ def run_adjoint(args, rank, world, local):
 def run_batch(args, rank, world, local):
     """Independent SPD systems on seeded unstructured Delaunay meshes (half Poisson, half plane-strain
     elasticity, dof counts log-uniform on [10k, 500k], per-element lognormal coefficients with sigma
-    1.5): a step solves all of them to a relative residual of 1e-8 in mixed precision with one launch
-    of the batch graph.  Beside it, the same systems solved one after another by the single-system
-    FP64 path (and the single-system mixed path), on the same hierarchies."""
+    1.5): a step solves all of them to a relative residual of 1e-8 in mixed precision as one segmented
+    system (lina_gpu_segbatch: every level the block-diagonal concatenation of the systems' levels,
+    per-system FCG scalars and stopping, one graph launch).  Beside it, the same systems in one graph with
+    a branch per system, and solved one after another by the single-system FP64 and mixed paths, on the
+    same hierarchies."""
     from fem_gb300 import lina, problems
     # with several ranks each solves its dof-balanced share of the systems (no exchange)
     plan = problems.batch_shard(problems.batch_plan(args.batch_count, seed=0), rank, world)
@@ -691,11 +693,14 @@ def run_batch(args, rank, world, local):
     t_setup = time.perf_counter() - t0
     dofs = int(sum(s.n for s in systems))
     nnz = int(sum(s.nnz for s in systems))
+    t0 = time.perf_counter()
+    seg = lina.SegmentedBatch(amgs)
+    t_seg = time.perf_counter() - t0
     batch = lina.Batch(amgs, stop=lina.STOP_RELATIVE)
     bs = [s.b for s in systems]
     bd = [lina.DeviceArray.from_host(b) for b in bs]
     for _ in range(args.warmup):
-        batch.solve(bd, tol=args.tol, device=True)
+        seg.solve(bd, tol=args.tol, device=True)
     barrier(world)
     clocks = ClockSampler(local)
     clocks.start()
@@ -703,18 +708,23 @@ def run_batch(args, rank, world, local):
     # device-resident inputs and outputs
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        _, infos = batch.solve(bd, tol=args.tol, device=True)
+        _, infos = seg.solve(bd, tol=args.tol, device=True)
     ms = max_over_ranks((time.perf_counter() - t0) * 1e3, world)
     launches = lina.launches() - launches0
     # end to end: host arrays in and out
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        xs, infos = batch.solve(bs, tol=args.tol)
+        xs, infos = seg.solve(bs, tol=args.tol)
     ms_e2e = max_over_ranks((time.perf_counter() - t0) * 1e3, world)
     clocks.stop()
     worst = max(i.true_rel_residual for i in infos)
     its = [i.iterations for i in infos]
     assert all(i.status == 0 for i in infos), [i.status for i in infos]
+    # the same systems as one graph with a branch per system (each system's own hierarchy and kernels)
+    batch.solve(bd, tol=args.tol, device=True)
+    t0 = time.perf_counter()
+    _, infos_b = batch.solve(bd, tol=args.tol, device=True)
+    t_branches = max_over_ranks(time.perf_counter() - t0, world)
     # the single-system paths, one system after another
     t0 = time.perf_counter()
     loop_mixed_its = [a.pcg(b, tol=args.tol, max_iter=1000)[1].iterations for a, b in zip(amgs, bs)]
@@ -736,7 +746,8 @@ def run_batch(args, rank, world, local):
     value = n_sys * args.steps / (ms / 1e3)
     e2e = n_sys * args.steps / (ms_e2e / 1e3)
     out = common_line(f"batched AMG-PCG: systems/s over {n_sys} unstructured systems ({dofs} dofs) to rel. res. "
-                      f"{args.tol:g}, one graph launch", value, "systems/s", world, args.steps, args.warmup, ms,
+                      f"{args.tol:g}, segmented hierarchy, one graph launch", value, "systems/s", world, args.steps,
+                      args.warmup, ms,
                       "f32 preconditioner / f64 Krylov", "synthetic (seeded Delaunay meshes, lognormal coefficients)",
                       {"workload": f"{n_sys} systems, half P1 Poisson and half P1 plane-strain elasticity on seeded "
                                    "Delaunay meshes, dofs log-uniform on [10k, 500k], sigma 1.5; "
@@ -746,21 +757,24 @@ def run_batch(args, rank, world, local):
                       {"value": e2e, "unit": "systems/s", "h2d_bytes_per_step": 8 * dofs,
                        "d2h_bytes_per_step": 8 * dofs}, launches, clocks)
     out["dofs_per_s"] = value * dofs / n_sys
+    out["branch_graph_systems_per_s"] = n_sys / t_branches
     out["loop_fp64_systems_per_s"] = n_sys / t_loop64
     out["loop_mixed_systems_per_s"] = n_sys / t_loop_mixed
     out["batch_over_loop_fp64"] = value / (n_sys / t_loop64)
     out["iterations"] = {"batch_min": min(its), "batch_max": max(its), "batch_sum": int(sum(its)),
+                         "branch_graph_sum": int(sum(i.iterations for i in infos_b)),
                          "loop_fp64_sum": int(sum(i.iterations for i in loop64)),
                          "loop_mixed_sum": int(sum(loop_mixed_its))}
     out["worst_true_rel_residual"] = worst
-    out["setup_s"] = {"meshes_and_assembly": t_mesh, "amg_setup": t_setup}
-    # the dominant kernel: the colour sweeps of the largest system's level with the most entries
-    big = max(range(len(systems)), key=lambda k: systems[k].nnz)
-    for a in amgs:
-        a.set_smoother(lina.SMOOTHER_MC_SOR, 1.0, lina.PREC_MIXED)
-    out["roofline"] = sweep_roofline(amgs[big], bd[big], lina.DeviceArray(systems[big].n), args.tol,
-                                     lina.STOP_RELATIVE, 0, 2,
-                                     f"FP32 multicolour-SOR colour sweeps of the largest system ({systems[big].n} dofs)")
+    out["setup_s"] = {"meshes_and_assembly": t_mesh, "amg_setup": t_setup, "segmented_hierarchy": t_seg}
+    rows, ents = seg.levels()
+    out["segmented_levels"] = {"rows": rows, "entries": ents}
+    # the dominant kernel: the colour sweeps of the combined hierarchy's finest level (all systems' rows),
+    # timed in solves of the whole block-diagonal system on the combined hierarchy
+    comb = seg.hierarchy()
+    bcat = lina.DeviceArray.from_host(np.concatenate(bs))
+    out["roofline"] = sweep_roofline(comb, bcat, lina.DeviceArray(comb.n), args.tol, lina.STOP_RELATIVE, 0, 1,
+                                     "FP32 multicolour-SOR colour launches of the segmented hierarchy")
     out["cpu_baseline"] = None
     if rank == 0 and not args.no_cpu:
         from oracle import port

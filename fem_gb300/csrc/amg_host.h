@@ -60,6 +60,11 @@ struct CoarseSolver {
     bool inverted = true;
     std::vector<double> diag_inv;   // 1/a_ii for rows outside the block (0 inside)
     std::vector<int> in_block;      // 1 if row is part of the dense block
+    // a block-diagonal coarsest level (several independent systems): block k holds the block positions
+    // [blocks[k], blocks[k+1]) with its inverse at inv[inv_offsets[k]], row-major; empty: one block
+    std::vector<int> blocks;
+    std::vector<long> inv_offsets;
+    std::vector<char> block_inverted;  // per block (blocks non-empty): false = inverted at upload
 };
 
 struct HostHierarchy {

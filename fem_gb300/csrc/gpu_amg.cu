@@ -554,17 +554,29 @@ __global__ void coarse_gather_kernel(int n, const TX* __restrict__ b, const int*
     }
 }
 
-// dense FP64 GEMV with the block inverse: one warp per block row
+// dense FP64 GEMV with the block inverse: one warp per block row.  A block-diagonal coarsest level
+// (rblk non-null: the block of each block row, its first position boff[k] and inverse offset ioff[k])
+// multiplies each row by its own block only; with one block the arithmetic is the same.
 template <typename TX>
 __global__ void coarse_gemv_kernel(int m, const double* __restrict__ inv, const double* __restrict__ bblk,
-                                   const int* __restrict__ brows, TX* __restrict__ x) {
+                                   const int* __restrict__ brows, TX* __restrict__ x, const int* __restrict__ rblk,
+                                   const int* __restrict__ boff, const long* __restrict__ ioff) {
     pdl_wait();
     const int lane = threadIdx.x & 31;
     for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < m;
          r += ((long)gridDim.x * blockDim.x) >> 5) {
-        const double* row = inv + r * (long)m;
+        long base = r * (long)m;
+        int m0 = 0, len = m;
+        if (rblk) {
+            const int k = rblk[r];
+            m0 = boff[k];
+            len = boff[k + 1] - m0;
+            base = ioff[k] + (r - m0) * (long)len;
+        }
+        const double* row = inv + base;
+        const double* bb = bblk + m0;
         double s = 0.0;
-        for (int j = lane; j < m; j += 32) s += row[j] * bblk[j];
+        for (int j = lane; j < len; j += 32) s += row[j] * bb[j];
         s = warp_sum(s);
         if (lane == 0) x[brows[r]] = TX(s);
     }
@@ -1222,14 +1234,17 @@ struct DCsr {
 // layout (FP32 and FP64): one thread per row (SELL-32; long rows software-pipelined) for levels of
 // 100k rows or more; a group of lanes per row for the small coarse levels, 8 lanes from 8k rows
 // (enough rows to fill the GPU, several loads in flight per lane), wider groups below.
-int csrv_lanes_for(const lina::Csr& c) {
-    const double avg = c.n > 0 ? double(c.nnz()) / c.n : 0.0;
+int csrv_lanes_for_shape(long n, double avg) {
     if (g_layout == 1) return 0;
     if (g_layout >= 3) return 4 << (g_layout - 3);
-    if (g_layout == 0 && c.n >= 100000 && avg <= 256.0) return 0;
+    if (g_layout == 0 && n >= 100000 && avg <= 256.0) return 0;
     if (avg < 8.0) return 4;
-    if (c.n >= 8000) return 8;
+    if (n >= 8000) return 8;
     return avg >= 24.0 ? 16 : 8;
+}
+
+int csrv_lanes_for(const lina::Csr& c) {
+    return csrv_lanes_for_shape(c.n, c.n > 0 ? double(c.nnz()) / c.n : 0.0);
 }
 
 // Host-side SELL-32 construction; `order` lists the rows per group (colour)
@@ -1536,12 +1551,17 @@ struct lina_gpu_amg {
     double* c_inv = nullptr;
     double* c_dginv = nullptr;
     double* c_bblk = nullptr;
+    int *c_rblk = nullptr, *c_boff = nullptr;  // block-diagonal coarsest level (else null)
+    long* c_ioff = nullptr;
     // finest-level extras
     double* isoinv = nullptr;  // 1/a for isolated rows of the finest level, 0 elsewhere
     double* signs = nullptr;   // only when make_positive_diag flipped a row
     DCsr Aorig;                // unflipped finest matrix when signs exist (Krylov SpMV)
     bool has_signs = false;
     bool host_only = false;
+    // segmented batch: per level, the rows of the largest system's level (layout choice), else empty
+    std::vector<long> seg_max_rows;
+    long lanes_rows = 0;
     int timed_level = 0;       // level whose smoother sweeps LINA_PCG_TIME_KERNELS times (most entries)
     // maps for lina_gpu_amg_update_values (built on first use, finest level)
     bool upd_built = false;
@@ -1639,7 +1659,10 @@ struct lina_gpu_amg {
             set_err("matrix entry with column %d outside [0, %d)", c.col[bad], ncols);
             return LINA_GPU_EINVAL;
         }
-        d.lanes = csrv_lanes_for(c);
+        // a level of a segmented batch takes the layout of its largest system's level (lanes_rows rows):
+        // concatenated small levels keep the lane groups their long rows need
+        d.lanes = lanes_rows > 0 ? csrv_lanes_for_shape(std::min<long>(lanes_rows, c.n), c.n > 0 ? double(c.nnz()) / c.n : 0.0)
+                                 : csrv_lanes_for(c);
         if (d.lanes > 0) {
             // CSR-vector: sanitise placeholder columns outside the operand, keep the CSR arrays
             std::vector<int> colc(c.col);
@@ -1892,8 +1915,10 @@ struct lina_gpu_amg {
         const int n = lv[0].n;
         go(coarse_gather_kernel<TX>, grid_for(n, kThreads), stream, n, b, c_inblock, c_blockpos,
                                                                                  c_dginv, c_bblk, x);
-        if (cm > 0) go(coarse_gemv_kernel<TX>, grid_for((long)cm * 32, kThreads), stream, 
-            cm, c_inv, c_bblk, c_brows, x);
+        if (cm > 0)
+            go(coarse_gemv_kernel<TX>, grid_for((long)cm * 32, kThreads), stream, cm, (const double*)c_inv,
+               (const double*)c_bblk, (const int*)c_brows, x, (const int*)c_rblk, (const int*)c_boff,
+               (const long*)c_ioff);
     }
 
     // pre-smoothing from the zero guess (plus the isolated-row fix on the finest level)
@@ -2312,6 +2337,7 @@ int upload_hierarchy(lina_gpu_amg* h) {
         lina::HostLevel& hl = H.lv[l];
         DLevel& L = h->lv[l];
         L.n = hl.A.n;
+        h->lanes_rows = h->seg_max_rows.empty() ? 0 : h->seg_max_rows[l];
         if ((rc = h->upload_csr(L.A, hl.A))) return rc;
         std::vector<double> dinv(L.n, 0.0);
         for (int i = 0; i < L.n; i++) {
@@ -2343,6 +2369,7 @@ int upload_hierarchy(lina_gpu_amg* h) {
         if ((rc = h->alloc(&L.b32, L.n))) return rc;
         if ((rc = h->alloc(&L.r32, L.n))) return rc;
     }
+    h->lanes_rows = 0;
     // coarsest block
     lina::CoarseSolver& cs = H.coarse;
     h->cm = (int)cs.block_rows.size();
@@ -2352,13 +2379,34 @@ int upload_hierarchy(lina_gpu_amg* h) {
     if ((rc = h->upload(&h->c_inblock, cs.in_block.data(), cs.in_block.size()))) return rc;
     if ((rc = h->upload(&h->c_blockpos, blockpos.data(), blockpos.size()))) return rc;
     if ((rc = h->upload(&h->c_inv, cs.inv.data(), cs.inv.size()))) return rc;
-    if (!cs.inverted) {  // a large block: inverted in place on the device
+    if (cs.blocks.empty()) {
+        if (!cs.inverted) {  // a large block: inverted in place on the device
+            int* err = nullptr;
+            if ((rc = h->alloc(&err, 1))) return rc;
+            std::string msg;
+            if ((rc = lina::dense_inverse(h->cm, h->c_inv, g_dense_method, h->stream, err, msg))) {
+                set_err("%s", msg.c_str());
+                return rc;
+            }
+        }
+    } else {  // block-diagonal: each block's inverse at its offset, large ones inverted on the device
+        const int nb = (int)cs.blocks.size() - 1;
+        std::vector<int> rblk(std::max(h->cm, 1), 0);
+        for (int k = 0; k < nb; k++)
+            for (int r = cs.blocks[k]; r < cs.blocks[k + 1]; r++) rblk[r] = k;
+        if ((rc = h->upload(&h->c_rblk, rblk.data(), rblk.size()))) return rc;
+        if ((rc = h->upload(&h->c_boff, cs.blocks.data(), cs.blocks.size()))) return rc;
+        if ((rc = h->upload(&h->c_ioff, cs.inv_offsets.data(), cs.inv_offsets.size()))) return rc;
         int* err = nullptr;
-        if ((rc = h->alloc(&err, 1))) return rc;
-        std::string msg;
-        if ((rc = lina::dense_inverse(h->cm, h->c_inv, g_dense_method, h->stream, err, msg))) {
-            set_err("%s", msg.c_str());
-            return rc;
+        for (int k = 0; k < nb; k++) {
+            if (cs.block_inverted[k]) continue;
+            if (!err && (rc = h->alloc(&err, 1))) return rc;
+            std::string msg;
+            if ((rc = lina::dense_inverse(cs.blocks[k + 1] - cs.blocks[k], h->c_inv + cs.inv_offsets[k],
+                                          g_dense_method, h->stream, err, msg))) {
+                set_err("%s", msg.c_str());
+                return rc;
+            }
         }
     }
     if ((rc = h->upload(&h->c_dginv, cs.diag_inv.data(), cs.diag_inv.size()))) return rc;
@@ -3710,6 +3758,665 @@ int lina_gpu_batch_solve(lina_gpu_batch* B, const double* const* b, double* cons
 int lina_gpu_batch_size(const lina_gpu_batch* B) { return B ? (int)B->sys.size() : 0; }
 
 int lina_gpu_batch_destroy(lina_gpu_batch* B) {
+    delete B;
+    return 0;
+}
+
+}  // extern "C"
+
+// =================================================================== segmented batched solves
+// Many independent systems solved as one: every level of one hierarchy is the block-diagonal
+// concatenation of the systems' levels (a segmented CSR: system i's rows, and its columns, follow the
+// rows of systems 0..i-1), so each kernel of the V-cycle streams all systems' rows in one launch.  A
+// system whose hierarchy is shallower than the deepest one is padded below its coarsest level with
+// copies of that level (P = R = I); a V-cycle returns there the exact coarse solution, as the system's
+// own V-cycle does, and the padded levels cost a few sweeps of its small coarsest matrix.  The coarsest
+// level is solved block by block with each system's own dense inverse.  The Krylov loop is FCG(m) per
+// system: its reductions are segmented (fixed chunks of rows that never straddle two systems, summed
+// per system in chunk order), each system has its own scalars, stops at its own tolerance and then
+// keeps x and r while the others continue; one CUDA graph with a device-side while loop runs until
+// every system has stopped.
+namespace {
+
+constexpr int kSegChunk = 4096;  // rows per task of the segmented kernels
+
+struct SegScalars {
+    double s, s_old, pq, alpha, rr, r0, tol, tnorm2;
+    double tj[kFcgMax], pqh[kFcgMax], cj[kFcgMax];
+    int iter, base, active, maxit, status, pad;
+};
+
+enum { SEG_DOT = 0, SEG_PQ = 1, SEG_RR = 2, SEG_NORM_B = 3, SEG_NORM_T = 4 };
+
+// the block's sums of v[0..NV) into out[0..NV)
+template <int NV>
+__device__ void seg_block_sums(const double (&v)[NV], double* out) {
+    __shared__ double sm[NV][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+        const double x = warp_sum(v[k]);
+        if (lane == 0) sm[k][wid] = x;
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            double x = (lane < nw) ? sm[k][lane] : 0.0;
+            x = warp_sum(x);
+            if (lane == 0) out[k] = x;
+        }
+    }
+    __syncthreads();  // sm is reused by the block's next task
+}
+
+// s = r.z and t_j = z.q_{k-j} (j = 1..min(k - base, M)) per task of an active system
+template <typename TZ, int M>
+__global__ void __launch_bounds__(kThreads) seg_fcg_dot_kernel(int ntask, const int4* __restrict__ task, long n,
+                                                               const double* __restrict__ r,
+                                                               const TZ* __restrict__ z, const double* __restrict__ qh,
+                                                               const SegScalars* __restrict__ sc,
+                                                               double* __restrict__ part) {
+    pdl_wait();
+    for (int t = blockIdx.x; t < ntask; t += gridDim.x) {
+        const int4 tk = task[t];
+        double v[M + 1];
+#pragma unroll
+        for (int j = 0; j <= M; j++) v[j] = 0.0;
+        if (sc[tk.x].active) {
+            const int k = sc[tk.x].iter;
+            const int nprev = min(k - sc[tk.x].base, M);
+            const double* qs[M];
+#pragma unroll
+            for (int j = 1; j <= M; j++) qs[j - 1] = qh + (size_t)((k - j + M * kFcgMax) % M) * n;
+            for (long i = tk.y + threadIdx.x; i < tk.z; i += blockDim.x) {
+                const double zi = double(z[i]);
+                v[0] += r[i] * zi;
+#pragma unroll
+                for (int j = 1; j <= M; j++)
+                    if (j <= nprev) v[j] += zi * qs[j - 1][i];
+            }
+        }
+        seg_block_sums<M + 1>(v, part + (size_t)t * (M + 1));
+    }
+}
+
+// p = z - sum_j c_j p_{k-j} per task of an active system
+template <typename TZ, int M>
+__global__ void __launch_bounds__(kThreads) seg_fcg_update_p_kernel(int ntask, const int4* __restrict__ task, long n,
+                                                                    const TZ* __restrict__ z,
+                                                                    const double* __restrict__ ph,
+                                                                    double* __restrict__ p,
+                                                                    const SegScalars* __restrict__ sc) {
+    pdl_wait();
+    for (int t = blockIdx.x; t < ntask; t += gridDim.x) {
+        const int4 tk = task[t];
+        if (!sc[tk.x].active) continue;
+        const int k = sc[tk.x].iter;
+        const int nprev = min(k - sc[tk.x].base, M);
+        double c[M];
+        const double* ps[M];
+#pragma unroll
+        for (int j = 1; j <= M; j++) {
+            c[j - 1] = sc[tk.x].cj[j - 1];
+            ps[j - 1] = ph + (size_t)((k - j + M * kFcgMax) % M) * n;
+        }
+        for (long i = tk.y + threadIdx.x; i < tk.z; i += blockDim.x) {
+            double pi = double(z[i]);
+#pragma unroll
+            for (int j = 1; j <= M; j++)
+                if (j <= nprev) pi -= c[j - 1] * ps[j - 1][i];
+            p[i] = pi;
+        }
+    }
+}
+
+// a.b per task
+__global__ void __launch_bounds__(kThreads) seg_dot_kernel(int ntask, const int4* __restrict__ task,
+                                                           const double* __restrict__ a, const double* __restrict__ b,
+                                                           double* __restrict__ part) {
+    pdl_wait();
+    for (int t = blockIdx.x; t < ntask; t += gridDim.x) {
+        const int4 tk = task[t];
+        double v[1] = {0.0};
+        for (long i = tk.y + threadIdx.x; i < tk.z; i += blockDim.x) v[0] += a[i] * b[i];
+        seg_block_sums<1>(v, part + t);
+    }
+}
+
+// x += alpha p, r -= alpha q, ring slot (iter mod M) <- p, q for active systems; r.r per task
+template <int M>
+__global__ void __launch_bounds__(kThreads) seg_update_xr_kernel(int ntask, const int4* __restrict__ task, long n,
+                                                                 double* __restrict__ x, double* __restrict__ r,
+                                                                 const double* __restrict__ p,
+                                                                 const double* __restrict__ q, double* __restrict__ ph,
+                                                                 double* __restrict__ qh,
+                                                                 const SegScalars* __restrict__ sc,
+                                                                 double* __restrict__ part) {
+    pdl_wait();
+    for (int t = blockIdx.x; t < ntask; t += gridDim.x) {
+        const int4 tk = task[t];
+        double v[1] = {0.0};
+        if (sc[tk.x].active) {
+            const double alpha = sc[tk.x].alpha;
+            const size_t slot = (size_t)(sc[tk.x].iter % M) * n;
+            for (long i = tk.y + threadIdx.x; i < tk.z; i += blockDim.x) {
+                const double pi = p[i], qi = q[i];
+                x[i] += alpha * pi;
+                const double ri = r[i] - alpha * qi;
+                r[i] = ri;
+                v[0] += ri * ri;
+                ph[slot + i] = pi;
+                qh[slot + i] = qi;
+            }
+        } else {
+            for (long i = tk.y + threadIdx.x; i < tk.z; i += blockDim.x) v[0] += r[i] * r[i];
+        }
+        seg_block_sums<1>(v, part + t);
+    }
+}
+
+// Per system (one warp each): its tasks' partials summed in task order, then the scalars of MODE.  In
+// SEG_RR the kernel also sets the loop condition: some system still active.
+template <int MODE, int M>
+__global__ void __launch_bounds__(1024) seg_finish_kernel(int S, const int* __restrict__ tbeg,
+                                                          const double* __restrict__ part, SegScalars* sc,
+                                                          cudaGraphConditionalHandle hd, int set_cond) {
+    pdl_wait();
+    constexpr int W = (MODE == SEG_DOT) ? M + 1 : 1;
+    __shared__ int any;
+    if (threadIdx.x == 0) any = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int mine = 0;
+    for (int s = w; s < S; s += nw) {
+        double tot[W];
+#pragma unroll
+        for (int k = 0; k < W; k++) {
+            double x = 0.0;
+            for (int t = tbeg[s] + lane; t < tbeg[s + 1]; t += 32) x += part[(size_t)t * W + k];
+            tot[k] = warp_sum(x);
+        }
+        if (lane != 0) continue;
+        SegScalars& c = sc[s];
+        if constexpr (MODE == SEG_DOT) {
+            if (c.active) {
+                const int k = c.iter;
+                const int nprev = min(k - c.base, M);
+                c.s_old = c.s;
+                c.s = tot[0];
+#pragma unroll
+                for (int j = 1; j <= M; j++) {
+                    c.tj[j - 1] = tot[j];
+                    c.cj[j - 1] = (j <= nprev) ? tot[j] / c.pqh[(k - j + M * kFcgMax) % M] : 0.0;
+                }
+            }
+        } else if constexpr (MODE == SEG_PQ) {
+            if (c.active) {
+                c.pq = tot[0];
+                c.alpha = c.s / tot[0];
+            }
+        } else if constexpr (MODE == SEG_RR) {
+            c.rr = tot[0];
+            if (c.active) {
+                c.pqh[c.iter % M] = c.pq;
+                c.iter += 1;
+                const double rel = sqrt(c.rr) / c.r0;
+                if (!isfinite(rel)) {
+                    c.status = LINA_GPU_EBREAKDOWN;
+                    c.active = 0;
+                } else if (rel <= c.tol || c.iter >= c.maxit) {
+                    c.active = 0;
+                }
+            }
+            mine |= c.active;
+        } else if constexpr (MODE == SEG_NORM_B) {
+            c.r0 = sqrt(tot[0]);
+            c.rr = tot[0];
+            c.iter = 0;
+            c.base = 0;
+            c.status = 0;
+            c.s = 0.0;
+            c.active = (c.r0 > 0.0 && isfinite(c.r0) && c.maxit > 0) ? 1 : 0;
+            mine |= c.active;
+        } else {
+            c.tnorm2 = tot[0];
+        }
+    }
+    if constexpr (MODE == SEG_RR || MODE == SEG_NORM_B) {
+        if (mine) atomicOr(&any, 1);
+        __syncthreads();
+        if (threadIdx.x == 0 && set_cond) cudaGraphSetConditional(hd, any ? 1u : 0u);
+    }
+}
+
+// combined hierarchy: level l of system i is its level l - (D - d_i), or a copy of its coarsest level
+struct SegLevelMap {
+    std::vector<std::vector<int>> off;  // off[l][i]: first row of system i on combined level l (size S+1)
+};
+
+lina::Csr identity_csr(int n) {
+    lina::Csr I;
+    I.n = n;
+    I.ncols = n;
+    I.ptr.resize(n + 1);
+    I.col.resize(n);
+    I.val.assign(n, 1.0);
+    for (int i = 0; i <= n; i++) I.ptr[i] = i;
+    for (int i = 0; i < n; i++) I.col[i] = i;
+    return I;
+}
+
+// block-diagonal concatenation of parts (each with its row and column offsets)
+lina::Csr concat_csr(const std::vector<const lina::Csr*>& parts, const std::vector<int>& roff,
+                     const std::vector<int>& coff, int ncols) {
+    lina::Csr C;
+    long nnz = 0;
+    for (const lina::Csr* p : parts) nnz += p->nnz();
+    C.n = roff.back();
+    C.ncols = ncols;
+    C.ptr.assign(C.n + 1, 0);
+    C.col.resize(nnz);
+    C.val.resize(nnz);
+    long at = 0;
+    for (size_t i = 0; i < parts.size(); i++) {
+        const lina::Csr& P = *parts[i];
+        for (int r = 0; r < P.n; r++) C.ptr[roff[i] + r + 1] = (int)(at + P.ptr[r + 1]);
+        for (long k = 0; k < P.nnz(); k++) {
+            C.col[at + k] = P.col[k] + coff[i];
+            C.val[at + k] = P.val[k];
+        }
+        at += P.nnz();
+    }
+    return C;
+}
+
+int combine_hierarchies(const std::vector<lina_gpu_amg*>& sys, lina::HostHierarchy& C, SegLevelMap& map) {
+    const int S = (int)sys.size();
+    int D = 0;
+    for (auto* h : sys) D = std::max(D, h->depth);
+    auto lev = [&](int i, int l) { return l - (D - sys[i]->depth); };  // system i's own level (< 0: padded)
+    C.params = sys[0]->host.params;
+    C.params.depth = D;
+    C.lv.assign(D, lina::HostLevel());
+    map.off.assign(D, std::vector<int>(S + 1, 0));
+    for (int l = 0; l < D; l++)
+        for (int i = 0; i < S; i++) {
+            const int li = std::max(lev(i, l), 0);
+            map.off[l][i + 1] = map.off[l][i] + sys[i]->host.lv[li].A.n;
+        }
+    for (int l = 0; l < D; l++) {
+        std::vector<const lina::Csr*> parts(S);
+        for (int i = 0; i < S; i++) parts[i] = &sys[i]->host.lv[std::max(lev(i, l), 0)].A;
+        lina::HostLevel& L = C.lv[l];
+        L.A = concat_csr(parts, map.off[l], map.off[l], map.off[l][S]);
+        L.dof_level.assign(L.A.n, 0);
+        for (int i = 0; i < S; i++) {
+            const lina::HostLevel& Hi = sys[i]->host.lv[std::max(lev(i, l), 0)];
+            if ((int)Hi.dof_level.size() == Hi.A.n)
+                std::copy(Hi.dof_level.begin(), Hi.dof_level.end(), L.dof_level.begin() + map.off[l][i]);
+        }
+        if (l == 0) continue;
+        L.labels.assign(L.A.n, lina::kCoarse);
+        std::vector<lina::Csr> ids;
+        ids.reserve(S);
+        std::vector<const lina::Csr*> ps(S), rs(S);
+        for (int i = 0; i < S; i++) {
+            const int li = lev(i, l);
+            if (li >= 1) {
+                const lina::HostLevel& Hi = sys[i]->host.lv[li];
+                ps[i] = &Hi.P;
+                rs[i] = &Hi.R;
+                if ((int)Hi.labels.size() == Hi.A.n)
+                    std::copy(Hi.labels.begin(), Hi.labels.end(), L.labels.begin() + map.off[l][i]);
+            } else {
+                ids.push_back(identity_csr(sys[i]->host.lv[0].A.n));
+                ps[i] = rs[i] = &ids.back();
+            }
+        }
+        L.P = concat_csr(ps, map.off[l], map.off[l - 1], map.off[l - 1][S]);
+        L.R = concat_csr(rs, map.off[l - 1], map.off[l], map.off[l][S]);
+        L.coarse_size = map.off[l - 1][S];
+    }
+    // the coarsest level: each system's own dense block
+    lina::CoarseSolver& cs = C.coarse;
+    cs = lina::CoarseSolver();
+    cs.n = map.off[0][S];
+    cs.in_block.assign(cs.n, 0);
+    cs.diag_inv.assign(cs.n, 0.0);
+    cs.blocks.assign(1, 0);
+    cs.inv_offsets.assign(1, 0);
+    for (int i = 0; i < S; i++) {
+        const lina::CoarseSolver& ci = sys[i]->host.coarse;
+        const int o = map.off[0][i];
+        for (int r : ci.block_rows) cs.block_rows.push_back(r + o);
+        for (int r = 0; r < ci.n; r++) {
+            cs.in_block[o + r] = ci.in_block[r];
+            cs.diag_inv[o + r] = ci.diag_inv[r];
+        }
+        cs.inv.insert(cs.inv.end(), ci.inv.begin(), ci.inv.end());
+        cs.blocks.push_back((int)cs.block_rows.size());
+        cs.inv_offsets.push_back((long)cs.inv.size());
+        cs.block_inverted.push_back(ci.inverted ? 1 : 0);
+    }
+    cs.inverted = true;
+    return 0;
+}
+
+}  // namespace
+
+struct lina_gpu_segbatch {
+    std::vector<lina_gpu_amg*> sys;
+    lina_gpu_amg* comb = nullptr;   // the combined hierarchy (owned)
+    std::vector<int> off;           // finest rows of system i: [off[i], off[i+1])
+    int ntask = 0;
+    int4* task = nullptr;           // (system, first row, end row, 0)
+    int* tbeg = nullptr;            // tasks of system i: [tbeg[i], tbeg[i+1])
+    double* part = nullptr;         // ntask x (M + 1)
+    SegScalars* sc = nullptr;       // device, one per system
+    SegScalars* sc_host = nullptr;  // pinned
+    int m = 1;                      // FCG history
+    cudaGraphExec_t exec = nullptr;
+    long k_iter = 0;                // kernels per iteration
+    ~lina_gpu_segbatch() {
+        if (comb && comb->stream) cudaStreamSynchronize(comb->stream);
+        if (exec) cudaGraphExecDestroy(exec);
+        if (sc_host) cudaFreeHost(sc_host);
+        delete comb;  // frees task, tbeg, part, sc (allocated through it)
+    }
+};
+
+namespace {
+
+template <int M>
+void seg_issue_iteration(lina_gpu_segbatch* B, cudaGraphConditionalHandle hd, int set_cond) {
+    lina_gpu_amg* h = B->comb;
+    const long n = h->lv[h->depth - 1].n;
+    const int S = (int)B->sys.size();
+    const bool mixed = (h->opt.precision == LINA_PREC_MIXED);
+    const int gt = std::min(B->ntask, kGridCap);
+    cudaStream_t st = h->stream;
+    h->precondition(h->kr, h->kz, false);
+    if (mixed)
+        go(seg_fcg_dot_kernel<float, M>, gt, st, B->ntask, (const int4*)B->task, n, (const double*)h->kr,
+           (const float*)h->kz32, (const double*)h->kqh, (const SegScalars*)B->sc, B->part);
+    else
+        go(seg_fcg_dot_kernel<double, M>, gt, st, B->ntask, (const int4*)B->task, n, (const double*)h->kr,
+           (const double*)h->kz, (const double*)h->kqh, (const SegScalars*)B->sc, B->part);
+    launch(seg_finish_kernel<SEG_DOT, M>, dim3(1), dim3(1024), 0, st, S, (const int*)B->tbeg,
+           (const double*)B->part, B->sc, hd, 0);
+    if (mixed)
+        go(seg_fcg_update_p_kernel<float, M>, gt, st, B->ntask, (const int4*)B->task, n, (const float*)h->kz32,
+           (const double*)h->kph, h->kp, (const SegScalars*)B->sc);
+    else
+        go(seg_fcg_update_p_kernel<double, M>, gt, st, B->ntask, (const int4*)B->task, n, (const double*)h->kz,
+           (const double*)h->kph, h->kp, (const SegScalars*)B->sc);
+    h->csr<double, M_SPMV>(h->krylov_matrix(), h->kp, h->kq);
+    go(seg_dot_kernel, gt, st, B->ntask, (const int4*)B->task, (const double*)h->kp, (const double*)h->kq, B->part);
+    launch(seg_finish_kernel<SEG_PQ, M>, dim3(1), dim3(1024), 0, st, S, (const int*)B->tbeg, (const double*)B->part,
+           B->sc, hd, 0);
+    go(seg_update_xr_kernel<M>, gt, st, B->ntask, (const int4*)B->task, n, h->kx, h->kr, (const double*)h->kp,
+       (const double*)h->kq, h->kph, h->kqh, (const SegScalars*)B->sc, B->part);
+    launch(seg_finish_kernel<SEG_RR, M>, dim3(1), dim3(1024), 0, st, S, (const int*)B->tbeg, (const double*)B->part,
+           B->sc, hd, set_cond);
+}
+
+void seg_issue(lina_gpu_segbatch* B, cudaGraphConditionalHandle hd, int set_cond) {
+    switch (B->m) {
+        case 1: seg_issue_iteration<1>(B, hd, set_cond); break;
+        case 2: seg_issue_iteration<2>(B, hd, set_cond); break;
+        case 3: seg_issue_iteration<3>(B, hd, set_cond); break;
+        case 4: seg_issue_iteration<4>(B, hd, set_cond); break;
+        case 5: seg_issue_iteration<5>(B, hd, set_cond); break;
+        case 6: seg_issue_iteration<6>(B, hd, set_cond); break;
+        case 7: seg_issue_iteration<7>(B, hd, set_cond); break;
+        default: seg_issue_iteration<8>(B, hd, set_cond); break;
+    }
+}
+
+int seg_build_graph(lina_gpu_segbatch* B) {
+    lina_gpu_amg* h = B->comb;
+    cudaGraph_t g = nullptr;
+    CK(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle hd;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&hd, g, 1, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams cp = {};
+    cudaGraphNode_t node;
+    if (e == cudaSuccess) {
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = hd;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp);
+    }
+    if (e == cudaSuccess)
+        e = cudaStreamBeginCaptureToGraph(h->stream, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        set_err("segmented batch graph: %s", cudaGetErrorString(e));
+        return LINA_GPU_ECUDA;
+    }
+    const unsigned long long before = g_launches;
+    seg_issue(B, hd, 1);
+    B->k_iter = (long)(g_launches - before);
+    g_launches = before;
+    cudaGraph_t body = nullptr;
+    e = cudaStreamEndCapture(h->stream, &body);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&B->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        B->exec = nullptr;
+        set_err("segmented batch graph: %s", cudaGetErrorString(e));
+        return LINA_GPU_ECUDA;
+    }
+    return 0;
+}
+
+// the per-system norms of v (SEG_NORM_B: ||b|| and the start of the loop; SEG_NORM_T: ||b - A x||^2)
+template <int MODE>
+void seg_norms(lina_gpu_segbatch* B, const double* v) {
+    lina_gpu_amg* h = B->comb;
+    const int gt = std::min(B->ntask, kGridCap);
+    go(seg_dot_kernel, gt, h->stream, B->ntask, (const int4*)B->task, v, v, B->part);
+    launch(seg_finish_kernel<MODE, 1>, dim3(1), dim3(1024), 0, h->stream, (int)B->sys.size(), (const int*)B->tbeg,
+           (const double*)B->part, B->sc, (cudaGraphConditionalHandle)0, 0);
+}
+
+}  // namespace
+
+extern "C" {
+
+int lina_gpu_segbatch_create(int count, lina_gpu_amg* const* systems, lina_gpu_segbatch** out) {
+    if (count < 1 || !systems || !out) {
+        set_err("lina_gpu_segbatch_create: invalid argument");
+        return LINA_GPU_EINVAL;
+    }
+    *out = nullptr;
+    const lina_gpu_amg* s0 = systems[0];
+    for (int i = 0; i < count; i++) {
+        const lina_gpu_amg* h = systems[i];
+        if (!h || h->host_only || h->has_signs || h->depth < 1 || h->opt.smoother != s0->opt.smoother ||
+            h->opt.omega != s0->opt.omega || h->opt.precision != s0->opt.precision ||
+            h->opt.smoothing_iterations != s0->opt.smoothing_iterations ||
+            (h->opt.coarsening == LINA_AGGRESSIVE) != (s0->opt.coarsening == LINA_AGGRESSIVE) ||
+            h->opt.aggr_smoothing_iterations != s0->opt.aggr_smoothing_iterations) {
+            set_err("lina_gpu_segbatch_create: system %d is not a device hierarchy with the first system's smoother, "
+                    "precision and sweeps (or its rows were sign-flipped)", i);
+            return LINA_GPU_EINVAL;
+        }
+    }
+    lina_gpu_segbatch* B = new lina_gpu_segbatch();
+    B->sys.assign(systems, systems + count);
+    lina_gpu_amg* c = new lina_gpu_amg();
+    B->comb = c;
+    SegLevelMap map;
+    combine_hierarchies(B->sys, c->host, map);
+    c->opt = s0->opt;
+    c->depth = (int)c->host.lv.size();
+    c->opt.depth = c->depth;
+    c->seg_max_rows.assign(c->depth, 0);
+    for (int l = 0; l < c->depth; l++)
+        for (int i = 0; i < count; i++)
+            c->seg_max_rows[l] = std::max<long>(c->seg_max_rows[l], map.off[l][i + 1] - map.off[l][i]);
+    c->fcg_m = s0->fcg_m;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete B;
+        set_err("cudaStreamCreate failed");
+        return LINA_GPU_ECUDA;
+    }
+    int rc = upload_hierarchy(c);
+    if (!rc) {
+        B->m = std::max(c->history(), 1);
+        if (B->m >= 2) rc = c->ensure_history();
+        if (!rc && B->m == 1) {  // a ring of one slot for the two-term recurrence
+            const size_t n = (size_t)c->lv[c->depth - 1].n;
+            if (!(rc = c->alloc(&c->kph, n))) rc = c->alloc(&c->kqh, n);
+        }
+    }
+    if (rc) {
+        delete B;
+        return rc;
+    }
+    B->off = map.off[c->depth - 1];
+    std::vector<int4> tasks;
+    std::vector<int> tbeg(count + 1, 0);
+    for (int i = 0; i < count; i++) {
+        for (int r = B->off[i]; r < B->off[i + 1]; r += kSegChunk)
+            tasks.push_back(make_int4(i, r, std::min(r + kSegChunk, B->off[i + 1]), 0));
+        tbeg[i + 1] = (int)tasks.size();
+    }
+    B->ntask = (int)tasks.size();
+    if ((rc = c->upload(&B->task, tasks.data(), tasks.size())) || (rc = c->upload(&B->tbeg, tbeg.data(), tbeg.size())) ||
+        (rc = c->alloc(&B->part, (size_t)B->ntask * (kFcgMax + 1))) || (rc = c->alloc(&B->sc, count))) {
+        delete B;
+        return rc;
+    }
+    if (cudaMallocHost((void**)&B->sc_host, count * sizeof(SegScalars)) != cudaSuccess) {
+        delete B;
+        set_err("cudaMallocHost failed");
+        return LINA_GPU_ECUDA;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    if ((rc = seg_build_graph(B))) {
+        delete B;
+        return rc;
+    }
+    *out = B;
+    return 0;
+}
+
+int lina_gpu_segbatch_solve(lina_gpu_segbatch* B, const double* const* b, double* const* x, double tol, int max_iter,
+                            int flags, lina_gpu_solve_info* infos) {
+    if (!B || !b || !x || max_iter < 1 || !(tol > 0.0)) {
+        set_err("lina_gpu_segbatch_solve: invalid argument");
+        return LINA_GPU_EINVAL;
+    }
+    const int S = (int)B->sys.size();
+    for (int i = 0; i < S; i++)
+        if (!b[i] || !x[i]) {
+            set_err("lina_gpu_segbatch_solve: missing vector of system %d", i);
+            return LINA_GPU_EINVAL;
+        }
+    lina_gpu_amg* h = B->comb;
+    cudaStream_t st = h->stream;
+    const bool dev = (flags & LINA_PCG_DEVICE_PTRS) != 0;
+    const long n = h->lv[h->depth - 1].n;
+    for (int i = 0; i < S; i++)
+        CK(cudaMemcpyAsync(h->kb + B->off[i], b[i], (size_t)(B->off[i + 1] - B->off[i]) * sizeof(double),
+                           dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+    // x = 0, r = b, per-system ||b||, tolerance and limit
+    CK(cudaMemsetAsync(h->kx, 0, n * sizeof(double), st));
+    CK(cudaMemcpyAsync(h->kr, h->kb, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemsetAsync(B->sc, 0, S * sizeof(SegScalars), st));
+    for (int i = 0; i < S; i++) {
+        B->sc_host[i] = SegScalars{};
+        B->sc_host[i].tol = tol;
+        B->sc_host[i].maxit = max_iter;
+    }
+    CK(cudaMemcpyAsync(B->sc, B->sc_host, S * sizeof(SegScalars), cudaMemcpyHostToDevice, st));
+    seg_norms<SEG_NORM_B>(B, h->kb);
+    std::vector<int> restarts(S, 0);
+    int rounds = 0;
+    const bool host_loop = (flags & LINA_PCG_HOST_LOOP) != 0;
+    for (;;) {
+        if (host_loop) {  // iteration by iteration from the host (kernels visible to a profiler)
+            for (int it = 0; it < max_iter; it++) {
+                seg_issue(B, (cudaGraphConditionalHandle)0, 0);
+                CK(cudaMemcpyAsync(B->sc_host, B->sc, S * sizeof(SegScalars), cudaMemcpyDeviceToHost, st));
+                CK(cudaStreamSynchronize(st));
+                bool any = false;
+                for (int i = 0; i < S; i++) any = any || B->sc_host[i].active;
+                if (!any) break;
+            }
+        } else {
+            CK(cudaGraphLaunch(B->exec, st));
+        }
+        // the true residual of every system
+        h->csr<double, M_RESID>(h->krylov_matrix(), h->kx, h->kt, h->kb);
+        seg_norms<SEG_NORM_T>(B, h->kt);
+        CK(cudaMemcpyAsync(B->sc_host, B->sc, S * sizeof(SegScalars), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        long its = 0;
+        for (int i = 0; i < S; i++) its = std::max<long>(its, B->sc_host[i].iter - B->sc_host[i].base);
+        g_launches += (unsigned long long)(its * B->k_iter + 3);
+        // systems whose recursive residual met the rule but whose true residual does not: restart
+        // from the true residual (a new recurrence; FCG history cleared) while iterations remain
+        bool again = false;
+        for (int i = 0; i < S; i++) {
+            SegScalars& c = B->sc_host[i];
+            const double trel = c.r0 > 0.0 ? std::sqrt(c.tnorm2) / c.r0 : 0.0;
+            if (c.status == 0 && c.r0 > 0.0 && trel > tol && c.iter < max_iter && rounds < 8) {
+                CK(cudaMemcpyAsync(h->kr + B->off[i], h->kt + B->off[i],
+                                   (size_t)(B->off[i + 1] - B->off[i]) * sizeof(double), cudaMemcpyDeviceToDevice,
+                                   st));
+                c.active = 1;
+                c.base = c.iter;
+                restarts[i]++;
+                again = true;
+            }
+        }
+        if (!again) break;
+        rounds++;
+        CK(cudaMemcpyAsync(B->sc, B->sc_host, S * sizeof(SegScalars), cudaMemcpyHostToDevice, st));
+    }
+    for (int i = 0; i < S; i++)
+        CK(cudaMemcpyAsync(x[i], h->kx + B->off[i], (size_t)(B->off[i + 1] - B->off[i]) * sizeof(double),
+                           dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    int rc = 0;
+    for (int i = 0; i < S; i++) {
+        const SegScalars& c = B->sc_host[i];
+        lina_gpu_solve_info inf{};
+        inf.iterations = c.iter;
+        inf.rel_residual = c.r0 > 0.0 ? std::sqrt(c.rr) / c.r0 : 0.0;
+        inf.true_rel_residual = c.r0 > 0.0 ? std::sqrt(c.tnorm2) / c.r0 : 0.0;
+        inf.status = c.status;
+        if (!inf.status && inf.true_rel_residual > tol) inf.status = LINA_GPU_ENOCONV;
+        inf.restarts = restarts[i];
+        if (infos) infos[i] = inf;
+        if (inf.status && !rc) rc = inf.status == LINA_GPU_ENOCONV ? LINA_GPU_ENOCONV : inf.status;
+    }
+    return rc;
+}
+
+int lina_gpu_segbatch_levels(const lina_gpu_segbatch* B, int* depth, long* rows, long* entries) {
+    if (!B || !depth) return LINA_GPU_EINVAL;
+    *depth = B->comb->depth;
+    for (int l = 0; l < B->comb->depth; l++) {
+        if (rows) rows[l] = B->comb->lv[l].n;
+        if (entries) entries[l] = B->comb->lv[l].A.nnz;
+    }
+    return 0;
+}
+
+int lina_gpu_segbatch_hierarchy(lina_gpu_segbatch* B, lina_gpu_amg** out) {
+    if (!B || !out) return LINA_GPU_EINVAL;
+    *out = B->comb;
+    return 0;
+}
+
+int lina_gpu_segbatch_destroy(lina_gpu_segbatch* B) {
     delete B;
     return 0;
 }

@@ -114,6 +114,12 @@ def lib():
                                            C.POINTER(SolveInfo)]),
         "lina_gpu_batch_size": (C.c_int, [vp]),
         "lina_gpu_batch_destroy": (C.c_int, [vp]),
+        "lina_gpu_segbatch_create": (C.c_int, [C.c_int, C.POINTER(vp), C.POINTER(vp)]),
+        "lina_gpu_segbatch_solve": (C.c_int, [vp, C.POINTER(vp), C.POINTER(vp), C.c_double, C.c_int, C.c_int,
+                                              C.POINTER(SolveInfo)]),
+        "lina_gpu_segbatch_levels": (C.c_int, [vp, ip, C.POINTER(C.c_long), C.POINTER(C.c_long)]),
+        "lina_gpu_segbatch_hierarchy": (C.c_int, [vp, C.POINTER(vp)]),
+        "lina_gpu_segbatch_destroy": (C.c_int, [vp]),
         "lina_gpu_vcycle": (C.c_int, [vp, vp, vp]),
         "lina_gpu_spmv": (C.c_int, [vp, C.c_int, vp, vp]),
         "lina_gpu_amg_depth": (C.c_int, [vp]),
@@ -627,6 +633,67 @@ class Batch:
             pass
 
 
+class SegmentedBatch(Batch):
+    """Independent systems solved as one segmented system (lina_gpu_segbatch_*): block-diagonal combined
+    hierarchy, per-system FCG scalars and stopping, one graph launch."""
+
+    def __init__(self, systems):
+        self.systems = list(systems)
+        self.sizes = [a.n for a in self.systems]
+        arr = (C.c_void_p * len(self.systems))(*[a.h.value if isinstance(a.h, C.c_void_p) else a.h
+                                                  for a in self.systems])
+        h = C.c_void_p()
+        self.h = None
+        _check(lib().lina_gpu_segbatch_create(len(self.systems), arr, C.byref(h)), "segmented batch create")
+        self.h = h
+
+    def solve(self, bs, tol=1e-8, max_iter=1000, device=False, host_loop=False):
+        """bs: host arrays (or DeviceArray with device=True); returns (xs, [SolveInfo]).  host_loop: the
+        iterations launched from the host (for profiling)."""
+        k = len(self.systems)
+        if device:
+            xs = [DeviceArray(n) for n in self.sizes]
+            bp = (C.c_void_p * k)(*[b.ptr for b in bs])
+            xp = (C.c_void_p * k)(*[x.ptr for x in xs])
+        else:
+            bb = [np.ascontiguousarray(b, dtype=np.float64) for b in bs]
+            xs = [np.zeros(n) for n in self.sizes]
+            bp = (C.c_void_p * k)(*[b.ctypes.data for b in bb])
+            xp = (C.c_void_p * k)(*[x.ctypes.data for x in xs])
+        infos = (SolveInfo * k)()
+        rc = lib().lina_gpu_segbatch_solve(self.h, bp, xp, tol, max_iter,
+                                           (PCG_DEVICE_PTRS if device else 0) | (PCG_HOST_LOOP if host_loop else 0),
+                                           infos)
+        if rc not in (0, ENOCONV):
+            raise LinaError(f"segmented batch solve failed ({rc}): {last_error()}")
+        return xs, list(infos)
+
+    def hierarchy(self):
+        """The combined hierarchy as an AMG object that does not own it (valid while the batch lives)."""
+        h = C.c_void_p()
+        _check(lib().lina_gpu_segbatch_hierarchy(self.h, C.byref(h)), "segmented batch hierarchy")
+        a = AMG.__new__(AMG)
+        a.h = h
+        a.borrowed = True
+        a.depth = lib().lina_gpu_amg_depth(h)
+        a.n = a.level_size(a.depth - 1)
+        return a
+
+    def levels(self):
+        """(rows, entries) per level of the combined hierarchy, coarsest first."""
+        d = C.c_int()
+        _check(lib().lina_gpu_segbatch_levels(self.h, C.byref(d), None, None), "segmented batch levels")
+        rows = (C.c_long * d.value)()
+        ent = (C.c_long * d.value)()
+        _check(lib().lina_gpu_segbatch_levels(self.h, C.byref(d), rows, ent), "segmented batch levels")
+        return list(rows), list(ent)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().lina_gpu_segbatch_destroy(self.h)
+            self.h = None
+
+
 def gmres(M: "Matrix", b, ilu: "ILU | None" = None, amg: "AMG | None" = None, precon_precision=PREC_FP64, tol=1e-8,
           i_max=30, max_iter=1000, check_each=False, y0=None, apply_precon=False):
     """Restarted GMRES on the GPU with a right preconditioner; returns (y, SolveInfo), y the
@@ -810,7 +877,7 @@ class AMG:
         return lib().lina_gpu_coarse_block_size(self.h)
 
     def close(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and not getattr(self, "borrowed", False):
             lib().lina_gpu_amg_destroy(self.h)
             self.h = None
 

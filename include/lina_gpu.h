@@ -151,6 +151,29 @@ int lina_gpu_batch_solve(lina_gpu_batch* batch, const double* const* b, double* 
                          int max_iter, int flags, lina_gpu_solve_info* infos);
 int lina_gpu_batch_size(const lina_gpu_batch* batch);
 int lina_gpu_batch_destroy(lina_gpu_batch* batch);
+/* Segmented batch: the same independent systems solved as one.  Every level of one combined hierarchy
+   is the block-diagonal concatenation of the systems' levels (a shallower system padded below its
+   coarsest level with copies of it), the coarsest level is solved with each system's own dense
+   inverse, and the Krylov loop is FCG(m) per system with segmented reductions (each system its own
+   scalars and stopping test, ||b_i - A_i x_i|| <= tol ||b_i||, confirmed on the true residual with
+   restarts): each kernel streams all systems' rows in one launch, and one graph launch runs until every
+   system has stopped.  The systems must be device hierarchies with one smoother, precision and sweep
+   count and no sign-flipped rows; the batch copies them at creation (later changes to a system do not
+   reach it).  Solutions start from zero. */
+typedef struct lina_gpu_segbatch lina_gpu_segbatch;
+int lina_gpu_segbatch_create(int count, lina_gpu_amg* const* systems, lina_gpu_segbatch** out);
+/* b[i], x[i] as for lina_gpu_batch_solve; infos may be NULL; flags: LINA_PCG_DEVICE_PTRS, and
+   LINA_PCG_HOST_LOOP to launch the iterations from the host instead of the graph.  Returns 0,
+   LINA_GPU_ENOCONV when a system did not converge, or another error. */
+int lina_gpu_segbatch_solve(lina_gpu_segbatch* batch, const double* const* b, double* const* x, double tol,
+                            int max_iter, int flags, lina_gpu_solve_info* infos);
+/* the combined hierarchy: depth, and per level (0 = coarsest) rows and stored entries (arrays of depth) */
+int lina_gpu_segbatch_levels(const lina_gpu_segbatch* batch, int* depth, long* rows, long* entries);
+/* the combined hierarchy itself (owned by the batch; valid until lina_gpu_segbatch_destroy): a hierarchy
+   of the block-diagonal system, usable with lina_gpu_pcg (one global recurrence over all systems), for
+   example to time its kernels */
+int lina_gpu_segbatch_hierarchy(lina_gpu_segbatch* batch, lina_gpu_amg** out);
+int lina_gpu_segbatch_destroy(lina_gpu_segbatch* batch);
 /* AMG_solve (LinA/Multigrid.c:1863): V-cycles from the initial guess X until ||F - A X|| / ||F - A X0||
    <= eps or max_iter cycles; flags may hold LINA_PCG_DEVICE_PTRS.  Returns the cycles done and the
    final relative residual. */
