@@ -351,7 +351,13 @@ def run_gb300(args, rank, world, local):
                               "err_vs_ref_tight": float(np.linalg.norm(xr[idx] - xt) / np.linalg.norm(xt))}
         amg.set_smoother(smoother, omega, lina.PREC_MIXED)
         it_ref = int(g["pcg_jacobi_it"])
-        parity = {"reference_iterations": it_ref, "reference_rule": ref_rule,
+        # the device hierarchy (set-up with Galerkin products on the GPU) against the reference's,
+        # SHA-256 of every level's labels, A, P and R
+        from tests.golden import digest as D
+        got = D.level_digest(amg.level, depth)
+        mism = sorted(k for k, v in got.items() if v != str(g[f"sha_{k}"]))
+        parity = {"hierarchy_sha256_equal_reference": not mism, "hierarchy_mismatches": mism[:5],
+                  "reference_iterations": it_ref, "reference_rule": ref_rule,
                   "mixed_iterations_vs_reference": ref_rule["mixed"]["iterations"] / it_ref,
                   "err_vs_ref_tight": float(np.linalg.norm(x_mixed[idx] - xt) / np.linalg.norm(xt)),
                   "reference_sor_iterations": int(g["pcg_refsor_it"]) if "pcg_refsor_it" in g else None}
