@@ -43,6 +43,12 @@ int g_layout = 0;  // 0 automatic, 1 SELL-32, 2 lane groups (size chosen per mat
 // steps win; at 49,152 the levels whose colours need several passes of the cluster's lane groups
 // made whole solves up to 30 % slower.
 int g_fused_rows = 24576;
+// damped Jacobi: levels of at most this many stored entries (and g_fused_rows rows) run a V-cycle step as
+// one cluster launch; off by default.  Measured on the 2.1M-dof elasticity hierarchy (GB300, mixed, 30
+// iterations): 1,199 us per iteration unfused, 1,215 us fusing level 1 (13k entries), 1,231 us levels 1-2,
+// 1,283 us levels 1-3: the separate launches overlap one another (programmatic dependent launch), a
+// cluster launch waits for its predecessor to drain and for 16 free SMs.
+long g_fused_jacobi_entries = 0;
 // 16: SELL-32 matrices with long rows uploaded afterwards also get 16-bit column offsets (two bases
 // per slice, where every slice's columns fit), read by FP32 passes; 32: int columns only
 int g_sell_bits = 16;
@@ -1161,8 +1167,29 @@ __device__ __forceinline__ void fused_sweeps(const FusedStep& st, TX* xs, const 
     }
 }
 
-// dynamic shared memory of a block: a copy of x (n entries)
-template <typename TX, bool PRE>
+// nu damped-Jacobi sweeps y = x + w dinv (b - A x): each row's sum over the natural-order lane groups
+// (the order of csrv_kernel), read from the block's copy cur and stored into every block's copy nxt; a
+// cluster barrier after each sweep.  Returns the copy holding the result.
+template <typename TX>
+__device__ __forceinline__ TX* fused_jacobi_sweeps(const FusedStep& st, int nu, TX* cur, TX* nxt,
+                                                   const TX* __restrict__ b, const TX* __restrict__ dinv) {
+    const TX w = TX(st.w);
+    const cg::cluster_group cl = cg::this_cluster();
+    for (int k = 0; k < nu; k++) {
+        fused_rows<TX>(0, st.n, st.aS, st.aptr, st.acol, (const TX*)st.aval, LocalRead<TX>{cur},
+                       [&](int i, TX sum, int sub) {
+                           broadcast_x(nxt, i, cur[i] + w * __ldg(dinv + i) * (__ldg(b + i) - sum), sub, st.aS);
+                       });
+        cl.sync();
+        TX* t = cur;
+        cur = nxt;
+        nxt = t;
+    }
+    return cur;
+}
+
+// dynamic shared memory of a block: a copy of x (n entries), two for damped Jacobi (JAC)
+template <typename TX, bool PRE, bool JAC>
 __global__ void __launch_bounds__(kFuseThreads, 1) fused_step_kernel(const FusedStep st) {
     pdl_wait();
     extern __shared__ __align__(16) unsigned char fused_smem[];
@@ -1171,6 +1198,41 @@ __global__ void __launch_bounds__(kFuseThreads, 1) fused_step_kernel(const Fused
     TX* xg = (TX*)st.x;
     const TX* b = (const TX*)st.b;
     const TX* dinv = (const TX*)st.dinv;
+    if constexpr (JAC) {
+        // Jacobi: the first pre-sweep from the zero guess needs no product (x = w dinv b, as
+        // jacobi_first_kernel), so every block forms all of it in its own copy
+        TX* other = xs + st.n;
+        const TX w = TX(st.w);
+        for (int j = (int)threadIdx.x; j < st.n; j += blockDim.x)
+            xs[j] = PRE ? (st.nu > 0 ? w * __ldg(dinv + j) * __ldg(b + j) : TX(0)) : __ldcg(xg + j);
+        cl.sync();  // every block runs before any remote store
+        TX* res;
+        if (PRE) {
+            res = fused_jacobi_sweeps<TX>(st, st.nu > 0 ? st.nu - 1 : 0, xs, other, b, dinv);
+            TX* r = (TX*)st.r;
+            fused_rows<TX>(0, st.n, st.aS, st.aptr, st.acol, (const TX*)st.aval, LocalRead<TX>{res},
+                           [&](int i, TX sum, int sub) {
+                               if (sub == 0) r[i] = b[i] - sum;
+                           });
+            cl.sync();
+            TX* cb = (TX*)st.cb;
+            fused_rows<TX>(0, st.nc, st.rS, st.rptr, st.rcol, (const TX*)st.rval, GlobalRead<TX>{r},
+                           [&](int i, TX sum, int sub) {
+                               if (sub == 0) cb[i] = sum;
+                           });
+        } else {
+            fused_rows<TX>(0, st.n, st.pS, st.pptr, st.pcol, (const TX*)st.pval, GlobalRead<TX>{(const TX*)st.e},
+                           [&](int i, TX sum, int sub) { broadcast_x(xs, i, xs[i] + sum, sub, st.pS); });
+            cl.sync();
+            res = fused_jacobi_sweeps<TX>(st, st.nu, xs, other, b, dinv);
+        }
+        // the last sweep (or the start) ended with a cluster barrier: every copy of res is final
+        const int chunk = (st.n + (int)cl.num_blocks() - 1) / (int)cl.num_blocks();
+        const int lo = (int)cl.block_rank() * chunk, hi = min(st.n, lo + chunk);
+        for (int j = lo + (int)threadIdx.x; j < hi; j += blockDim.x) xg[j] = res[j];
+        cl.sync();  // no block leaves while another may still store into its shared memory
+        return;
+    }
     for (int j = (int)threadIdx.x; j < st.n; j += blockDim.x) xs[j] = PRE ? TX(0) : __ldcg(xg + j);
     cl.sync();
     if (PRE) {
@@ -2006,6 +2068,10 @@ struct lina_gpu_amg {
     // block's shared memory)
     bool fusable(const DLevel& L, bool timed) const {
         const long copy_bytes = (long)L.n * (opt.precision == LINA_PREC_MIXED ? 4 : 8);
+        if (opt.smoother == LINA_SMOOTHER_JACOBI)  // two copies of x (the sweeps alternate)
+            return g_fused_rows > 0 && g_fused_jacobi_entries > 0 && !timed && L.n <= g_fused_rows &&
+                   L.A.nnz <= g_fused_jacobi_entries && 2 * copy_bytes <= kFusedSmemMax && L.A.lanes > 0 &&
+                   L.R.lanes > 0 && L.P.lanes > 0;
         return g_fused_rows > 0 && opt.smoother == LINA_SMOOTHER_MC_SOR && !timed && L.n <= g_fused_rows &&
                copy_bytes <= kFusedSmemMax &&
                L.ncolours > 0 && L.Acol.lanes > 0 && L.Acol.d_group_row && L.Acol.d_head && L.A.lanes > 0 &&
@@ -2014,6 +2080,14 @@ struct lina_gpu_amg {
 
     template <typename TX, bool PRE>
     void launch_fused(DLevel& L, DLevel& C, int nu, const TX* b, TX* x, const TX* e) {
+        if (opt.smoother == LINA_SMOOTHER_JACOBI)
+            launch_fused_as<TX, PRE, true>(L, C, nu, b, x, e);
+        else
+            launch_fused_as<TX, PRE, false>(L, C, nu, b, x, e);
+    }
+
+    template <typename TX, bool PRE, bool JAC>
+    void launch_fused_as(DLevel& L, DLevel& C, int nu, const TX* b, TX* x, const TX* e) {
         FusedStep st;
         st.n = L.n;
         st.nc = C.n;
@@ -2052,11 +2126,11 @@ struct lina_gpu_amg {
         st.r = lvx<TX>(L, 3);
         st.cb = lvx<TX>(C, 2);
         st.w = opt.omega;
-        const int K = fused_cluster_size<TX, PRE>();
+        const int K = fused_cluster_size<TX, PRE, JAC>();
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(K);
         cfg.blockDim = dim3(kFuseThreads);
-        cfg.dynamicSmemBytes = (size_t)L.n * sizeof(TX);
+        cfg.dynamicSmemBytes = (size_t)(JAC ? 2 : 1) * L.n * sizeof(TX);
         cfg.stream = stream;
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -2066,23 +2140,23 @@ struct lina_gpu_amg {
         cfg.attrs = attr;
         cfg.numAttrs = 1;
         g_launches++;
-        cudaLaunchKernelEx(&cfg, fused_step_kernel<TX, PRE>, st);
+        cudaLaunchKernelEx(&cfg, fused_step_kernel<TX, PRE, JAC>, st);
     }
 
     // 16 blocks per cluster where the GPU schedules such clusters, else (or with LINA_FUSED_CLUSTER=8)
     // the portable 8.  Measured on the batch workload's 24-system sample: 16 blocks 3 % faster in total
     // (the large elasticity systems gain, the 10k-row ones lose 2 %).
-    template <typename TX, bool PRE>
+    template <typename TX, bool PRE, bool JAC>
     static int fused_cluster_size() {
         static int k = 0;
         if (k == 0) {
             k = 8;
             const char* env = getenv("LINA_FUSED_CLUSTER");
             const bool want16 = !(env && atoi(env) == 8);
-            cudaFuncSetAttribute(fused_step_kernel<TX, PRE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            cudaFuncSetAttribute(fused_step_kernel<TX, PRE, JAC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  kFusedSmemMax);
             if (want16 &&
-                cudaFuncSetAttribute(fused_step_kernel<TX, PRE>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+                cudaFuncSetAttribute(fused_step_kernel<TX, PRE, JAC>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
                     cudaSuccess) {
                 cudaLaunchConfig_t cfg = {};
                 cfg.gridDim = dim3(16);
@@ -2096,7 +2170,7 @@ struct lina_gpu_amg {
                 cfg.attrs = attr;
                 cfg.numAttrs = 1;
                 int nclusters = 0;
-                if (cudaOccupancyMaxActiveClusters(&nclusters, fused_step_kernel<TX, PRE>, &cfg) == cudaSuccess &&
+                if (cudaOccupancyMaxActiveClusters(&nclusters, fused_step_kernel<TX, PRE, JAC>, &cfg) == cudaSuccess &&
                     nclusters > 0)
                     k = 16;
             }
@@ -2526,6 +2600,15 @@ int lina_gpu_set_fused_rows(int max_rows) {
         return LINA_GPU_EINVAL;
     }
     g_fused_rows = max_rows;
+    return 0;
+}
+
+int lina_gpu_set_fused_jacobi_entries(long max_entries) {
+    if (max_entries < 0) {
+        set_err("lina_gpu_set_fused_jacobi_entries: max_entries must be >= 0");
+        return LINA_GPU_EINVAL;
+    }
+    g_fused_jacobi_entries = max_entries;
     return 0;
 }
 

@@ -137,6 +137,7 @@ def lib():
         "lina_gpu_set_device": (C.c_int, [C.c_int]),
         "lina_gpu_set_layout": (C.c_int, [C.c_int]),
         "lina_gpu_set_fused_rows": (C.c_int, [C.c_int]),
+        "lina_gpu_set_fused_jacobi_entries": (C.c_int, [C.c_long]),
         "lina_gpu_set_sell_index_bits": (C.c_int, [C.c_int]),
         "lina_gpu_set_sell_quads": (C.c_int, [C.c_int]),
         "lina_gpu_set_pdl": (C.c_int, [C.c_int]),
@@ -296,12 +297,19 @@ def set_layout(layout: int):
 
 
 FUSED_ROWS_DEFAULT = 24576
+FUSED_JACOBI_ENTRIES_DEFAULT = 0
 
 
 def set_fused_rows(max_rows: int):
     """Levels of at most max_rows rows run a multicolour-SOR V-cycle step as one cluster launch
     (0: one launch per colour)."""
     _check(lib().lina_gpu_set_fused_rows(int(max_rows)), "set fused rows")
+
+
+def set_fused_jacobi_entries(max_entries: int):
+    """Damped Jacobi: levels of at most max_entries stored entries run a V-cycle step as one cluster
+    launch (0: never)."""
+    _check(lib().lina_gpu_set_fused_jacobi_entries(int(max_entries)), "set fused Jacobi entries")
 
 
 def set_sell_index_bits(bits: int):

@@ -432,6 +432,10 @@ int lina_gpu_set_layout(int layout);
    launch per colour and step; the results are bit-identical.  0 turns this off.  Takes effect for
    solves issued afterwards (a hierarchy's captured solve graph keeps the choice it was captured with). */
 int lina_gpu_set_fused_rows(int max_rows);
+/* damped Jacobi: levels of at most max_entries stored entries (and the rows above) run each V-cycle step
+   as one cluster launch, two copies of x in shared memory (default 0 = never: measured slower than the
+   separate launches on GB300); the results are those of the separate launches, bit for bit */
+int lina_gpu_set_fused_jacobi_entries(long max_entries);
 /* 16 (default): SELL-32 matrices with long rows (at least 24 stored entries per row on average)
    uploaded afterwards also get 16-bit column indices, a 15-bit offset from one of two bases per
    slice of 32 rows, where every slice's columns fit two such windows; FP32 passes read those (2

@@ -1,4 +1,5 @@
-"""Cluster-fused multicolour-SOR V-cycle steps (lina_gpu_set_fused_rows).
+"""Cluster-fused V-cycle steps: multicolour SOR (lina_gpu_set_fused_rows) and damped Jacobi
+(lina_gpu_set_fused_jacobi_entries).
 
 The fused launch computes every row as the per-colour launches do, so V-cycles, FMG passes and
 whole PCG solves must agree bit for bit with the fusion on and off; the reference parity of the
@@ -81,3 +82,53 @@ def test_pcg_identical(case, precision):
 def test_fused_rows_validation():
     with pytest.raises(lina.LinaError):
         lina.set_fused_rows(-1)
+
+
+# ---------------------------------------------------------------- damped Jacobi (two copies of x)
+def build_jacobi(s, depth, coarsening, precision, entries):
+    lina.set_fused_jacobi_entries(entries)
+    try:
+        return lina.AMG.from_system(s, depth=depth, coarsening=coarsening, smoother=lina.SMOOTHER_JACOBI,
+                                    omega=0.6, precision=precision)
+    finally:
+        lina.set_fused_jacobi_entries(lina.FUSED_JACOBI_ENTRIES_DEFAULT)
+
+
+def _with_entries(entries, f):
+    lina.set_fused_jacobi_entries(entries)
+    try:
+        return f()
+    finally:
+        lina.set_fused_jacobi_entries(lina.FUSED_JACOBI_ENTRIES_DEFAULT)
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+@pytest.mark.parametrize("precision", [lina.PREC_FP64, lina.PREC_MIXED])
+def test_jacobi_vcycle_and_pcg_identical(case, precision):
+    """Every level of these hierarchies fits the fused step (entries cap raised): V-cycles and whole
+    solves with the fused damped-Jacobi steps equal the separate launches bit for bit."""
+    name, s, depth, coarsening = case
+    big = 1 << 40
+    on = build_jacobi(s, depth, coarsening, precision, big)
+    off = build_jacobi(s, depth, coarsening, precision, 0)
+    r = np.random.default_rng(2).uniform(-1, 1, s.n)
+    z_on = _with_entries(big, lambda: on.vcycle(r))
+    z_off = _with_entries(0, lambda: off.vcycle(r))
+    assert np.array_equal(z_on, z_off)
+    x1, i1 = _with_entries(big, lambda: on.pcg(s.b, tol=1e-8, max_iter=500, stop=lina.STOP_RELATIVE))
+    x2, i2 = _with_entries(0, lambda: off.pcg(s.b, tol=1e-8, max_iter=500, stop=lina.STOP_RELATIVE))
+    assert i1.status == 0 and i1.iterations == i2.iterations
+    assert np.array_equal(x1, x2)
+
+
+def test_jacobi_fused_levels_of_an_elasticity_hierarchy():
+    """A 257 x 257 elasticity hierarchy with the levels of up to 400,000 entries fused: a mixed solve
+    equals the unfused one bit for bit."""
+    s = problems.elasticity_p1(257)
+    res = []
+    for entries in (400000, 0):
+        amg = build_jacobi(s, 7, lina.STANDARD, lina.PREC_MIXED, entries)
+        res.append(_with_entries(entries, lambda: amg.pcg(s.b, tol=1e-8, max_iter=500)))
+    (x1, i1), (x2, i2) = res
+    assert i1.status == 0 and i1.iterations == i2.iterations
+    assert np.array_equal(x1, x2)
