@@ -3,6 +3,7 @@
     python -m fem_gb300.kernel_bench --m 1025 --reps 3              # finest matrix
     python -m fem_gb300.kernel_bench --m 1025 --level 8 --reps 3    # a level of the AMG hierarchy
     python -m fem_gb300.kernel_bench --m 1025 --solve --reps 2      # whole mixed-precision solves
+    python -m fem_gb300.kernel_bench --segbatch 24 --reps 2         # a segmented batch, host-launched
 
 Builds the degraded plane-strain elasticity matrix (m x m nodes, 2 m^2 unknowns) or, with
 --level, the AMG hierarchy of the benchmark (standard coarsening, depth 10, matrix tolerance
@@ -13,6 +14,10 @@ in isolation with little device memory in use.
 --solve instead builds the benchmark's device hierarchy (damped Jacobi, omega 0.6, mixed precision) and
 runs `reps` AMG-PCG solves to the relative residual 1e-8, each iteration launched from the host rather
 than from the captured graph (a profiler cannot see the kernels of a graph with conditional nodes).
+
+--segbatch K builds the first K systems of the batched workload (seeded Delaunay meshes, the workload's
+hierarchy settings: standard coarsening, matrix_tol 0.3, multicolour SOR, mixed precision), their
+segmented batch, and runs `reps` of its iterations launched from the host.
 """
 from __future__ import annotations
 
@@ -36,9 +41,13 @@ def main():
                     help="comma-separated sizes m: time the device inverse of a dense m x m block with FP64 CUDA "
                          "cores and with FP64 tensor cores instead")
     ap.add_argument("--solve", action="store_true", help="whole solves, launched iteration by iteration")
+    ap.add_argument("--segbatch", type=int, default=0, help="a segmented batch of this many workload systems")
     args = ap.parse_args()
     if args.solve:
         solve(args)
+        return
+    if args.segbatch:
+        segbatch(args.segbatch, args.reps)
         return
     if args.dense_inverse:
         dense_inverse(int(v) for v in args.dense_inverse.split(","))
@@ -84,6 +93,21 @@ def solve(args):
         print({"iterations": info.iterations, "status": info.status, "ms": (time.perf_counter() - t0) * 1e3,
                "launches": lina.launches()}, flush=True)
     amg.close()
+
+
+def segbatch(count, iterations):
+    plan = problems.batch_plan(96, seed=0)[:count]
+    systems = [problems.batch_system(*p) for p in plan]
+    amgs = [lina.AMG.from_system(s, depth=problems.batch_depth(s.n), coarsening=lina.STANDARD,
+                                 smoother=lina.SMOOTHER_MC_SOR, omega=1.0, precision=lina.PREC_MIXED, matrix_tol=0.3)
+            for s in systems]
+    bd = [lina.DeviceArray.from_host(s.b) for s in systems]
+    seg = lina.SegmentedBatch(amgs)
+    rows, ents = seg.levels()
+    t0 = time.perf_counter()
+    seg.solve(bd, tol=1e-8, max_iter=iterations, device=True, host_loop=True)
+    print({"systems": count, "depths": [a.depth for a in amgs], "level_rows": rows, "level_entries": ents,
+           "iterations": iterations, "ms": (time.perf_counter() - t0) * 1e3}, flush=True)
 
 
 def dense_inverse(sizes, reps=3):
