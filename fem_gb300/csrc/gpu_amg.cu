@@ -1624,6 +1624,20 @@ struct lina_gpu_amg {
     // segmented batch: per level, the rows of the largest system's level (layout choice), else empty
     std::vector<long> seg_max_rows;
     long lanes_rows = 0;
+    // lina_gpu_amg_recompute: per level, where each CSR entry of A sits in the device layouts (natural,
+    // quads, colour-grouped) and a fingerprint of A's pattern, kept from the first recompute on so that
+    // later ones with the same patterns only move values
+    struct LevelMaps {
+        int *posA = nullptr, *posQ = nullptr, *posC = nullptr;
+        uint64_t pattern = 0;
+        long nnz = 0;
+    };
+    std::vector<LevelMaps> rmaps;
+    bool keep_maps = false;
+    double* rstage = nullptr;  // staging for a level's new values
+    long rstage_n = 0;
+    int* rerr = nullptr;       // error word of the device coarse inverse
+    std::vector<int> c_block_rows;  // the coarse block rows of the uploaded coarse solver
     int timed_level = 0;       // level whose smoother sweeps LINA_PCG_TIME_KERNELS times (most entries)
     // maps for lina_gpu_amg_update_values (built on first use, finest level)
     bool upd_built = false;
@@ -2402,6 +2416,48 @@ struct lina_gpu_amg {
 
 namespace {
 
+// 64-bit fingerprint of a CSR pattern (row pointers and column indices): FNV-1a over fixed chunks, the
+// chunk values combined in order
+uint64_t pattern_fingerprint_csr(const lina::Csr& A) {
+    const long np = (long)A.ptr.size(), nc = (long)A.col.size();
+    constexpr long kChunk = 1L << 20;
+    const long chunks = (np + kChunk - 1) / kChunk + (nc + kChunk - 1) / kChunk;
+    std::vector<uint64_t> part(chunks);
+#pragma omp parallel for schedule(static)
+    for (long c = 0; c < chunks; c++) {
+        const long pc = (np + kChunk - 1) / kChunk;
+        const int* a = c < pc ? A.ptr.data() : A.col.data();
+        const long n = c < pc ? np : nc;
+        const long lo = (c < pc ? c : c - pc) * kChunk, hi = std::min(n, lo + kChunk);
+        uint64_t h = 1469598103934665603ull;
+        for (long k = lo; k < hi; k++) {
+            h ^= (uint32_t)a[k];
+            h *= 1099511628211ull;
+        }
+        part[c] = h;
+    }
+    uint64_t h = 1469598103934665603ull ^ (uint64_t)np ^ ((uint64_t)nc << 32);
+    for (uint64_t v : part) {
+        h ^= v;
+        h *= 1099511628211ull;
+    }
+    return h;
+}
+
+// the Jacobi diagonal of a level (1/a_ii; 0 for a zero diagonal and for undecided rows of levels >= 1)
+void level_dinv(const lina::HostLevel& hl, int l, std::vector<double>& dinv) {
+    const int n = hl.A.n;
+    dinv.assign(n, 0.0);
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; i++) {
+        double d = 0.0;
+        for (int p = hl.A.ptr[i]; p < hl.A.ptr[i + 1]; p++)
+            if (hl.A.col[p] == i) d = hl.A.val[p];
+        const bool skip = (l > 0 && !hl.labels.empty() && hl.labels[i] == lina::kUndecided);
+        dinv[i] = (skip || d == 0.0) ? 0.0 : 1.0 / d;
+    }
+}
+
 int upload_hierarchy(lina_gpu_amg* h) {
     lina::HostHierarchy& H = h->host;
     const int depth = h->depth;
@@ -2412,15 +2468,11 @@ int upload_hierarchy(lina_gpu_amg* h) {
         DLevel& L = h->lv[l];
         L.n = hl.A.n;
         h->lanes_rows = h->seg_max_rows.empty() ? 0 : h->seg_max_rows[l];
-        if ((rc = h->upload_csr(L.A, hl.A))) return rc;
-        std::vector<double> dinv(L.n, 0.0);
-        for (int i = 0; i < L.n; i++) {
-            double d = 0.0;
-            for (int p = hl.A.ptr[i]; p < hl.A.ptr[i + 1]; p++)
-                if (hl.A.col[p] == i) d = hl.A.val[p];
-            bool skip = (l > 0 && !hl.labels.empty() && hl.labels[i] == lina::kUndecided);
-            dinv[i] = (skip || d == 0.0) ? 0.0 : 1.0 / d;
-        }
+        std::vector<int> posA, posQ, posC;
+        if ((rc = h->upload_csr(L.A, hl.A, nullptr, h->keep_maps ? &posA : nullptr, h->keep_maps ? &posQ : nullptr)))
+            return rc;
+        std::vector<double> dinv;
+        level_dinv(hl, l, dinv);
         std::vector<float> dinv32(dinv.begin(), dinv.end());
         if ((rc = h->upload(&L.dinv64, dinv.data(), dinv.size()))) return rc;
         if ((rc = h->upload(&L.dinv32, dinv32.data(), dinv32.size()))) return rc;
@@ -2431,7 +2483,27 @@ int upload_hierarchy(lina_gpu_amg* h) {
             L.ncolours = lina::greedy_colouring(hl.A, colour);
             std::vector<std::vector<int>> groups(L.ncolours);
             for (int i = 0; i < L.n; i++) groups[colour[i]].push_back(i);
-            if ((rc = h->upload_csr(L.Acol, hl.A, &groups))) return rc;
+            if ((rc = h->upload_csr(L.Acol, hl.A, &groups, h->keep_maps ? &posC : nullptr))) return rc;
+        }
+        if (h->keep_maps) {  // in-place value updates of later recomputes
+            if ((int)h->rmaps.size() != depth) h->rmaps.assign(depth, lina_gpu_amg::LevelMaps());
+            lina_gpu_amg::LevelMaps& M = h->rmaps[l];
+            const long nnz = hl.A.nnz();
+            auto up = [&](int** dst, std::vector<int>& pos) -> int {
+                if (pos.empty()) {  // values in CSR order (lane-group layout)
+                    pos.resize(nnz);
+                    for (long k = 0; k < nnz; k++) pos[k] = (int)k;
+                }
+                return h->upload(dst, pos.data(), pos.size());
+            };
+            if ((rc = up(&M.posA, posA))) return rc;
+            M.posQ = nullptr;
+            if (L.A.q_val && !posQ.empty() && (rc = h->upload(&M.posQ, posQ.data(), posQ.size()))) return rc;
+            M.posC = nullptr;
+            if (l > 0 && (rc = up(&M.posC, posC))) return rc;
+            M.pattern = pattern_fingerprint_csr(hl.A);
+            M.nnz = nnz;
+            CK(cudaStreamSynchronize(h->stream));  // the host maps go out of scope
         }
         // work vectors
         if ((rc = h->alloc(&L.x64, L.n))) return rc;
@@ -2447,6 +2519,7 @@ int upload_hierarchy(lina_gpu_amg* h) {
     // coarsest block
     lina::CoarseSolver& cs = H.coarse;
     h->cm = (int)cs.block_rows.size();
+    h->c_block_rows = cs.block_rows;
     std::vector<int> blockpos(cs.n, 0);
     for (int k = 0; k < h->cm; k++) blockpos[cs.block_rows[k]] = k;
     if ((rc = h->upload(&h->c_brows, cs.block_rows.data(), cs.block_rows.size()))) return rc;
@@ -2811,6 +2884,80 @@ int lina_gpu_amg_load(const char* dir, const lina_gpu_amg_options* opt, int host
     return 0;
 }
 
+}  // extern "C"
+
+namespace {
+
+// New values of every level on unchanged patterns (lina_gpu_amg_recompute after the first): each level's
+// entries scattered into its device layouts, its Jacobi diagonal, the finest isolated-row inverses and
+// the coarse inverse replaced in place; the device pointers (and a captured solve graph) stay valid.
+// Returns 0, 1 when some pattern (or the coarse block) differs from the uploaded one, or an error.
+int refresh_values(lina_gpu_amg* h) {
+    const lina::HostHierarchy& H = h->host;
+    const int depth = h->depth;
+    if ((int)h->rmaps.size() != depth) return 1;
+    for (int l = 0; l < depth; l++)
+        if (H.lv[l].A.nnz() != h->rmaps[l].nnz || pattern_fingerprint_csr(H.lv[l].A) != h->rmaps[l].pattern) return 1;
+    if (H.coarse.block_rows != h->c_block_rows || !H.coarse.blocks.empty()) return 1;
+    long most = 0;
+    for (int l = 0; l < depth; l++) most = std::max<long>(most, H.lv[l].A.nnz());
+    int rc;
+    if (most > h->rstage_n) {
+        if ((rc = h->alloc(&h->rstage, most))) return rc;
+        h->rstage_n = most;
+    }
+    cudaStream_t st = h->stream;
+    for (int l = 0; l < depth; l++) {
+        const lina::HostLevel& hl = H.lv[l];
+        DLevel& L = h->lv[l];
+        const lina_gpu_amg::LevelMaps& M = h->rmaps[l];
+        CK(cudaMemcpyAsync(h->rstage, hl.A.val.data(), hl.A.nnz() * sizeof(double), cudaMemcpyHostToDevice, st));
+        go(update_values_kernel, grid_for(hl.A.nnz(), kThreads), st, (long)hl.A.nnz(), (const double*)h->rstage,
+           (const int*)M.posA, (const int*)M.posC, L.A.v64, L.A.v32, L.Acol.v64, L.Acol.v32, (const int*)M.posQ,
+           reinterpret_cast<float*>(L.A.q_val));
+        std::vector<double> dinv;
+        level_dinv(hl, l, dinv);
+        std::vector<float> dinv32(dinv.begin(), dinv.end());
+        CK(cudaMemcpyAsync(L.dinv64, dinv.data(), dinv.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(L.dinv32, dinv32.data(), dinv32.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));  // the staging buffer and the host vectors are reused
+    }
+    // coarsest level: the new dense block (inverted here or on the device) and 1/a_ii elsewhere
+    const lina::CoarseSolver& cs = H.coarse;
+    CK(cudaMemcpyAsync(h->c_inv, cs.inv.data(), cs.inv.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (!cs.inverted) {
+        if (!h->rerr && (rc = h->alloc(&h->rerr, 1))) return rc;
+        std::string msg;
+        if ((rc = lina::dense_inverse(h->cm, h->c_inv, g_dense_method, st, h->rerr, msg))) {
+            set_err("%s", msg.c_str());
+            return rc;
+        }
+    }
+    CK(cudaMemcpyAsync(h->c_dginv, cs.diag_inv.data(), cs.diag_inv.size() * sizeof(double), cudaMemcpyHostToDevice,
+                       st));
+    // the finest level's isolated rows
+    const int nf = H.lv[depth - 1].A.n;
+    std::vector<double> iso(nf, 0.0);
+    if (depth > 1) {
+        const lina::HostLevel& F = H.lv[depth - 1];
+        for (int i = 0; i < nf; i++)
+            if (F.labels[i] == lina::kIsolated)
+                for (int p = F.A.ptr[i]; p < F.A.ptr[i + 1]; p++)
+                    if (F.A.val[p] != 0.0) {
+                        iso[i] = 1.0 / F.A.val[p];
+                        break;
+                    }
+    }
+    CK(cudaMemcpyAsync(h->isoinv, iso.data(), iso.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    // the finest-level update maps of lina_gpu_amg_update_values stay valid (same pattern and layouts)
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
 int lina_gpu_amg_recompute(lina_gpu_amg* h, int n, const int* rowptr, const int* col, const double* val) {
     if (!h || !valid_csr(n, rowptr, col) || !val) {
         set_err("lina_gpu_amg_recompute: invalid input");
@@ -2822,6 +2969,10 @@ int lina_gpu_amg_recompute(lina_gpu_amg* h, int n, const int* rowptr, const int*
     }
     // the reference keeps the setup's signs and does not flip the new matrix
     if (h->host_only) return 0;
+    if (!h->has_signs && !h->rmaps.empty()) {
+        const int rc = refresh_values(h);
+        if (rc != 1) return rc;  // done (0) or failed; 1: a pattern changed, rebuild
+    }
     h->drop_graph();
     for (void* p : h->allocations) cudaFree(p);
     h->allocations.clear();
@@ -2833,7 +2984,13 @@ int lina_gpu_amg_recompute(lina_gpu_amg* h, int n, const int* rowptr, const int*
     h->kph = h->kqh = nullptr;
     h->hist_m = 0;
     h->Aorig = DCsr();
+    h->rmaps.clear();
+    h->rstage = nullptr;
+    h->rstage_n = 0;
+    h->rerr = nullptr;
+    h->keep_maps = !h->has_signs;
     int rc = upload_hierarchy(h);
+    h->keep_maps = false;
     if (rc) return rc;
     if (h->has_signs) rc = h->upload_csr(h->Aorig, csr_from(n, rowptr, col, val));
     return rc;

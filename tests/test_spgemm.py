@@ -98,3 +98,40 @@ def test_device_hierarchy_setup_and_recompute_match_host(name, capfd):
         assert same(dev.level(l).A, host.level(l).A), f"level {l} after recompute"
     # the products ran on the GPU (the library says so on stderr when it falls back to the host)
     assert "Galerkin product on the host" not in capfd.readouterr().err
+
+
+def _symmetric_scale(s, seed, amount):
+    rows = np.repeat(np.arange(s.n), np.diff(s.indptr))
+    key = np.minimum(rows, s.indices) * s.n + np.maximum(rows, s.indices)
+    _, inv = np.unique(key, return_inverse=True)
+    return s.data * (1.0 + amount * np.random.default_rng(seed).random(inv.max() + 1)[inv])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["poisson33_std", "elast17_std"])
+@pytest.mark.parametrize("precision", [lina.PREC_FP64, lina.PREC_MIXED])
+def test_repeated_recompute_updates_values_in_place(name, precision):
+    """The first recompute rebuilds the device hierarchy and keeps where every entry sits in its layouts;
+    later recomputes on the same patterns only move values.  A hierarchy recomputed twice (the second time
+    in place) solves exactly as one recomputed once, with a rebuild, to the same matrix; and the captured
+    solve graph of the first keeps working."""
+    g = load_golden(name)
+    s = system_for(name)
+    depth, coarsening = int(g["depth"]), int(g["coarsening"])
+    opts = dict(depth=depth, coarsening=coarsening, precision=precision)
+    v2, v3 = _symmetric_scale(s, 4, 0.2), _symmetric_scale(s, 5, 0.3)
+    twice = lina.AMG.from_system(s, **opts)
+    twice.pcg(s.b, tol=1e-8, max_iter=500)  # a captured graph before the recomputes
+    twice.recompute(s.indptr, s.indices, v2)
+    twice.pcg(s.b, tol=1e-8, max_iter=500)
+    twice.recompute(s.indptr, s.indices, v3)
+    once = lina.AMG.from_system(s, **opts)
+    once.recompute(s.indptr, s.indices, v3)
+    for l in range(depth):
+        assert same(twice.level(l).A, once.level(l).A), f"level {l}"
+    r = np.random.default_rng(6).uniform(-1, 1, s.n)
+    assert np.array_equal(twice.vcycle(r), once.vcycle(r))
+    x1, i1 = twice.pcg(s.b, tol=1e-8, max_iter=500)
+    x2, i2 = once.pcg(s.b, tol=1e-8, max_iter=500)
+    assert i1.status == 0 and i1.iterations == i2.iterations
+    assert np.array_equal(x1, x2)
