@@ -49,6 +49,10 @@ int g_fused_rows = 24576;
 // 1,283 us levels 1-3: the separate launches overlap one another (programmatic dependent launch), a
 // cluster launch waits for its predecessor to drain and for 16 free SMs.
 long g_fused_jacobi_entries = 0;
+// segmented batches: the cluster-fused multicolour-SOR step on concatenated levels, one cluster per group
+// of whole systems; off by default.  Measured on the 96-system workload (GB300): 803 ms per batch solve
+// with it against 714 ms with one launch per colour (a group's sweeps run on one cluster's 16 SMs).
+int g_fused_groups = 0;
 // 16: SELL-32 matrices with long rows uploaded afterwards also get 16-bit column offsets (two bases
 // per slice, where every slice's columns fit), read by FP32 passes; 32: int columns only
 int g_sell_bits = 16;
@@ -962,10 +966,20 @@ struct FusedStep {
     double w;
 };
 
+// A cluster's share of a level made of independent systems (a segmented batch): the rows [r0, r1) of
+// whole systems, their coarse rows [c0, c1), and at granges + c the positions of its rows of colour c in
+// the colour order.  Its rows couple only to its own rows, so each cluster sweeps on its own.
+struct FusedGroup {
+    int r0, r1, c0, c1;
+    const int2* granges;
+};
+
+// a block's copy of x, holding the rows [off, off + rows) of the level
 template <typename TX>
 struct LocalRead {
     const TX* p;
-    __device__ __forceinline__ TX get(int j) const { return p[j]; }
+    int off;
+    __device__ __forceinline__ TX get(int j) const { return p[j - off]; }
 };
 template <typename TX>
 struct GlobalRead {
@@ -975,10 +989,10 @@ struct GlobalRead {
 
 // entry i of every block's copy of x := v, the group's S lanes sharing the stores
 template <typename TX>
-__device__ __forceinline__ void broadcast_x(TX* xs, int i, TX v, int sub, int S) {
+__device__ __forceinline__ void broadcast_x(TX* xs, int i, TX v, int sub, int S, int off = 0) {
     const cg::cluster_group cl = cg::this_cluster();
     const int K = (int)cl.num_blocks();
-    for (int r = sub; r < K; r += S) cl.map_shared_rank(xs, (unsigned)r)[i] = v;
+    for (int r = sub; r < K; r += S) cl.map_shared_rank(xs, (unsigned)r)[i - off] = v;
 }
 
 // sum_k val_k v_col_k over one row by a group of S lanes (the order of csrv_kernel); the butterfly
@@ -1077,12 +1091,13 @@ __device__ __forceinline__ void fetch_sweep_row(SweepRow<TX>& p, bool valid, int
 // from the fetched entries, the rest as csrv_kernel walks them), stored into every copy of x
 template <typename TX>
 __device__ __forceinline__ void sweep_fetched_row(const SweepRow<TX>& p, bool valid, int sub, int S, TX w,
-                                                  const FusedStep& st, const TX* __restrict__ sval, TX* xs) {
+                                                  const FusedStep& st, const TX* __restrict__ sval, TX* xs,
+                                                  int off = 0) {
     TX sum = TX(0);
     if (valid) {
         TX xv[4];
 #pragma unroll
-        for (int j = 0; j < 4; j++) xv[j] = p.c[j] >= 0 ? xs[p.c[j]] : TX(0);
+        for (int j = 0; j < 4; j++) xv[j] = p.c[j] >= 0 ? xs[p.c[j] - off] : TX(0);
 #pragma unroll
         for (int j = 0; j < 4; j++)
             if (p.c[j] >= 0) sum += TX(p.v[j]) * xv[j];
@@ -1092,16 +1107,16 @@ __device__ __forceinline__ void sweep_fetched_row(const SweepRow<TX>& p, bool va
                       c3 = __ldg(st.scol + k + 3 * S);
             const TX v0 = __ldg(sval + k), v1 = __ldg(sval + k + S), v2 = __ldg(sval + k + 2 * S),
                      v3 = __ldg(sval + k + 3 * S);
-            const TX x0 = xs[c0], x1 = xs[c1], x2 = xs[c2], x3 = xs[c3];
+            const TX x0 = xs[c0 - off], x1 = xs[c1 - off], x2 = xs[c2 - off], x3 = xs[c3 - off];
             sum += TX(v0) * x0;
             sum += TX(v1) * x1;
             sum += TX(v2) * x2;
             sum += TX(v3) * x3;
         }
-        for (; k < p.e0; k += S) sum += TX(__ldg(sval + k)) * xs[__ldg(st.scol + k)];
+        for (; k < p.e0; k += S) sum += TX(__ldg(sval + k)) * xs[__ldg(st.scol + k) - off];
     }
     for (int o = S / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, S);
-    if (valid) broadcast_x(xs, p.i, xs[p.i] + w * p.di * (p.bi - sum), sub, S);
+    if (valid) broadcast_x(xs, p.i, xs[p.i - off] + w * p.di * (p.bi - sum), sub, S, off);
 }
 
 __device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
@@ -1112,9 +1127,12 @@ __device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.w
 // ahead, its entries, b and 1/a_ii one colour ahead, so after a barrier only shared-memory reads of
 // x are on the critical path.  Colours with more rows than the cluster has lane groups sweep the
 // remaining rows directly.
+// off: the first row of the level the block's copy of x holds; granges: per colour the position range
+// of the cluster's rows in the colour order (null: the whole colour, st.sgroup)
 template <typename TX>
 __device__ __forceinline__ void fused_sweeps(const FusedStep& st, TX* xs, const TX* __restrict__ b,
-                                             const TX* __restrict__ dinv) {
+                                             const TX* __restrict__ dinv, int off = 0,
+                                             const int2* __restrict__ granges = nullptr) {
     const TX w = TX(st.w);
     const TX* sval = (const TX*)st.sval;
     const int S = st.sS;
@@ -1128,8 +1146,14 @@ __device__ __forceinline__ void fused_sweeps(const FusedStep& st, TX* xs, const 
     // colour of a step and its position range
     auto range = [&](int step, int& r0, int& r1) {
         const int c = step % st.ncolours;
-        r0 = __ldg(st.sgroup + c);
-        r1 = __ldg(st.sgroup + c + 1);
+        if (granges) {
+            const int2 g = __ldg(granges + c);
+            r0 = g.x;
+            r1 = g.y;
+        } else {
+            r0 = __ldg(st.sgroup + c);
+            r1 = __ldg(st.sgroup + c + 1);
+        }
     };
     int r0, r1, n0, n1, m0, m1;
     range(0, r0, r1);
@@ -1149,12 +1173,12 @@ __device__ __forceinline__ void fused_sweeps(const FusedStep& st, TX* xs, const 
             h2 = load_head<TX>(st, m0 + first, m0 + first < m1);
         }
         if (step + 1 < steps) build_sweep_row<TX>(nxt, h1, n0 + first < n1, sub, S, st, sval, b, dinv);
-        sweep_fetched_row<TX>(cur, r0 + first < r1, sub, S, w, st, sval, xs);
+        sweep_fetched_row<TX>(cur, r0 + first < r1, sub, S, w, st, sval, xs, off);
         for (int gb = r0 + warp * per_warp + nwarps * per_warp; gb < r1; gb += nwarps * per_warp) {
             const int g = gb + lane / S;
             SweepRow<TX> q;
             fetch_sweep_row<TX>(q, g < r1, g, sub, S, st, sval, b, dinv);
-            sweep_fetched_row<TX>(q, g < r1, sub, S, w, st, sval, xs);
+            sweep_fetched_row<TX>(q, g < r1, sub, S, w, st, sval, xs, off);
         }
         cluster_arrive();
         cluster_wait();
@@ -1190,7 +1214,8 @@ __device__ __forceinline__ TX* fused_jacobi_sweeps(const FusedStep& st, int nu, 
 
 // dynamic shared memory of a block: a copy of x (n entries), two for damped Jacobi (JAC)
 template <typename TX, bool PRE, bool JAC>
-__global__ void __launch_bounds__(kFuseThreads, 1) fused_step_kernel(const FusedStep st) {
+__global__ void __launch_bounds__(kFuseThreads, 1) fused_step_kernel(const FusedStep st,
+                                                                     const FusedGroup* __restrict__ groups) {
     pdl_wait();
     extern __shared__ __align__(16) unsigned char fused_smem[];
     const cg::cluster_group cl = cg::this_cluster();
@@ -1233,31 +1258,43 @@ __global__ void __launch_bounds__(kFuseThreads, 1) fused_step_kernel(const Fused
         cl.sync();  // no block leaves while another may still store into its shared memory
         return;
     }
-    for (int j = (int)threadIdx.x; j < st.n; j += blockDim.x) xs[j] = PRE ? TX(0) : __ldcg(xg + j);
+    // the cluster's rows: a group of whole systems (groups non-null), else the whole level
+    int r0 = 0, r1 = st.n, c0 = 0, c1 = st.nc;
+    const int2* granges = nullptr;
+    if (groups) {
+        const FusedGroup& g = groups[blockIdx.x / cl.num_blocks()];
+        r0 = g.r0;
+        r1 = g.r1;
+        c0 = g.c0;
+        c1 = g.c1;
+        granges = g.granges;
+    }
+    const int nr = r1 - r0;
+    for (int j = (int)threadIdx.x; j < nr; j += blockDim.x) xs[j] = PRE ? TX(0) : __ldcg(xg + r0 + j);
     cl.sync();
     if (PRE) {
-        fused_sweeps<TX>(st, xs, b, dinv);
+        fused_sweeps<TX>(st, xs, b, dinv, r0, granges);
         TX* r = (TX*)st.r;
-        fused_rows<TX>(0, st.n, st.aS, st.aptr, st.acol, (const TX*)st.aval, LocalRead<TX>{xs},
+        fused_rows<TX>(r0, r1, st.aS, st.aptr, st.acol, (const TX*)st.aval, LocalRead<TX>{xs, r0},
                        [&](int i, TX sum, int sub) {
                            if (sub == 0) r[i] = b[i] - sum;
                        });
         cl.sync();
         TX* cb = (TX*)st.cb;
-        fused_rows<TX>(0, st.nc, st.rS, st.rptr, st.rcol, (const TX*)st.rval, GlobalRead<TX>{r},
+        fused_rows<TX>(c0, c1, st.rS, st.rptr, st.rcol, (const TX*)st.rval, GlobalRead<TX>{r},
                        [&](int i, TX sum, int sub) {
                            if (sub == 0) cb[i] = sum;
                        });
     } else {
-        fused_rows<TX>(0, st.n, st.pS, st.pptr, st.pcol, (const TX*)st.pval, GlobalRead<TX>{(const TX*)st.e},
-                       [&](int i, TX sum, int sub) { broadcast_x(xs, i, xs[i] + sum, sub, st.pS); });
+        fused_rows<TX>(r0, r1, st.pS, st.pptr, st.pcol, (const TX*)st.pval, GlobalRead<TX>{(const TX*)st.e},
+                       [&](int i, TX sum, int sub) { broadcast_x(xs, i, xs[i - r0] + sum, sub, st.pS, r0); });
         cl.sync();
-        fused_sweeps<TX>(st, xs, b, dinv);
+        fused_sweeps<TX>(st, xs, b, dinv, r0, granges);
     }
     // the sweeps ended with a cluster barrier: every copy is final; each block writes its share
-    const int chunk = (st.n + (int)cl.num_blocks() - 1) / (int)cl.num_blocks();
-    const int lo = (int)cl.block_rank() * chunk, hi = min(st.n, lo + chunk);
-    for (int j = lo + (int)threadIdx.x; j < hi; j += blockDim.x) xg[j] = xs[j];
+    const int chunk = (nr + (int)cl.num_blocks() - 1) / (int)cl.num_blocks();
+    const int lo = (int)cl.block_rank() * chunk, hi = min(nr, lo + chunk);
+    for (int j = lo + (int)threadIdx.x; j < hi; j += blockDim.x) xg[r0 + j] = xs[j];
     cl.sync();  // no block leaves while another may still store into its shared memory
 }
 
@@ -1547,6 +1584,10 @@ struct DLevel {
     int n = 0;
     DCsr A, P, R;
     DCsr Acol;  // rows grouped by colour (multicolour SOR)
+    // a level of independent systems (segmented batch): the cluster-fused multicolour-SOR step runs one
+    // cluster per group of whole systems (ngroups > 0)
+    int ngroups = 0, max_group_rows = 0;
+    FusedGroup* d_groups = nullptr;
     double* dinv64 = nullptr;
     float* dinv32 = nullptr;
     int ncolours = 0;
@@ -1623,6 +1664,7 @@ struct lina_gpu_amg {
     bool host_only = false;
     // segmented batch: per level, the rows of the largest system's level (layout choice), else empty
     std::vector<long> seg_max_rows;
+    std::vector<std::vector<int>> seg_off;  // per level, the first row of each system (and the end)
     long lanes_rows = 0;
     // lina_gpu_amg_recompute: per level, where each CSR entry of A sits in the device layouts (natural,
     // quads, colour-grouped) and a fingerprint of A's pattern, kept from the first recompute on so that
@@ -2086,8 +2128,10 @@ struct lina_gpu_amg {
             return g_fused_rows > 0 && g_fused_jacobi_entries > 0 && !timed && L.n <= g_fused_rows &&
                    L.A.nnz <= g_fused_jacobi_entries && 2 * copy_bytes <= kFusedSmemMax && L.A.lanes > 0 &&
                    L.R.lanes > 0 && L.P.lanes > 0;
-        return g_fused_rows > 0 && opt.smoother == LINA_SMOOTHER_MC_SOR && !timed && L.n <= g_fused_rows &&
-               copy_bytes <= kFusedSmemMax &&
+        const bool whole = L.n <= g_fused_rows && copy_bytes <= kFusedSmemMax;
+        const bool grouped = L.ngroups > 0 && L.max_group_rows <= g_fused_rows &&
+                             (long)L.max_group_rows * (opt.precision == LINA_PREC_MIXED ? 4 : 8) <= kFusedSmemMax;
+        return g_fused_rows > 0 && opt.smoother == LINA_SMOOTHER_MC_SOR && !timed && (whole || grouped) &&
                L.ncolours > 0 && L.Acol.lanes > 0 && L.Acol.d_group_row && L.Acol.d_head && L.A.lanes > 0 &&
                L.R.lanes > 0 && L.P.lanes > 0;
     }
@@ -2141,20 +2185,25 @@ struct lina_gpu_amg {
         st.cb = lvx<TX>(C, 2);
         st.w = opt.omega;
         const int K = fused_cluster_size<TX, PRE, JAC>();
+        // whole systems in groups, one cluster each, where the level is too large for one cluster
+        const bool grouped = !JAC && L.ngroups > 0 && L.n > g_fused_rows;
         cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(K);
+        cfg.gridDim = dim3(K * (grouped ? L.ngroups : 1));
         cfg.blockDim = dim3(kFuseThreads);
-        cfg.dynamicSmemBytes = (size_t)(JAC ? 2 : 1) * L.n * sizeof(TX);
+        cfg.dynamicSmemBytes = (size_t)(JAC ? 2 : 1) * (grouped ? L.max_group_rows : L.n) * sizeof(TX);
         cfg.stream = stream;
-        cudaLaunchAttribute attr[1];
+        cudaLaunchAttribute attr[2];
         attr[0].id = cudaLaunchAttributeClusterDimension;
         attr[0].val.clusterDim.x = K;
         attr[0].val.clusterDim.y = 1;
         attr[0].val.clusterDim.z = 1;
+        attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[1].val.programmaticStreamSerializationAllowed = 1;
         cfg.attrs = attr;
-        cfg.numAttrs = 1;
+        cfg.numAttrs = g_pdl ? 2 : 1;
         g_launches++;
-        cudaLaunchKernelEx(&cfg, fused_step_kernel<TX, PRE, JAC>, st);
+        cudaLaunchKernelEx(&cfg, fused_step_kernel<TX, PRE, JAC>, st,
+                           grouped ? (const FusedGroup*)L.d_groups : (const FusedGroup*)nullptr);
     }
 
     // 16 blocks per cluster where the GPU schedules such clusters, else (or with LINA_FUSED_CLUSTER=8)
@@ -2458,6 +2507,64 @@ void level_dinv(const lina::HostLevel& hl, int l, std::vector<double>& dinv) {
     }
 }
 
+// The groups of a segmented level for the cluster-fused multicolour-SOR step: consecutive whole systems
+// while their rows fit g_fused_rows.  Built only where every row of a group couples only to rows of its
+// group (A), every restricted row reads only its rows (R), and every prolongated row only its coarse rows
+// (P): then each cluster's reads and stores of its copy of x stay inside the copy.
+int build_fused_groups(lina_gpu_amg* h, int l, const lina::HostLevel& hl,
+                       const std::vector<std::vector<int>>& colours) {
+    DLevel& L = h->lv[l];
+    const std::vector<int>& off = h->seg_off[l];
+    const std::vector<int>& coff = h->seg_off[l - 1];
+    const int S = (int)off.size() - 1;
+    if (!g_fused_groups || g_fused_rows <= 0 || L.Acol.lanes <= 0 || L.A.lanes <= 0 || L.R.lanes <= 0 ||
+        L.P.lanes <= 0 || L.n <= g_fused_rows || L.ncolours <= 0)
+        return 0;
+    std::vector<int4> grp;  // (r0, r1, c0, c1)
+    for (int i = 0; i < S;) {
+        if (off[i + 1] - off[i] > g_fused_rows) return 0;  // a system too large for one cluster
+        int j = i + 1;
+        while (j < S && off[j + 1] - off[i] <= g_fused_rows) j++;
+        grp.push_back(make_int4(off[i], off[j], coff[i], coff[j]));
+        i = j;
+    }
+    auto inside = [](const lina::Csr& M, int row0, int row1, int col0, int col1) {
+        for (int r = row0; r < row1; r++)
+            for (int p = M.ptr[r]; p < M.ptr[r + 1]; p++)
+                if (M.col[p] < col0 || M.col[p] >= col1) return false;
+        return true;
+    };
+    for (const int4& g : grp)
+        if (!inside(hl.A, g.x, g.y, g.x, g.y) || !inside(hl.R, g.z, g.w, g.x, g.y) || !inside(hl.P, g.x, g.y, g.z, g.w))
+            return 0;
+    // per group and colour: the positions of the group's rows of that colour in the colour order
+    const int G = (int)grp.size(), C = L.ncolours;
+    std::vector<int2> ranges((size_t)G * C);
+    for (int c = 0; c < C; c++) {
+        const std::vector<int>& rows = colours[c];
+        const int base = L.Acol.group_row[c];
+        for (int k = 0; k < G; k++) {
+            const int b0 = (int)(std::lower_bound(rows.begin(), rows.end(), grp[k].x) - rows.begin());
+            const int b1 = (int)(std::lower_bound(rows.begin(), rows.end(), grp[k].y) - rows.begin());
+            ranges[(size_t)k * C + c] = make_int2(base + b0, base + b1);
+        }
+    }
+    int2* d_ranges = nullptr;
+    int rc;
+    if ((rc = h->upload(&d_ranges, ranges.data(), ranges.size()))) return rc;
+    std::vector<FusedGroup> fg(G);
+    int most = 0;
+    for (int k = 0; k < G; k++) {
+        fg[k] = FusedGroup{grp[k].x, grp[k].y, grp[k].z, grp[k].w, d_ranges + (size_t)k * C};
+        most = std::max(most, grp[k].y - grp[k].x);
+    }
+    if ((rc = h->upload(&L.d_groups, fg.data(), fg.size()))) return rc;
+    CK(cudaStreamSynchronize(h->stream));
+    L.ngroups = G;
+    L.max_group_rows = most;
+    return 0;
+}
+
 int upload_hierarchy(lina_gpu_amg* h) {
     lina::HostHierarchy& H = h->host;
     const int depth = h->depth;
@@ -2484,6 +2591,7 @@ int upload_hierarchy(lina_gpu_amg* h) {
             std::vector<std::vector<int>> groups(L.ncolours);
             for (int i = 0; i < L.n; i++) groups[colour[i]].push_back(i);
             if ((rc = h->upload_csr(L.Acol, hl.A, &groups, h->keep_maps ? &posC : nullptr))) return rc;
+            if (!h->seg_off.empty() && (rc = build_fused_groups(h, l, hl, groups))) return rc;
         }
         if (h->keep_maps) {  // in-place value updates of later recomputes
             if ((int)h->rmaps.size() != depth) h->rmaps.assign(depth, lina_gpu_amg::LevelMaps());
@@ -2673,6 +2781,11 @@ int lina_gpu_set_fused_rows(int max_rows) {
         return LINA_GPU_EINVAL;
     }
     g_fused_rows = max_rows;
+    return 0;
+}
+
+int lina_gpu_set_fused_groups(int on) {
+    g_fused_groups = on ? 1 : 0;
     return 0;
 }
 
@@ -4499,6 +4612,7 @@ int lina_gpu_segbatch_create(int count, lina_gpu_amg* const* systems, lina_gpu_s
     for (int l = 0; l < c->depth; l++)
         for (int i = 0; i < count; i++)
             c->seg_max_rows[l] = std::max<long>(c->seg_max_rows[l], map.off[l][i + 1] - map.off[l][i]);
+    c->seg_off = map.off;
     c->fcg_m = s0->fcg_m;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete B;

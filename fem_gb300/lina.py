@@ -138,6 +138,7 @@ def lib():
         "lina_gpu_set_layout": (C.c_int, [C.c_int]),
         "lina_gpu_set_fused_rows": (C.c_int, [C.c_int]),
         "lina_gpu_set_fused_jacobi_entries": (C.c_int, [C.c_long]),
+        "lina_gpu_set_fused_groups": (C.c_int, [C.c_int]),
         "lina_gpu_set_sell_index_bits": (C.c_int, [C.c_int]),
         "lina_gpu_set_sell_quads": (C.c_int, [C.c_int]),
         "lina_gpu_set_pdl": (C.c_int, [C.c_int]),
@@ -304,6 +305,12 @@ def set_fused_rows(max_rows: int):
     """Levels of at most max_rows rows run a multicolour-SOR V-cycle step as one cluster launch
     (0: one launch per colour)."""
     _check(lib().lina_gpu_set_fused_rows(int(max_rows)), "set fused rows")
+
+
+def set_fused_groups(on: bool):
+    """Segmented batches created afterwards run the multicolour-SOR step of concatenated levels as one
+    cluster per group of whole systems (off by default)."""
+    _check(lib().lina_gpu_set_fused_groups(int(bool(on))), "set fused groups")
 
 
 def set_fused_jacobi_entries(max_entries: int):

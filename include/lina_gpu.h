@@ -436,6 +436,12 @@ int lina_gpu_set_fused_rows(int max_rows);
    as one cluster launch, two copies of x in shared memory (default 0 = never: measured slower than the
    separate launches on GB300); the results are those of the separate launches, bit for bit */
 int lina_gpu_set_fused_jacobi_entries(long max_entries);
+/* segmented batches created afterwards: run the multicolour-SOR step of concatenated levels as one
+   cluster per group of whole systems (at most the fused-rows limit each); default 0 = off (measured
+   slower than one launch per colour on GB300).  The sweeps equal the colour launches'; residuals and
+   transfers sum rows in lane-group order (separate FP32 launches on levels of 20,000 rows or more use the
+   quad layout's stored order), so results agree to rounding. */
+int lina_gpu_set_fused_groups(int on);
 /* 16 (default): SELL-32 matrices with long rows (at least 24 stored entries per row on average)
    uploaded afterwards also get 16-bit column indices, a 15-bit offset from one of two bases per
    slice of 32 rows, where every slice's columns fit two such windows; FP32 passes read those (2

@@ -102,3 +102,37 @@ def test_segbatch_rejects_mixed_settings():
     b = _hierarchies(s[1:], lina.PREC_FP64, [int(g[f"{NAMES[1]}_depth"])])
     with pytest.raises(lina.LinaError):
         lina.SegmentedBatch(a + b)
+
+
+@pytest.mark.gpu
+@gpu
+def test_segbatch_grouped_fused_steps_match_colour_launches():
+    """The concatenated small levels run the cluster-fused multicolour-SOR step, one cluster per group of
+    whole systems.  Its sweeps compute every row as the colour launches do; its residual and transfers
+    sum each row in lane-group order, where the separate FP32 launches on levels of 20,000 rows or more
+    read the quad layout (stored order), so the solves agree to rounding: the same iteration counts, both
+    meeting the rule, solutions within 1e-6 of each other."""
+    plan = problems.batch_plan(count=12, seed=3, lo=10_000, hi=80_000)
+    systems = [problems.batch_system(*p) for p in plan]
+    amgs = _hierarchies(systems, lina.PREC_MIXED, smoother=lina.SMOOTHER_MC_SOR, omega=1.0, matrix_tol=0.3)
+    lina.set_fused_groups(True)
+    try:
+        on = lina.SegmentedBatch(amgs)
+    finally:
+        lina.set_fused_groups(False)
+    lina.set_fused_rows(0)
+    try:
+        off = lina.SegmentedBatch(amgs)
+    finally:
+        lina.set_fused_rows(lina.FUSED_ROWS_DEFAULT)
+    bs = [s.b for s in systems]
+    x1, i1 = on.solve(bs, tol=1e-8, max_iter=1000)
+    lina.set_fused_rows(0)
+    try:
+        x2, i2 = off.solve(bs, tol=1e-8, max_iter=1000)
+    finally:
+        lina.set_fused_rows(lina.FUSED_ROWS_DEFAULT)
+    for a, b, p, q in zip(x1, x2, i1, i2):
+        assert p.status == 0 and q.status == 0 and p.true_rel_residual <= 1e-8 and q.true_rel_residual <= 1e-8
+        assert p.iterations == q.iterations
+        assert rel(a, b) <= 1e-6
