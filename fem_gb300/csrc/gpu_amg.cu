@@ -53,6 +53,9 @@ long g_fused_jacobi_entries = 0;
 // of whole systems; off by default.  Measured on the 96-system workload (GB300): 803 ms per batch solve
 // with it against 714 ms with one launch per colour (a group's sweeps run on one cluster's 16 SMs).
 int g_fused_groups = 0;
+// per-level layout autotuning at upload (lina_gpu_set_autotune) for hierarchies created afterwards;
+// segmented batches always tune their concatenated levels
+int g_autotune = 0;
 // 16: SELL-32 matrices with long rows uploaded afterwards also get 16-bit column offsets (two bases
 // per slice, where every slice's columns fit), read by FP32 passes; 32: int columns only
 int g_sell_bits = 16;
@@ -1666,6 +1669,11 @@ struct lina_gpu_amg {
     std::vector<long> seg_max_rows;
     std::vector<std::vector<int>> seg_off;  // per level, the first row of each system (and the end)
     long lanes_rows = 0;
+    // layout autotuning: on for this hierarchy, the lanes per row forced on the next uploads (-1: the
+    // rule), and per level the choice made (-1: not tuned), kept for later re-uploads (recompute)
+    bool autotune = false;
+    int force_lanes = -1;
+    std::vector<int> tuned_lanes;
     // lina_gpu_amg_recompute: per level, where each CSR entry of A sits in the device layouts (natural,
     // quads, colour-grouped) and a fingerprint of A's pattern, kept from the first recompute on so that
     // later ones with the same patterns only move values
@@ -1778,9 +1786,11 @@ struct lina_gpu_amg {
             return LINA_GPU_EINVAL;
         }
         // a level of a segmented batch takes the layout of its largest system's level (lanes_rows rows):
-        // concatenated small levels keep the lane groups their long rows need
-        d.lanes = lanes_rows > 0 ? csrv_lanes_for_shape(std::min<long>(lanes_rows, c.n), c.n > 0 ? double(c.nnz()) / c.n : 0.0)
-                                 : csrv_lanes_for(c);
+        // concatenated small levels keep the lane groups their long rows need; an autotuned level the
+        // layout measured fastest (force_lanes)
+        d.lanes = force_lanes >= 0 ? force_lanes
+                  : lanes_rows > 0 ? csrv_lanes_for_shape(std::min<long>(lanes_rows, c.n), c.n > 0 ? double(c.nnz()) / c.n : 0.0)
+                                   : csrv_lanes_for(c);
         if (d.lanes > 0) {
             // CSR-vector: sanitise placeholder columns outside the operand, keep the CSR arrays
             std::vector<int> colc(c.col);
@@ -2565,6 +2575,84 @@ int build_fused_groups(lina_gpu_amg* h, int l, const lina::HostLevel& hl,
     return 0;
 }
 
+// Layout autotuning of one level: the level's matrix uploaded in each candidate layout (one thread per
+// row, i.e. SELL-32 and for FP32 the quad layout; or 4, 8 or 16 lanes per row), timed with CUDA events
+// over 5 smoother sweeps plus a residual in the hierarchy's precision (multicolour SOR: every colour of
+// a sweep), after 2 untimed sweeps; the fastest is kept.  The temporary uploads are released.
+template <typename TX>
+int autotune_level(lina_gpu_amg* h, const lina::HostLevel& hl, int l, const std::vector<std::vector<int>>& colours,
+                   int* best_out) {
+    const int n = hl.A.n;
+    const bool sor = h->opt.smoother == LINA_SMOOTHER_MC_SOR;
+    const size_t mark = h->allocations.size();
+    const long mark_bytes = h->dev_bytes;
+    int rc = 0;
+    TX *x = nullptr, *y = nullptr, *b = nullptr, *dv = nullptr;
+    std::vector<double> d64;
+    level_dinv(hl, l, d64);
+    std::vector<TX> dinv(d64.begin(), d64.end()), ones(n, TX(1));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    float best_ms = 0.f;
+    int best = -1;
+    const TX w = TX(h->opt.omega);
+    std::string report;
+    if ((rc = h->alloc(&x, n)) || (rc = h->alloc(&y, n)) || (rc = h->upload(&b, ones.data(), ones.size())) ||
+        (rc = h->upload(&dv, dinv.data(), dinv.size())))
+        goto done;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        rc = LINA_GPU_ECUDA;
+        goto done;
+    }
+    for (int cand : {0, 4, 8, 16}) {
+        DCsr A, Ac;
+        h->force_lanes = cand;
+        rc = h->upload_csr(A, hl.A);
+        if (!rc && sor) rc = h->upload_csr(Ac, hl.A, &colours);
+        h->force_lanes = -1;
+        if (rc) goto done;
+        CK(cudaMemsetAsync(x, 0, (size_t)n * sizeof(TX), h->stream));
+        auto sweep = [&]() {
+            if (sor) {
+                for (int c = 0; c < (int)colours.size(); c++) h->csr_group<TX, M_SOR>(Ac, c, x, x, b, dv, w);
+            } else {
+                h->csr<TX, M_JACOBI>(A, x, y, b, dv, w);
+                std::swap(x, y);
+            }
+        };
+        for (int k = 0; k < 2; k++) sweep();
+        cudaEventRecord(e0, h->stream);
+        for (int k = 0; k < 5; k++) sweep();
+        h->csr<TX, M_RESID>(A, x, y, b);
+        cudaEventRecord(e1, h->stream);
+        if (cudaEventSynchronize(e1) != cudaSuccess) {
+            rc = LINA_GPU_ECUDA;
+            goto done;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        char buf[64];
+        snprintf(buf, sizeof buf, " %s %.1f us", cand ? (std::to_string(cand) + " lanes").c_str() : "one thread",
+                 ms * 1e3 / 5);
+        report += buf;
+        if (best < 0 || ms < best_ms) {
+            best_ms = ms;
+            best = cand;
+        }
+    }
+    if (getenv("LINA_SETUP_TIMING"))
+        fprintf(stderr, "autotune level %d (%d rows, %ld entries):%s per sweep -> %s\n", l, n, (long)hl.A.nnz(),
+                report.c_str(), best ? (std::to_string(best) + " lanes").c_str() : "one thread");
+done:
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaStreamSynchronize(h->stream);
+    for (size_t k = mark; k < h->allocations.size(); k++) cudaFree(h->allocations[k]);
+    h->allocations.resize(mark);
+    h->dev_bytes = mark_bytes;
+    if (!rc) *best_out = best;
+    return rc;
+}
+
 int upload_hierarchy(lina_gpu_amg* h) {
     lina::HostHierarchy& H = h->host;
     const int depth = h->depth;
@@ -2575,6 +2663,29 @@ int upload_hierarchy(lina_gpu_amg* h) {
         DLevel& L = h->lv[l];
         L.n = hl.A.n;
         h->lanes_rows = h->seg_max_rows.empty() ? 0 : h->seg_max_rows[l];
+        // layout autotuning of the levels below the finest (their choice is kept for re-uploads)
+        // (levels of more than 50M entries, and the finest level, keep the rule: one thread per row, and
+        // their candidate uploads would cost seconds.  Measured on the 96-system segmented batch: its
+        // levels of 100M and 153M entries time fastest with one thread per row, as the rule chooses, and
+        // tuning them doubled the batch's creation time, 9 s to 18 s)
+        if (h->autotune && l > 0 && l < depth - 1 && hl.A.n >= 2000 && hl.A.nnz() <= 50000000L) {
+            if ((int)h->tuned_lanes.size() != depth) h->tuned_lanes.assign(depth, -1);
+            if (h->tuned_lanes[l] < 0) {
+                std::vector<int> colour;
+                std::vector<std::vector<int>> cgroups;
+                if (h->opt.smoother == LINA_SMOOTHER_MC_SOR) {
+                    const int nc = lina::greedy_colouring(hl.A, colour);
+                    cgroups.assign(nc, std::vector<int>());
+                    for (int i = 0; i < L.n; i++) cgroups[colour[i]].push_back(i);
+                }
+                int best = -1;
+                rc = h->opt.precision == LINA_PREC_MIXED ? autotune_level<float>(h, hl, l, cgroups, &best)
+                                                         : autotune_level<double>(h, hl, l, cgroups, &best);
+                if (rc) return rc;
+                h->tuned_lanes[l] = best;
+            }
+        }
+        h->force_lanes = ((int)h->tuned_lanes.size() == depth) ? h->tuned_lanes[l] : -1;
         std::vector<int> posA, posQ, posC;
         if ((rc = h->upload_csr(L.A, hl.A, nullptr, h->keep_maps ? &posA : nullptr, h->keep_maps ? &posQ : nullptr)))
             return rc;
@@ -2584,8 +2695,11 @@ int upload_hierarchy(lina_gpu_amg* h) {
         if ((rc = h->upload(&L.dinv64, dinv.data(), dinv.size()))) return rc;
         if ((rc = h->upload(&L.dinv32, dinv32.data(), dinv32.size()))) return rc;
         if (l > 0) {
+            const int tuned = h->force_lanes;  // the autotuned layout is A's (and its colour-grouped copy's)
+            h->force_lanes = -1;
             if ((rc = h->upload_csr(L.P, hl.P))) return rc;
             if ((rc = h->upload_csr(L.R, hl.R))) return rc;
+            h->force_lanes = tuned;
             std::vector<int> colour;
             L.ncolours = lina::greedy_colouring(hl.A, colour);
             std::vector<std::vector<int>> groups(L.ncolours);
@@ -2613,6 +2727,7 @@ int upload_hierarchy(lina_gpu_amg* h) {
             M.nnz = nnz;
             CK(cudaStreamSynchronize(h->stream));  // the host maps go out of scope
         }
+        h->force_lanes = -1;
         // work vectors
         if ((rc = h->alloc(&L.x64, L.n))) return rc;
         if ((rc = h->alloc(&L.t64, L.n))) return rc;
@@ -2784,6 +2899,11 @@ int lina_gpu_set_fused_rows(int max_rows) {
     return 0;
 }
 
+int lina_gpu_set_autotune(int on) {
+    g_autotune = on ? 1 : 0;
+    return 0;
+}
+
 int lina_gpu_set_fused_groups(int on) {
     g_fused_groups = on ? 1 : 0;
     return 0;
@@ -2870,6 +2990,7 @@ static int amg_create_impl(int n, const int* rowptr, const int* col, const doubl
     }
     *out = nullptr;
     lina_gpu_amg* h = new lina_gpu_amg();
+    h->autotune = g_autotune != 0;
     h->opt = *opt;
     h->depth = opt->depth;
     lina::AmgParams p;
@@ -2950,6 +3071,7 @@ int lina_gpu_amg_load(const char* dir, const lina_gpu_amg_options* opt, int host
     }
     *out = nullptr;
     lina_gpu_amg* h = new lina_gpu_amg();
+    h->autotune = g_autotune != 0;
     if (!lina::amg_load_host(dir, h->host, host_only ? 0 : g_coarse_device_rows)) {
         set_err("AMG load: %s", h->host.error.c_str());
         delete h;
@@ -4613,6 +4735,7 @@ int lina_gpu_segbatch_create(int count, lina_gpu_amg* const* systems, lina_gpu_s
         for (int i = 0; i < count; i++)
             c->seg_max_rows[l] = std::max<long>(c->seg_max_rows[l], map.off[l][i + 1] - map.off[l][i]);
     c->seg_off = map.off;
+    c->autotune = true;  // the concatenated levels' layouts are measured
     c->fcg_m = s0->fcg_m;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete B;

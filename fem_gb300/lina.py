@@ -139,6 +139,7 @@ def lib():
         "lina_gpu_set_fused_rows": (C.c_int, [C.c_int]),
         "lina_gpu_set_fused_jacobi_entries": (C.c_int, [C.c_long]),
         "lina_gpu_set_fused_groups": (C.c_int, [C.c_int]),
+        "lina_gpu_set_autotune": (C.c_int, [C.c_int]),
         "lina_gpu_set_sell_index_bits": (C.c_int, [C.c_int]),
         "lina_gpu_set_sell_quads": (C.c_int, [C.c_int]),
         "lina_gpu_set_pdl": (C.c_int, [C.c_int]),
@@ -305,6 +306,11 @@ def set_fused_rows(max_rows: int):
     """Levels of at most max_rows rows run a multicolour-SOR V-cycle step as one cluster launch
     (0: one launch per colour)."""
     _check(lib().lina_gpu_set_fused_rows(int(max_rows)), "set fused rows")
+
+
+def set_autotune(on: bool):
+    """Hierarchies created afterwards measure each level's candidate layouts at upload and keep the fastest."""
+    _check(lib().lina_gpu_set_autotune(int(bool(on))), "set autotune")
 
 
 def set_fused_groups(on: bool):

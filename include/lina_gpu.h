@@ -442,6 +442,13 @@ int lina_gpu_set_fused_jacobi_entries(long max_entries);
    transfers sum rows in lane-group order (separate FP32 launches on levels of 20,000 rows or more use the
    quad layout's stored order), so results agree to rounding. */
 int lina_gpu_set_fused_groups(int on);
+/* hierarchies created (or loaded) afterwards time every level below the finest (at least 2,000 rows,
+   at most 50M stored entries) in
+   each candidate layout at upload (one thread per row, or 4, 8 or 16 lanes per row), 5 smoother sweeps
+   plus a residual in their precision, and keep the fastest (default 0 = the fixed layout rule; segmented
+   batches always tune).  The choice depends on timings, so two hierarchies of one matrix may differ in
+   layout and hence in rounding.  LINA_SETUP_TIMING prints the times. */
+int lina_gpu_set_autotune(int on);
 /* 16 (default): SELL-32 matrices with long rows (at least 24 stored entries per row on average)
    uploaded afterwards also get 16-bit column indices, a 15-bit offset from one of two bases per
    slice of 32 rows, where every slice's columns fit two such windows; FP32 passes read those (2

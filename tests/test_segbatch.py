@@ -136,3 +136,25 @@ def test_segbatch_grouped_fused_steps_match_colour_launches():
         assert p.status == 0 and q.status == 0 and p.true_rel_residual <= 1e-8 and q.true_rel_residual <= 1e-8
         assert p.iterations == q.iterations
         assert rel(a, b) <= 1e-6
+
+
+@pytest.mark.gpu
+@gpu
+@pytest.mark.parametrize("smoother,omega", [(lina.SMOOTHER_JACOBI, 0.6), (lina.SMOOTHER_MC_SOR, 1.0)])
+def test_autotuned_hierarchy_solves(smoother, omega):
+    """A hierarchy whose level layouts were measured at upload (lina_gpu_set_autotune) solves to the
+    rule, with the iteration count of the rule-chosen layouts within 1."""
+    s = problems.elasticity_p1(129)
+    res = []
+    for tune in (True, False):
+        lina.set_autotune(tune)
+        try:
+            a = lina.AMG.from_system(s, depth=6, coarsening=lina.STANDARD, smoother=smoother, omega=omega,
+                                     precision=lina.PREC_MIXED)
+        finally:
+            lina.set_autotune(False)
+        res.append(a.pcg(s.b, tol=1e-8, max_iter=500))
+    (x1, i1), (x2, i2) = res
+    assert i1.status == 0 and i1.true_rel_residual <= 1e-8
+    assert abs(i1.iterations - i2.iterations) <= 1
+    assert rel(x1, x2) <= 1e-6
