@@ -2598,6 +2598,10 @@ int autotune_level(lina_gpu_amg* h, const lina::HostLevel& hl, int l, const std:
     int best = -1;
     const TX w = TX(h->opt.omega);
     std::string report;
+    const int rule = h->lanes_rows > 0 ? csrv_lanes_for_shape(std::min<long>(h->lanes_rows, n),
+                                                               n > 0 ? double(hl.A.nnz()) / n : 0.0)
+                                        : csrv_lanes_for(hl.A);
+    float rule_ms = 0.f;
     if ((rc = h->alloc(&x, n)) || (rc = h->alloc(&y, n)) || (rc = h->upload(&b, ones.data(), ones.size())) ||
         (rc = h->upload(&dv, dinv.data(), dinv.size())))
         goto done;
@@ -2605,10 +2609,6 @@ int autotune_level(lina_gpu_amg* h, const lina::HostLevel& hl, int l, const std:
         rc = LINA_GPU_ECUDA;
         goto done;
     }
-    const int rule = h->lanes_rows > 0 ? csrv_lanes_for_shape(std::min<long>(h->lanes_rows, n),
-                                                               n > 0 ? double(hl.A.nnz()) / n : 0.0)
-                                        : csrv_lanes_for(hl.A);
-    float rule_ms = 0.f;
     for (int cand : {0, 4, 8, 16}) {
         DCsr A, Ac;
         h->force_lanes = cand;
