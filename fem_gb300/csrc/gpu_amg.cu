@@ -248,13 +248,16 @@ __device__ __forceinline__ int sell_col(unsigned short d, int2 base) {
     return ((d & 0x8000u) ? base.y : base.x) + (int)(d & 0x7fffu);
 }
 
+// rowseg / act (segmented batches, else null): the system of every row and whether it is still iterating;
+// the rows of systems that have stopped are skipped (their values are not used any more)
 template <typename TV, typename TX, int MODE, bool LONG, typename TI>
 __global__ void __launch_bounds__(kThreads) sell_kernel(int npos, int nrows, const int* __restrict__ rowmap,
                                                         const int* __restrict__ sptr, const int2* __restrict__ sbase,
                                                         const TI* __restrict__ col, const TV* __restrict__ val,
                                                         const TX* x, TX* y, const TX* __restrict__ b,
                                                         const TX* __restrict__ dinv, TX w, const TX* z,
-                                                        double* partials, unsigned* ticket, KScalars* sc) {
+                                                        double* partials, unsigned* ticket, KScalars* sc,
+                                                        const int* __restrict__ rowseg, const int* __restrict__ act) {
     pdl_wait();
     double dot = 0.0;
     // grid-stride over slice positions (npos is a multiple of 32, so warps stay whole); positions
@@ -262,6 +265,7 @@ __global__ void __launch_bounds__(kThreads) sell_kernel(int npos, int nrows, con
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < npos; t += gridDim.x * blockDim.x) {
         const int i = rowmap ? rowmap[t] : t;
         if (i < 0 || i >= nrows) continue;
+        if (rowseg && !act[rowseg[i]]) continue;
         const int sl = t >> 5, lane = t & 31;
         const int p0 = sptr[sl];
         const int len = (sptr[sl + 1] - p0) >> 5;
@@ -374,12 +378,14 @@ __global__ void __launch_bounds__(kThreads, 5) sellq_kernel(int n, const int* __
                                                             const float4* __restrict__ val4, const float* x,
                                                             float* y, const float* __restrict__ b,
                                                             const float* __restrict__ dinv, float w,
-                                                            const float* z) {
+                                                            const float* z, const int* __restrict__ rowseg,
+                                                            const int* __restrict__ act) {
     pdl_wait();
     const int npos = ((n + 31) >> 5) << 5;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < npos; t += gridDim.x * blockDim.x) {
         const int i = t;
         if (i >= n) continue;
+        if (rowseg && !act[rowseg[i]]) continue;  // a stopped system of a segmented batch
         const int sl = t >> 5, lane = t & 31;
         const int g0 = sptr[sl] >> 2;
         const int ng = (sptr[sl + 1] - sptr[sl]) >> 7;  // groups of four per row
@@ -1314,6 +1320,10 @@ struct DCsr {
     double* v64 = nullptr;
     float* v32 = nullptr;
     int* rowmap = nullptr;          // row of each position (-1 = padding), null = natural order
+    // segmented batches: the system of every row and the per-system iterating flags (rows of stopped
+    // systems are skipped by the row-per-thread kernels while mask_rows is set), else null
+    const int* rowseg = nullptr;
+    const int* act = nullptr;
     // SELL-32 in quads with 16-bit offsets (sellq_kernel), for the FP32 passes in natural order; null
     // when the matrix is colour-grouped, uses the lane-group layout, or a slice's columns do not fit
     int* q_sptr = nullptr;
@@ -1672,6 +1682,7 @@ struct lina_gpu_amg {
     // layout autotuning: on for this hierarchy, the lanes per row forced on the next uploads (-1: the
     // rule), and per level the choice made (-1: not tuned), kept for later re-uploads (recompute)
     bool autotune = false;
+    bool mask_rows = false;  // the segmented iteration: skip the rows of systems that have stopped
     int force_lanes = -1;
     std::vector<int> tuned_lanes;
     // lina_gpu_amg_recompute: per level, where each CSR entry of A sits in the device layouts (natural,
@@ -1922,26 +1933,29 @@ struct lina_gpu_amg {
                 g_launches--;  // counted by launch()
                 launch(sellq_kernel<MODE>, dim3(grid), dim3(kThreads), 0, stream, m.n, (const int*)m.q_sptr,
                        (const int2*)m.q_base, (const uint2*)m.q_col, (const float4*)m.q_val, (const float*)x,
-                       (float*)y, (const float*)b, (const float*)dinv, (float)w, (const float*)z);
+                       (float*)y, (const float*)b, (const float*)dinv, (float)w, (const float*)z,
+                       mask_rows ? m.rowseg : (const int*)nullptr, m.act);
                 return;
             }
         }
         g_launches--;  // counted by launch()
         const dim3 gd(grid), bd(kThreads);
+        // row indices of a natural-order range start at 32 slice0; of the colour order, they are global
+        const int* rseg = (mask_rows && m.rowseg) ? (rm ? m.rowseg : m.rowseg + (size_t)32 * slice0) : nullptr;
         if (sizeof(TX) == 4 && m.col16) {
             const int2* sb = m.sbase + slice0;
             if (m.long_rows)
                 launch(sell_kernel<TV, TX, MODE, true, unsigned short>, gd, bd, 0, stream, npos, nrows, rm, sp, sb,
-                       (const unsigned short*)m.col16, val, x, y, b, dinv, w, z, partials, ticket, sc);
+                       (const unsigned short*)m.col16, val, x, y, b, dinv, w, z, partials, ticket, sc, rseg, m.act);
             else
                 launch(sell_kernel<TV, TX, MODE, false, unsigned short>, gd, bd, 0, stream, npos, nrows, rm, sp, sb,
-                       (const unsigned short*)m.col16, val, x, y, b, dinv, w, z, partials, ticket, sc);
+                       (const unsigned short*)m.col16, val, x, y, b, dinv, w, z, partials, ticket, sc, rseg, m.act);
         } else if (m.long_rows) {
             launch(sell_kernel<TV, TX, MODE, true, int>, gd, bd, 0, stream, npos, nrows, rm, sp, (const int2*)nullptr,
-                   (const int*)m.col, val, x, y, b, dinv, w, z, partials, ticket, sc);
+                   (const int*)m.col, val, x, y, b, dinv, w, z, partials, ticket, sc, rseg, m.act);
         } else {
             launch(sell_kernel<TV, TX, MODE, false, int>, gd, bd, 0, stream, npos, nrows, rm, sp, (const int2*)nullptr,
-                   (const int*)m.col, val, x, y, b, dinv, w, z, partials, ticket, sc);
+                   (const int*)m.col, val, x, y, b, dinv, w, z, partials, ticket, sc, rseg, m.act);
         }
         if (MODE == M_DOT) launch(dot_finish_kernel, dim3(1), dim3(1024), 0, stream, grid, (const double*)partials, sc);
     }
@@ -1956,7 +1970,8 @@ struct lina_gpu_amg {
                 const int grid = (((m.n + 31) / 32) * 32 + kThreads - 1) / kThreads;
                 launch(sellq_kernel<MODE>, dim3(grid), dim3(kThreads), 0, stream, m.n, (const int*)m.q_sptr,
                        (const int2*)m.q_base, (const uint2*)m.q_col, (const float4*)m.q_val, (const float*)x,
-                       (float*)y, (const float*)b, (const float*)dinv, (float)w, (const float*)z);
+                       (float*)y, (const float*)b, (const float*)dinv, (float)w, (const float*)z,
+                       mask_rows ? m.rowseg : (const int*)nullptr, m.act);
                 return;
             }
         }
@@ -4404,7 +4419,7 @@ __global__ void __launch_bounds__(kThreads) seg_update_xr_kernel(int ntask, cons
 template <int MODE, int M>
 __global__ void __launch_bounds__(1024) seg_finish_kernel(int S, const int* __restrict__ tbeg,
                                                           const double* __restrict__ part, SegScalars* sc,
-                                                          cudaGraphConditionalHandle hd, int set_cond) {
+                                                          cudaGraphConditionalHandle hd, int set_cond, int* act) {
     pdl_wait();
     constexpr int W = (MODE == SEG_DOT) ? M + 1 : 1;
     __shared__ int any;
@@ -4453,6 +4468,7 @@ __global__ void __launch_bounds__(1024) seg_finish_kernel(int S, const int* __re
                 }
             }
             mine |= c.active;
+            act[s] = c.active;
         } else if constexpr (MODE == SEG_NORM_B) {
             c.r0 = sqrt(tot[0]);
             c.rr = tot[0];
@@ -4462,6 +4478,7 @@ __global__ void __launch_bounds__(1024) seg_finish_kernel(int S, const int* __re
             c.s = 0.0;
             c.active = (c.r0 > 0.0 && isfinite(c.r0) && c.maxit > 0) ? 1 : 0;
             mine |= c.active;
+            act[s] = c.active;
         } else {
             c.tnorm2 = tot[0];
         }
@@ -4597,6 +4614,7 @@ struct lina_gpu_segbatch {
     int* tbeg = nullptr;            // tasks of system i: [tbeg[i], tbeg[i+1])
     double* part = nullptr;         // ntask x (M + 1)
     SegScalars* sc = nullptr;       // device, one per system
+    int* act = nullptr;             // device, one per system: still iterating (the row masks read it)
     SegScalars* sc_host = nullptr;  // pinned
     int m = 1;                      // FCG history
     cudaGraphExec_t exec = nullptr;
@@ -4627,7 +4645,7 @@ void seg_issue_iteration(lina_gpu_segbatch* B, cudaGraphConditionalHandle hd, in
         go(seg_fcg_dot_kernel<double, M>, gt, st, B->ntask, (const int4*)B->task, n, (const double*)h->kr,
            (const double*)h->kz, (const double*)h->kqh, (const SegScalars*)B->sc, B->part);
     launch(seg_finish_kernel<SEG_DOT, M>, dim3(1), dim3(1024), 0, st, S, (const int*)B->tbeg,
-           (const double*)B->part, B->sc, hd, 0);
+           (const double*)B->part, B->sc, hd, 0, B->act);
     if (mixed)
         go(seg_fcg_update_p_kernel<float, M>, gt, st, B->ntask, (const int4*)B->task, n, (const float*)h->kz32,
            (const double*)h->kph, h->kp, (const SegScalars*)B->sc);
@@ -4637,11 +4655,11 @@ void seg_issue_iteration(lina_gpu_segbatch* B, cudaGraphConditionalHandle hd, in
     h->csr<double, M_SPMV>(h->krylov_matrix(), h->kp, h->kq);
     go(seg_dot_kernel, gt, st, B->ntask, (const int4*)B->task, (const double*)h->kp, (const double*)h->kq, B->part);
     launch(seg_finish_kernel<SEG_PQ, M>, dim3(1), dim3(1024), 0, st, S, (const int*)B->tbeg, (const double*)B->part,
-           B->sc, hd, 0);
+           B->sc, hd, 0, B->act);
     go(seg_update_xr_kernel<M>, gt, st, B->ntask, (const int4*)B->task, n, h->kx, h->kr, (const double*)h->kp,
        (const double*)h->kq, h->kph, h->kqh, (const SegScalars*)B->sc, B->part);
     launch(seg_finish_kernel<SEG_RR, M>, dim3(1), dim3(1024), 0, st, S, (const int*)B->tbeg, (const double*)B->part,
-           B->sc, hd, set_cond);
+           B->sc, hd, set_cond, B->act);
 }
 
 void seg_issue(lina_gpu_segbatch* B, cudaGraphConditionalHandle hd, int set_cond) {
@@ -4681,7 +4699,9 @@ int seg_build_graph(lina_gpu_segbatch* B) {
         return LINA_GPU_ECUDA;
     }
     const unsigned long long before = g_launches;
+    h->mask_rows = true;
     seg_issue(B, hd, 1);
+    h->mask_rows = false;
     B->k_iter = (long)(g_launches - before);
     g_launches = before;
     cudaGraph_t body = nullptr;
@@ -4703,7 +4723,7 @@ void seg_norms(lina_gpu_segbatch* B, const double* v) {
     const int gt = std::min(B->ntask, kGridCap);
     go(seg_dot_kernel, gt, h->stream, B->ntask, (const int4*)B->task, v, v, B->part);
     launch(seg_finish_kernel<MODE, 1>, dim3(1), dim3(1024), 0, h->stream, (int)B->sys.size(), (const int*)B->tbeg,
-           (const double*)B->part, B->sc, (cudaGraphConditionalHandle)0, 0);
+           (const double*)B->part, B->sc, (cudaGraphConditionalHandle)0, 0, B->act);
 }
 
 }  // namespace
@@ -4773,10 +4793,27 @@ int lina_gpu_segbatch_create(int count, lina_gpu_amg* const* systems, lina_gpu_s
     }
     B->ntask = (int)tasks.size();
     if ((rc = c->upload(&B->task, tasks.data(), tasks.size())) || (rc = c->upload(&B->tbeg, tbeg.data(), tbeg.size())) ||
-        (rc = c->alloc(&B->part, (size_t)B->ntask * (kFcgMax + 1))) || (rc = c->alloc(&B->sc, count))) {
+        (rc = c->alloc(&B->part, (size_t)B->ntask * (kFcgMax + 1))) || (rc = c->alloc(&B->sc, count)) ||
+        (rc = c->alloc(&B->act, count))) {
         delete B;
         return rc;
     }
+    // the system of every row of every level, for the row masks of the iteration
+    for (int l = 0; l < c->depth; l++) {
+        std::vector<int> seg(map.off[l][count]);
+        for (int i = 0; i < count; i++)
+            for (int r = map.off[l][i]; r < map.off[l][i + 1]; r++) seg[r] = i;
+        int* d = nullptr;
+        if ((rc = c->upload(&d, seg.data(), seg.size()))) {
+            delete B;
+            return rc;
+        }
+        DLevel& L = c->lv[l];
+        L.A.rowseg = L.Acol.rowseg = L.P.rowseg = d;
+        L.A.act = L.Acol.act = L.P.act = L.R.act = B->act;
+        if (l + 1 < c->depth) c->lv[l + 1].R.rowseg = d;  // R of level l+1 has level l's rows
+    }
+    CK(cudaMemsetAsync(B->act, 0, count * sizeof(int), c->stream));
     if (cudaMallocHost((void**)&B->sc_host, count * sizeof(SegScalars)) != cudaSuccess) {
         delete B;
         set_err("cudaMallocHost failed");
@@ -4827,7 +4864,9 @@ int lina_gpu_segbatch_solve(lina_gpu_segbatch* B, const double* const* b, double
     for (;;) {
         if (host_loop) {  // iteration by iteration from the host (kernels visible to a profiler)
             for (int it = 0; it < max_iter; it++) {
+                h->mask_rows = true;
                 seg_issue(B, (cudaGraphConditionalHandle)0, 0);
+                h->mask_rows = false;
                 CK(cudaMemcpyAsync(B->sc_host, B->sc, S * sizeof(SegScalars), cudaMemcpyDeviceToHost, st));
                 CK(cudaStreamSynchronize(st));
                 bool any = false;
@@ -4864,6 +4903,10 @@ int lina_gpu_segbatch_solve(lina_gpu_segbatch* B, const double* const* b, double
         if (!again) break;
         rounds++;
         CK(cudaMemcpyAsync(B->sc, B->sc_host, S * sizeof(SegScalars), cudaMemcpyHostToDevice, st));
+        std::vector<int> act_host(S);
+        for (int i = 0; i < S; i++) act_host[i] = B->sc_host[i].active;
+        CK(cudaMemcpyAsync(B->act, act_host.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));  // act_host goes out of scope
     }
     for (int i = 0; i < S; i++)
         CK(cudaMemcpyAsync(x[i], h->kx + B->off[i], (size_t)(B->off[i + 1] - B->off[i]) * sizeof(double),
