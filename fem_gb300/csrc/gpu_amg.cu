@@ -1001,7 +1001,19 @@ template <typename TX>
 __device__ __forceinline__ void broadcast_x(TX* xs, int i, TX v, int sub, int S, int off = 0) {
     const cg::cluster_group cl = cg::this_cluster();
     const int K = (int)cl.num_blocks();
+    if (K == 1) {
+        if (sub == 0) xs[i - off] = v;
+        return;
+    }
     for (int r = sub; r < K; r += S) cl.map_shared_rank(xs, (unsigned)r)[i - off] = v;
+}
+
+// the barrier between phases of a fused step: a block barrier where the cluster is one block
+__device__ __forceinline__ void fused_sync(const cg::cluster_group& cl) {
+    if (cl.num_blocks() == 1)
+        __syncthreads();
+    else
+        cl.sync();
 }
 
 // sum_k val_k v_col_k over one row by a group of S lanes (the order of csrv_kernel); the butterfly
@@ -1189,8 +1201,12 @@ __device__ __forceinline__ void fused_sweeps(const FusedStep& st, TX* xs, const 
             fetch_sweep_row<TX>(q, g < r1, g, sub, S, st, sval, b, dinv);
             sweep_fetched_row<TX>(q, g < r1, sub, S, w, st, sval, xs, off);
         }
-        cluster_arrive();
-        cluster_wait();
+        if (cl.num_blocks() == 1) {
+            __syncthreads();
+        } else {
+            cluster_arrive();
+            cluster_wait();
+        }
         cur = nxt;
         r0 = n0;
         r1 = n1;
@@ -1213,7 +1229,7 @@ __device__ __forceinline__ TX* fused_jacobi_sweeps(const FusedStep& st, int nu, 
                        [&](int i, TX sum, int sub) {
                            broadcast_x(nxt, i, cur[i] + w * __ldg(dinv + i) * (__ldg(b + i) - sum), sub, st.aS);
                        });
-        cl.sync();
+        fused_sync(cl);
         TX* t = cur;
         cur = nxt;
         nxt = t;
@@ -1239,7 +1255,7 @@ __global__ void __launch_bounds__(kFuseThreads, 1) fused_step_kernel(const Fused
         const TX w = TX(st.w);
         for (int j = (int)threadIdx.x; j < st.n; j += blockDim.x)
             xs[j] = PRE ? (st.nu > 0 ? w * __ldg(dinv + j) * __ldg(b + j) : TX(0)) : __ldcg(xg + j);
-        cl.sync();  // every block runs before any remote store
+        fused_sync(cl);  // every block runs before any remote store
         TX* res;
         if (PRE) {
             res = fused_jacobi_sweeps<TX>(st, st.nu > 0 ? st.nu - 1 : 0, xs, other, b, dinv);
@@ -1248,7 +1264,7 @@ __global__ void __launch_bounds__(kFuseThreads, 1) fused_step_kernel(const Fused
                            [&](int i, TX sum, int sub) {
                                if (sub == 0) r[i] = b[i] - sum;
                            });
-            cl.sync();
+            fused_sync(cl);
             TX* cb = (TX*)st.cb;
             fused_rows<TX>(0, st.nc, st.rS, st.rptr, st.rcol, (const TX*)st.rval, GlobalRead<TX>{r},
                            [&](int i, TX sum, int sub) {
@@ -1257,14 +1273,14 @@ __global__ void __launch_bounds__(kFuseThreads, 1) fused_step_kernel(const Fused
         } else {
             fused_rows<TX>(0, st.n, st.pS, st.pptr, st.pcol, (const TX*)st.pval, GlobalRead<TX>{(const TX*)st.e},
                            [&](int i, TX sum, int sub) { broadcast_x(xs, i, xs[i] + sum, sub, st.pS); });
-            cl.sync();
+            fused_sync(cl);
             res = fused_jacobi_sweeps<TX>(st, st.nu, xs, other, b, dinv);
         }
         // the last sweep (or the start) ended with a cluster barrier: every copy of res is final
         const int chunk = (st.n + (int)cl.num_blocks() - 1) / (int)cl.num_blocks();
         const int lo = (int)cl.block_rank() * chunk, hi = min(st.n, lo + chunk);
         for (int j = lo + (int)threadIdx.x; j < hi; j += blockDim.x) xg[j] = res[j];
-        cl.sync();  // no block leaves while another may still store into its shared memory
+        fused_sync(cl);  // no block leaves while another may still store into its shared memory
         return;
     }
     // the cluster's rows: a group of whole systems (groups non-null), else the whole level
@@ -1280,7 +1296,7 @@ __global__ void __launch_bounds__(kFuseThreads, 1) fused_step_kernel(const Fused
     }
     const int nr = r1 - r0;
     for (int j = (int)threadIdx.x; j < nr; j += blockDim.x) xs[j] = PRE ? TX(0) : __ldcg(xg + r0 + j);
-    cl.sync();
+    fused_sync(cl);
     if (PRE) {
         fused_sweeps<TX>(st, xs, b, dinv, r0, granges);
         TX* r = (TX*)st.r;
@@ -1288,7 +1304,7 @@ __global__ void __launch_bounds__(kFuseThreads, 1) fused_step_kernel(const Fused
                        [&](int i, TX sum, int sub) {
                            if (sub == 0) r[i] = b[i] - sum;
                        });
-        cl.sync();
+        fused_sync(cl);
         TX* cb = (TX*)st.cb;
         fused_rows<TX>(c0, c1, st.rS, st.rptr, st.rcol, (const TX*)st.rval, GlobalRead<TX>{r},
                        [&](int i, TX sum, int sub) {
@@ -1297,14 +1313,197 @@ __global__ void __launch_bounds__(kFuseThreads, 1) fused_step_kernel(const Fused
     } else {
         fused_rows<TX>(r0, r1, st.pS, st.pptr, st.pcol, (const TX*)st.pval, GlobalRead<TX>{(const TX*)st.e},
                        [&](int i, TX sum, int sub) { broadcast_x(xs, i, xs[i - r0] + sum, sub, st.pS, r0); });
-        cl.sync();
+        fused_sync(cl);
         fused_sweeps<TX>(st, xs, b, dinv, r0, granges);
     }
     // the sweeps ended with a cluster barrier: every copy is final; each block writes its share
     const int chunk = (nr + (int)cl.num_blocks() - 1) / (int)cl.num_blocks();
     const int lo = (int)cl.block_rank() * chunk, hi = min(nr, lo + chunk);
     for (int j = lo + (int)threadIdx.x; j < hi; j += blockDim.x) xg[r0 + j] = xs[j];
-    cl.sync();  // no block leaves while another may still store into its shared memory
+    fused_sync(cl);  // no block leaves while another may still store into its shared memory
+}
+
+// ------------------------------------------------------------ staged fused steps
+// A fused step whose sweeps read nothing but shared memory.  At upload the level's rows are dealt to
+// the K blocks of a cluster colour by colour (each block takes a contiguous share of every colour's
+// rows) and each block's share is packed into two fixed-size images: ints (per colour the block's first
+// local position, then its rows, their entry offsets and their columns) and values (the rows' entries,
+// then omega / a_ii; gathered again on the device whenever the level's values or omega change).  A step
+// copies its block's images into shared memory with asynchronous copies issued before it waits for the
+// previous kernel, gathers b for its rows, and sweeps colour by colour from shared memory: the only
+// traffic of a colour is the new entries of x, stored into every block's copy, and a cluster barrier (a
+// block barrier where K is 1).  The pre-step's residual is summed from the images too where the natural
+// matrix has the same lane groups; restriction and prolongation read R, P and the vectors from global
+// memory as the unstaged step does.  Rows are summed by the lane groups and in the order of csrv_kernel,
+// so results are bit-identical to the per-colour launches.
+constexpr int kStagedSmemMax = 210 * 1024;
+
+struct StagedPlan {
+    const int* img;    // K int images of `ints` ints
+    const void* vals;  // K value images of `nvals` values (TX)
+    int ints, nvals;
+    int pslots;               // b slots (the largest share's positions, a multiple of 4)
+    int o_row, o_off, o_col;  // sections of an int image
+    int o_dinv;               // 1/a_ii in a value image
+    int xbytes;               // the copy of x, a multiple of 16 bytes
+};
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(smem)),
+                 "l"(gmem)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+// sum_k val_k x_col_k over entries [k0, k1) of the shared images by a group of S lanes, in the order of
+// csrv_kernel; the butterfly leaves the sum in every lane of the group
+template <typename TX>
+__device__ __forceinline__ TX staged_row_sum(bool valid, int k0, int k1, int sub, int S, const int* scol,
+                                             const TX* sv, const TX* xs) {
+    TX sum = TX(0);
+    if (valid) {
+        // eight, then four strides at a time: the loads of a batch are in flight together (the sums
+        // stay in order)
+        int k = k0 + sub;
+        for (; k + 7 * S < k1; k += 8 * S) {
+            int c[8];
+            TX v[8], x[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                c[j] = scol[k + j * S];
+                v[j] = sv[k + j * S];
+            }
+#pragma unroll
+            for (int j = 0; j < 8; j++) x[j] = xs[c[j]];
+#pragma unroll
+            for (int j = 0; j < 8; j++) sum += v[j] * x[j];
+        }
+        if (k + 3 * S < k1) {
+            const int c0 = scol[k], c1 = scol[k + S], c2 = scol[k + 2 * S], c3 = scol[k + 3 * S];
+            const TX v0 = sv[k], v1 = sv[k + S], v2 = sv[k + 2 * S], v3 = sv[k + 3 * S];
+            const TX x0 = xs[c0], x1 = xs[c1], x2 = xs[c2], x3 = xs[c3];
+            sum += v0 * x0;
+            sum += v1 * x1;
+            sum += v2 * x2;
+            sum += v3 * x3;
+            k += 4 * S;
+        }
+        for (; k < k1; k += S) sum += sv[k] * xs[scol[k]];
+    }
+    for (int o = S / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, S);
+    return sum;
+}
+
+// f(q, sum, sub) for every local position q of [q0, q1), called by every lane of its group.  Consecutive
+// positions share a warp: an FP64 instruction costs the SM's FP64 pipe the same with one active lane as
+// with 32, so rows are packed into as few warps as possible.
+template <typename TX, typename F>
+__device__ __forceinline__ void staged_rows(int q0, int q1, int S, const int* soff, const int* scol, const TX* sv,
+                                            const TX* xs, F f) {
+    const int lane = threadIdx.x & 31, sub = lane & (S - 1);
+    const int warp = (int)(threadIdx.x >> 5), nwarps = (int)(blockDim.x >> 5);
+    const int per_warp = 32 / S;
+    for (int qb = q0 + warp * per_warp; qb < q1; qb += nwarps * per_warp) {
+        const int q = qb + lane / S;
+        const bool valid = q < q1;
+        const TX sum = staged_row_sum<TX>(valid, valid ? soff[q] : 0, valid ? soff[q + 1] : 0, sub, S, scol, sv, xs);
+        if (valid) f(q, sum, sub);
+    }
+}
+
+template <typename TX, bool PRE>
+__global__ void __launch_bounds__(kFuseThreads, 1) staged_step_kernel(const FusedStep st, const StagedPlan sp) {
+    extern __shared__ __align__(16) unsigned char staged_smem[];
+    const cg::cluster_group cl = cg::this_cluster();
+    const int K = (int)cl.num_blocks(), rank = (int)cl.block_rank();
+    TX* xs = reinterpret_cast<TX*>(staged_smem);
+    TX* sv = reinterpret_cast<TX*>(staged_smem + sp.xbytes);
+    TX* sb = sv + sp.nvals;
+    int* si = reinterpret_cast<int*>(sb + sp.pslots);
+    {  // the block's images (static between value refreshes): copied while the previous kernel drains
+        const char* gi = reinterpret_cast<const char*>(sp.img + (long)rank * sp.ints);
+        const char* gv = reinterpret_cast<const char*>(static_cast<const TX*>(sp.vals) + (long)rank * sp.nvals);
+        const int ni = sp.ints / 4, nv = sp.nvals * (int)sizeof(TX) / 16;
+        for (int j = (int)threadIdx.x; j < ni; j += blockDim.x) cp_async16(reinterpret_cast<char*>(si) + 16 * j, gi + 16 * j);
+        for (int j = (int)threadIdx.x; j < nv; j += blockDim.x) cp_async16(reinterpret_cast<char*>(sv) + 16 * j, gv + 16 * j);
+    }
+    pdl_wait();
+    TX* xg = (TX*)st.x;
+    const TX* b = (const TX*)st.b;
+    for (int j = (int)threadIdx.x; j < st.n; j += blockDim.x) xs[j] = PRE ? TX(0) : __ldcg(xg + j);
+    cp_async_wait_all();
+    __syncthreads();
+    const int C = st.ncolours, P = si[C];
+    const int *srow = si + sp.o_row, *soff = si + sp.o_off, *scol = si + sp.o_col;
+    const TX* swdi = sv + sp.o_dinv;  // omega / a_ii
+    for (int q = (int)threadIdx.x; q < P; q += blockDim.x) sb[q] = __ldg(b + srow[q]);
+    fused_sync(cl);  // every copy of x is set before any remote store
+    if (!PRE) {
+        fused_rows<TX>(0, st.n, st.pS, st.pptr, st.pcol, (const TX*)st.pval, GlobalRead<TX>{(const TX*)st.e},
+                       [&](int i, TX sum, int sub) { broadcast_x(xs, i, xs[i] + sum, sub, st.pS); });
+        fused_sync(cl);
+    }
+    const int S = st.sS;
+    const int steps = st.nu * C;
+    for (int step = 0; step < steps; step++) {
+        const int c = step % C;
+        staged_rows<TX>(si[c], si[c + 1], S, soff, scol, sv, xs, [&](int q, TX sum, int sub) {
+            const int i = srow[q];
+            broadcast_x(xs, i, xs[i] + swdi[q] * (sb[q] - sum), sub, S);
+        });
+        fused_sync(cl);
+    }
+    if (PRE) {
+        TX* r = (TX*)st.r;
+        if (st.aS == S) {  // the natural matrix sums its rows in the same lane groups: from the images
+            staged_rows<TX>(0, P, S, soff, scol, sv, xs, [&](int q, TX sum, int sub) {
+                if (sub == 0) r[srow[q]] = sb[q] - sum;
+            });
+        } else {
+            fused_rows<TX>(0, st.n, st.aS, st.aptr, st.acol, (const TX*)st.aval, LocalRead<TX>{xs, 0},
+                           [&](int i, TX sum, int sub) {
+                               if (sub == 0) r[i] = b[i] - sum;
+                           });
+        }
+        fused_sync(cl);
+        TX* cb = (TX*)st.cb;
+        fused_rows<TX>(0, st.nc, st.rS, st.rptr, st.rcol, (const TX*)st.rval, GlobalRead<TX>{r},
+                       [&](int i, TX sum, int sub) {
+                           if (sub == 0) cb[i] = sum;
+                       });
+    }
+    // the sweeps ended with a barrier: every copy is final; each block writes its share
+    const int chunk = (st.n + K - 1) / K;
+    const int lo = rank * chunk, hi = min(st.n, lo + chunk);
+    for (int j = lo + (int)threadIdx.x; j < hi; j += blockDim.x) xg[j] = xs[j];
+    fused_sync(cl);  // no block leaves while another may still store into its shared memory
+}
+
+// the value images of a staged level from its colour-grouped matrix and 1/a_ii: src >= 0 an entry,
+// src <= -2 omega / a_ii of row -2 - src (the product the sweep forms first: w * dinv[i] * (b[i] - sum)
+// associates as (w * dinv[i]) * (...)), -1 padding
+__global__ void stage_gather_kernel(long n, const int* __restrict__ src, const double* __restrict__ a64,
+                                    const float* __restrict__ a32, const double* __restrict__ d64,
+                                    const float* __restrict__ d32, double w, double* __restrict__ o64,
+                                    float* __restrict__ o32) {
+    pdl_wait();
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int s = src[i];
+        double v = 0.0;
+        float f = 0.f;
+        if (s >= 0) {
+            v = a64[s];
+            f = a32[s];
+        } else if (s <= -2) {
+            v = w * d64[-2 - s];
+            f = float(w) * d32[-2 - s];
+        }
+        o64[i] = v;
+        o32[i] = f;
+    }
 }
 
 struct DCsr {
@@ -1601,6 +1800,14 @@ struct DLevel {
     // cluster per group of whole systems (ngroups > 0)
     int ngroups = 0, max_group_rows = 0;
     FusedGroup* d_groups = nullptr;
+    int fuse_k = 0;  // blocks per cluster of the level's fused step (0: the largest the GPU schedules)
+    // the staged fused step (stage_k blocks, 0: none); images as StagedPlan describes them
+    int stage_k = 0, stage_ints = 0, stage_nvals = 0, stage_pslots = 0;
+    int stage_o_row = 0, stage_o_off = 0, stage_o_col = 0, stage_o_dinv = 0;
+    int* stage_int = nullptr;
+    int* stage_src = nullptr;  // per value slot: the CSR entry, -2 - row for 1/a_ii, -1 padding
+    double* stage_v64 = nullptr;
+    float* stage_v32 = nullptr;
     double* dinv64 = nullptr;
     float* dinv32 = nullptr;
     int ncolours = 0;
@@ -2209,7 +2416,12 @@ struct lina_gpu_amg {
         st.r = lvx<TX>(L, 3);
         st.cb = lvx<TX>(C, 2);
         st.w = opt.omega;
-        const int K = fused_cluster_size<TX, PRE, JAC>();
+        if (!JAC && L.stage_k > 0 && !(L.ngroups > 0 && L.n > g_fused_rows) &&
+            L.stage_k <= staged_cluster_max<TX, PRE>()) {
+            launch_staged<TX, PRE>(L, st);
+            return;
+        }
+        const int K = fused_blocks<TX, PRE, JAC>(L);
         // whole systems in groups, one cluster each, where the level is too large for one cluster
         const bool grouped = !JAC && L.ngroups > 0 && L.n > g_fused_rows;
         cudaLaunchConfig_t cfg = {};
@@ -2234,13 +2446,90 @@ struct lina_gpu_amg {
     // 16 blocks per cluster where the GPU schedules such clusters, else (or with LINA_FUSED_CLUSTER=8)
     // the portable 8.  Measured on the batch workload's 24-system sample: 16 blocks 3 % faster in total
     // (the large elasticity systems gain, the 10k-row ones lose 2 %).
+    template <typename TX, bool PRE>
+    void launch_staged(const DLevel& L, const FusedStep& st) {
+        StagedPlan sp;
+        sp.img = L.stage_int;
+        sp.vals = sizeof(TX) == 8 ? (const void*)L.stage_v64 : (const void*)L.stage_v32;
+        sp.ints = L.stage_ints;
+        sp.nvals = L.stage_nvals;
+        sp.pslots = L.stage_pslots;
+        sp.o_row = L.stage_o_row;
+        sp.o_off = L.stage_o_off;
+        sp.o_col = L.stage_o_col;
+        sp.o_dinv = L.stage_o_dinv;
+        sp.xbytes = (int)(((long)L.n * sizeof(TX) + 15) / 16 * 16);
+        const int K = L.stage_k;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(K);
+        cfg.blockDim = dim3(kFuseThreads);
+        cfg.dynamicSmemBytes =
+            (size_t)sp.xbytes + (size_t)(sp.nvals + sp.pslots) * sizeof(TX) + (size_t)sp.ints * sizeof(int);
+        cfg.stream = stream;
+        cudaLaunchAttribute attr[2];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = K;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[1].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = g_pdl ? 2 : 1;
+        g_launches++;
+        cudaLaunchKernelEx(&cfg, staged_step_kernel<TX, PRE>, st, sp);
+    }
+
+    // the largest cluster of staged steps the GPU schedules with a full block of shared memory (16 where
+    // it allows non-portable clusters, else 8)
+    template <typename TX, bool PRE>
+    static int staged_cluster_max() {
+        static int k = 0;
+        if (k == 0) {
+            k = 8;
+            cudaFuncSetAttribute(staged_step_kernel<TX, PRE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 kStagedSmemMax);
+            if (cudaFuncSetAttribute(staged_step_kernel<TX, PRE>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+                cudaSuccess) {
+                cudaLaunchConfig_t cfg = {};
+                cfg.gridDim = dim3(16);
+                cfg.blockDim = dim3(kFuseThreads);
+                cfg.dynamicSmemBytes = kStagedSmemMax;
+                cudaLaunchAttribute attr[1];
+                attr[0].id = cudaLaunchAttributeClusterDimension;
+                attr[0].val.clusterDim.x = 16;
+                attr[0].val.clusterDim.y = 1;
+                attr[0].val.clusterDim.z = 1;
+                cfg.attrs = attr;
+                cfg.numAttrs = 1;
+                int nclusters = 0;
+                if (cudaOccupancyMaxActiveClusters(&nclusters, staged_step_kernel<TX, PRE>, &cfg) == cudaSuccess &&
+                    nclusters > 0)
+                    k = 16;
+            }
+            cudaGetLastError();  // a refused attribute or query leaves no error behind
+        }
+        return k;
+    }
+
+    template <typename TX, bool PRE, bool JAC>
+    static int fused_blocks(const DLevel& L) {
+        const int kmax = fused_cluster_size<TX, PRE, JAC>();
+        static int forced = -1;
+        if (forced < 0) {
+            const char* env = getenv("LINA_FUSED_CLUSTER");
+            const int v = env ? atoi(env) : 0;
+            forced = (v == 1 || v == 2 || v == 4 || v == 8 || v == 16) ? v : 0;
+        }
+        const int k = forced ? forced : L.fuse_k;
+        return k > 0 ? std::min(k, kmax) : kmax;
+    }
+
     template <typename TX, bool PRE, bool JAC>
     static int fused_cluster_size() {
         static int k = 0;
         if (k == 0) {
             k = 8;
-            const char* env = getenv("LINA_FUSED_CLUSTER");
-            const bool want16 = !(env && atoi(env) == 8);
+            const bool want16 = true;
             cudaFuncSetAttribute(fused_step_kernel<TX, PRE, JAC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  kFusedSmemMax);
             if (want16 &&
@@ -2676,6 +2965,100 @@ done:
     return rc;
 }
 
+// the value images of a staged level, from its current entries and 1/a_ii
+int stage_refresh(lina_gpu_amg* h, DLevel& L) {
+    if (L.stage_k <= 0) return 0;
+    const long n = (long)L.stage_k * L.stage_nvals;
+    go(stage_gather_kernel, grid_for(n, kThreads), h->stream, n, (const int*)L.stage_src, (const double*)L.Acol.v64,
+       (const float*)L.Acol.v32, (const double*)L.dinv64, (const float*)L.dinv32, h->opt.omega, L.stage_v64,
+       L.stage_v32);
+    CK(cudaGetLastError());
+    return 0;
+}
+
+static inline int pad4(long v) { return (int)((v + 3) / 4 * 4); }
+
+// The staged plan of a level (see staged_step_kernel) for a cluster of K blocks, the largest the GPU
+// schedules (16 on GB300; LINA_STAGED_K=1|2|4|8 asks for fewer); none where the images, with a copy of
+// x, do not fit a block's shared memory in FP64 (such levels' fused steps read the matrix from global
+// memory).  The largest cluster is the fastest: GB300's SM runs one FP64 warp instruction about every
+// 19 cycles, whatever its active lanes, so a colour of many rows is bound by the FP64 pipes of the
+// blocks that share it (P1 Poisson 257 x 257, FP64 solves: 10.3 ms with one block per level, 9.6 with
+// four, 8.7 with eight, 8.6 with sixteen).
+int build_stage(lina_gpu_amg* h, DLevel& L, const lina::Csr& A, const std::vector<std::vector<int>>& groups) {
+    L.stage_k = 0;
+    const int n = L.n, C = L.ncolours, S = L.Acol.lanes;
+    if (S <= 0 || C <= 0 || (long)n * 8 > kStagedSmemMax || (int)groups.size() != C) return 0;
+    int K = lina_gpu_amg::staged_cluster_max<double, true>();
+    if (const char* e = getenv("LINA_STAGED_K")) {
+        const int v = atoi(e);
+        if (v == 1 || v == 2 || v == 4 || v == 8 || v == 16) K = std::min(K, v);
+    }
+    auto share = [&](int c, int r, int& a, int& b) {
+        const long len = (long)groups[c].size();
+        a = (int)(len * r / K);
+        b = (int)(len * (r + 1) / K);
+    };
+    int pmax = 0;
+    long emax = 0;
+    for (int r = 0; r < K; r++) {
+        int P = 0;
+        long E = 0;
+        for (int c = 0; c < C; c++) {
+            int a, b;
+            share(c, r, a, b);
+            P += b - a;
+            for (int t = a; t < b; t++) E += A.ptr[groups[c][t] + 1] - A.ptr[groups[c][t]];
+        }
+        pmax = std::max(pmax, P);
+        emax = std::max(emax, E);
+    }
+    const int o_row = pad4(C + 1), o_off = o_row + pad4(pmax), o_col = o_off + pad4(pmax + 1);
+    const long ints = (long)o_col + pad4(emax);
+    const long nvals = (long)pad4(emax) + pad4(pmax);
+    const long bytes = ((long)n * 8 + 15) / 16 * 16 + (nvals + pad4(pmax)) * 8 + ints * 4;
+    if (bytes > kStagedSmemMax) return 0;
+    std::vector<int> img((size_t)K * ints, 0), src((size_t)K * nvals, -1);
+    for (int r = 0; r < K; r++) {
+        int* I = img.data() + (size_t)r * ints;
+        int* V = src.data() + (size_t)r * nvals;
+        int q = 0, e = 0;
+        for (int c = 0; c < C; c++) {
+            I[c] = q;
+            int a, b;
+            share(c, r, a, b);
+            for (int t = a; t < b; t++, q++) {
+                const int i = groups[c][t];
+                I[o_row + q] = i;
+                I[o_off + q] = e;
+                V[pad4(emax) + q] = -2 - i;
+                for (int k = A.ptr[i]; k < A.ptr[i + 1]; k++, e++) {
+                    I[o_col + e] = (A.col[k] >= 0 && A.col[k] < n) ? A.col[k] : 0;  // placeholders hold 0.0
+                    V[e] = k;
+                }
+            }
+        }
+        I[C] = q;
+        I[o_off + q] = e;
+    }
+    int rc;
+    if ((rc = h->upload(&L.stage_int, img.data(), img.size()))) return rc;
+    if ((rc = h->upload(&L.stage_src, src.data(), src.size()))) return rc;
+    if ((rc = h->alloc(&L.stage_v64, src.size()))) return rc;
+    if ((rc = h->alloc(&L.stage_v32, src.size()))) return rc;
+    L.stage_k = K;
+    L.stage_ints = (int)ints;
+    L.stage_nvals = (int)nvals;
+    L.stage_pslots = pad4(pmax);
+    L.stage_o_row = o_row;
+    L.stage_o_off = o_off;
+    L.stage_o_col = o_col;
+    L.stage_o_dinv = pad4(emax);
+    if ((rc = stage_refresh(h, L))) return rc;
+    // the host images must outlive the asynchronous uploads
+    return cudaStreamSynchronize(h->stream) == cudaSuccess ? 0 : LINA_GPU_ECUDA;
+}
+
 int upload_hierarchy(lina_gpu_amg* h) {
     lina::HostHierarchy& H = h->host;
     const int depth = h->depth;
@@ -2728,6 +3111,7 @@ int upload_hierarchy(lina_gpu_amg* h) {
             std::vector<std::vector<int>> groups(L.ncolours);
             for (int i = 0; i < L.n; i++) groups[colour[i]].push_back(i);
             if ((rc = h->upload_csr(L.Acol, hl.A, &groups, h->keep_maps ? &posC : nullptr))) return rc;
+            if ((rc = build_stage(h, L, hl.A, groups))) return rc;
             if (!h->seg_off.empty() && (rc = build_fused_groups(h, l, hl, groups))) return rc;
         }
         if (h->keep_maps) {  // in-place value updates of later recomputes
@@ -3178,6 +3562,7 @@ int refresh_values(lina_gpu_amg* h) {
         std::vector<float> dinv32(dinv.begin(), dinv.end());
         CK(cudaMemcpyAsync(L.dinv64, dinv.data(), dinv.size() * sizeof(double), cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(L.dinv32, dinv32.data(), dinv32.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+        if ((rc = stage_refresh(h, L))) return rc;
         CK(cudaStreamSynchronize(st));  // the staging buffer and the host vectors are reused
     }
     // coarsest level: the new dense block (inverted here or on the device) and 1/a_ii elsewhere
@@ -3334,6 +3719,7 @@ int lina_gpu_amg_update_values(lina_gpu_amg* h, const double* val, int flags) {
        reinterpret_cast<float*>(L.A.q_val));
     go(update_diag_kernel, grid_for(L.n, kThreads), h->stream, L.n, v, (const int*)h->upd_ptr,
        (const int*)h->upd_diagpos, (const unsigned char*)h->upd_isolated, L.dinv64, L.dinv32, h->isoinv);
+    if ((rc = stage_refresh(h, L))) return rc;
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(h->stream));
     return 0;
@@ -3350,10 +3736,17 @@ int lina_gpu_amg_set_smoother(lina_gpu_amg* h, int smoother, double omega, int p
         set_err("lina_gpu_amg_set_smoother: invalid argument");
         return LINA_GPU_EINVAL;
     }
+    const bool new_omega = omega != h->opt.omega;
     h->opt.smoother = smoother;
     h->opt.omega = omega;
     h->opt.precision = precision;
     h->drop_graph();
+    if (new_omega && !h->host_only) {
+        int rc;
+        for (DLevel& L : h->lv)
+            if ((rc = stage_refresh(h, L))) return rc;
+        CK(cudaStreamSynchronize(h->stream));
+    }
     return 0;
 }
 

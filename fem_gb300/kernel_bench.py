@@ -3,6 +3,7 @@
     python -m fem_gb300.kernel_bench --m 1025 --reps 3              # finest matrix
     python -m fem_gb300.kernel_bench --m 1025 --level 8 --reps 3    # a level of the AMG hierarchy
     python -m fem_gb300.kernel_bench --m 1025 --solve --reps 2      # whole mixed-precision solves
+    python -m fem_gb300.kernel_bench --solve --poisson --reps 3     # whole FP64 solves of P1 Poisson 257 x 257
     python -m fem_gb300.kernel_bench --segbatch 24 --reps 2         # a segmented batch, host-launched
 
 Builds the degraded plane-strain elasticity matrix (m x m nodes, 2 m^2 unknowns) or, with
@@ -14,6 +15,8 @@ in isolation with little device memory in use.
 --solve instead builds the benchmark's device hierarchy (damped Jacobi, omega 0.6, mixed precision) and
 runs `reps` AMG-PCG solves to the relative residual 1e-8, each iteration launched from the host rather
 than from the captured graph (a profiler cannot see the kernels of a graph with conditional nodes).
+With --poisson the solves are those of the P1 Poisson workload (257 x 257 nodes, aggressive coarsening,
+depth 6, 2 + 2 multicolour-SOR sweeps with omega 1, FP64, stopping rule ||r|| / ||M^-1 r0|| <= 1e-8).
 
 --segbatch K builds the first K systems of the batched workload (seeded Delaunay meshes, the workload's
 hierarchy settings: standard coarsening, matrix_tol 0.3, multicolour SOR, mixed precision), their
@@ -41,6 +44,8 @@ def main():
                     help="comma-separated sizes m: time the device inverse of a dense m x m block with FP64 CUDA "
                          "cores and with FP64 tensor cores instead")
     ap.add_argument("--solve", action="store_true", help="whole solves, launched iteration by iteration")
+    ap.add_argument("--poisson", action="store_true", help="with --solve: the P1 Poisson 257 x 257 workload")
+    ap.add_argument("--mixed", action="store_true", help="with --solve --poisson: the FP32 V-cycle instead of FP64")
     ap.add_argument("--segbatch", type=int, default=0, help="a segmented batch of this many workload systems")
     args = ap.parse_args()
     if args.solve:
@@ -82,14 +87,24 @@ def main():
 
 def solve(args):
     lina.set_sell_index_bits(args.sell_bits)
-    s = problems.elasticity_p1(args.m)
-    amg = lina.AMG.from_system(s, depth=args.depth, coarsening=lina.STANDARD, smoother=lina.SMOOTHER_JACOBI,
-                               omega=0.6, precision=lina.PREC_MIXED, matrix_tol=args.matrix_tol)
+    if args.poisson:
+        s = problems.poisson_p1(257, seed=0)
+        amg = lina.AMG.from_system(s, depth=6, coarsening=lina.AGGRESSIVE, smoother=lina.SMOOTHER_MC_SOR,
+                                   omega=1.0, precision=lina.PREC_MIXED if args.mixed else lina.PREC_FP64)
+        stop, flags = lina.STOP_REFERENCE, lina.PCG_NORMALIZE | lina.PCG_FINAL_PRECON
+    else:
+        s = problems.elasticity_p1(args.m)
+        amg = lina.AMG.from_system(s, depth=args.depth, coarsening=lina.STANDARD, smoother=lina.SMOOTHER_JACOBI,
+                                   omega=0.6, precision=lina.PREC_MIXED, matrix_tol=args.matrix_tol)
+        stop, flags = lina.STOP_RELATIVE, 0
+    if args.poisson:
+        print({"level_sizes": amg.sizes(),
+               "colours": [int(amg.colours(l).max()) + 1 for l in range(1, amg.depth)]}, flush=True)
     b = lina.DeviceArray.from_host(s.b)
     x = lina.DeviceArray(s.n)
     for _ in range(args.reps):
         t0 = time.perf_counter()
-        info = amg.pcg_device(b, x, tol=1e-8, max_iter=2000, stop=lina.STOP_RELATIVE, flags=lina.PCG_HOST_LOOP)
+        info = amg.pcg_device(b, x, tol=1e-8, max_iter=2000, stop=stop, flags=flags | lina.PCG_HOST_LOOP)
         print({"iterations": info.iterations, "status": info.status, "ms": (time.perf_counter() - t0) * 1e3,
                "launches": lina.launches()}, flush=True)
     amg.close()
