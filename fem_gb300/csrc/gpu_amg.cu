@@ -2989,7 +2989,11 @@ int build_stage(lina_gpu_amg* h, DLevel& L, const lina::Csr& A, const std::vecto
     L.stage_k = 0;
     const int n = L.n, C = L.ncolours, S = L.Acol.lanes;
     if (S <= 0 || C <= 0 || (long)n * 8 > kStagedSmemMax || (int)groups.size() != C) return 0;
-    int K = lina_gpu_amg::staged_cluster_max<double, true>();
+    // every variant's launch attributes are set here, outside any stream capture
+    int K = std::min(std::min(lina_gpu_amg::staged_cluster_max<double, true>(),
+                              lina_gpu_amg::staged_cluster_max<double, false>()),
+                     std::min(lina_gpu_amg::staged_cluster_max<float, true>(),
+                              lina_gpu_amg::staged_cluster_max<float, false>()));
     if (const char* e = getenv("LINA_STAGED_K")) {
         const int v = atoi(e);
         if (v == 1 || v == 2 || v == 4 || v == 8 || v == 16) K = std::min(K, v);
