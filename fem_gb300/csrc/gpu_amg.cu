@@ -1800,7 +1800,6 @@ struct DLevel {
     // cluster per group of whole systems (ngroups > 0)
     int ngroups = 0, max_group_rows = 0;
     FusedGroup* d_groups = nullptr;
-    int fuse_k = 0;  // blocks per cluster of the level's fused step (0: the largest the GPU schedules)
     // the staged fused step (stage_k blocks, 0: none); images as StagedPlan describes them
     int stage_k = 0, stage_ints = 0, stage_nvals = 0, stage_pslots = 0;
     int stage_o_row = 0, stage_o_off = 0, stage_o_col = 0, stage_o_dinv = 0;
@@ -2421,7 +2420,7 @@ struct lina_gpu_amg {
             launch_staged<TX, PRE>(L, st);
             return;
         }
-        const int K = fused_blocks<TX, PRE, JAC>(L);
+        const int K = fused_blocks<TX, PRE, JAC>();
         // whole systems in groups, one cluster each, where the level is too large for one cluster
         const bool grouped = !JAC && L.ngroups > 0 && L.n > g_fused_rows;
         cudaLaunchConfig_t cfg = {};
@@ -2443,9 +2442,7 @@ struct lina_gpu_amg {
                            grouped ? (const FusedGroup*)L.d_groups : (const FusedGroup*)nullptr);
     }
 
-    // 16 blocks per cluster where the GPU schedules such clusters, else (or with LINA_FUSED_CLUSTER=8)
-    // the portable 8.  Measured on the batch workload's 24-system sample: 16 blocks 3 % faster in total
-    // (the large elasticity systems gain, the 10k-row ones lose 2 %).
+    // the staged step of a level: one cluster of its plan's blocks (see staged_step_kernel)
     template <typename TX, bool PRE>
     void launch_staged(const DLevel& L, const FusedStep& st) {
         StagedPlan sp;
@@ -2511,8 +2508,10 @@ struct lina_gpu_amg {
         return k;
     }
 
+    // blocks per cluster of an unstaged fused step: the largest cluster the GPU schedules, or fewer with
+    // LINA_FUSED_CLUSTER (1, 2, 4 or 8)
     template <typename TX, bool PRE, bool JAC>
-    static int fused_blocks(const DLevel& L) {
+    static int fused_blocks() {
         const int kmax = fused_cluster_size<TX, PRE, JAC>();
         static int forced = -1;
         if (forced < 0) {
@@ -2520,21 +2519,21 @@ struct lina_gpu_amg {
             const int v = env ? atoi(env) : 0;
             forced = (v == 1 || v == 2 || v == 4 || v == 8 || v == 16) ? v : 0;
         }
-        const int k = forced ? forced : L.fuse_k;
-        return k > 0 ? std::min(k, kmax) : kmax;
+        return forced > 0 ? std::min(forced, kmax) : kmax;
     }
 
+    // 16 blocks per cluster where the GPU schedules such clusters, else the portable 8.  Measured on the
+    // batch workload's 24-system sample: 16 blocks 3 % faster in total (the large elasticity systems
+    // gain, the 10k-row ones lose 2 %).
     template <typename TX, bool PRE, bool JAC>
     static int fused_cluster_size() {
         static int k = 0;
         if (k == 0) {
             k = 8;
-            const bool want16 = true;
             cudaFuncSetAttribute(fused_step_kernel<TX, PRE, JAC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  kFusedSmemMax);
-            if (want16 &&
-                cudaFuncSetAttribute(fused_step_kernel<TX, PRE, JAC>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
-                    cudaSuccess) {
+            if (cudaFuncSetAttribute(fused_step_kernel<TX, PRE, JAC>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+                cudaSuccess) {
                 cudaLaunchConfig_t cfg = {};
                 cfg.gridDim = dim3(16);
                 cfg.blockDim = dim3(kFuseThreads);
