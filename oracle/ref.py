@@ -231,6 +231,58 @@ class RefAMG:
             self.ptr = None
 
 
+class RefHierarchy:
+    """A reference hierarchy read back as arrays (sizes and per-level A, labels, P, R), detached from the
+    library: the result of :func:`hierarchy`."""
+
+    def __init__(self, sizes, levels):
+        self._sizes = list(sizes)
+        self._levels = list(levels)
+        self.depth = len(self._levels)
+
+    def sizes(self):
+        return list(self._sizes)
+
+    def level(self, lv) -> RefLevel:
+        return self._levels[lv]
+
+
+def _hierarchy_child(n, indptr, indices, data, dof, depth, sm, aggr_sm, coarsening):
+    from types import SimpleNamespace
+    sysm = SimpleNamespace(n=n, indptr=indptr, indices=indices, data=data, dof=dof)
+    R = RefAMG(sysm, depth, sm, aggr_sm, coarsening)
+    return R.sizes(), [R.level(lv) for lv in range(depth)]
+
+
+_HIERARCHIES: dict = {}
+
+
+def hierarchy(sysm, depth, sm=2, aggr_sm=2, coarsening=AGGRESSIVE) -> RefHierarchy:
+    """AMG_setup of the reference on a CSR system, run in a child process of its own (spawned) and
+    remembered for the rest of the session by the system's bytes and the settings.
+
+    After one large set-up the reference's later set-ups in the same process run many times slower
+    (a 33k-dof elasticity hierarchy: 5 s the first time, 90-110 s the next; the allocator's state
+    after the reference frees its row lists, which malloc_trim does not undo).  A child process per
+    set-up keeps every run at its first-run speed and the test process's heap clean."""
+    import hashlib
+    import multiprocessing as mp
+
+    ip_ = np.ascontiguousarray(sysm.indptr, dtype=np.int32)
+    ix_ = np.ascontiguousarray(sysm.indices, dtype=np.int32)
+    dt_ = np.ascontiguousarray(sysm.data, dtype=np.float64)
+    h = hashlib.sha256()
+    for a in (ip_, ix_, dt_):
+        h.update(a.tobytes())
+    key = (h.hexdigest(), int(sysm.dof), depth, sm, aggr_sm, coarsening)
+    if key not in _HIERARCHIES:
+        with mp.get_context("spawn").Pool(1) as pool:
+            sizes, levels = pool.apply(_hierarchy_child, (int(sysm.n), ip_, ix_, dt_, int(sysm.dof), depth, sm,
+                                                          aggr_sm, coarsening))
+        _HIERARCHIES[key] = RefHierarchy(sizes, levels)
+    return _HIERARCHIES[key]
+
+
 def pcg_stock(sysm, depth, smoother=SMOOTHER_MC_SOR, omega=1.6, tol=1e-8, max_iter=500):
     """PCG_default + PCG_set_AMG_preconditioner + pcg on the reference; returns (x, iterations, residuum)."""
     A = RefMatrix.from_csr(sysm.n, sysm.indptr, sysm.indices, sysm.data)

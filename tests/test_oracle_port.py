@@ -61,7 +61,7 @@ PORT_LIVE = [c for c in LIVE if c[0] != "elast129_aggr"]
 def test_port_setup_matches_live_reference(case):
     _, factory, depth, coarsening = case
     s = factory()
-    R = ref.RefAMG(s, depth, 2, 2, coarsening)
+    R = ref.hierarchy(s, depth, 2, 2, coarsening)
     P = port.PortAMG.setup(s, depth, coarsening)
     assert P.sizes() == R.sizes()
     for l in range(depth):

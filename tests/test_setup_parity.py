@@ -52,7 +52,7 @@ LIVE = [
 def test_hierarchy_matches_live_reference(case):
     _, factory, depth, coarsening = case
     s = factory()
-    R = ref.RefAMG(s, depth, 2, 2, coarsening)
+    R = ref.hierarchy(s, depth, 2, 2, coarsening)
     G = lina.AMG.from_system(s, host_only=True, depth=depth, coarsening=coarsening)
     assert G.sizes() == R.sizes()
     for l in range(depth):
