@@ -16,7 +16,8 @@ in isolation with little device memory in use.
 runs `reps` AMG-PCG solves to the relative residual 1e-8, each iteration launched from the host rather
 than from the captured graph (a profiler cannot see the kernels of a graph with conditional nodes).
 With --poisson the solves are those of the P1 Poisson workload (257 x 257 nodes, aggressive coarsening,
-depth 6, 2 + 2 multicolour-SOR sweeps with omega 1, FP64, stopping rule ||r|| / ||M^-1 r0|| <= 1e-8).
+depth 6, 2 + 2 multicolour-SOR sweeps with omega 1, FP64, stopping rule ||r|| / ||M^-1 r0|| <= 1e-8);
+--mixed runs its V-cycle in FP32 instead (for comparison: the workload itself is FP64).
 
 --segbatch K builds the first K systems of the batched workload (seeded Delaunay meshes, the workload's
 hierarchy settings: standard coarsening, matrix_tol 0.3, multicolour SOR, mixed precision), their
